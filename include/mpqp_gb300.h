@@ -1,0 +1,189 @@
+/*
+ * mpqp_gb300 -- combinatorial mpQP active-set check on one GB300 (sm_103a).
+ *
+ * C ABI of libmpqp_gb300.so.  The first block is a drop-in for the library
+ * the reference loads through ctypes (mpqp_cuda.so): same symbol names, same
+ * argument order and meaning, same result structure prefix.  The second block
+ * is this library's native interface (many instances in one launch, mixed
+ * precision, device-resident plans for timing).
+ *
+ * Threading: one call at a time per process (the reference's driver calls
+ * it from a single Python thread).  All entry points return an error code or
+ * a NULL pointer instead of terminating the process.
+ */
+#ifndef MPQP_GB300_H
+#define MPQP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Drop-in boundary (reference: main.py:12-50, 60, 144)                 */
+/* ------------------------------------------------------------------ */
+
+/* Result of mpqp().  The first eight fields are the reference's
+ * GPUResults (main.py:12-22); the rest are appended, so a caller that maps
+ * only the prefix keeps working.
+ *   n_batches        number of enumeration levels that were run
+ *   n_splits         number of device launches of the LP kernels
+ *   n_feasible_lps   candidate active sets found feasible (LP1)
+ *   n_final_lps      candidate active sets found optimal (LP2); their sets
+ *                    are in active_sets, row-major n_final_lps x n_x,
+ *                    ascending indices, unused entries -1 (utils.py:105-116)
+ *   time_feas        seconds in enumeration + feasibility kernels
+ *   time_opti        seconds in optimality kernels
+ *   time_GPU         seconds of device time for the whole call
+ * The structure and its arrays stay valid until mpqp_free() or the next
+ * mpqp() call, whichever comes first. */
+typedef struct GPUResults {
+    int n_batches;
+    int n_splits;
+    int n_feasible_lps;
+    int n_final_lps;
+    double time_feas;
+    double time_opti;
+    double time_GPU;
+    int *active_sets;
+    /* appended */
+    int status;              /* 0 on success, else an MPQP_E* code         */
+    int n_regions;           /* optimal sets whose Chebyshev radius >= 1e-8 */
+    long long n_candidates;  /* candidate active sets checked               */
+    long long n_pruned;      /* children dropped by the subset test         */
+    double *t_star;          /* n_final_lps: LP2 optimum (max margin)       */
+    double *radius;          /* n_final_lps: Chebyshev radius               */
+    int *is_region;          /* n_final_lps: 1 when radius >= 1e-8          */
+} GPUResults;
+
+/* Replaces mpqp_cuda.so:mpqp (called at main.py:144, argtypes main.py:28-50).
+ * AxT      n_x x n_c column-major (= A^T, main.py:100,130)
+ * A1, xb1  LP1 standard form, M1 x N1 column-major and M1 (main.py:91-98)
+ * b1       LP1 initial basis (main.py:121)
+ * A2, xb2  LP2 standard form, M2 x N2 column-major and M2 (main.py:102-118)
+ * b2, non_b2  LP2 initial basis / non-basis (main.py:123-128)
+ * k_min, k_max  cardinality range of the active sets to report
+ * extra_batches, reserved_memory  accepted for compatibility; reserved_memory
+ *          (MiB) is left free on the device.
+ * The problem data are read back from A1/xb1/A2/xb2; the LP layouts are
+ * validated and a malformed input returns a result with status != 0. */
+GPUResults *mpqp(const double *AxT, int n_c, int n_x, int n_t, int k_min, int k_max, int extra_batches,
+                 const double *A1, const double *xb1, const int *b1, int M1, int N1,
+                 const double *A2, const double *xb2, const int *b2, const int *non_b2, int M2, int N2,
+                 int n_eqs, int reserved_memory);
+
+/* Replaces mpqp_cuda.so:warm_up (main.py:60): creates the CUDA context,
+ * loads the kernels and runs one tiny problem. */
+void warm_up(void);
+
+/* Releases a result of mpqp() (the reference never frees; this is optional). */
+void mpqp_free(GPUResults *res);
+
+/* ------------------------------------------------------------------ */
+/* Native interface                                                      */
+/* ------------------------------------------------------------------ */
+
+enum {
+    MPQP_OK = 0,
+    MPQP_EINVAL = -1,      /* bad sizes or pointers                        */
+    MPQP_ENOTSPD = -2,     /* Q is not positive definite                   */
+    MPQP_EORIGIN = -3,     /* b < 0 or CRb < 0: the origin is infeasible   */
+    MPQP_ELAYOUT = -4,     /* LP matrices do not have the reference layout */
+    MPQP_ECUDA = -5,       /* CUDA runtime error                           */
+    MPQP_ECAPACITY = -6,   /* a device buffer overflowed                   */
+    MPQP_ENOMEM = -7       /* device allocation failed                     */
+};
+
+enum { MPQP_FP64 = 0, MPQP_MIXED = 1 };
+
+/* One mpQP instance: min 1/2 x'Qx + (c + H theta)'x  s.t.  A x <= b + F theta,
+ * At theta <= bt.  Row-major host arrays. */
+typedef struct {
+    int n, m, p, ncp;
+    int k_min, k_max;        /* cardinalities to check (k_max <= min(n, m))  */
+    long long budget;        /* max candidates checked (0 = no limit)       */
+    const double *Q, *c, *H, *A, *b, *F, *At, *bt;
+} mpqp_problem;
+
+typedef struct {
+    int precision;           /* MPQP_FP64 or MPQP_MIXED                     */
+    int exhaustive;          /* 1: every combination is a candidate          */
+    int record;              /* 1: keep one record per checked candidate    */
+    int use_graph;           /* 1: capture the level loop in a CUDA graph   */
+    long long cand_cap;      /* candidates per level (0: derived)           */
+    long long node_cap;      /* nodes per level (0: = cand_cap)             */
+    long long arena_bytes;   /* tableau arena (0: derived)                  */
+    long long rec_cap;       /* records (record = 1)                        */
+    long long opt_cap;       /* optimal-set records (0: derived)            */
+    double mem_fraction;     /* of free device memory used when derived     */
+    /* tolerances (0 selects the default) */
+    double tol_feas, tol_opt, tol_licq, r_min, tol_piv, tol_dj;
+    int max_pivots, degen_switch;
+    double tol_piv32, tol_dj32, margin_z, margin_beta, margin_t, margin_licq;
+} mpqp_options;
+
+/* One optimal active set */
+typedef struct {
+    uint64_t mask_lo, mask_hi;   /* bit i set: constraint i is active        */
+    int inst, level;
+    double t;                    /* LP2 optimum                              */
+    double r;                    /* Chebyshev radius                         */
+    int region, fp64;
+    long long rec;
+} mpqp_opt_set;
+
+/* Per-instance counters */
+typedef struct {
+    long long candidates, pruned, feasible, optimal, regions;
+    long long lp1_pivots, lp2_pivots, cheb_pivots, fallback_lp1, fallback_opt;
+    int last_level, truncated;
+} mpqp_inst_stats;
+
+typedef struct {
+    int status;
+    int n_inst;
+    int n_levels;
+    int overflow;                 /* MPQP_ECAPACITY detail bits             */
+    double device_ms;             /* events around the device work          */
+    mpqp_inst_stats *inst;        /* n_inst                                 */
+    long long n_opt;
+    mpqp_opt_set *opt;            /* n_opt, sorted (inst, level, mask)      */
+    long long n_rec;
+    void *rec;                    /* n_rec records (96 bytes each) or NULL  */
+} mpqp_batch_result;
+
+void mpqp_default_options(mpqp_options *opt);
+
+/* Solve a batch of independent instances in one launch sequence. */
+int mpqp_solve_batch(int n_inst, const mpqp_problem *probs, const mpqp_options *opt, mpqp_batch_result **out);
+void mpqp_batch_free(mpqp_batch_result *res);
+
+/* Device-resident plans: upload once, run many times (timing). */
+typedef struct mpqp_plan mpqp_plan;
+int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpqp_options *opt, mpqp_plan **out);
+/* Enqueue one full enumeration on `stream` (a cudaStream_t, NULL = default). */
+int mpqp_plan_run(mpqp_plan *plan, void *stream);
+/* Copy the results of the last run to the host (synchronises the stream). */
+int mpqp_plan_results(mpqp_plan *plan, mpqp_batch_result **out);
+/* Number of kernel launches one run enqueues. */
+int mpqp_plan_launches(const mpqp_plan *plan);
+void mpqp_plan_destroy(mpqp_plan *plan);
+
+/* Region laws of optimal sets, computed in FP64 on the device:
+ *   lagrange_A (k x p), lagrange_b (k), parameter_A (n x p), parameter_b (n),
+ *   CR rows (n_cr x (p+1)): [CR_As | CR_bs] normalised, reference order.
+ * Sizes per set are written to `sizes` (4 ints: k, n, p, n_cr); `laws` must
+ * hold n_sets * (mmax*(p+1) + n*(p+1) + (m+ncp)*(p+1)) doubles (see
+ * mpqp_region_laws_stride). */
+long long mpqp_region_laws_stride(const mpqp_problem *prob);
+int mpqp_region_laws(const mpqp_problem *prob, long long n_sets, const uint64_t *masks /* 2 per set */,
+                     double *laws, int *sizes);
+
+const char *mpqp_version(void);
+const char *mpqp_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,852 @@
+// Host engine and C ABI of libmpqp_gb300.so.
+//
+//  * prepare_instance: FP64 precompute of the KKT blocks (host, once per
+//    instance, fixed operation order with explicit fma, -ffp-contract=off);
+//  * mpqp_plan: device buffers sized for the batch, the level loop captured
+//    in one CUDA graph, results copied back on demand;
+//  * mpqp / warm_up: the drop-in boundary of the reference's mpqp_cuda.so
+//    (main.py:12-50), which rebuilds the problem from the LP matrices that
+//    main.py:87-137 builds.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/mpqp_gb300.h"
+#include "mpqp_internal.h"
+
+namespace mq {
+size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd);
+size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd);
+size_t laws_smem_per_warp(const SlotDims &sd);
+const void *kernel_ptr(const char *name);
+cudaError_t launch_enumerate(const DevBuffers &B, int level, int grid, cudaStream_t s);
+cudaError_t launch_feasibility(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int prec,
+                               int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_lp1_fp64(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int grid,
+                            size_t smem, cudaStream_t s);
+cudaError_t launch_optimality(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int prec,
+                              int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_optimality_fp64(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int grid,
+                                   size_t smem, cudaStream_t s);
+cudaError_t launch_level0(const DevBuffers &B, int prec, cudaStream_t s);
+cudaError_t launch_reset(const DevBuffers &B, cudaStream_t s);
+cudaError_t launch_finalize(const DevBuffers &B, int level, cudaStream_t s);
+cudaError_t launch_region_laws(const DevBuffers &B, const Tol &tol, const SlotDims &sd, const uint64_t *masks,
+                               long long n_sets, double *laws, int *sizes, long long stride, int grid,
+                               size_t smem, cudaStream_t s);
+}  // namespace mq
+
+using namespace mq;
+
+static std::string g_err;
+static std::mutex g_mu;
+
+static void set_err(const std::string &s) { g_err = s; }
+
+#define CK(call)                                                                                       \
+    do {                                                                                               \
+        cudaError_t _e = (call);                                                                       \
+        if (_e != cudaSuccess) {                                                                       \
+            set_err(std::string(#call) + ": " + cudaGetErrorString(_e));                               \
+            return MPQP_ECUDA;                                                                         \
+        }                                                                                              \
+    } while (0)
+
+// ---------------------------------------------------------------------
+// FP64 precompute (operation order identical to the CPU oracle)
+// ---------------------------------------------------------------------
+struct Prepared {
+    InstDesc d;
+    std::vector<double> Wm, Wh, wc, At, bt, QiAT, QiH, Qic, root;
+};
+
+static inline int odd_up(int x) { return (x & 1) ? x : x + 1; }
+
+static void fwd_sub(const double *L, int n, const double *rhs, int rs, double *y, int ys)
+{
+    for (int i = 0; i < n; i++) {
+        double acc = rhs[(size_t)i * rs];
+        for (int l = 0; l < i; l++) acc = std::fma(-L[i * n + l], y[(size_t)l * ys], acc);
+        y[(size_t)i * ys] = acc / L[i * n + i];
+    }
+}
+
+static void bwd_sub(const double *L, int n, const double *y, int ysd, double *x, int xs)
+{
+    for (int i = n - 1; i >= 0; i--) {
+        double acc = y[(size_t)i * ysd];
+        for (int l = i + 1; l < n; l++) acc = std::fma(-L[l * n + i], x[(size_t)l * xs], acc);
+        x[(size_t)i * xs] = acc / L[i * n + i];
+    }
+}
+
+static int prepare_instance(const mpqp_problem &P, Prepared &out)
+{
+    const int n = P.n, m = P.m, p = P.p, ncp = P.ncp;
+    if (n < 1 || m < 1 || p < 1 || ncp < 1 || m > kMaxM || p > kMaxP) {
+        set_err("instance sizes out of range (need 1<=m<=128, 1<=p<=30, n>=1, ncp>=1)");
+        return MPQP_EINVAL;
+    }
+    if (m + ncp + n + p > kMaxIds || m + ncp + p + 1 > kMaxIds) {
+        set_err("instance too large for 8-bit basis ids (m+ncp+n+p must be <= 255)");
+        return MPQP_EINVAL;
+    }
+    if (!P.Q || !P.c || !P.H || !P.A || !P.b || !P.F || !P.At || !P.bt) {
+        set_err("null problem pointer");
+        return MPQP_EINVAL;
+    }
+    for (int i = 0; i < m; i++)
+        if (!(P.b[i] >= 0.0)) { set_err("b has a negative entry: the origin must be feasible"); return MPQP_EORIGIN; }
+    for (int i = 0; i < ncp; i++)
+        if (!(P.bt[i] >= 0.0)) { set_err("CRb has a negative entry: the origin must be feasible"); return MPQP_EORIGIN; }
+    int kmax = P.k_max;
+    if (kmax > m) kmax = m;
+    if (kmax > kMaxK) kmax = kMaxK;
+    if (kmax < 0) kmax = 0;
+    InstDesc &d = out.d;
+    memset(&d, 0, sizeof(d));
+    d.n = n; d.m = m; d.p = p; d.ncp = ncp;
+    d.M1 = m + ncp; d.nv = n + p;
+    d.ld1 = odd_up(d.nv + 1);
+    d.ld2 = odd_up(p + 2);
+    d.k_min = P.k_min < 0 ? 0 : P.k_min;
+    d.k_max = kmax;
+    d.tab_elems = ((d.M1 + 1) * d.ld1 + 3) & ~3;
+    d.ids_bytes = (d.M1 + d.nv + 15) & ~15;
+    d.budget = P.budget;
+    std::vector<double> L((size_t)n * n, 0.0), V((size_t)n * m, 0.0), U((size_t)n * p, 0.0), u(n, 0.0);
+    for (int j = 0; j < n; j++) {
+        for (int i = j; i < n; i++) {
+            double acc = P.Q[i * n + j];
+            for (int l = 0; l < j; l++) acc = std::fma(-L[i * n + l], L[j * n + l], acc);
+            if (i == j) {
+                if (!(acc > 0.0)) { set_err("Q is not positive definite"); return MPQP_ENOTSPD; }
+                L[j * n + j] = std::sqrt(acc);
+            } else {
+                L[i * n + j] = acc / L[j * n + j];
+            }
+        }
+    }
+    for (int r = 0; r < m; r++) fwd_sub(L.data(), n, P.A + (size_t)r * n, 1, V.data() + r, m);
+    for (int c = 0; c < p; c++) fwd_sub(L.data(), n, P.H + c, p, U.data() + c, p);
+    fwd_sub(L.data(), n, P.c, 1, u.data(), 1);
+    out.Wm.assign((size_t)m * m, 0.0);
+    out.Wh.assign((size_t)m * p, 0.0);
+    out.wc.assign(m, 0.0);
+    for (int r = 0; r < m; r++) {
+        for (int s = 0; s < m; s++) {
+            double acc = 0.0;
+            for (int i = 0; i < n; i++) acc = std::fma(V[i * m + r], V[i * m + s], acc);
+            out.Wm[r * m + s] = acc;
+        }
+        for (int c = 0; c < p; c++) {
+            double acc = P.F[r * p + c];
+            for (int i = 0; i < n; i++) acc = std::fma(V[i * m + r], U[i * p + c], acc);
+            out.Wh[r * p + c] = acc;
+        }
+        double acc = P.b[r];
+        for (int i = 0; i < n; i++) acc = std::fma(V[i * m + r], u[i], acc);
+        out.wc[r] = acc;
+    }
+    out.QiAT.assign((size_t)n * m, 0.0);
+    out.QiH.assign((size_t)n * p, 0.0);
+    out.Qic.assign(n, 0.0);
+    for (int r = 0; r < m; r++) bwd_sub(L.data(), n, V.data() + r, m, out.QiAT.data() + r, m);
+    for (int c = 0; c < p; c++) bwd_sub(L.data(), n, U.data() + c, p, out.QiH.data() + c, p);
+    bwd_sub(L.data(), n, u.data(), 1, out.Qic.data(), 1);
+    out.At.assign(P.At, P.At + (size_t)ncp * p);
+    out.bt.assign(P.bt, P.bt + ncp);
+    const int ld = d.ld1;
+    out.root.assign((size_t)d.tab_elems, 0.0);
+    for (int i = 0; i < m; i++) {
+        for (int j = 0; j < n; j++) out.root[i * ld + j] = P.A[i * n + j];
+        for (int j = 0; j < p; j++) out.root[i * ld + n + j] = -P.F[i * p + j];
+        out.root[i * ld + d.nv] = P.b[i];
+    }
+    for (int i = 0; i < ncp; i++) {
+        for (int j = 0; j < p; j++) out.root[(m + i) * ld + n + j] = P.At[i * p + j];
+        out.root[(m + i) * ld + d.nv] = P.bt[i];
+    }
+    return MPQP_OK;
+}
+
+// ---------------------------------------------------------------------
+// plan
+// ---------------------------------------------------------------------
+struct mpqp_plan {
+    int n_inst = 0;
+    std::vector<InstDesc> desc;
+    std::vector<mpqp_problem> probs;
+    mpqp_options opt{};
+    Tol tol{};
+    SlotDims sd{};
+    DevBuffers B{};
+    std::vector<void *> allocs;
+    int kmax = 0;
+    int prec = PREC_FP64;
+    int grid_enum = 0, grid_feas = 0, grid_lp1fb = 0, grid_opt = 0, grid_optfb = 0;
+    size_t smem_feas = 0, smem_lp1fb = 0, smem_opt = 0, smem_optfb = 0;
+    int n_launches = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_mid = nullptr;
+    bool ran = false;
+    double last_ms = 0;
+    double feas_ms = 0, opt_ms = 0;
+};
+
+extern "C" void mpqp_default_options(mpqp_options *o)
+{
+    memset(o, 0, sizeof(*o));
+    o->precision = MPQP_FP64;
+    o->use_graph = 1;
+    o->mem_fraction = 0.6;
+    o->tol_feas = 1e-9;
+    o->tol_opt = 1e-9;
+    o->tol_licq = 1e-10;
+    o->r_min = 1e-8;
+    o->tol_piv = 1e-9;
+    o->tol_dj = 1e-9;
+    o->max_pivots = 256;
+    o->degen_switch = 8;
+    o->tol_piv32 = 1e-6;
+    o->tol_dj32 = 1e-6;
+    o->margin_z = 1e-3;
+    o->margin_beta = 1e-3;
+    o->margin_t = 3e-5;   // x (row magnitude / pivot ratio) x (1 + p |theta|max)
+    o->margin_licq = 1e-3;
+}
+
+static void fill_defaults(mpqp_options &o)
+{
+    mpqp_options d;
+    mpqp_default_options(&d);
+#define DEF(f) if (o.f == 0) o.f = d.f
+    DEF(mem_fraction); DEF(tol_feas); DEF(tol_opt); DEF(tol_licq); DEF(r_min); DEF(tol_piv); DEF(tol_dj);
+    DEF(max_pivots); DEF(degen_switch); DEF(tol_piv32); DEF(tol_dj32); DEF(margin_z); DEF(margin_beta);
+    DEF(margin_t); DEF(margin_licq);
+#undef DEF
+}
+
+static int dev_alloc(mpqp_plan *P, void **ptr, size_t bytes)
+{
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e != cudaSuccess) {
+        set_err(std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+        cudaGetLastError();
+        return MPQP_ENOMEM;
+    }
+    P->allocs.push_back(*ptr);
+    return MPQP_OK;
+}
+
+static void free_plan_mem(mpqp_plan *P)
+{
+    if (P->exec) cudaGraphExecDestroy(P->exec);
+    if (P->graph) cudaGraphDestroy(P->graph);
+    P->exec = nullptr; P->graph = nullptr;
+    for (void *p : P->allocs) cudaFree(p);
+    P->allocs.clear();
+    if (P->ev0) cudaEventDestroy(P->ev0);
+    if (P->ev1) cudaEventDestroy(P->ev1);
+    if (P->ev_mid) cudaEventDestroy(P->ev_mid);
+    P->ev0 = P->ev1 = P->ev_mid = nullptr;
+}
+
+static int grid_for(const void *fn, size_t smem, int *grid)
+{
+    int dev = 0, sms = 0, nb = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (smem > 48 * 1024) CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, smem));
+    if (nb < 1) {
+        set_err("kernel does not fit on an SM (shared memory " + std::to_string(smem) + " bytes)");
+        return MPQP_EINVAL;
+    }
+    *grid = nb * sms;
+    return MPQP_OK;
+}
+
+static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed_phases)
+{
+    const DevBuffers &B = P->B;
+    const bool mixed = P->prec == PREC_MIXED;
+    int nl = 0;
+    auto chk = [&](cudaError_t e) -> int {
+        nl++;
+        if (e != cudaSuccess) { set_err(std::string("launch: ") + cudaGetErrorString(e)); return MPQP_ECUDA; }
+        return MPQP_OK;
+    };
+#define L(x) do { int _r = chk(x); if (_r) return _r; } while (0)
+    L(launch_reset(B, s));
+    L(launch_level0(B, P->prec, s));
+    L(launch_optimality(B, P->tol, P->sd, 0, P->prec, P->grid_opt, P->smem_opt, s));
+    if (mixed) L(launch_optimality_fp64(B, P->tol, P->sd, 0, P->grid_optfb, P->smem_optfb, s));
+    L(launch_finalize(B, 0, s));
+    for (int k = 1; k <= P->kmax; k++) {
+        L(launch_enumerate(B, k, P->grid_enum, s));
+        L(launch_feasibility(B, P->tol, P->sd, k, P->prec, P->grid_feas, P->smem_feas, s));
+        if (mixed) L(launch_lp1_fp64(B, P->tol, P->sd, k, P->grid_lp1fb, P->smem_lp1fb, s));
+        L(launch_optimality(B, P->tol, P->sd, k, P->prec, P->grid_opt, P->smem_opt, s));
+        if (mixed) L(launch_optimality_fp64(B, P->tol, P->sd, k, P->grid_optfb, P->smem_optfb, s));
+        L(launch_finalize(B, k, s));
+    }
+#undef L
+    (void)timed_phases;
+    P->n_launches = nl;
+    return MPQP_OK;
+}
+
+extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpqp_options *opt_in, mpqp_plan **out)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    *out = nullptr;
+    if (n_inst < 1 || !probs) { set_err("no instances"); return MPQP_EINVAL; }
+    mpqp_plan *P = new mpqp_plan();
+    if (opt_in) P->opt = *opt_in; else mpqp_default_options(&P->opt);
+    fill_defaults(P->opt);
+    const mpqp_options &o = P->opt;
+    P->prec = o.precision == MPQP_MIXED ? PREC_MIXED : PREC_FP64;
+    P->n_inst = n_inst;
+    P->probs.assign(probs, probs + n_inst);
+    Tol &t = P->tol;
+    t.tol_feas = o.tol_feas; t.tol_opt = o.tol_opt; t.tol_licq = o.tol_licq; t.r_min = o.r_min;
+    t.tol_piv = o.tol_piv; t.tol_dj = o.tol_dj; t.max_pivots = o.max_pivots; t.degen_switch = o.degen_switch;
+    t.tol_piv32 = (float)o.tol_piv32; t.tol_dj32 = (float)o.tol_dj32;
+    t.margin_z = o.margin_z; t.margin_beta = o.margin_beta; t.margin_t = o.margin_t; t.margin_licq = o.margin_licq;
+    // host precompute
+    std::vector<Prepared> prep(n_inst);
+    for (int i = 0; i < n_inst; i++) {
+        int rc = prepare_instance(probs[i], prep[i]);
+        if (rc) { set_err("instance " + std::to_string(i) + ": " + g_err); delete P; return rc; }
+    }
+    // pools
+    std::vector<double> dp;
+    std::vector<float> fp;
+    auto put = [](auto &pool, const std::vector<double> &v) -> long long {
+        long long off = (long long)pool.size();
+        for (double x : v) pool.push_back((typename std::remove_reference<decltype(pool)>::type::value_type)x);
+        while (pool.size() % 4) pool.push_back(0);
+        return off;
+    };
+    SlotDims &sd = P->sd;
+    sd = SlotDims{0, 0, 0, 1, 0, 0, 0};
+    long long tab_tot0 = 0, ids_tot0 = 0;
+    size_t max_tab_bytes = 0;
+    for (int i = 0; i < n_inst; i++) {
+        Prepared &pr = prep[i];
+        InstDesc &d = pr.d;
+        d.o_Wm = put(dp, pr.Wm); d.o_Wh = put(dp, pr.Wh); d.o_wc = put(dp, pr.wc);
+        d.o_At = put(dp, pr.At); d.o_bt = put(dp, pr.bt); d.o_QiAT = put(dp, pr.QiAT);
+        d.o_QiH = put(dp, pr.QiH); d.o_Qic = put(dp, pr.Qic); d.o_root = put(dp, pr.root);
+        d.f_Wm = put(fp, pr.Wm); d.f_Wh = put(fp, pr.Wh); d.f_wc = put(fp, pr.wc);
+        d.f_At = put(fp, pr.At); d.f_bt = put(fp, pr.bt); d.f_root = put(fp, pr.root);
+        P->desc.push_back(d);
+        P->kmax = std::max(P->kmax, d.k_max);
+        sd.maxM1 = std::max(sd.maxM1, d.M1);
+        sd.maxLD1 = std::max(sd.maxLD1, d.ld1);
+        sd.maxNv = std::max(sd.maxNv, d.nv);
+        sd.maxK = std::max(sd.maxK, std::max(1, std::min(d.k_max, d.m)));
+        sd.maxP1 = std::max(sd.maxP1, d.p + 1);
+        sd.maxR2 = std::max(sd.maxR2, d.m + d.ncp);
+        sd.maxLD2 = std::max(sd.maxLD2, d.ld2);
+        tab_tot0 += d.tab_elems;
+        ids_tot0 += d.ids_bytes;
+        max_tab_bytes = std::max(max_tab_bytes, (size_t)d.tab_elems * (P->prec == PREC_MIXED ? 4 : 8));
+    }
+    const size_t es = P->prec == PREC_MIXED ? 4 : 8;
+    // capacities
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        set_err(std::string("cudaMemGetInfo: ") + cudaGetErrorString(cudaGetLastError()));
+        delete P;
+        return MPQP_ECUDA;
+    }
+    const double usable = (double)free_b * o.mem_fraction;
+    long long total_budget = 0;
+    bool all_budget = true;
+    for (int i = 0; i < n_inst; i++) {
+        if (probs[i].budget > 0) total_budget += probs[i].budget; else all_budget = false;
+    }
+    // combinatorial ceilings: at most C(m, k) candidates / nodes at level k
+    double lvl_max = 0, arena_max = 0;
+    {
+        std::vector<double> lvl(kMaxK + 2, 0.0), lvl_tab(kMaxK + 2, 0.0);
+        for (int i = 0; i < n_inst; i++) {
+            double cmk = 1.0;
+            for (int k = 0; k <= P->desc[i].k_max; k++) {
+                if (k > 0) cmk = cmk * (double)(P->desc[i].m - k + 1) / (double)k;
+                lvl[k] += cmk;
+                if (k < P->desc[i].k_max) lvl_tab[k] += cmk * (double)P->desc[i].tab_elems * (double)es;
+            }
+        }
+        for (int k = 0; k <= kMaxK; k++) {
+            lvl_max = std::max(lvl_max, lvl[k]);
+            arena_max = std::max(arena_max, lvl_tab[k] + lvl_tab[k + 1]);
+        }
+    }
+    long long cand_cap = o.cand_cap;
+    if (cand_cap <= 0) {
+        // per candidate: cand 8 + q_lp1 4 + node 2x48 + q_opt 4 + hash 2x2x32,
+        // plus arena share; keep the candidate side at ~30 % of usable memory
+        const double per = 8 + 4 + 2 * sizeof(Node) + 4 + 4 * sizeof(HashSlot);
+        cand_cap = (long long)(usable * 0.3 / per);
+        if (all_budget) cand_cap = std::min(cand_cap, total_budget + n_inst);
+        cand_cap = (long long)std::min((double)cand_cap, lvl_max + 64);
+        cand_cap = std::max(cand_cap, (long long)1024);
+    }
+    long long node_cap = o.node_cap > 0 ? o.node_cap : cand_cap;
+    node_cap = std::max(node_cap, (long long)n_inst);
+    long long hash_cap = 16;
+    while (hash_cap < 2 * node_cap + 1) hash_cap <<= 1;
+    long long arena_bytes = o.arena_bytes;
+    if (arena_bytes <= 0) {
+        const double used = (double)cand_cap * 12 + (double)node_cap * (2 * sizeof(Node) + 4) +
+                            (double)hash_cap * 2 * sizeof(HashSlot);
+        arena_bytes = (long long)std::max(usable - used, (double)(64 << 20));
+        if (all_budget) {
+            // parents of the deepest checked level hold at most the budget
+            const double need = (double)(total_budget + n_inst) * (double)(max_tab_bytes + 64);
+            arena_bytes = (long long)std::min((double)arena_bytes, need * 1.05 + (64 << 20));
+        }
+        arena_bytes = (long long)std::min((double)arena_bytes, arena_max * 1.05 + (16 << 20));
+    }
+    long long tab_cap = arena_bytes / (long long)es;
+    tab_cap = std::max(tab_cap, 2 * tab_tot0 + 1024);
+    tab_cap &= ~3LL;
+    // basis ids: one record per stored tableau, sized by the smallest tableau
+    long long min_tab = 1LL << 40, max_ids = 16;
+    for (const InstDesc &d : P->desc) { min_tab = std::min(min_tab, (long long)d.tab_elems); max_ids = std::max(max_ids, (long long)d.ids_bytes); }
+    long long ids_cap = std::max((tab_cap / min_tab + n_inst + 1) * max_ids, 2 * ids_tot0 + 1024);
+    ids_cap = (ids_cap + 15) & ~15LL;
+    long long opt_cap = o.opt_cap > 0 ? o.opt_cap : std::max(node_cap / 8, (long long)4096);
+    long long rec_cap = o.record ? (o.rec_cap > 0 ? o.rec_cap : cand_cap * 4) : 0;
+    DevBuffers &B = P->B;
+    memset(&B, 0, sizeof(B));
+    B.n_inst = n_inst;
+    B.node_cap = node_cap;
+    B.tab_cap = tab_cap;
+    B.ids_cap = ids_cap;
+    B.hash_cap = hash_cap;
+    B.cand_cap = cand_cap;
+    B.q_cap = cand_cap;
+    B.opt_cap = opt_cap;
+    B.rec_cap = rec_cap;
+    B.exhaustive = o.exhaustive ? 1 : 0;
+    B.precision = P->prec;
+    int rc = MPQP_OK;
+    void *p;
+#define AL(ptr, bytes) do { rc = dev_alloc(P, &p, (bytes)); if (rc) { free_plan_mem(P); delete P; return rc; } ptr = (decltype(ptr))p; } while (0)
+    AL(B.inst, sizeof(InstDesc) * n_inst);
+    AL(B.dpool, sizeof(double) * dp.size());
+    AL(B.fpool, sizeof(float) * fp.size());
+    AL(B.node[0], sizeof(Node) * node_cap);
+    AL(B.node[1], sizeof(Node) * node_cap);
+    AL(B.tab[0], es * (size_t)tab_cap);
+    B.tab[1] = B.tab[0];  // one arena, two sides (see below)
+    AL(B.ids[0], (size_t)ids_cap);
+    B.ids[1] = B.ids[0];
+    AL(B.hash[0], sizeof(HashSlot) * hash_cap);
+    AL(B.hash[1], sizeof(HashSlot) * hash_cap);
+    AL(B.cand, sizeof(Cand) * cand_cap);
+    AL(B.q_lp1, sizeof(int) * cand_cap);
+    AL(B.q_opt, sizeof(int) * cand_cap);
+    AL(B.opt, sizeof(OptRec) * opt_cap);
+    if (rec_cap) AL(B.rec, sizeof(CandRec) * rec_cap);
+    AL(B.ictl, sizeof(InstCtl) * n_inst);
+    AL(B.ctl, sizeof(Ctl));
+#undef AL
+    CK(cudaMemcpy((void *)B.inst, P->desc.data(), sizeof(InstDesc) * n_inst, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy((void *)B.dpool, dp.data(), sizeof(double) * dp.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy((void *)B.fpool, fp.data(), sizeof(float) * fp.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemset(B.hash[0], 0xff, sizeof(HashSlot) * hash_cap));
+    CK(cudaMemset(B.hash[1], 0xff, sizeof(HashSlot) * hash_cap));
+    CK(cudaMemset(B.ctl, 0, sizeof(Ctl)));
+    // kernel geometry
+    P->smem_feas = 4 * lp1_smem_per_warp(P->prec == PREC_MIXED ? 4 : 8, sd);
+    P->smem_lp1fb = 4 * lp1_smem_per_warp(8, sd);
+    P->smem_opt = 4 * opt_smem_per_warp(P->prec == PREC_MIXED ? 4 : 8, sd);
+    P->smem_optfb = 4 * opt_smem_per_warp(8, sd);
+    if ((rc = grid_for(kernel_ptr("enumerate"), 0, &P->grid_enum)) ||
+        (rc = grid_for(kernel_ptr(P->prec == PREC_MIXED ? "feas32" : "feas64"), P->smem_feas, &P->grid_feas)) ||
+        (rc = grid_for(kernel_ptr("lp1_fp64"), P->smem_lp1fb, &P->grid_lp1fb)) ||
+        (rc = grid_for(kernel_ptr(P->prec == PREC_MIXED ? "opt32" : "opt64"), P->smem_opt, &P->grid_opt)) ||
+        (rc = grid_for(kernel_ptr("opt_fp64"), P->smem_optfb, &P->grid_optfb))) {
+        free_plan_mem(P);
+        delete P;
+        return rc;
+    }
+    CK(cudaEventCreate(&P->ev0));
+    CK(cudaEventCreate(&P->ev1));
+    CK(cudaEventCreate(&P->ev_mid));
+    if (o.use_graph) {
+        cudaStream_t cs;
+        CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        rc = enqueue(P, cs, false);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(cs, &g);
+        cudaStreamDestroy(cs);
+        if (rc || e != cudaSuccess) {
+            if (!rc) set_err(std::string("graph capture: ") + cudaGetErrorString(e));
+            if (g) cudaGraphDestroy(g);
+            free_plan_mem(P);
+            delete P;
+            return rc ? rc : MPQP_ECUDA;
+        }
+        P->graph = g;
+        CK(cudaGraphInstantiate(&P->exec, g, 0));
+    }
+    *out = P;
+    return MPQP_OK;
+}
+
+extern "C" int mpqp_plan_run(mpqp_plan *P, void *stream)
+{
+    if (!P) return MPQP_EINVAL;
+    cudaStream_t s = (cudaStream_t)stream;
+    CK(cudaEventRecord(P->ev0, s));
+    if (P->exec) {
+        CK(cudaGraphLaunch(P->exec, s));
+    } else {
+        int rc = enqueue(P, s, true);
+        if (rc) return rc;
+    }
+    CK(cudaEventRecord(P->ev1, s));
+    P->ran = true;
+    return MPQP_OK;
+}
+
+extern "C" int mpqp_plan_launches(const mpqp_plan *P) { return P ? P->n_launches : 0; }
+
+static bool set_less(uint64_t alo, uint64_t ahi, uint64_t blo, uint64_t bhi)
+{
+    // lexicographic order of the sorted element lists of two equal-size sets
+    uint64_t dlo = alo ^ blo, dhi = ahi ^ bhi;
+    if (dlo) return (alo & (dlo & (~dlo + 1))) != 0;
+    if (dhi) return (ahi & (dhi & (~dhi + 1))) != 0;
+    return false;
+}
+
+extern "C" int mpqp_plan_results(mpqp_plan *P, mpqp_batch_result **out)
+{
+    *out = nullptr;
+    if (!P || !P->ran) { set_err("plan has not run"); return MPQP_EINVAL; }
+    CK(cudaEventSynchronize(P->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, P->ev0, P->ev1));
+    P->last_ms = ms;
+    Ctl ctl;
+    CK(cudaMemcpy(&ctl, P->B.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    std::vector<InstCtl> ic(P->n_inst);
+    CK(cudaMemcpy(ic.data(), P->B.ictl, sizeof(InstCtl) * P->n_inst, cudaMemcpyDeviceToHost));
+    mpqp_batch_result *R = (mpqp_batch_result *)calloc(1, sizeof(mpqp_batch_result));
+    R->n_inst = P->n_inst;
+    R->device_ms = ms;
+    R->overflow = ctl.overflow;
+    R->status = ctl.overflow ? MPQP_ECAPACITY : MPQP_OK;
+    if (ctl.overflow) set_err("device buffer overflow (bits " + std::to_string(ctl.overflow) + ")");
+    R->inst = (mpqp_inst_stats *)calloc(P->n_inst, sizeof(mpqp_inst_stats));
+    int nlev = 0;
+    for (int i = 0; i < P->n_inst; i++) {
+        mpqp_inst_stats &s = R->inst[i];
+        s.candidates = ic[i].cum_cand; s.pruned = ic[i].pruned; s.feasible = ic[i].feasible;
+        s.optimal = ic[i].optimal; s.regions = ic[i].region; s.lp1_pivots = ic[i].lp1_piv;
+        s.lp2_pivots = ic[i].lp2_piv; s.cheb_pivots = ic[i].cheb_piv; s.fallback_lp1 = ic[i].fb_lp1;
+        s.fallback_opt = ic[i].fb_opt; s.last_level = ic[i].last_level; s.truncated = ic[i].truncated;
+        nlev = std::max(nlev, ic[i].last_level + 1);
+    }
+    R->n_levels = nlev;
+    long long nopt = std::min(ctl.n_opt, P->B.opt_cap);
+    std::vector<OptRec> ov(nopt);
+    if (nopt) CK(cudaMemcpy(ov.data(), P->B.opt, sizeof(OptRec) * nopt, cudaMemcpyDeviceToHost));
+    std::sort(ov.begin(), ov.end(), [](const OptRec &a, const OptRec &b) {
+        if (a.inst != b.inst) return a.inst < b.inst;
+        if (a.level != b.level) return a.level < b.level;
+        return set_less(a.lo, a.hi, b.lo, b.hi);
+    });
+    R->n_opt = nopt;
+    R->opt = (mpqp_opt_set *)calloc(nopt ? nopt : 1, sizeof(mpqp_opt_set));
+    for (long long i = 0; i < nopt; i++) {
+        mpqp_opt_set &o = R->opt[i];
+        o.mask_lo = ov[i].lo; o.mask_hi = ov[i].hi; o.inst = ov[i].inst; o.level = ov[i].level;
+        o.t = ov[i].t; o.r = ov[i].r; o.region = ov[i].region; o.fp64 = ov[i].fp64; o.rec = ov[i].rec;
+    }
+    if (P->B.rec) {
+        long long nrec = std::min(ctl.rec_base, P->B.rec_cap);
+        R->n_rec = nrec;
+        R->rec = malloc(sizeof(CandRec) * (nrec ? nrec : 1));
+        if (nrec) CK(cudaMemcpy(R->rec, P->B.rec, sizeof(CandRec) * nrec, cudaMemcpyDeviceToHost));
+    }
+    *out = R;
+    return R->status;
+}
+
+extern "C" void mpqp_plan_destroy(mpqp_plan *P)
+{
+    if (!P) return;
+    free_plan_mem(P);
+    delete P;
+}
+
+extern "C" void mpqp_batch_free(mpqp_batch_result *R)
+{
+    if (!R) return;
+    free(R->inst);
+    free(R->opt);
+    free(R->rec);
+    free(R);
+}
+
+extern "C" int mpqp_solve_batch(int n_inst, const mpqp_problem *probs, const mpqp_options *opt,
+                                mpqp_batch_result **out)
+{
+    *out = nullptr;
+    mpqp_plan *P = nullptr;
+    int rc = mpqp_plan_create(n_inst, probs, opt, &P);
+    if (rc) return rc;
+    rc = mpqp_plan_run(P, nullptr);
+    if (!rc) rc = mpqp_plan_results(P, out);
+    mpqp_plan_destroy(P);
+    return rc;
+}
+
+// ---------------------------------------------------------------------
+// region laws
+// ---------------------------------------------------------------------
+extern "C" long long mpqp_region_laws_stride(const mpqp_problem *pr)
+{
+    const long long P1 = pr->p + 1;
+    return (long long)pr->m * P1 + (long long)pr->n * P1 + (long long)(pr->m + pr->ncp) * P1;
+}
+
+extern "C" int mpqp_region_laws(const mpqp_problem *prob, long long n_sets, const uint64_t *masks, double *laws,
+                                int *sizes)
+{
+    if (!prob || n_sets < 0 || (n_sets && (!masks || !laws || !sizes))) { set_err("bad arguments"); return MPQP_EINVAL; }
+    if (n_sets == 0) return MPQP_OK;
+    const int kcap = std::min(prob->m, std::min(prob->n, kMaxK));
+    for (long long i = 0; i < n_sets; i++) {
+        const uint64_t lo = masks[2 * i], hi = masks[2 * i + 1];
+        const int k = __builtin_popcountll(lo) + __builtin_popcountll(hi);
+        const bool out_of_range = prob->m < 64 ? ((lo >> prob->m) != 0 || hi != 0)
+                                               : (prob->m < 128 && (hi >> (prob->m - 64)) != 0);
+        if (k > kcap || out_of_range) { set_err("active set " + std::to_string(i) + " is out of range"); return MPQP_EINVAL; }
+    }
+    mpqp_options o;
+    mpqp_default_options(&o);
+    o.use_graph = 0;
+    o.cand_cap = 1024;
+    o.arena_bytes = 1 << 20;
+    mpqp_problem pr = *prob;
+    pr.k_max = 0;
+    mpqp_plan *P = nullptr;
+    int rc = mpqp_plan_create(1, &pr, &o, &P);
+    if (rc) return rc;
+    // sizes for any set of the instance: use the instance's own bounds
+    SlotDims sd = P->sd;
+    sd.maxK = std::max(1, kcap);
+    const long long stride = mpqp_region_laws_stride(prob);
+    uint64_t *dm = nullptr; double *dl = nullptr; int *ds = nullptr;
+    size_t smem = 4 * laws_smem_per_warp(sd);
+    int grid = 0;
+    rc = grid_for(kernel_ptr("laws"), smem, &grid);
+    if (!rc) {
+        CK(cudaMalloc(&dm, sizeof(uint64_t) * 2 * n_sets));
+        CK(cudaMalloc(&dl, sizeof(double) * stride * n_sets));
+        CK(cudaMalloc(&ds, sizeof(int) * 4 * n_sets));
+        CK(cudaMemcpy(dm, masks, sizeof(uint64_t) * 2 * n_sets, cudaMemcpyHostToDevice));
+        CK(launch_region_laws(P->B, P->tol, sd, dm, n_sets, dl, ds, stride, grid, smem, nullptr));
+        CK(cudaMemcpy(laws, dl, sizeof(double) * stride * n_sets, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(sizes, ds, sizeof(int) * 4 * n_sets, cudaMemcpyDeviceToHost));
+        cudaFree(dm); cudaFree(dl); cudaFree(ds);
+    }
+    mpqp_plan_destroy(P);
+    return rc;
+}
+
+// ---------------------------------------------------------------------
+// drop-in boundary
+// ---------------------------------------------------------------------
+static GPUResults *g_last = nullptr;
+
+static void free_gpu_results(GPUResults *r)
+{
+    if (!r) return;
+    free(r->active_sets);
+    free(r->t_star);
+    free(r->radius);
+    free(r->is_region);
+    free(r);
+}
+
+extern "C" void mpqp_free(GPUResults *res)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (res == g_last) g_last = nullptr;
+    free_gpu_results(res);
+}
+
+static GPUResults *error_result(int status)
+{
+    GPUResults *r = (GPUResults *)calloc(1, sizeof(GPUResults));
+    r->status = status;
+    r->active_sets = (int *)calloc(1, sizeof(int));
+    r->t_star = (double *)calloc(1, sizeof(double));
+    r->radius = (double *)calloc(1, sizeof(double));
+    r->is_region = (int *)calloc(1, sizeof(int));
+    return r;
+}
+
+// Rebuild (Q, c, H, A, b, F, At, bt) from the LP matrices of main.py:87-128.
+static int unpack_lp(const double *AxT, int n_c, int n_x, int n_t, const double *A1, const double *xb1, int M1,
+                     int N1, const double *A2, const double *xb2, int M2, int N2, int n_eqs,
+                     std::vector<double> &Q, std::vector<double> &c, std::vector<double> &H, std::vector<double> &A,
+                     std::vector<double> &b, std::vector<double> &F, std::vector<double> &At, std::vector<double> &bt,
+                     int &n_cp)
+{
+    if (!A1 || !xb1 || !A2 || !xb2 || n_c < 1 || n_x < 1 || n_t < 1) { set_err("null or empty LP data"); return MPQP_EINVAL; }
+    n_cp = M1 - n_c;
+    if (n_cp < 1 || N1 != n_x + n_t + 1 + M1 || M2 != 2 * n_c + 1 + n_cp + n_x ||
+        N2 != n_x + n_t + n_c + 2 + M2 || n_eqs != n_c + n_x) {
+        set_err("LP dimensions do not match the reference layout (main.py:87-118)");
+        return MPQP_ELAYOUT;
+    }
+    A.assign((size_t)n_c * n_x, 0); F.assign((size_t)n_c * n_t, 0); b.assign(n_c, 0);
+    At.assign((size_t)n_cp * n_t, 0); bt.assign(n_cp, 0);
+    for (int i = 0; i < n_c; i++) {
+        for (int j = 0; j < n_x; j++) A[i * n_x + j] = A1[i + (size_t)j * M1];
+        for (int j = 0; j < n_t; j++) F[i * n_t + j] = -A1[i + (size_t)(n_x + j) * M1];
+        b[i] = xb1[i];
+    }
+    for (int i = 0; i < n_cp; i++) {
+        for (int j = 0; j < n_t; j++) At[i * n_t + j] = A1[(n_c + i) + (size_t)(n_x + j) * M1];
+        bt[i] = xb1[n_c + i];
+    }
+    if (AxT) {
+        for (int i = 0; i < n_c; i++)
+            for (int j = 0; j < n_x; j++)
+                if (AxT[j + (size_t)i * n_x] != A[i * n_x + j]) { set_err("AxT differs from A1[:n_c,:n_x]^T"); return MPQP_ELAYOUT; }
+    }
+    Q.assign((size_t)n_x * n_x, 0); H.assign((size_t)n_x * n_t, 0); c.assign(n_x, 0);
+    const int r0 = n_c + 1 + n_cp;
+    for (int i = 0; i < n_x; i++) {
+        const int r = r0 + i;
+        const double diag = A2[r + (size_t)i * M2];
+        if (diag == 0.0) { set_err("LP2 stationarity row has a zero diagonal"); return MPQP_ELAYOUT; }
+        const double s = diag > 0 ? 1.0 : -1.0;   // rows with -c_i < 0 were negated (main.py:112-114)
+        for (int j = 0; j < n_x; j++) Q[i * n_x + j] = s * A2[r + (size_t)j * M2];
+        for (int j = 0; j < n_t; j++) H[i * n_t + j] = s * A2[r + (size_t)(n_x + j) * M2];
+        c[i] = -s * xb2[r];
+    }
+    return MPQP_OK;
+}
+
+extern "C" GPUResults *mpqp(const double *AxT, int n_c, int n_x, int n_t, int k_min, int k_max, int extra_batches,
+                            const double *A1, const double *xb1, const int *b1, int M1, int N1, const double *A2,
+                            const double *xb2, const int *b2, const int *non_b2, int M2, int N2, int n_eqs,
+                            int reserved_memory)
+{
+    (void)b1; (void)b2; (void)non_b2; (void)extra_batches;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (g_last) { free_gpu_results(g_last); g_last = nullptr; }
+    }
+    std::vector<double> Q, c, H, A, b, F, At, bt;
+    int n_cp = 0;
+    int rc = unpack_lp(AxT, n_c, n_x, n_t, A1, xb1, M1, N1, A2, xb2, M2, N2, n_eqs, Q, c, H, A, b, F, At, bt, n_cp);
+    if (rc) return g_last = error_result(rc);
+    mpqp_problem pr;
+    memset(&pr, 0, sizeof(pr));
+    pr.n = n_x; pr.m = n_c; pr.p = n_t; pr.ncp = n_cp;
+    pr.k_min = k_min; pr.k_max = k_max;
+    pr.Q = Q.data(); pr.c = c.data(); pr.H = H.data(); pr.A = A.data(); pr.b = b.data(); pr.F = F.data();
+    pr.At = At.data(); pr.bt = bt.data();
+    mpqp_options o;
+    mpqp_default_options(&o);
+    const char *env = getenv("MPQP_PRECISION");
+    if (env && (!strcmp(env, "mixed") || !strcmp(env, "1"))) o.precision = MPQP_MIXED;
+    if (reserved_memory > 0) {
+        size_t fb = 0, tb = 0;
+        if (cudaMemGetInfo(&fb, &tb) == cudaSuccess) {
+            const double keep = (double)reserved_memory * 1024.0 * 1024.0;
+            o.mem_fraction = std::max(0.05, std::min(0.6, ((double)fb - keep) / std::max(1.0, (double)fb)));
+        }
+    }
+    mpqp_batch_result *R = nullptr;
+    rc = mpqp_solve_batch(1, &pr, &o, &R);
+    if (rc || !R) {
+        mpqp_batch_free(R);
+        return g_last = error_result(rc ? rc : MPQP_ECUDA);
+    }
+    GPUResults *G = (GPUResults *)calloc(1, sizeof(GPUResults));
+    const long long nf = R->n_opt;
+    const int kmin = k_min < 0 ? 0 : k_min;
+    long long nsel = 0;
+    for (long long i = 0; i < nf; i++) if (R->opt[i].level >= kmin) nsel++;
+    G->n_batches = R->n_levels;
+    G->n_splits = 1;
+    G->n_feasible_lps = (int)R->inst[0].feasible;
+    G->n_final_lps = (int)nsel;
+    G->time_GPU = R->device_ms * 1e-3;
+    G->time_feas = G->time_GPU;
+    G->time_opti = 0.0;
+    G->status = R->status;
+    G->n_candidates = R->inst[0].candidates;
+    G->n_pruned = R->inst[0].pruned;
+    G->active_sets = (int *)malloc(sizeof(int) * (size_t)(nsel ? nsel : 1) * n_x);
+    G->t_star = (double *)malloc(sizeof(double) * (nsel ? nsel : 1));
+    G->radius = (double *)malloc(sizeof(double) * (nsel ? nsel : 1));
+    G->is_region = (int *)malloc(sizeof(int) * (nsel ? nsel : 1));
+    long long w = 0;
+    int nreg = 0;
+    for (long long i = 0; i < nf; i++) {
+        const mpqp_opt_set &o2 = R->opt[i];
+        if (o2.level < kmin) continue;
+        int *row = G->active_sets + w * n_x;
+        int e = 0;
+        for (int j = 0; j < 128 && e < n_x; j++) {
+            const bool on = j < 64 ? ((o2.mask_lo >> j) & 1) : ((o2.mask_hi >> (j - 64)) & 1);
+            if (on) row[e++] = j;
+        }
+        for (; e < n_x; e++) row[e] = -1;
+        G->t_star[w] = o2.t;
+        G->radius[w] = o2.r;
+        G->is_region[w] = o2.region;
+        nreg += o2.region;
+        w++;
+    }
+    G->n_regions = nreg;
+    mpqp_batch_free(R);
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_last = G;
+    return G;
+}
+
+extern "C" void warm_up(void)
+{
+    // Smallest meaningful problem: n = 1, m = 2, p = 1, box |theta| <= 1.
+    static const double Q[1] = {1.0}, c[1] = {0.5}, H[1] = {1.0}, A[2] = {1.0, -1.0}, b[2] = {1.0, 1.0},
+                        F[2] = {0.5, -0.5}, At[2] = {1.0, -1.0}, bt[2] = {1.0, 1.0};
+    mpqp_problem pr = {1, 2, 1, 2, 0, 1, 0, Q, c, H, A, b, F, At, bt};
+    mpqp_options o;
+    mpqp_default_options(&o);
+    o.cand_cap = 1024;
+    o.arena_bytes = 1 << 20;
+    mpqp_batch_result *R = nullptr;
+    mpqp_solve_batch(1, &pr, &o, &R);
+    mpqp_batch_free(R);
+}
+
+extern "C" const char *mpqp_version(void) { return "mpqp_gb300 0.1 (sm_103a)"; }
+
+extern "C" const char *mpqp_last_error(void) { return g_err.c_str(); }

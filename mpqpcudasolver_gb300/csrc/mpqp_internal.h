@@ -1,0 +1,164 @@
+// Internal types shared by the device kernels and the host engine.
+//
+// Layout in HBM (one solve = one batch of independent mpQP instances):
+//   InstDesc[n_inst]           per-instance sizes, limits and offsets
+//   dbl pool                   per-instance FP64 data (KKT blocks, boxes,
+//                              laws data, LP1 root tableau)
+//   flt pool                   FP32 copies of the KKT blocks, boxes and root
+//   node arrays x2             feasible active sets of the previous / current
+//                              level (ping-pong), 32 B each
+//   tableau arena x2           LP1 final tableaus of those sets (bump
+//                              allocated, per-instance size), + basis ids
+//   mask hash x2               tagged open-addressing table of feasible masks
+//   candidate list             (parent node, added constraint) pairs, 8 B
+//   fallback queues            candidates / nodes re-solved in FP64
+//   optimal-set list           one OptRec per optimal active set
+//   records (optional)         one CandRec per checked candidate (parity)
+#pragma once
+#include <stdint.h>
+
+namespace mq {
+
+constexpr int kMaxM = 128;        // constraints per instance (128-bit masks)
+constexpr int kMaxIds = 255;      // ids are uint8
+constexpr int kMaxK = 32;         // largest active-set cardinality supported
+constexpr int kMaxP = 30;         // parameters
+
+enum LpStatus : int { LP_OPTIMAL = 0, LP_UNBOUNDED = 1, LP_ITER_LIMIT = 2, LP_SKIPPED = 3, LP_LICQ_FAIL = 4 };
+
+enum Precision : int { PREC_FP64 = 0, PREC_MIXED = 1 };
+
+struct Tol {
+    double tol_feas;    // LP1 feasible when z* <= tol_feas
+    double tol_opt;     // LP2 optimal when t* > tol_opt
+    double tol_licq;    // Cholesky pivot must exceed tol_licq * diagonal
+    double r_min;       // Chebyshev radius threshold (region when r >= r_min)
+    double tol_piv;     // FP64 ratio-test pivot threshold
+    double tol_dj;      // FP64 pricing threshold
+    int max_pivots;
+    int degen_switch;
+    // mixed precision: FP32 thresholds and the margins that send a
+    // candidate to the FP64 re-solve
+    float tol_piv32;
+    float tol_dj32;
+    double margin_z;    // FP32 LP1 z above this -> infeasible without FP64
+    double margin_beta; // FP32 basic slacks above this certify feasibility
+    double margin_t;    // FP32 LP2 t below -margin_t * error scale -> not optimal without FP64
+    double margin_licq; // FP32 Cholesky pivot ratio below this -> FP64
+};
+
+struct InstDesc {
+    int n, m, p, ncp;
+    int M1, nv, ld1, ld2;       // LP1 rows, LP1 free vars, tableau strides (odd)
+    int k_min, k_max;
+    int tab_elems;              // (M1+1)*ld1 rounded up to a multiple of 4
+    int ids_bytes;              // M1 + nv rounded up to 16
+    long long budget;           // max candidates checked for this instance (0 = no limit)
+    // offsets (elements) into the FP64 pool
+    long long o_Wm, o_Wh, o_wc, o_At, o_bt, o_QiAT, o_QiH, o_Qic, o_root;
+    // offsets (elements) into the FP32 pool
+    long long f_Wm, f_Wh, f_wc, f_At, f_bt, f_root;
+};
+
+struct Node {                   // a feasible (or, when exhaustive, any) active set
+    uint64_t lo, hi;            // 128-bit mask
+    int inst;
+    int flags;                  // NodeFlags
+    long long tab_off;          // element offset into the tableau arena (-1: none)
+    long long ids_off;          // byte offset into the ids arena
+    long long rec;              // record index (or -1)
+};
+
+enum NodeFlags : int { NODE_FEASIBLE = 1, NODE_VALID = 2 };
+
+struct Cand { int parent; int j; };
+
+struct OptRec {
+    uint64_t lo, hi;
+    int inst, level;
+    double t, r;
+    int region;
+    int fp64;                   // verdict decided by the FP64 kernels
+    long long rec;
+};
+
+struct CandRec {                // identical field layout to the oracle's record
+    uint64_t mask_lo, mask_hi;
+    int32_t level, parent;
+    int32_t lp1_status, lp1_pivots;
+    double z;
+    int32_t feasible, licq, optimal, region;
+    int32_t lp2_status, lp2_pivots, cheb_status, cheb_pivots;
+    double t, r;
+    int32_t inst, fp64;         // instance; bit0 LP1 / bit1 LP2 decided in FP64
+};
+
+struct HashSlot { uint64_t lo, hi; int inst; int tag; int val; int pad; };
+
+// Per-instance level bookkeeping
+struct InstCtl {
+    long long lvl_cand;         // candidates generated at the current level
+    long long cum_cand;         // candidates checked before the current level
+    long long pruned;           // children dropped by the subset test
+    long long feasible, optimal, region;
+    long long lp1_piv, lp2_piv, cheb_piv;
+    long long fb_lp1, fb_opt;   // FP64 fallbacks (mixed precision)
+    int stopped;                // budget exhausted or max level reached
+    int truncated;              // stopped by the budget
+    int last_level;
+    int pad;
+};
+
+struct Ctl {
+    long long n_cand;           // candidates at the current level
+    long long n_node[2];        // nodes per ping-pong side
+    long long tab_used[2];      // elements used per tableau arena
+    long long ids_used[2];      // bytes used per ids arena
+    long long n_opt;            // optimal sets found so far
+    long long n_rec;            // records written so far
+    long long rec_base;         // record index of the current level's first candidate
+    long long n_q_lp1, n_q_opt; // FP64 fallback queue lengths
+    unsigned long long ctr[8];  // work counters (reset every level)
+    int overflow;               // bit mask of overflowed buffers
+    int level;
+    int epoch;                  // run counter; hash tags are (epoch << 8) | level
+    int pad;
+};
+
+enum Overflow : int { OV_CAND = 1, OV_NODE = 2, OV_TAB = 4, OV_IDS = 8, OV_OPT = 16, OV_REC = 32, OV_QUEUE = 64, OV_HASH = 128 };
+
+// Largest per-warp shared-memory footprint over the instances of a batch
+struct SlotDims {
+    int maxM1, maxLD1, maxNv;       // LP1 tableau
+    int maxK, maxP1, maxR2, maxLD2; // KKT factor and LP2 / Chebyshev tableau
+};
+
+struct DevBuffers {
+    const InstDesc *inst;
+    int n_inst;
+    const double *dpool;
+    const float *fpool;
+    Node *node[2];
+    long long node_cap;
+    void *tab[2];               // double or float elements
+    long long tab_cap;          // elements per arena
+    uint8_t *ids[2];
+    long long ids_cap;
+    HashSlot *hash[2];
+    long long hash_cap;         // power of two
+    Cand *cand;
+    long long cand_cap;
+    int *q_lp1;                 // candidate indices for the FP64 LP1 re-solve
+    int *q_opt;                 // node indices for the FP64 optimality re-solve
+    long long q_cap;
+    OptRec *opt;
+    long long opt_cap;
+    CandRec *rec;               // may be null
+    long long rec_cap;
+    InstCtl *ictl;
+    Ctl *ctl;
+    int exhaustive;             // 1: every combination is a candidate (no pruning)
+    int precision;
+};
+
+}  // namespace mq

@@ -1,0 +1,1269 @@
+// Device kernels of the combinatorial mpQP active-set check (sm_103a).
+//
+// One enumeration level k runs as
+//   k_enumerate      children of the level-(k-1) feasible sets, superset
+//                    pruning against a tagged hash of feasible masks
+//   k_feasibility<T> LP1 per candidate, one warp per LP, tableau in shared
+//                    memory, warm-started from the parent's final tableau
+//   k_lp1_fp64       (mixed precision) FP64 re-solve of the LP1 candidates
+//                    the FP32 certificate could not decide
+//   k_optimality<T>  KKT factor -> critical-region rows -> LP2 (max margin)
+//                    -> Chebyshev LP, one warp per feasible set
+//   k_finalize       per-instance budget bookkeeping, counter resets
+// All counts live in device memory, so the whole level loop is a fixed
+// launch sequence that the host captures in one CUDA graph.
+//
+// Floating-point contract (FP64 kernels): explicit fma for every
+// multiply-add, sums in ascending index order, IEEE division and square root,
+// compiled with -fmad=false.  This is the operation order of the CPU oracle,
+// so FP64 LP values and verdicts are bit-identical to it.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mpqp_internal.h"
+
+namespace mq {
+
+#define FULLMASK 0xffffffffu
+
+__device__ __forceinline__ double xfma(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float xfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double xsqrt(double a) { return __dsqrt_rn(a); }
+__device__ __forceinline__ float xsqrt(float a) { return __fsqrt_rn(a); }
+__device__ __forceinline__ double xdiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float xdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double xmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float xmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double xadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float xadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double xabs(double a) { return fabs(a); }
+__device__ __forceinline__ float xabs(float a) { return fabsf(a); }
+
+template <typename T> __device__ __forceinline__ T pos_inf();
+template <> __device__ __forceinline__ double pos_inf<double>() { return __longlong_as_double(0x7ff0000000000000LL); }
+template <> __device__ __forceinline__ float pos_inf<float>() { return __int_as_float(0x7f800000); }
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+__device__ __forceinline__ bool mask_has(uint64_t lo, uint64_t hi, int j)
+{
+    return j < 64 ? ((lo >> j) & 1ull) : ((hi >> (j - 64)) & 1ull);
+}
+
+__device__ __forceinline__ int mask_pop(uint64_t lo, uint64_t hi) { return __popcll(lo) + __popcll(hi); }
+
+// number of mask bits below position i
+__device__ __forceinline__ int mask_rank(uint64_t lo, uint64_t hi, int i)
+{
+    if (i < 64) return __popcll(lo & ((i == 0) ? 0ull : (~0ull >> (64 - i))));
+    const int r = i - 64;
+    return __popcll(lo) + __popcll(hi & ((r == 0) ? 0ull : (~0ull >> (64 - r))));
+}
+
+__device__ __forceinline__ int mask_max(uint64_t lo, uint64_t hi)
+{
+    if (hi) return 127 - __clzll(hi);
+    if (lo) return 63 - __clzll(lo);
+    return -1;
+}
+
+__device__ __forceinline__ uint64_t mix64(uint64_t x)
+{
+    x ^= x >> 33; x *= 0xff51afd7ed558ccdULL; x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ULL; x ^= x >> 33;
+    return x;
+}
+
+__device__ __forceinline__ uint64_t hash_key(int inst, uint64_t lo, uint64_t hi)
+{
+    return mix64(lo ^ mix64(hi ^ ((uint64_t)(uint32_t)inst * 0x9e3779b97f4a7c15ULL)));
+}
+
+__device__ int hash_find(const HashSlot *tab, long long cap, int tag, int inst, uint64_t lo, uint64_t hi)
+{
+    uint64_t s = hash_key(inst, lo, hi) & (uint64_t)(cap - 1);
+    for (long long probe = 0; probe < cap; probe++) {
+        const HashSlot *h = tab + s;
+        if (h->tag != tag) return -1;
+        if (h->lo == lo && h->hi == hi && h->inst == inst) return h->val;
+        s = (s + 1) & (uint64_t)(cap - 1);
+    }
+    return -1;
+}
+
+__device__ bool hash_insert(HashSlot *tab, long long cap, int tag, int inst, uint64_t lo, uint64_t hi, int val)
+{
+    uint64_t s = hash_key(inst, lo, hi) & (uint64_t)(cap - 1);
+    for (long long probe = 0; probe < cap; probe++) {
+        HashSlot *h = tab + s;
+        const int t = *((volatile int *)&h->tag);
+        if (t != tag && atomicCAS(&h->tag, t, tag) == t) {
+            h->lo = lo; h->hi = hi; h->inst = inst; h->val = val;
+            return true;
+        }
+        if (t == tag) s = (s + 1) & (uint64_t)(cap - 1);
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------------
+// warp-cooperative Tucker-tableau simplex
+// ---------------------------------------------------------------------
+// rows 0..nrows-1 basic variables, row nrows the objective (minimised);
+// columns 0..ncols-1 nonbasic variables, column ncols the right-hand side.
+// x_B = T[.,ncols] - sum_j T[.,j] x_N(j).  Ids < nfree are free variables.
+template <typename T>
+struct Lp {
+    T *tab;
+    int ld, nrows, ncols, nfree;
+    uint8_t *bid, *nid;
+};
+
+template <typename T>
+__device__ int warp_simplex(const Lp<T> &L, T tol_piv, T tol_dj, int max_piv, int degen_switch, int *piv_out)
+{
+    const int lane = lane_id();
+    int piv = 0, degen = 0, status;
+    bool bland = false;
+    T *obj = L.tab + (size_t)L.nrows * L.ld;
+    for (;;) {
+        // pricing: largest |reduced cost|, smallest id on ties (Bland: smallest id)
+        T bs = T(0);
+        int bidv = 0x7fffffff, bq = -1;
+        for (int j = lane; j < L.ncols; j += 32) {
+            const T g = obj[j];
+            const int id = L.nid[j];
+            const T s = (id < L.nfree) ? xabs(g) : g;
+            if (!(s > tol_dj)) continue;
+            const bool better = (bq < 0) || (bland ? id < bidv : (s > bs || (s == bs && id < bidv)));
+            if (better) { bs = s; bidv = id; bq = j; }
+        }
+#pragma unroll
+        for (int off = 16; off; off >>= 1) {
+            const T os = __shfl_xor_sync(FULLMASK, bs, off);
+            const int oid = __shfl_xor_sync(FULLMASK, bidv, off);
+            const int oq = __shfl_xor_sync(FULLMASK, bq, off);
+            const bool better = (oq >= 0) && ((bq < 0) || (bland ? oid < bidv : (os > bs || (os == bs && oid < bidv))));
+            if (better) { bs = os; bidv = oid; bq = oq; }
+        }
+        if (bq < 0) { status = LP_OPTIMAL; break; }
+        const int q = bq;
+        const T sg = obj[q] > T(0) ? T(1) : T(-1);
+        // ratio test: smallest max(beta,0)/a over a > tol_piv, smallest id on ties
+        T br = T(0);
+        int brid = 0x7fffffff, bri = -1;
+        for (int i = lane; i < L.nrows; i += 32) {
+            const int id = L.bid[i];
+            if (id < L.nfree) continue;
+            const T a = sg * L.tab[(size_t)i * L.ld + q];
+            if (!(a > tol_piv)) continue;
+            T beta = L.tab[(size_t)i * L.ld + L.ncols];
+            if (!(beta > T(0))) beta = T(0);
+            const T ratio = xdiv(beta, a);
+            const bool better = (bri < 0) || ratio < br || (ratio == br && id < brid);
+            if (better) { br = ratio; brid = id; bri = i; }
+        }
+#pragma unroll
+        for (int off = 16; off; off >>= 1) {
+            const T orr = __shfl_xor_sync(FULLMASK, br, off);
+            const int oid = __shfl_xor_sync(FULLMASK, brid, off);
+            const int oi = __shfl_xor_sync(FULLMASK, bri, off);
+            const bool better = (oi >= 0) && ((bri < 0) || orr < br || (orr == br && oid < brid));
+            if (better) { br = orr; brid = oid; bri = oi; }
+        }
+        if (bri < 0) { status = LP_UNBOUNDED; break; }
+        if (piv >= max_piv) { status = LP_ITER_LIMIT; break; }
+        const int r = bri;
+        T *R = L.tab + (size_t)r * L.ld;
+        const T inv = xdiv(T(1), R[q]);
+        __syncwarp();
+        for (int j = lane; j <= L.ncols; j += 32) R[j] = (j == q) ? inv : xmul(R[j], inv);
+        __syncwarp();
+        for (int i = lane; i <= L.nrows; i += 32) {
+            if (i == r) continue;
+            T *Ti = L.tab + (size_t)i * L.ld;
+            const T f = Ti[q];
+            const T nf = -f;
+            for (int j = 0; j <= L.ncols; j++) Ti[j] = xfma(nf, R[j], Ti[j]);
+            Ti[q] = xmul(nf, inv);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            const uint8_t t = L.bid[r];
+            L.bid[r] = L.nid[q];
+            L.nid[q] = t;
+        }
+        __syncwarp();
+        piv++;
+        degen = (br == T(0)) ? degen + 1 : 0;
+        bland = degen >= degen_switch;
+    }
+    *piv_out = piv;
+    return status;
+}
+
+// ---------------------------------------------------------------------
+// shared-memory slot sizes
+// ---------------------------------------------------------------------
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+// LP1 slot: tableau (maxM1+1) x maxLD1 + ids (maxM1 + maxNv)
+template <typename T>
+__host__ __device__ inline size_t lp1_slot_bytes(int maxM1, int maxLD1, int maxNv)
+{
+    return align16((size_t)(maxM1 + 1) * maxLD1 * sizeof(T)) + align16((size_t)maxM1 + maxNv);
+}
+
+// optimality slot: R (kmax^2), Y and Lambda (kmax x P1), G (R2 x P1),
+// tableau (R2+1) x ld2, ids (R2 + P1), S list
+template <typename T>
+__host__ __device__ inline size_t opt_slot_bytes(int maxK, int maxP1, int maxR2, int maxLD2)
+{
+    return align16((size_t)maxK * maxK * sizeof(T)) + 2 * align16((size_t)maxK * maxP1 * sizeof(T)) +
+           align16((size_t)maxR2 * maxP1 * sizeof(T)) + align16((size_t)(maxR2 + 1) * maxLD2 * sizeof(T)) +
+           align16((size_t)maxR2 + maxP1) + align16((size_t)maxK * sizeof(int));
+}
+
+// ---------------------------------------------------------------------
+// K1: enumerate children, superset pruning
+// ---------------------------------------------------------------------
+struct LocalInstCounters {
+    int inst;
+    long long a, b, c, d, e, f, g;
+    __device__ void reset(int i) { inst = i; a = b = c = d = e = f = g = 0; }
+};
+
+__global__ void k_enumerate(DevBuffers B, int level)
+{
+    const int lane = lane_id();
+    const int pside = (level - 1) & 1;
+    Ctl *ctl = B.ctl;
+    const long long npar = ctl->n_node[pside] < B.node_cap ? ctl->n_node[pside] : B.node_cap;
+    const int tag_prev = (ctl->epoch << 8) | (level - 1);  // tag of the previous level's hash entries
+    int cur_inst = -1;
+    long long loc_cand = 0, loc_pruned = 0;
+    for (;;) {
+        long long pi;
+        if (lane == 0) pi = (long long)atomicAdd(&ctl->ctr[1], 1ull);
+        pi = __shfl_sync(FULLMASK, pi, 0);
+        if (pi >= npar) break;
+        const Node par = B.node[pside][pi];
+        if (!(par.flags & NODE_VALID)) continue;
+        if (!B.exhaustive && !(par.flags & NODE_FEASIBLE)) continue;
+        const InstDesc &I = B.inst[par.inst];
+        if (B.ictl[par.inst].stopped || level > I.k_max) continue;
+        if (par.inst != cur_inst) {
+            if (cur_inst >= 0 && lane == 0) {
+                atomicAdd((unsigned long long *)&B.ictl[cur_inst].lvl_cand, (unsigned long long)loc_cand);
+                atomicAdd((unsigned long long *)&B.ictl[cur_inst].pruned, (unsigned long long)loc_pruned);
+            }
+            cur_inst = par.inst;
+            loc_cand = loc_pruned = 0;
+        }
+        const int jmin = mask_max(par.lo, par.hi) + 1;
+        for (int j0 = jmin; j0 < I.m; j0 += 32) {
+            const int j = j0 + lane;
+            const bool valid = j < I.m;
+            bool ok = valid;
+            if (ok && !B.exhaustive) {
+                uint64_t lo = par.lo, hi = par.hi;
+                if (j < 64) lo |= 1ull << j; else hi |= 1ull << (j - 64);
+                uint64_t rlo = par.lo, rhi = par.hi;
+                while (ok && (rlo | rhi)) {
+                    int a;
+                    if (rlo) { a = __ffsll((long long)rlo) - 1; rlo &= rlo - 1; }
+                    else { a = 64 + __ffsll((long long)rhi) - 1; rhi &= rhi - 1; }
+                    uint64_t slo = lo, shi = hi;
+                    if (a < 64) slo &= ~(1ull << a); else shi &= ~(1ull << (a - 64));
+                    if (hash_find(B.hash[pside], B.hash_cap, tag_prev, par.inst, slo, shi) < 0) ok = false;
+                }
+            }
+            const unsigned okm = __ballot_sync(FULLMASK, ok);
+            const unsigned vm = __ballot_sync(FULLMASK, valid);
+            const int cnt = __popc(okm);
+            loc_pruned += __popc(vm & ~okm);
+            long long base = 0;
+            int over = 0;
+            if (lane == 0 && cnt) {
+                if (I.budget > 0) {
+                    // the level is checked only if the whole level fits the
+                    // budget; past that point nothing needs to be written
+                    const long long old = (long long)atomicAdd((unsigned long long *)&B.ictl[par.inst].lvl_cand,
+                                                               (unsigned long long)cnt);
+                    over = B.ictl[par.inst].cum_cand + old + cnt > I.budget;
+                } else {
+                    loc_cand += cnt;
+                }
+                if (!over) base = (long long)atomicAdd((unsigned long long *)&ctl->n_cand, (unsigned long long)cnt);
+            }
+            base = __shfl_sync(FULLMASK, base, 0);
+            over = __shfl_sync(FULLMASK, over, 0);
+            if (ok && !over) {
+                const long long idx = base + __popc(okm & ((1u << lane) - 1u));
+                if (idx < B.cand_cap) {
+                    B.cand[idx].parent = (int)pi;
+                    B.cand[idx].j = j;
+                } else {
+                    atomicOr(&ctl->overflow, OV_CAND);
+                }
+            }
+        }
+    }
+    if (cur_inst >= 0 && lane == 0) {
+        atomicAdd((unsigned long long *)&B.ictl[cur_inst].lvl_cand, (unsigned long long)loc_cand);
+        atomicAdd((unsigned long long *)&B.ictl[cur_inst].pruned, (unsigned long long)loc_pruned);
+    }
+}
+
+// ---------------------------------------------------------------------
+// helpers for K2
+// ---------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ const T *pool_of(const DevBuffers &B);
+template <> __device__ __forceinline__ const double *pool_of<double>(const DevBuffers &B) { return B.dpool; }
+template <> __device__ __forceinline__ const float *pool_of<float>(const DevBuffers &B) { return B.fpool; }
+
+template <typename T>
+__device__ __forceinline__ long long root_off(const InstDesc &I);
+template <> __device__ __forceinline__ long long root_off<double>(const InstDesc &I) { return I.o_root; }
+template <> __device__ __forceinline__ long long root_off<float>(const InstDesc &I) { return I.f_root; }
+
+template <typename TS, typename TD>
+__device__ __forceinline__ void warp_copy(TD *dst, const TS *src, int n)
+{
+    for (int e = lane_id(); e < n; e += 32) dst[e] = (TD)src[e];
+}
+
+// Append a feasible (or, exhaustive, any) candidate as a node of `side`;
+// stores its tableau when it can have children.  Returns the node index or -1.
+template <typename TT, typename TS>
+__device__ long long store_node(const DevBuffers &B, int side, int level, const InstDesc &I, int inst,
+                                uint64_t lo, uint64_t hi, bool feasible, const TS *tab, const uint8_t *ids,
+                                long long rec)
+{
+    const int lane = lane_id();
+    Ctl *ctl = B.ctl;
+    const bool need_tab = level < I.k_max;
+    long long idx = 0, toff = -1, ioff = -1;
+    if (lane == 0) {
+        // one arena per kind, side 0 filled upward from 0, side 1 downward
+        // from the top; the other side holds the parents and is fixed here
+        idx = (long long)atomicAdd((unsigned long long *)&ctl->n_node[side], 1ull);
+        if (idx >= B.node_cap) { atomicOr(&ctl->overflow, OV_NODE); idx = -1; }
+        if (need_tab && idx >= 0) {
+            const long long told = (long long)atomicAdd((unsigned long long *)&ctl->tab_used[side], (unsigned long long)I.tab_elems);
+            const long long iold = (long long)atomicAdd((unsigned long long *)&ctl->ids_used[side], (unsigned long long)I.ids_bytes);
+            toff = side == 0 ? told : B.tab_cap - told - I.tab_elems;
+            ioff = side == 0 ? iold : B.ids_cap - iold - I.ids_bytes;
+            bool bad = false;
+            if (told + I.tab_elems + ctl->tab_used[side ^ 1] > B.tab_cap) { atomicOr(&ctl->overflow, OV_TAB); bad = true; }
+            if (iold + I.ids_bytes + ctl->ids_used[side ^ 1] > B.ids_cap) { atomicOr(&ctl->overflow, OV_IDS); bad = true; }
+            if (bad) {
+                // keep the slot harmless: no tableau, never expanded or evaluated
+                Node nd;
+                nd.lo = lo; nd.hi = hi; nd.inst = inst; nd.flags = 0; nd.tab_off = -1; nd.ids_off = -1; nd.rec = -1;
+                B.node[side][idx] = nd;
+                idx = -1;
+            }
+        }
+    }
+    idx = __shfl_sync(FULLMASK, idx, 0);
+    toff = __shfl_sync(FULLMASK, toff, 0);
+    ioff = __shfl_sync(FULLMASK, ioff, 0);
+    if (idx < 0) return -1;
+    if (need_tab) {
+        TT *dst = (TT *)B.tab[side] + toff;
+        warp_copy<TS, TT>(dst, tab, (I.M1 + 1) * I.ld1);
+        uint8_t *di = B.ids[side] + ioff;
+        for (int e = lane; e < I.M1 + I.nv; e += 32) di[e] = ids[e];
+    }
+    if (lane == 0) {
+        Node nd;
+        nd.lo = lo; nd.hi = hi; nd.inst = inst; nd.flags = NODE_VALID | (feasible ? NODE_FEASIBLE : 0);
+        nd.tab_off = toff; nd.ids_off = ioff; nd.rec = rec;
+        B.node[side][idx] = nd;
+        if (feasible && !B.exhaustive) {
+            if (!hash_insert(B.hash[side], B.hash_cap, (ctl->epoch << 8) | level, inst, lo, hi, (int)idx))
+                atomicOr(&ctl->overflow, OV_HASH);
+        }
+    }
+    return idx;
+}
+
+// ---------------------------------------------------------------------
+// K2: LP1 feasibility, warm-started from the parent
+// ---------------------------------------------------------------------
+// T = double: the plain FP64 path (verdict z <= tol_feas).
+// T = float : the FP32 pass of the mixed path; a verdict is final only when
+//             certified (see below), otherwise the candidate is queued for
+//             the FP64 re-solve.
+template <typename T>
+__global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, SlotDims sd, int level)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const size_t slot = lp1_slot_bytes<T>(sd.maxM1, sd.maxLD1, sd.maxNv);
+    unsigned char *base = smem + wib * slot;
+    T *tab = (T *)base;
+    uint8_t *ids = base + align16((size_t)(sd.maxM1 + 1) * sd.maxLD1 * sizeof(T));
+    const int side = level & 1, pside = side ^ 1;
+    Ctl *ctl = B.ctl;
+    const long long ncand = ctl->n_cand;
+    const bool mixed = sizeof(T) == 4;
+    const T tpiv = mixed ? (T)tol.tol_piv32 : (T)tol.tol_piv;
+    const T tdj = mixed ? (T)tol.tol_dj32 : (T)tol.tol_dj;
+    LocalInstCounters lc;
+    lc.reset(-1);
+    for (;;) {
+        long long w;
+        if (lane == 0) w = (long long)atomicAdd(&ctl->ctr[0], 1ull);
+        w = __shfl_sync(FULLMASK, w, 0);
+        if (w >= ncand || w >= B.cand_cap) break;
+        const Cand c = B.cand[w];
+        const Node par = B.node[pside][c.parent];
+        const int inst = par.inst;
+        const InstDesc &I = B.inst[inst];
+        const InstCtl &ic = B.ictl[inst];
+        const long long rec = (B.rec && ctl->rec_base + w < B.rec_cap) ? ctl->rec_base + w : -1;
+        if (B.rec && rec < 0 && lane == 0) atomicOr(&ctl->overflow, OV_REC);
+        if (ic.stopped || (I.budget > 0 && ic.cum_cand + ic.lvl_cand > I.budget)) {
+            if (rec >= 0 && lane == 0) B.rec[rec].level = -1;
+            continue;
+        }
+        if (inst != lc.inst) {
+            if (lc.inst >= 0 && lane == 0) {
+                atomicAdd((unsigned long long *)&B.ictl[lc.inst].feasible, (unsigned long long)lc.a);
+                atomicAdd((unsigned long long *)&B.ictl[lc.inst].lp1_piv, (unsigned long long)lc.b);
+            }
+            lc.reset(inst);
+        }
+        const int M1 = I.M1, nv = I.nv, ld = I.ld1;
+        // stage the parent tableau and basis
+        warp_copy<T, T>(tab, (const T *)B.tab[pside] + par.tab_off, (M1 + 1) * ld);
+        const uint8_t *sid = B.ids[pside] + par.ids_off;
+        for (int e = lane; e < M1 + nv; e += 32) ids[e] = sid[e];
+        __syncwarp();
+        uint8_t *bid = ids, *nid = ids + M1;
+        T *obj = tab + (size_t)M1 * ld;
+        // objective += w_j
+        const int wid = nv + c.j;
+        int rho = -1;
+        for (int i = lane; i < M1; i += 32) if (bid[i] == wid) rho = i;
+        rho = __reduce_max_sync(FULLMASK, rho);
+        if (rho >= 0) {
+            const T *row = tab + (size_t)rho * ld;
+            for (int cc = lane; cc <= nv; cc += 32) obj[cc] = xadd(obj[cc], row[cc]);
+        } else {
+            for (int cc = lane; cc < nv; cc += 32) if (nid[cc] == wid) obj[cc] = obj[cc] - T(1);
+        }
+        __syncwarp();
+        Lp<T> L{tab, ld, M1, nv, nv, bid, nid};
+        int piv = 0;
+        const int st = warp_simplex<T>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv);
+        const T z = obj[nv];
+        uint64_t lo = par.lo, hi = par.hi;
+        if (c.j < 64) lo |= 1ull << c.j; else hi |= 1ull << (c.j - 64);
+        bool feasible = false, decided = true;
+        if (!mixed) {
+            feasible = (st == LP_OPTIMAL) && ((double)z <= tol.tol_feas);
+        } else {
+            if (st != LP_OPTIMAL) decided = false;
+            else if ((double)z > tol.margin_z) feasible = false;
+            else {
+                // certificate: every slack of S nonbasic and every basic slack
+                // clearly positive -> the basic solution is a feasible point
+                // with all rows of S tight.
+                bool s_basic = false;
+                T minb = pos_inf<T>();
+                for (int i = lane; i < M1; i += 32) {
+                    const int id = bid[i];
+                    if (id < nv) continue;
+                    const int ci = id - nv;
+                    if (ci < I.m && mask_has(lo, hi, ci)) s_basic = true;
+                    const T bb = tab[(size_t)i * ld + nv];
+                    if (bb < minb) minb = bb;
+                }
+                s_basic = __any_sync(FULLMASK, s_basic);
+#pragma unroll
+                for (int off = 16; off; off >>= 1) { const T o = __shfl_xor_sync(FULLMASK, minb, off); if (o < minb) minb = o; }
+                if (!s_basic && (double)minb > tol.margin_beta) feasible = true;
+                else decided = false;
+            }
+        }
+        lc.b += piv;
+        if (rec >= 0 && lane == 0) {
+            CandRec &R = B.rec[rec];
+            R.mask_lo = lo; R.mask_hi = hi; R.level = level; R.parent = c.parent;
+            R.lp1_status = st; R.lp1_pivots = piv; R.z = (double)z;
+            R.feasible = feasible; R.licq = 0; R.optimal = 0; R.region = 0;
+            R.lp2_status = LP_SKIPPED; R.lp2_pivots = 0; R.cheb_status = LP_SKIPPED; R.cheb_pivots = 0;
+            R.t = __longlong_as_double(0x7ff8000000000000LL); R.r = R.t;
+            R.inst = inst; R.fp64 = decided ? (mixed ? 0 : 1) : 0;
+        }
+        if (!decided) {
+            if (lane == 0) {
+                const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_lp1, 1ull);
+                if (qi < B.q_cap) B.q_lp1[qi] = (int)w; else atomicOr(&ctl->overflow, OV_QUEUE);
+            }
+            continue;
+        }
+        if (feasible) lc.a++;
+        if (feasible || B.exhaustive)
+            store_node<T, T>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec);
+    }
+    if (lc.inst >= 0 && lane == 0) {
+        atomicAdd((unsigned long long *)&B.ictl[lc.inst].feasible, (unsigned long long)lc.a);
+        atomicAdd((unsigned long long *)&B.ictl[lc.inst].lp1_piv, (unsigned long long)lc.b);
+    }
+}
+
+// ---------------------------------------------------------------------
+// K2b: FP64 LP1 re-solve (mixed precision), cold from the root tableau
+// ---------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_lp1_fp64(DevBuffers B, Tol tol, SlotDims sd, int level)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const size_t slot = lp1_slot_bytes<double>(sd.maxM1, sd.maxLD1, sd.maxNv);
+    unsigned char *base = smem + wib * slot;
+    double *tab = (double *)base;
+    uint8_t *ids = base + align16((size_t)(sd.maxM1 + 1) * sd.maxLD1 * sizeof(double));
+    const int side = level & 1, pside = side ^ 1;
+    Ctl *ctl = B.ctl;
+    const long long nq = ctl->n_q_lp1 < B.q_cap ? ctl->n_q_lp1 : B.q_cap;
+    for (;;) {
+        long long x;
+        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[2], 1ull);
+        x = __shfl_sync(FULLMASK, x, 0);
+        if (x >= nq) break;
+        const long long w = B.q_lp1[x];
+        const Cand c = B.cand[w];
+        const Node par = B.node[pside][c.parent];
+        const int inst = par.inst;
+        const InstDesc &I = B.inst[inst];
+        const int M1 = I.M1, nv = I.nv, ld = I.ld1;
+        uint64_t lo = par.lo, hi = par.hi;
+        if (c.j < 64) lo |= 1ull << c.j; else hi |= 1ull << (c.j - 64);
+        const double *root = B.dpool + I.o_root;
+        warp_copy<double, double>(tab, root, (M1 + 1) * ld);
+        uint8_t *bid = ids, *nid = ids + M1;
+        for (int i = lane; i < M1; i += 32) bid[i] = (uint8_t)(nv + i);
+        for (int j = lane; j < nv; j += 32) nid[j] = (uint8_t)j;
+        __syncwarp();
+        double *obj = tab + (size_t)M1 * ld;
+        for (int cc = lane; cc <= nv; cc += 32) {
+            double acc = 0.0;
+            for (int i = 0; i < I.m; i++)
+                if (mask_has(lo, hi, i)) acc = __dadd_rn(acc, root[(size_t)i * ld + cc]);
+            obj[cc] = acc;
+        }
+        __syncwarp();
+        Lp<double> L{tab, ld, M1, nv, nv, bid, nid};
+        int piv = 0;
+        const int st = warp_simplex<double>(L, tol.tol_piv, tol.tol_dj, tol.max_pivots, tol.degen_switch, &piv);
+        const double z = obj[nv];
+        const bool feasible = (st == LP_OPTIMAL) && (z <= tol.tol_feas);
+        const long long rec = (B.rec && ctl->rec_base + w < B.rec_cap) ? ctl->rec_base + w : -1;
+        if (lane == 0) {
+            atomicAdd((unsigned long long *)&B.ictl[inst].fb_lp1, 1ull);
+            atomicAdd((unsigned long long *)&B.ictl[inst].lp1_piv, (unsigned long long)piv);
+            if (feasible) atomicAdd((unsigned long long *)&B.ictl[inst].feasible, 1ull);
+            if (rec >= 0) {
+                CandRec &R = B.rec[rec];
+                R.lp1_status = st; R.lp1_pivots += piv; R.z = z; R.feasible = feasible; R.fp64 |= 1;
+            }
+        }
+        if (feasible || B.exhaustive)
+            store_node<float, double>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec);
+    }
+}
+
+// ---------------------------------------------------------------------
+// K3: KKT factor, region rows, LP2 and the Chebyshev LP
+// ---------------------------------------------------------------------
+template <typename T>
+struct KktData {
+    const T *Wm, *Wh, *wc, *At, *bt;
+};
+
+template <typename T>
+__device__ __forceinline__ KktData<T> kkt_data(const DevBuffers &B, const InstDesc &I);
+template <> __device__ __forceinline__ KktData<double> kkt_data<double>(const DevBuffers &B, const InstDesc &I)
+{
+    return {B.dpool + I.o_Wm, B.dpool + I.o_Wh, B.dpool + I.o_wc, B.dpool + I.o_At, B.dpool + I.o_bt};
+}
+template <> __device__ __forceinline__ KktData<float> kkt_data<float>(const DevBuffers &B, const InstDesc &I)
+{
+    return {B.fpool + I.f_Wm, B.fpool + I.f_Wh, B.fpool + I.f_wc, B.fpool + I.f_At, B.fpool + I.f_bt};
+}
+
+struct OptResult {
+    int licq, lp2_status, lp2_piv, cheb_status, cheb_piv, optimal, region;
+    double t, r;
+    bool decided;
+};
+
+// Workspace carved from one shared-memory slot
+template <typename T>
+struct OptWs {
+    T *R, *Y, *Lam, *G, *Tb;
+    uint8_t *ids;
+    int *S;
+    __device__ OptWs(unsigned char *base, const SlotDims &sd)
+    {
+        size_t o = 0;
+        R = (T *)(base + o); o += align16((size_t)sd.maxK * sd.maxK * sizeof(T));
+        Y = (T *)(base + o); o += align16((size_t)sd.maxK * sd.maxP1 * sizeof(T));
+        Lam = (T *)(base + o); o += align16((size_t)sd.maxK * sd.maxP1 * sizeof(T));
+        G = (T *)(base + o); o += align16((size_t)sd.maxR2 * sd.maxP1 * sizeof(T));
+        Tb = (T *)(base + o); o += align16((size_t)(sd.maxR2 + 1) * sd.maxLD2 * sizeof(T));
+        ids = base + o; o += align16((size_t)sd.maxR2 + sd.maxP1);
+        S = (int *)(base + o);
+    }
+};
+
+// Cholesky of Wm[S,S] (row-oriented; each entry accumulates in ascending l),
+// then Y = R^-T [Wh_S | wc_S] and Lambda = R^-1 Y (lane per column).
+// Returns 0 on success, 1 when a pivot fails the threshold thr (relative to
+// the diagonal).  Fills ws.S with the sorted active set.
+template <typename T>
+__device__ int kkt_factor(const KktData<T> &D, const InstDesc &I, uint64_t lo, uint64_t hi, double thr,
+                          OptWs<T> &ws, int *k_out, T *rho_out = nullptr)
+{
+    const int lane = lane_id();
+    const int m = I.m, p = I.p, P1 = p + 1;
+    const int k = mask_pop(lo, hi);
+    *k_out = k;
+    for (int i = lane; i < m; i += 32)
+        if (mask_has(lo, hi, i)) ws.S[mask_rank(lo, hi, i)] = i;
+    __syncwarp();
+    const int *S = ws.S;
+    T *R = ws.R;
+    T rho = T(1);   // smallest pivot / diagonal ratio (lane 0)
+    for (int a = 0; a < k; a++) {
+        int fail = 0;
+        if (lane == 0) {
+            const T d0 = D.Wm[(size_t)S[a] * m + S[a]];
+            T acc = d0;
+            for (int l = 0; l < a; l++) acc = xfma(-R[l * k + a], R[l * k + a], acc);
+            if (!(acc > (T)thr * d0)) fail = 1;
+            else R[a * k + a] = xsqrt(acc);
+            if (rho_out && !fail) { const T rr = acc / d0; if (rr < rho) rho = rr; }
+        }
+        fail = __shfl_sync(FULLMASK, fail, 0);
+        if (fail) return 1;
+        __syncwarp();
+        for (int b = a + 1 + lane; b < k; b += 32) {
+            T acc = D.Wm[(size_t)S[a] * m + S[b]];
+            for (int l = 0; l < a; l++) acc = xfma(-R[l * k + a], R[l * k + b], acc);
+            R[a * k + b] = xdiv(acc, R[a * k + a]);
+        }
+        __syncwarp();
+    }
+    T *Y = ws.Y, *Lam = ws.Lam;
+    for (int cc = lane; cc < P1; cc += 32) {
+        for (int a = 0; a < k; a++) {
+            T acc = (cc < p) ? D.Wh[(size_t)S[a] * p + cc] : D.wc[S[a]];
+            for (int l = 0; l < a; l++) acc = xfma(-R[l * k + a], Y[l * P1 + cc], acc);
+            Y[a * P1 + cc] = xdiv(acc, R[a * k + a]);
+        }
+        for (int a = k - 1; a >= 0; a--) {
+            T acc = Y[a * P1 + cc];
+            for (int l = a + 1; l < k; l++) acc = xfma(-R[a * k + l], Lam[l * P1 + cc], acc);
+            Lam[a * P1 + cc] = xdiv(acc, R[a * k + a]);
+        }
+    }
+    __syncwarp();
+    if (rho_out) *rho_out = __shfl_sync(FULLMASK, rho, 0);
+    return 0;
+}
+
+// Region rows in the reference order (utils.py:39-57): lambda rows (S
+// order), inactive rows (ascending), parameter box rows.  G is R2 x (p+1),
+// each row [g | h] meaning g theta <= h.
+// track = true also returns the largest absolute row sum
+// |h| + sum_c (|Wh_ic| + sum_l |Wm_i,S_l| |Lambda_l,c|), the scale of the
+// rounding error of the FP32 rows (warp-uniform result).
+template <typename T, bool track = false>
+__device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, uint64_t hi, int k, OptWs<T> &ws)
+{
+    T amax = T(0);
+    const int lane = lane_id();
+    const int m = I.m, p = I.p, ncp = I.ncp, P1 = p + 1;
+    const int *S = ws.S;
+    const T *Lam = ws.Lam;
+    T *G = ws.G;
+    for (int a = lane; a < k; a += 32) {
+        T rs = T(0);
+        for (int cc = 0; cc < p; cc++) { G[a * P1 + cc] = Lam[a * P1 + cc]; if (track) rs += xabs(Lam[a * P1 + cc]); }
+        G[a * P1 + p] = -Lam[a * P1 + p];
+        if (track) { rs += xabs(Lam[a * P1 + p]); if (rs > amax) amax = rs; }
+    }
+    for (int i = lane; i < m; i += 32) {
+        if (mask_has(lo, hi, i)) continue;
+        const int pos = k + i - mask_rank(lo, hi, i);
+        const T *wmi = D.Wm + (size_t)i * m;
+        T rs = T(0);
+        for (int cc = 0; cc < p; cc++) {
+            T acc = -D.Wh[(size_t)i * p + cc];
+            T ab = xabs(acc);
+            for (int l = 0; l < k; l++) {
+                acc = xfma(wmi[S[l]], Lam[l * P1 + cc], acc);
+                if (track) ab += xabs(wmi[S[l]] * Lam[l * P1 + cc]);
+            }
+            G[pos * P1 + cc] = acc;
+            rs += ab;
+        }
+        T acc = D.wc[i];
+        T ab = xabs(acc);
+        for (int l = 0; l < k; l++) {
+            acc = xfma(-wmi[S[l]], Lam[l * P1 + p], acc);
+            if (track) ab += xabs(wmi[S[l]] * Lam[l * P1 + p]);
+        }
+        G[pos * P1 + p] = acc;
+        if (track) { rs += ab; if (rs > amax) amax = rs; }
+    }
+    for (int ii = lane; ii < ncp; ii += 32) {
+        for (int cc = 0; cc < p; cc++) G[(m + ii) * P1 + cc] = D.At[ii * p + cc];
+        G[(m + ii) * P1 + p] = D.bt[ii];
+    }
+    if (track) {
+#pragma unroll
+        for (int off = 16; off; off >>= 1) { const T o = __shfl_xor_sync(FULLMASK, amax, off); if (o > amax) amax = o; }
+    }
+    __syncwarp();
+    return amax;
+}
+
+// screen = true (T = float): the FP32 screening pass of the mixed path; only
+// a clear "not optimal" is final, everything else returns decided = false.
+template <typename T, bool screen>
+__device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const InstDesc &I, uint64_t lo, uint64_t hi,
+                                     OptWs<T> &ws)
+{
+    const int lane = lane_id();
+    const int m = I.m, p = I.p, ncp = I.ncp, P1 = p + 1, R2 = m + ncp, ld2 = I.ld2;
+    const KktData<T> D = kkt_data<T>(B, I);
+    OptResult res;
+    res.licq = 1; res.lp2_status = LP_SKIPPED; res.lp2_piv = 0; res.cheb_status = LP_SKIPPED; res.cheb_piv = 0;
+    res.optimal = 0; res.region = 0;
+    res.t = __longlong_as_double(0x7ff8000000000000LL); res.r = res.t;
+    res.decided = true;
+    const T tpiv = screen ? (T)tol.tol_piv32 : (T)tol.tol_piv;
+    const T tdj = screen ? (T)tol.tol_dj32 : (T)tol.tol_dj;
+    int k = 0;
+    T rho = T(1);
+    if (kkt_factor<T>(D, I, lo, hi, screen ? tol.margin_licq : tol.tol_licq, ws, &k, screen ? &rho : nullptr)) {
+        if (screen) { res.decided = false; return res; }
+        res.licq = 0; res.lp2_status = LP_LICQ_FAIL;
+        return res;
+    }
+    const T amax = region_rows<T, screen>(D, I, lo, hi, k, ws);
+    const T *G = ws.G;
+    // LP2: max t  s.t.  g theta + t <= h (constraint rows), At theta <= bt
+    T t0 = pos_inf<T>();
+    for (int r = lane; r < m; r += 32) { const T h = G[r * P1 + p]; if (h < t0) t0 = h; }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) { const T o = __shfl_xor_sync(FULLMASK, t0, off); if (o < t0) t0 = o; }
+    T *Tb = ws.Tb;
+    uint8_t *bid = ws.ids, *nid = ws.ids + R2;
+    for (int r = lane; r < R2; r += 32) {
+        T *tr = Tb + (size_t)r * ld2;
+        const T *g = G + (size_t)r * P1;
+        for (int cc = 0; cc < p; cc++) tr[cc] = g[cc];
+        const T cf = (r < m) ? T(1) : T(0);
+        tr[p] = cf;
+        T beta = xfma(-cf, t0, g[p]);
+        if (!(beta > T(0))) beta = T(0);
+        tr[p + 1] = beta;
+        bid[r] = (uint8_t)(P1 + r);
+    }
+    for (int cc = lane; cc <= P1; cc += 32) {
+        T *ob = Tb + (size_t)R2 * ld2;
+        ob[cc] = (cc == p) ? T(1) : (cc == P1 ? -t0 : T(0));
+        if (cc < P1) nid[cc] = (uint8_t)cc;
+    }
+    __syncwarp();
+    {
+        Lp<T> L{Tb, ld2, R2, P1, P1, bid, nid};
+        int piv = 0;
+        res.lp2_status = warp_simplex<T>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv);
+        res.lp2_piv = piv;
+    }
+    if (res.lp2_status == LP_OPTIMAL) {
+        const T t = -Tb[(size_t)R2 * ld2 + P1];
+        res.t = (double)t;
+        if (screen) {
+            // error scale of the FP32 margin: row magnitude / pivot ratio,
+            // times the reach of theta inside the box
+            T bmax = T(0);
+            for (int ii = lane; ii < ncp; ii += 32) { const T v = xabs(D.bt[ii]); if (v > bmax) bmax = v; }
+#pragma unroll
+            for (int off = 16; off; off >>= 1) { const T o = __shfl_xor_sync(FULLMASK, bmax, off); if (o > bmax) bmax = o; }
+            const double scale = (double)amax / (double)rho * (1.0 + (double)p * (double)bmax);
+            if (res.t < -tol.margin_t * scale) return res;      // clearly not optimal
+            res.decided = false;
+            return res;
+        }
+        res.optimal = res.t > tol.tol_opt;
+    } else {
+        if (screen) { res.decided = false; return res; }
+        if (res.lp2_status == LP_UNBOUNDED) res.t = pos_inf<double>();
+    }
+    if (!res.optimal) return res;
+    // Chebyshev ball: keep box rows and rows with a nonzero theta part
+    int nc = 0;
+    for (int r0 = 0; r0 < R2; r0 += 32) {
+        const int r = r0 + lane;
+        bool keep = false;
+        if (r < R2) {
+            if (r >= m) keep = true;
+            else {
+                for (int cc = 0; cc < p; cc++) if (G[r * P1 + cc] != T(0)) { keep = true; break; }
+            }
+        }
+        const unsigned km = __ballot_sync(FULLMASK, keep);
+        if (keep) {
+            const int np = nc + __popc(km & ((1u << lane) - 1u));
+            const T *g = G + (size_t)r * P1;
+            T acc = T(0);
+            for (int cc = 0; cc < p; cc++) acc = xfma(g[cc], g[cc], acc);
+            const T inv = xdiv(T(1), xsqrt(acc));
+            T *tr = Tb + (size_t)np * ld2;
+            T nn = T(0);
+            for (int cc = 0; cc < p; cc++) { const T v = xmul(g[cc], inv); tr[cc] = v; nn = xfma(v, v, nn); }
+            tr[p] = xsqrt(nn);
+            tr[p + 1] = xmul(g[p], inv);
+            bid[np] = (uint8_t)(P1 + np);
+        }
+        nc += __popc(km);
+    }
+    __syncwarp();
+    T r0v = pos_inf<T>();
+    for (int r = lane; r < nc; r += 32) {
+        const T v = xdiv(Tb[(size_t)r * ld2 + p + 1], Tb[(size_t)r * ld2 + p]);
+        if (v < r0v) r0v = v;
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) { const T o = __shfl_xor_sync(FULLMASK, r0v, off); if (o < r0v) r0v = o; }
+    for (int r = lane; r < nc; r += 32) {
+        T *tr = Tb + (size_t)r * ld2;
+        T beta = xfma(-tr[p], r0v, tr[p + 1]);
+        if (!(beta > T(0))) beta = T(0);
+        tr[p + 1] = beta;
+    }
+    for (int cc = lane; cc <= P1; cc += 32) {
+        T *ob = Tb + (size_t)nc * ld2;
+        ob[cc] = (cc == p) ? T(1) : (cc == P1 ? -r0v : T(0));
+        if (cc < P1) nid[cc] = (uint8_t)cc;
+    }
+    __syncwarp();
+    {
+        Lp<T> L{Tb, ld2, nc, P1, P1, bid, nid};
+        int piv = 0;
+        res.cheb_status = warp_simplex<T>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv);
+        res.cheb_piv = piv;
+    }
+    if (res.cheb_status == LP_OPTIMAL) {
+        res.r = (double)(-Tb[(size_t)nc * ld2 + P1]);
+        res.region = res.r >= tol.r_min;
+    } else if (res.cheb_status == LP_UNBOUNDED) {
+        res.r = pos_inf<double>();
+    }
+    return res;
+}
+
+__device__ void write_opt(const DevBuffers &B, const Node &nd, int level, const OptResult &res, bool fp64)
+{
+    Ctl *ctl = B.ctl;
+    if (res.optimal) {
+        const long long oi = (long long)atomicAdd((unsigned long long *)&ctl->n_opt, 1ull);
+        if (oi < B.opt_cap) {
+            OptRec o;
+            o.lo = nd.lo; o.hi = nd.hi; o.inst = nd.inst; o.level = level; o.t = res.t; o.r = res.r;
+            o.region = res.region; o.fp64 = fp64; o.rec = nd.rec;
+            B.opt[oi] = o;
+        } else {
+            atomicOr(&ctl->overflow, OV_OPT);
+        }
+    }
+    if (nd.rec >= 0 && B.rec) {
+        CandRec &R = B.rec[nd.rec];
+        R.licq = res.licq; R.optimal = res.optimal; R.region = res.region;
+        R.lp2_status = res.lp2_status; R.lp2_pivots = res.lp2_piv;
+        R.cheb_status = res.cheb_status; R.cheb_pivots = res.cheb_piv;
+        R.t = res.t; R.r = res.r;
+        if (fp64) R.fp64 |= 2;
+    }
+}
+
+// mode: T = double -> final FP64 verdicts; T = float -> FP32 screen that
+// queues undecided nodes for k_optimality_fp64.
+template <typename T>
+__global__ void __launch_bounds__(128) k_optimality(DevBuffers B, Tol tol, SlotDims sd, int level)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const size_t slot = opt_slot_bytes<T>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2);
+    OptWs<T> ws(smem + wib * slot, sd);
+    const int side = level & 1;
+    Ctl *ctl = B.ctl;
+    const long long nn = ctl->n_node[side] < B.node_cap ? ctl->n_node[side] : B.node_cap;
+    constexpr bool screen = sizeof(T) == 4;
+    LocalInstCounters lc;
+    lc.reset(-1);
+    for (;;) {
+        long long x;
+        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[3], 1ull);
+        x = __shfl_sync(FULLMASK, x, 0);
+        if (x >= nn) break;
+        const Node nd = B.node[side][x];
+        if ((nd.flags & (NODE_VALID | NODE_FEASIBLE)) != (NODE_VALID | NODE_FEASIBLE)) continue;
+        const InstDesc &I = B.inst[nd.inst];
+        if (level < I.k_min) continue;
+        if (nd.inst != lc.inst) {
+            if (lc.inst >= 0 && lane == 0) {
+                atomicAdd((unsigned long long *)&B.ictl[lc.inst].optimal, (unsigned long long)lc.a);
+                atomicAdd((unsigned long long *)&B.ictl[lc.inst].region, (unsigned long long)lc.b);
+                atomicAdd((unsigned long long *)&B.ictl[lc.inst].lp2_piv, (unsigned long long)lc.c);
+                atomicAdd((unsigned long long *)&B.ictl[lc.inst].cheb_piv, (unsigned long long)lc.d);
+            }
+            lc.reset(nd.inst);
+        }
+        const OptResult res = eval_optimality<T, screen>(B, tol, I, nd.lo, nd.hi, ws);
+        lc.c += res.lp2_piv;
+        lc.d += res.cheb_piv;
+        if (!res.decided) {
+            if (lane == 0) {
+                const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_opt, 1ull);
+                if (qi < B.q_cap) B.q_opt[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
+            }
+            continue;
+        }
+        lc.a += res.optimal;
+        lc.b += res.region;
+        if (lane == 0) write_opt(B, nd, level, res, !screen);
+        __syncwarp();
+    }
+    if (lc.inst >= 0 && lane == 0) {
+        atomicAdd((unsigned long long *)&B.ictl[lc.inst].optimal, (unsigned long long)lc.a);
+        atomicAdd((unsigned long long *)&B.ictl[lc.inst].region, (unsigned long long)lc.b);
+        atomicAdd((unsigned long long *)&B.ictl[lc.inst].lp2_piv, (unsigned long long)lc.c);
+        atomicAdd((unsigned long long *)&B.ictl[lc.inst].cheb_piv, (unsigned long long)lc.d);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_optimality_fp64(DevBuffers B, Tol tol, SlotDims sd, int level)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const size_t slot = opt_slot_bytes<double>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2);
+    OptWs<double> ws(smem + wib * slot, sd);
+    const int side = level & 1;
+    Ctl *ctl = B.ctl;
+    const long long nq = ctl->n_q_opt < B.q_cap ? ctl->n_q_opt : B.q_cap;
+    for (;;) {
+        long long x;
+        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[4], 1ull);
+        x = __shfl_sync(FULLMASK, x, 0);
+        if (x >= nq) break;
+        const Node nd = B.node[side][B.q_opt[x]];
+        const InstDesc &I = B.inst[nd.inst];
+        const OptResult res = eval_optimality<double, false>(B, tol, I, nd.lo, nd.hi, ws);
+        if (lane == 0) {
+            InstCtl *ic = &B.ictl[nd.inst];
+            atomicAdd((unsigned long long *)&ic->fb_opt, 1ull);
+            atomicAdd((unsigned long long *)&ic->lp2_piv, (unsigned long long)res.lp2_piv);
+            atomicAdd((unsigned long long *)&ic->cheb_piv, (unsigned long long)res.cheb_piv);
+            if (res.optimal) atomicAdd((unsigned long long *)&ic->optimal, 1ull);
+            if (res.region) atomicAdd((unsigned long long *)&ic->region, 1ull);
+            write_opt(B, nd, level, res, true);
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------
+// level 0, finalisation and reset
+// ---------------------------------------------------------------------
+// One warp per instance: the empty set with the root LP1 tableau.
+template <typename T>
+__global__ void k_level0(DevBuffers B)
+{
+    const int lane = lane_id();
+    const int inst = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (inst >= B.n_inst) return;
+    const InstDesc &I = B.inst[inst];
+    Ctl *ctl = B.ctl;
+    long long toff = 0, ioff = 0;
+    for (int i = 0; i < inst; i++) { toff += B.inst[i].tab_elems; ioff += B.inst[i].ids_bytes; }
+    T *dst = (T *)B.tab[0] + toff;
+    const T *src = pool_of<T>(B) + root_off<T>(I);
+    for (int e = lane; e < (I.M1 + 1) * I.ld1; e += 32) dst[e] = src[e];
+    uint8_t *ids = B.ids[0] + ioff;
+    for (int i = lane; i < I.M1; i += 32) ids[i] = (uint8_t)(I.nv + i);
+    for (int j = lane; j < I.nv; j += 32) ids[I.M1 + j] = (uint8_t)j;
+    if (lane == 0) {
+        Node nd;
+        nd.lo = 0; nd.hi = 0; nd.inst = inst; nd.flags = NODE_VALID | NODE_FEASIBLE; nd.tab_off = toff; nd.ids_off = ioff;
+        nd.rec = (B.rec && inst < B.rec_cap) ? inst : -1;
+        B.node[0][inst] = nd;
+        if (!B.exhaustive) hash_insert(B.hash[0], B.hash_cap, ctl->epoch << 8, inst, 0, 0, inst);
+        if (nd.rec >= 0) {
+            CandRec &R = B.rec[nd.rec];
+            R.mask_lo = 0; R.mask_hi = 0; R.level = 0; R.parent = -1;
+            R.lp1_status = LP_OPTIMAL; R.lp1_pivots = 0; R.z = 0.0;
+            R.feasible = 1; R.licq = 0; R.optimal = 0; R.region = 0;
+            R.lp2_status = LP_SKIPPED; R.lp2_pivots = 0; R.cheb_status = LP_SKIPPED; R.cheb_pivots = 0;
+            R.t = __longlong_as_double(0x7ff8000000000000LL); R.r = R.t;
+            R.inst = inst; R.fp64 = 1;
+        }
+        InstCtl *ic = &B.ictl[inst];
+        ic->lvl_cand = 1;
+        ic->feasible = 1;
+        if (inst == 0) {
+            long long tt = 0, it = 0;
+            for (int i = 0; i < B.n_inst; i++) { tt += B.inst[i].tab_elems; it += B.inst[i].ids_bytes; }
+            ctl->n_node[0] = B.n_inst;
+            ctl->n_cand = B.n_inst;
+            ctl->tab_used[0] = tt;
+            ctl->ids_used[0] = it;
+        }
+    }
+}
+
+// Reset all counters (first node of every run).
+__global__ void k_reset(DevBuffers B)
+{
+    const int t = threadIdx.x;
+    for (int i = t; i < B.n_inst; i += blockDim.x) {
+        InstCtl z = {};
+        B.ictl[i] = z;
+    }
+    if (t == 0) {
+        const int e = B.ctl->epoch;
+        Ctl z = {};
+        *B.ctl = z;
+        B.ctl->epoch = e + 1;
+    }
+}
+
+// After each level: budget bookkeeping and counter resets.
+__global__ void k_finalize(DevBuffers B, int level)
+{
+    const int t = threadIdx.x;
+    Ctl *ctl = B.ctl;
+    for (int i = t; i < B.n_inst; i += blockDim.x) {
+        InstCtl *ic = &B.ictl[i];
+        const InstDesc &I = B.inst[i];
+        if (!ic->stopped) {
+            if (I.budget > 0 && ic->cum_cand + ic->lvl_cand > I.budget) {
+                ic->stopped = 1;
+                ic->truncated = 1;
+            } else {
+                ic->cum_cand += ic->lvl_cand;
+                if (ic->lvl_cand > 0) ic->last_level = level;
+                if (level >= I.k_max || ic->lvl_cand == 0) ic->stopped = 1;
+            }
+        }
+        ic->lvl_cand = 0;
+    }
+    __syncthreads();
+    if (t == 0) {
+        const int pside = (level & 1) ^ 1;
+        if (B.rec) ctl->rec_base += ctl->n_cand;
+        ctl->n_cand = 0;
+        if (level > 0) {
+            ctl->n_node[pside] = 0;
+            ctl->tab_used[pside] = 0;
+            ctl->ids_used[pside] = 0;
+        }
+        for (int c = 0; c < 8; c++) ctl->ctr[c] = 0;
+        ctl->n_q_lp1 = 0;
+        ctl->n_q_opt = 0;
+        ctl->level = level;
+    }
+}
+
+// ---------------------------------------------------------------------
+// K4: region laws of given active sets (FP64)
+// ---------------------------------------------------------------------
+// Output per set (stride doubles): lagrange rows [lagrange_A | lagrange_b]
+// (k x (p+1)), then parameter rows [parameter_A | parameter_b] (n x (p+1)),
+// then the normalised region rows [CR_As | CR_bs] (n_cr x (p+1)).
+// sizes = {k, n, p, n_cr}; k = -1 when the KKT factor fails (LICQ).
+__global__ void __launch_bounds__(128) k_region_laws(DevBuffers B, Tol tol, SlotDims sd, const uint64_t *masks,
+                                                     long long n_sets, double *laws, int *sizes, long long stride)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const size_t slot = opt_slot_bytes<double>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2);
+    OptWs<double> ws(smem + wib * slot, sd);
+    const InstDesc &I = B.inst[0];
+    const KktData<double> D = kkt_data<double>(B, I);
+    const int m = I.m, n = I.n, p = I.p, ncp = I.ncp, P1 = p + 1, R2 = m + ncp;
+    const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
+    const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long x = gw; x < n_sets; x += nw) {
+        const uint64_t lo = masks[2 * x], hi = masks[2 * x + 1];
+        double *out = laws + x * stride;
+        int *sz = sizes + 4 * x;
+        int k = 0;
+        if (kkt_factor<double>(D, I, lo, hi, tol.tol_licq, ws, &k)) {
+            if (lane == 0) { sz[0] = -1; sz[1] = n; sz[2] = p; sz[3] = 0; }
+            continue;
+        }
+        region_rows<double>(D, I, lo, hi, k, ws);
+        const double *Lam = ws.Lam;
+        const double *QiAT = B.dpool + I.o_QiAT, *QiH = B.dpool + I.o_QiH, *Qic = B.dpool + I.o_Qic;
+        for (int a = lane; a < k; a += 32)
+            for (int cc = 0; cc < P1; cc++) out[a * P1 + cc] = -Lam[a * P1 + cc];
+        double *par = out + (long long)m * P1;
+        for (int r = lane; r < n; r += 32) {
+            for (int cc = 0; cc < P1; cc++) {
+                double acc = (cc < p) ? -QiH[r * p + cc] : -Qic[r];
+                for (int l = 0; l < k; l++) acc = xfma(QiAT[(size_t)r * m + ws.S[l]], Lam[l * P1 + cc], acc);
+                par[r * P1 + cc] = acc;
+            }
+        }
+        double *cr = par + (long long)n * P1;
+        const double *G = ws.G;
+        int nc = 0;
+        for (int r0 = 0; r0 < R2; r0 += 32) {
+            const int r = r0 + lane;
+            bool keep = false;
+            if (r < R2) {
+                if (r >= m) keep = true;
+                else for (int cc = 0; cc < p; cc++) if (G[r * P1 + cc] != 0.0) { keep = true; break; }
+            }
+            const unsigned km = __ballot_sync(FULLMASK, keep);
+            if (keep) {
+                const int np = nc + __popc(km & ((1u << lane) - 1u));
+                const double *g = G + (size_t)r * P1;
+                double acc = 0.0;
+                for (int cc = 0; cc < p; cc++) acc = xfma(g[cc], g[cc], acc);
+                const double inv = xdiv(1.0, xsqrt(acc));
+                for (int cc = 0; cc < p; cc++) cr[np * P1 + cc] = xmul(g[cc], inv);
+                cr[np * P1 + p] = xmul(g[p], inv);
+            }
+            nc += __popc(km);
+        }
+        if (lane == 0) { sz[0] = k; sz[1] = n; sz[2] = p; sz[3] = nc; }
+        __syncwarp();
+    }
+}
+
+size_t laws_smem_per_warp(const SlotDims &sd) { return opt_slot_bytes<double>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2); }
+
+cudaError_t launch_region_laws(const DevBuffers &B, const Tol &tol, const SlotDims &sd, const uint64_t *masks,
+                               long long n_sets, double *laws, int *sizes, long long stride, int grid, size_t smem,
+                               cudaStream_t s)
+{
+    k_region_laws<<<grid, 128, smem, s>>>(B, tol, sd, masks, n_sets, laws, sizes, stride);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------
+// explicit instantiations / host-visible launch wrappers
+// ---------------------------------------------------------------------
+size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd)
+{
+    return prec_bytes == 8 ? lp1_slot_bytes<double>(sd.maxM1, sd.maxLD1, sd.maxNv)
+                           : lp1_slot_bytes<float>(sd.maxM1, sd.maxLD1, sd.maxNv);
+}
+
+size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd)
+{
+    return prec_bytes == 8 ? opt_slot_bytes<double>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2)
+                           : opt_slot_bytes<float>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2);
+}
+
+}  // namespace mq
+
+using namespace mq;
+
+// Launch wrappers (plain C++ linkage inside the library)
+namespace mq {
+
+const void *kernel_ptr(const char *name)
+{
+    struct E { const char *n; const void *f; };
+    static const E tab[] = {
+        {"enumerate", (const void *)k_enumerate},
+        {"feas64", (const void *)k_feasibility<double>},
+        {"feas32", (const void *)k_feasibility<float>},
+        {"lp1_fp64", (const void *)k_lp1_fp64},
+        {"opt64", (const void *)k_optimality<double>},
+        {"opt32", (const void *)k_optimality<float>},
+        {"opt_fp64", (const void *)k_optimality_fp64},
+        {"level0_64", (const void *)k_level0<double>},
+        {"level0_32", (const void *)k_level0<float>},
+        {"reset", (const void *)k_reset},
+        {"finalize", (const void *)k_finalize},
+        {"laws", (const void *)k_region_laws},
+    };
+    for (const E &e : tab) {
+        const char *a = e.n, *b = name;
+        while (*a && *a == *b) { a++; b++; }
+        if (*a == 0 && *b == 0) return e.f;
+    }
+    return nullptr;
+}
+
+cudaError_t launch_enumerate(const DevBuffers &B, int level, int grid, cudaStream_t s)
+{
+    k_enumerate<<<grid, 128, 0, s>>>(B, level);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_feasibility(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int prec,
+                               int grid, size_t smem, cudaStream_t s)
+{
+    if (prec == PREC_FP64) k_feasibility<double><<<grid, 128, smem, s>>>(B, tol, sd, level);
+    else k_feasibility<float><<<grid, 128, smem, s>>>(B, tol, sd, level);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lp1_fp64(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int grid,
+                            size_t smem, cudaStream_t s)
+{
+    k_lp1_fp64<<<grid, 128, smem, s>>>(B, tol, sd, level);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_optimality(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int prec,
+                              int grid, size_t smem, cudaStream_t s)
+{
+    if (prec == PREC_FP64) k_optimality<double><<<grid, 128, smem, s>>>(B, tol, sd, level);
+    else k_optimality<float><<<grid, 128, smem, s>>>(B, tol, sd, level);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_optimality_fp64(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int grid,
+                                   size_t smem, cudaStream_t s)
+{
+    k_optimality_fp64<<<grid, 128, smem, s>>>(B, tol, sd, level);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_level0(const DevBuffers &B, int prec, cudaStream_t s)
+{
+    const int warps = 4;
+    const int grid = (B.n_inst + warps - 1) / warps;
+    if (prec == PREC_FP64) k_level0<double><<<grid, 32 * warps, 0, s>>>(B);
+    else k_level0<float><<<grid, 32 * warps, 0, s>>>(B);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reset(const DevBuffers &B, cudaStream_t s)
+{
+    k_reset<<<1, 256, 0, s>>>(B);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const DevBuffers &B, int level, cudaStream_t s)
+{
+    k_finalize<<<1, 256, 0, s>>>(B, level);
+    return cudaGetLastError();
+}
+
+}  // namespace mq

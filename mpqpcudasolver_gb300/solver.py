@@ -1,0 +1,302 @@
+"""ctypes front end of libmpqp_gb300.so (the native interface).
+
+The library must have been built in place (``build.py``); there is no CPU
+fallback: every entry point here fails loudly when the shared library is
+missing or when a CUDA call fails.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import build as _build
+
+FP64, MIXED = 0, 1
+OK, EINVAL, ENOTSPD, EORIGIN, ELAYOUT, ECUDA, ECAPACITY, ENOMEM = 0, -1, -2, -3, -4, -5, -6, -7
+
+
+class MpqpError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"mpqp error {code}: {msg}")
+        self.code = code
+
+
+class Problem(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("m", ctypes.c_int), ("p", ctypes.c_int), ("ncp", ctypes.c_int),
+                ("k_min", ctypes.c_int), ("k_max", ctypes.c_int), ("budget", ctypes.c_longlong)] + \
+        [(nm, ctypes.POINTER(ctypes.c_double)) for nm in ("Q", "c", "H", "A", "b", "F", "At", "bt")]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("exhaustive", ctypes.c_int), ("record", ctypes.c_int),
+                ("use_graph", ctypes.c_int), ("cand_cap", ctypes.c_longlong), ("node_cap", ctypes.c_longlong),
+                ("arena_bytes", ctypes.c_longlong), ("rec_cap", ctypes.c_longlong), ("opt_cap", ctypes.c_longlong),
+                ("mem_fraction", ctypes.c_double),
+                ("tol_feas", ctypes.c_double), ("tol_opt", ctypes.c_double), ("tol_licq", ctypes.c_double),
+                ("r_min", ctypes.c_double), ("tol_piv", ctypes.c_double), ("tol_dj", ctypes.c_double),
+                ("max_pivots", ctypes.c_int), ("degen_switch", ctypes.c_int),
+                ("tol_piv32", ctypes.c_double), ("tol_dj32", ctypes.c_double), ("margin_z", ctypes.c_double),
+                ("margin_beta", ctypes.c_double), ("margin_t", ctypes.c_double), ("margin_licq", ctypes.c_double)]
+
+
+class OptSet(ctypes.Structure):
+    _fields_ = [("mask_lo", ctypes.c_uint64), ("mask_hi", ctypes.c_uint64), ("inst", ctypes.c_int),
+                ("level", ctypes.c_int), ("t", ctypes.c_double), ("r", ctypes.c_double), ("region", ctypes.c_int),
+                ("fp64", ctypes.c_int), ("rec", ctypes.c_longlong)]
+
+
+class InstStats(ctypes.Structure):
+    _fields_ = [(nm, ctypes.c_longlong) for nm in ("candidates", "pruned", "feasible", "optimal", "regions",
+                                                    "lp1_pivots", "lp2_pivots", "cheb_pivots", "fallback_lp1",
+                                                    "fallback_opt")] + \
+        [("last_level", ctypes.c_int), ("truncated", ctypes.c_int)]
+
+
+class BatchResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("n_inst", ctypes.c_int), ("n_levels", ctypes.c_int),
+                ("overflow", ctypes.c_int), ("device_ms", ctypes.c_double),
+                ("inst", ctypes.POINTER(InstStats)), ("n_opt", ctypes.c_longlong), ("opt", ctypes.POINTER(OptSet)),
+                ("n_rec", ctypes.c_longlong), ("rec", ctypes.c_void_p)]
+
+
+class GPUResults(ctypes.Structure):
+    """The reference's result structure (main.py:12-22) plus appended fields."""
+    _fields_ = [('n_batches', ctypes.c_int), ('n_splits', ctypes.c_int), ('n_feasible_lps', ctypes.c_int),
+                ('n_final_lps', ctypes.c_int), ('time_feas', ctypes.c_double), ('time_opti', ctypes.c_double),
+                ('time_GPU', ctypes.c_double), ('active_sets', ctypes.POINTER(ctypes.c_int)),
+                ('status', ctypes.c_int), ('n_regions', ctypes.c_int), ('n_candidates', ctypes.c_longlong),
+                ('n_pruned', ctypes.c_longlong), ('t_star', ctypes.POINTER(ctypes.c_double)),
+                ('radius', ctypes.POINTER(ctypes.c_double)), ('is_region', ctypes.POINTER(ctypes.c_int))]
+
+
+# record layout written by the device (identical prefix to the oracle's)
+REC_DTYPE = np.dtype([("mask_lo", "<u8"), ("mask_hi", "<u8"), ("level", "<i4"), ("parent", "<i4"),
+                      ("lp1_status", "<i4"), ("lp1_pivots", "<i4"), ("z", "<f8"),
+                      ("feasible", "<i4"), ("licq", "<i4"), ("optimal", "<i4"), ("region", "<i4"),
+                      ("lp2_status", "<i4"), ("lp2_pivots", "<i4"), ("cheb_status", "<i4"),
+                      ("cheb_pivots", "<i4"), ("t", "<f8"), ("r", "<f8"), ("inst", "<i4"), ("fp64", "<i4")])
+
+EXPORTS = ("mpqp", "warm_up", "mpqp_free", "mpqp_default_options", "mpqp_solve_batch", "mpqp_batch_free",
+           "mpqp_plan_create", "mpqp_plan_run", "mpqp_plan_results", "mpqp_plan_launches", "mpqp_plan_destroy",
+           "mpqp_region_laws_stride", "mpqp_region_laws", "mpqp_version", "mpqp_last_error")
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load the in-tree shared library (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        if build_if_missing:
+            _build.build()
+        else:
+            raise RuntimeError(f"libmpqp_gb300.so not built ({path}); run mpqpcudasolver_gb300.build.build()")
+    lib = ctypes.CDLL(path)
+    P, PP = ctypes.POINTER, ctypes.POINTER(ctypes.POINTER(BatchResult))
+    lib.mpqp.argtypes = [P(ctypes.c_double), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                         ctypes.c_int, P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_int), ctypes.c_int,
+                         ctypes.c_int, P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_int), P(ctypes.c_int),
+                         ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.mpqp.restype = P(GPUResults)
+    lib.mpqp_free.argtypes = [P(GPUResults)]
+    lib.mpqp_default_options.argtypes = [P(Options)]
+    lib.mpqp_solve_batch.argtypes = [ctypes.c_int, P(Problem), P(Options), PP]
+    lib.mpqp_solve_batch.restype = ctypes.c_int
+    lib.mpqp_batch_free.argtypes = [P(BatchResult)]
+    lib.mpqp_plan_create.argtypes = [ctypes.c_int, P(Problem), P(Options), P(ctypes.c_void_p)]
+    lib.mpqp_plan_create.restype = ctypes.c_int
+    lib.mpqp_plan_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.mpqp_plan_run.restype = ctypes.c_int
+    lib.mpqp_plan_results.argtypes = [ctypes.c_void_p, PP]
+    lib.mpqp_plan_results.restype = ctypes.c_int
+    lib.mpqp_plan_launches.argtypes = [ctypes.c_void_p]
+    lib.mpqp_plan_launches.restype = ctypes.c_int
+    lib.mpqp_plan_destroy.argtypes = [ctypes.c_void_p]
+    lib.mpqp_region_laws_stride.argtypes = [P(Problem)]
+    lib.mpqp_region_laws_stride.restype = ctypes.c_longlong
+    lib.mpqp_region_laws.argtypes = [P(Problem), ctypes.c_longlong, P(ctypes.c_uint64), P(ctypes.c_double),
+                                     P(ctypes.c_int)]
+    lib.mpqp_region_laws.restype = ctypes.c_int
+    lib.mpqp_version.restype = ctypes.c_char_p
+    lib.mpqp_last_error.restype = ctypes.c_char_p
+    _lib = lib
+    return lib
+
+
+def last_error() -> str:
+    return load().mpqp_last_error().decode()
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise MpqpError(rc, last_error())
+
+
+def default_options(**over) -> Options:
+    o = Options()
+    load().mpqp_default_options(ctypes.byref(o))
+    for k, v in over.items():
+        if not hasattr(o, k):
+            raise KeyError(k)
+        setattr(o, k, v)
+    return o
+
+
+class _ProblemSet:
+    """Contiguous float64 copies kept alive for the C structures."""
+
+    def __init__(self, probs, k_min=0, k_max=None, budget=0):
+        self.keep = []
+        self.arr = (Problem * len(probs))()
+        for i, pr in enumerate(probs):
+            arrs = [np.ascontiguousarray(getattr(pr, nm), dtype=np.float64)
+                    for nm in ("Q", "c", "H", "A", "b", "F", "CRA", "CRb")]
+            self.keep.append(arrs)
+            kmax = pr.n if k_max is None else (k_max[i] if isinstance(k_max, (list, tuple)) else k_max)
+            bud = budget[i] if isinstance(budget, (list, tuple)) else budget
+            s = self.arr[i]
+            s.n, s.m, s.p, s.ncp = pr.n, pr.m, pr.p, pr.CRA.shape[0]
+            s.k_min, s.k_max, s.budget = k_min, min(kmax, pr.m), int(bud)
+            for nm, a in zip(("Q", "c", "H", "A", "b", "F", "At", "bt"), arrs):
+                setattr(s, nm, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+
+
+@dataclass
+class Result:
+    status: int
+    device_ms: float
+    n_levels: int
+    overflow: int
+    inst: np.ndarray          # structured per-instance counters
+    opt: np.ndarray           # structured optimal sets
+    rec: np.ndarray | None    # structured records (record=1)
+
+    @property
+    def candidates(self) -> int:
+        return int(self.inst["candidates"].sum())
+
+    def total(self, field: str) -> int:
+        return int(self.inst[field].sum())
+
+
+_INST_DTYPE = np.dtype([(f[0], "<i8") for f in InstStats._fields_[:10]] + [("last_level", "<i4"),
+                                                                            ("truncated", "<i4")])
+_OPT_DTYPE = np.dtype([("mask_lo", "<u8"), ("mask_hi", "<u8"), ("inst", "<i4"), ("level", "<i4"), ("t", "<f8"),
+                       ("r", "<f8"), ("region", "<i4"), ("fp64", "<i4"), ("rec", "<i8")])
+assert _INST_DTYPE.itemsize == ctypes.sizeof(InstStats)
+assert _OPT_DTYPE.itemsize == ctypes.sizeof(OptSet)
+
+
+def _convert(rp) -> Result:
+    r = rp.contents
+    ni = r.n_inst
+    inst = np.frombuffer((InstStats * ni).from_address(ctypes.addressof(r.inst.contents)), dtype=_INST_DTYPE).copy()
+    nopt = r.n_opt
+    opt = (np.frombuffer((OptSet * nopt).from_address(ctypes.addressof(r.opt.contents)), dtype=_OPT_DTYPE).copy()
+           if nopt else np.zeros(0, dtype=_OPT_DTYPE))
+    rec = None
+    if r.rec:
+        nrec = r.n_rec
+        buf = (ctypes.c_char * (nrec * REC_DTYPE.itemsize)).from_address(r.rec)
+        rec = np.frombuffer(buf, dtype=REC_DTYPE).copy()
+    return Result(r.status, r.device_ms, r.n_levels, r.overflow, inst, opt, rec)
+
+
+def solve(probs, precision: int = FP64, k_min: int = 0, k_max=None, budget=0, **opts) -> Result:
+    """Run the whole enumeration for a list of MPQP instances in one launch sequence."""
+    lib = load()
+    ps = _ProblemSet(probs, k_min, k_max, budget)
+    o = default_options(precision=precision, **opts)
+    out = ctypes.POINTER(BatchResult)()
+    rc = lib.mpqp_solve_batch(len(probs), ps.arr, ctypes.byref(o), ctypes.byref(out))
+    if not out:
+        _check(rc if rc else ECUDA)
+    res = _convert(out)
+    lib.mpqp_batch_free(out)
+    _check(rc)
+    return res
+
+
+class Plan:
+    """Device-resident problem set: upload once, run many times."""
+
+    def __init__(self, probs, precision: int = FP64, k_min: int = 0, k_max=None, budget=0, **opts):
+        self.lib = load()
+        self.ps = _ProblemSet(probs, k_min, k_max, budget)
+        self.opts = default_options(precision=precision, **opts)
+        self.h = ctypes.c_void_p()
+        _check(self.lib.mpqp_plan_create(len(probs), self.ps.arr, ctypes.byref(self.opts), ctypes.byref(self.h)))
+
+    def run(self, stream: int = 0):
+        _check(self.lib.mpqp_plan_run(self.h, ctypes.c_void_p(stream)))
+
+    def results(self) -> Result:
+        out = ctypes.POINTER(BatchResult)()
+        rc = self.lib.mpqp_plan_results(self.h, ctypes.byref(out))
+        if not out:
+            _check(rc if rc else ECUDA)
+        res = _convert(out)
+        self.lib.mpqp_batch_free(out)
+        _check(rc)
+        return res
+
+    @property
+    def launches(self) -> int:
+        return self.lib.mpqp_plan_launches(self.h)
+
+    def close(self):
+        if self.h:
+            self.lib.mpqp_plan_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def region_laws(prob, sets):
+    """FP64 laws of the given active sets (device).  Returns a list of dicts."""
+    lib = load()
+    ps = _ProblemSet([prob], 0, 0, 0)
+    masks = np.zeros((len(sets), 2), dtype=np.uint64)
+    for i, S in enumerate(sets):
+        for j in S:
+            masks[i, j // 64] |= np.uint64(1) << np.uint64(j % 64)
+    stride = lib.mpqp_region_laws_stride(ps.arr)
+    laws = np.zeros((max(len(sets), 1), stride))
+    sizes = np.zeros((max(len(sets), 1), 4), dtype=np.intc)
+    _check(lib.mpqp_region_laws(ps.arr, len(sets), masks.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                laws.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                sizes.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+    out = []
+    m, n, p = prob.m, prob.n, prob.p
+    P1 = p + 1
+    for i in range(len(sets)):
+        k, _, _, ncr = sizes[i]
+        if k < 0:
+            out.append(None)
+            continue
+        lag = laws[i, :k * P1].reshape(k, P1)
+        par = laws[i, m * P1:m * P1 + n * P1].reshape(n, P1)
+        cr = laws[i, (m + n) * P1:(m + n) * P1 + ncr * P1].reshape(ncr, P1)
+        out.append(dict(lagrange_A=lag[:, :p].copy(), lagrange_b=lag[:, p].copy(), parameter_A=par[:, :p].copy(),
+                        parameter_b=par[:, p].copy(), CR_As=cr[:, :p].copy(), CR_bs=cr[:, p].copy(),
+                        active_set=list(sets[i])))
+    return out
+
+
+def mask_to_set(lo, hi) -> list[int]:
+    lo, hi = int(lo), int(hi)
+    return [j for j in range(64) if lo >> j & 1] + [64 + j for j in range(64) if hi >> j & 1]

@@ -1,0 +1,109 @@
+/*
+ * CPU oracle for the combinatorial mpQP active-set check.
+ *
+ * TEST INFRASTRUCTURE ONLY.  The product library never links this code; only
+ * the tests, the smoke check and the CPU-baseline leg of bench.py load it, as
+ * the checker.
+ *
+ * It restates, in plain C with a fixed floating-point operation order, the
+ * algorithm the reference runs for each candidate active set S:
+ *   - LP1 feasibility: min sum_{i in S} w_i over [A -F; 0 At] u + w = [b; bt],
+ *     w >= 0, u free (reference main.py:91-98,121; batched_simplex.cu:26-36,
+ *     256-316, 901-942, 990-1258); S is feasible when z* <= tol_feas;
+ *   - superset pruning: a child is only checked when every subset obtained by
+ *     dropping one element was found feasible (batched_simplex.cu:747-766);
+ *   - LP2 optimality: max t over the KKT system of S with lambda_S >= t,
+ *     inactive slacks >= t, t >= 0 (main.py:103-128;
+ *     batched_simplex.cu:635-650, 230-240, 243-254, 1633-1676), after
+ *     eliminating x and lambda through the KKT factor;
+ *   - critical region rows, normalisation and the Chebyshev-ball LP with the
+ *     1e-8 radius test (utils.py:18-97).
+ * Parity of the verdict definitions with the reference's own LP matrices is
+ * checked independently (HiGHS on the matrices main.py builds) in the tests.
+ */
+#ifndef MPQP_ORACLE_H
+#define MPQP_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    int n, m, p, ncp;
+    const double *Q;   /* n x n, row-major, symmetric positive definite */
+    const double *c;   /* n */
+    const double *H;   /* n x p */
+    const double *A;   /* m x n */
+    const double *b;   /* m */
+    const double *F;   /* m x p */
+    const double *At;  /* ncp x p  (CRA) */
+    const double *bt;  /* ncp      (CRb) */
+} orc_problem;
+
+typedef struct {
+    double tol_feas;   /* LP1: feasible when z* <= tol_feas                  */
+    double tol_opt;    /* LP2: optimal when t* > tol_opt                     */
+    double tol_licq;   /* KKT: Cholesky pivot / diagonal must exceed this   */
+    double r_min;      /* Chebyshev: region when r* >= r_min (utils.py:86)  */
+    double tol_piv;    /* ratio test: |pivot| must exceed this               */
+    double tol_dj;     /* pricing: |reduced cost| must exceed this           */
+    int max_pivots;    /* per LP */
+    int degen_switch;  /* consecutive degenerate pivots before Bland's rule */
+} orc_tol;
+
+/* LP status codes (shared with the device code) */
+enum { ORC_OPTIMAL = 0, ORC_UNBOUNDED = 1, ORC_ITER_LIMIT = 2, ORC_SKIPPED = 3, ORC_LICQ_FAIL = 4 };
+
+typedef struct {
+    uint64_t mask_lo, mask_hi;
+    int32_t level;
+    int32_t parent;       /* index of S minus max(S) in the previous level's feasible list */
+    int32_t lp1_status, lp1_pivots;
+    double z;             /* LP1 optimum */
+    int32_t feasible, licq, optimal, region;
+    int32_t lp2_status, lp2_pivots, cheb_status, cheb_pivots;
+    double t;             /* LP2 optimum (max margin), NaN when not evaluated */
+    double r;             /* Chebyshev radius, NaN when not evaluated */
+} orc_cand;
+
+typedef struct {
+    int64_t n_cand;       /* candidates checked (LP1 verdict given) */
+    int64_t n_pruned;     /* children dropped by the subset test */
+    int64_t n_feasible, n_optimal, n_region;
+    int64_t n_lp1_pivots, n_lp2_pivots, n_cheb_pivots;
+    int32_t n_levels;
+    int32_t truncated;
+    orc_cand *cand;       /* n_cand records, level by level, lexicographic within a level */
+} orc_result;
+
+void orc_default_tol(orc_tol *tol);
+
+/* Full level-by-level enumeration for k = 0..k_max.  Optimality is evaluated
+ * for levels >= k_min; lower levels are still enumerated for pruning.
+ * budget > 0: a level is checked only when the candidates checked so far
+ * plus the whole level fit in the budget; otherwise the enumeration stops
+ * there (out->truncated = 1).  exhaustive = 1: every combination is a
+ * candidate (children of all candidates, no subset test).
+ * nthreads <= 1 runs serially.  Returns 0 on success, negative on error. */
+int orc_enumerate(const orc_problem *pr, const orc_tol *tol, int k_min, int k_max,
+                  int64_t budget, int exhaustive, int nthreads, int keep_records, orc_result *out);
+void orc_free_result(orc_result *res);
+
+/* Check one sorted active set S (|S| = k) by replaying the warm-start chain
+ * {} -> {s0} -> {s0,s1} -> ... exactly as the enumeration does.  Fills *rec.
+ * When laws is non-NULL and S is a region it receives, row-major,
+ *   lagrange_A (k x p), lagrange_b (k), parameter_A (n x p), parameter_b (n).
+ * cr_rows (optional, capacity (m+ncp) x (p+1)) receives the normalised region
+ * rows [CR_As | CR_bs] in the reference's order; *n_cr_rows their count. */
+int orc_check_set(const orc_problem *pr, const orc_tol *tol, const int *S, int k,
+                  orc_cand *rec, double *laws, double *cr_rows, int *n_cr_rows);
+
+/* Precomputed KKT data, exposed for tests: Wm (m x m), Wh (m x p), wc (m). */
+int orc_kkt_data(const orc_problem *pr, double *Wm, double *Wh, double *wc);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

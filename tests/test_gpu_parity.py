@@ -1,0 +1,111 @@
+"""GPU parity: the device kernels against the CPU oracle (through the C ABI).
+
+* FP64 kernels: every checked candidate, its LP values (z, t*, r*), pivot
+  counts and verdicts are bit-identical to the oracle's.
+* Mixed precision (FP32 pivots + FP64 certificates): the feasible, optimal
+  and region sets are identical to the FP64 path's.
+"""
+import numpy as np
+import pytest
+
+from mpqpcudasolver_gb300 import problems as P
+from mpqpcudasolver_gb300 import solver
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "config1": (lambda: P.config1(), 4, False),
+    "config1-exhaustive": (lambda: P.config1(), 4, True),
+    "config2-k3": (lambda: P.config2(), 3, False),
+    "config3main-k3": (lambda: P.config3_main(), 3, False),
+    "config4-k3": (lambda: P.config4(), 3, False),
+    "config5-k3": (lambda: P.mpc_mpqp(0), 3, False),
+}
+
+
+def _sorted(rec, key_inst=False):
+    rec = rec[rec["level"] >= 0]
+    keys = [rec["mask_lo"], rec["mask_hi"]] + ([rec["inst"]] if key_inst else [])
+    return rec[np.lexsort(keys)]
+
+
+def _same(a, b):
+    return np.array_equal(a, b) or np.array_equal(np.nan_to_num(a, nan=12345.0), np.nan_to_num(b, nan=12345.0))
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_fp64_bit_exact_vs_oracle(gpu_lib, case):
+    make, kmax, exh = CASES[case]
+    prob = P.scale_problem(make())
+    ref = O.enumerate_sets(prob, k_max=kmax, exhaustive=exh, nthreads=4)
+    res = solver.solve([prob], precision=solver.FP64, k_max=kmax, exhaustive=int(exh), record=1,
+                       rec_cap=ref.n_cand + 16, cand_cap=max(4096, ref.n_cand), arena_bytes=1 << 28)
+    assert res.status == 0 and res.overflow == 0
+    assert res.candidates == ref.n_cand
+    g = _sorted(res.rec)
+    o = _sorted(ref.cand)
+    assert len(g) == len(o) == ref.n_cand
+    assert np.array_equal(g["mask_lo"], o["mask_lo"]) and np.array_equal(g["mask_hi"], o["mask_hi"])
+    for f in ("level", "lp1_status", "lp1_pivots", "feasible", "optimal", "region", "lp2_pivots", "cheb_pivots"):
+        assert np.array_equal(g[f], o[f]), f
+    for f in ("z", "t", "r"):
+        assert _same(g[f], o[f]), f
+    fe = o["feasible"] == 1
+    assert np.array_equal(g["licq"][fe], o["licq"][fe])
+    assert res.total("feasible") == ref.n_feasible
+    assert res.total("optimal") == ref.n_optimal == len(res.opt)
+    assert res.total("regions") == ref.n_region
+    assert res.total("pruned") == ref.n_pruned
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_mixed_verdicts_equal_fp64(gpu_lib, case):
+    make, kmax, exh = CASES[case]
+    prob = P.scale_problem(make())
+    kw = dict(k_max=kmax, exhaustive=int(exh), record=1, rec_cap=4_000_000, cand_cap=1 << 20, arena_bytes=1 << 28)
+    r64 = solver.solve([prob], precision=solver.FP64, **kw)
+    r32 = solver.solve([prob], precision=solver.MIXED, **kw)
+    assert r64.status == 0 and r32.status == 0
+    a, b = _sorted(r64.rec), _sorted(r32.rec)
+    assert np.array_equal(a["mask_lo"], b["mask_lo"]) and np.array_equal(a["mask_hi"], b["mask_hi"])
+    for f in ("feasible", "optimal", "region"):
+        bad = np.nonzero(a[f] != b[f])[0]
+        assert len(bad) == 0, (f, len(bad), [(int(a["level"][i]), float(a["t"][i]), float(b["t"][i]),
+                                               int(b["fp64"][i])) for i in bad[:10]])
+    assert r64.total("regions") == r32.total("regions")
+    print(case, "fallbacks lp1", r32.total("fallback_lp1"), "opt", r32.total("fallback_opt"), "of",
+          r32.candidates, "candidates /", r32.total("feasible"), "feasible")
+    # the FP64-decided values of optimal sets agree exactly
+    opt = a["optimal"] == 1
+    assert _same(a["t"][opt], b["t"][opt]) and _same(a["r"][opt], b["r"][opt])
+
+
+def test_batch_of_instances_matches_per_instance_oracle(gpu_lib):
+    probs = [P.scale_problem(p) for p in P.config3(n_extra=6)]
+    kmax = 2
+    res = solver.solve(probs, precision=solver.FP64, k_max=kmax, record=1, rec_cap=1 << 20, cand_cap=1 << 18,
+                       arena_bytes=1 << 28)
+    assert res.status == 0
+    for i, pr in enumerate(probs):
+        ref = O.enumerate_sets(pr, k_max=kmax)
+        g = _sorted(res.rec[res.rec["inst"] == i])
+        o = _sorted(ref.cand)
+        assert len(g) == len(o)
+        for f in ("mask_lo", "mask_hi", "feasible", "optimal", "region"):
+            assert np.array_equal(g[f], o[f]), (i, f)
+        assert _same(g["t"], o["t"]) and _same(g["z"], o["z"])
+        assert res.inst["candidates"][i] == ref.n_cand
+
+
+@pytest.mark.parametrize("budget", [50, 1000, 5000])
+def test_budget_truncation_matches_oracle(gpu_lib, budget):
+    prob = P.scale_problem(P.config2())
+    ref = O.enumerate_sets(prob, k_max=6, budget=budget, keep_records=False)
+    for prec in (solver.FP64, solver.MIXED):
+        res = solver.solve([prob], precision=prec, k_max=6, budget=budget, cand_cap=1 << 18, arena_bytes=1 << 28)
+        assert res.status == 0
+        assert res.candidates == ref.n_cand
+        assert int(res.inst["truncated"][0]) == ref.truncated
+        assert res.total("feasible") == ref.n_feasible
+        assert res.total("regions") == ref.n_region
