@@ -1,0 +1,375 @@
+#!/usr/bin/env python
+"""Benchmark: candidate active sets checked per second at m = 62.
+
+Workload (one "step" = one full enumeration of it, all levels, one launch
+sequence): the config-3 batch -- a random mpQP with n=12, m=62, p=6 whose
+candidate active sets of cardinality 0..6 are all checked (54.3M candidates),
+plus 32 random instances (seeds 1..32, n~U{5..15}, m~U{20..80}, p~U{2..6})
+enumerated up to |S| = n under a budget of 2^19 candidates each.  Inputs are
+seeded synthetic problems (no dataset exists for this metric).
+
+Our arm (default): the mixed-precision path (FP32 pivots and KKT solves, FP64
+certificates / re-solves) on a device-resident plan; the plain FP64 path runs
+once on the same workload for the speed-up and the identical-regions check.
+`--impl reference` times the CPU restatement of the reference's algorithm
+(the C oracle, all host threads) on a bounded sample of the same workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "candidate active sets checked/s at m=62 (mixed FP32/FP64 vs FP64), same regions"
+UNIT = "candidates/s"
+EXTRA_BUDGET = 1 << 19
+MAIN_KMAX = 6
+CPU_SAMPLE_KMAX = 4
+
+
+def workload():
+    from mpqpcudasolver_gb300 import problems as P
+    probs = [P.scale_problem(p) for p in P.config3(n_extra=32)]
+    kmax = [MAIN_KMAX] + [p.n for p in probs[1:]]
+    budget = [0] + [EXTRA_BUDGET] * (len(probs) - 1)
+    return probs, kmax, budget
+
+
+def config_dict(precision: str) -> dict:
+    return {"workload": f"config3: random mpQP n=12 m=62 p=6, all active sets |S|<=6, plus 32 random mpQPs "
+                        f"(seeds 1..32, n~U{{5..15}}, m~U{{20..80}}, p~U{{2..6}}) up to |S|=n, budget "
+                        f"{EXTRA_BUDGET} candidates each; one launch sequence per step",
+            "precision": precision, "instances": 33, "m": 62, "n": 12, "p": 6,
+            "l2": "flushed between steps (512 MiB write); working set (LP1 tableaus) also exceeds L2"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        rows = []
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    parts = [x.strip() for x in line.split(",")]
+                    if len(parts) >= 9:
+                        rows.append(parts)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())
+                if any(r[3].replace(".", "").isdigit() for r in rows) else None}
+
+
+def measured_peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    except Exception:
+        return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def lp1_hbm_bytes(probs, kmax, res, elem: int) -> float:
+    """Algorithmic HBM bytes of all LP1 (k_feasibility) launches of one step.
+
+    Per checked candidate (levels >= 1): candidate record 8 B, parent node
+    48 B, parent LP1 tableau (M1+1)*ld1*s and basis ids M1+nv (read).  Per
+    feasible child: node 48 B and hash slot 32 B (write); per child kept as a
+    parent of the next level: its tableau and ids (write).
+    """
+    total = 0.0
+    for i, pr in enumerate(probs):
+        M1, nv = pr.m + pr.CRA.shape[0], pr.n + pr.p
+        ld1 = (nv + 1) | 1
+        tab = (M1 + 1) * ld1 * elem
+        ids = M1 + nv
+        st = res.inst[i]
+        cand = int(st["candidates"]) - 1          # level 0 (empty set) has no parent
+        feas = int(st["feasible"]) - 1
+        stored = int(st["stored"])
+        total += cand * (8 + 48 + tab + ids) + feas * (48 + 32) + stored * (tab + ids)
+    return total
+
+
+def model_bytes_touched(probs, res, elem: int) -> float:
+    """Bytes-touched model of the hot path (scratchpad + HBM), per step:
+    8*m*(n+p+1) shared-data gather + 8*R*(p+2) region tableau per evaluated
+    set, plus 2*R_LP*C_LP*s per pivot, plus 16 B mask and verdict."""
+    total = 0.0
+    for i, pr in enumerate(probs):
+        st = res.inst[i]
+        m, n, p = pr.m, pr.n, pr.p
+        R = m + pr.CRA.shape[0]
+        lp1 = (R + 1) * (n + p + 1)
+        lp2 = (R + 1) * (p + 2)
+        total += st["candidates"] * 16 + st["feasible"] * (8 * m * (n + p + 1) + 8 * R * (p + 2))
+        total += 2 * elem * (st["lp1_pivots"] * lp1 + (st["lp2_pivots"] + st["cheb_pivots"]) * lp2)
+    return float(total)
+
+
+def same_regions(a, b) -> bool:
+    ka = {(int(o["inst"]), int(o["mask_lo"]), int(o["mask_hi"])) for o in a.opt if o["region"]}
+    kb = {(int(o["inst"]), int(o["mask_lo"]), int(o["mask_hi"])) for o in b.opt if o["region"]}
+    return ka == kb and len(a.opt) == len(b.opt)
+
+
+def dist_setup(n_gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        import torch
+        torch.cuda.set_device(local)
+        dist_mod.init_process_group(backend="nccl")
+        dist = dist_mod
+    return world, rank, local, dist
+
+
+def max_over_ranks(x: float, dist) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(steps: int = 1, warmup: int = 0) -> dict:
+    """The C oracle (restatement of the reference's algorithm) on the host:
+    the main m=62 instance, all candidates with |S| <= 4, every host thread."""
+    from mpqpcudasolver_gb300 import problems as P
+    from oracle import oracle as O
+    prob = P.scale_problem(P.config3_main())
+    threads = os.cpu_count() or 1
+    for _ in range(warmup):
+        O.enumerate_sets(prob, k_max=CPU_SAMPLE_KMAX, nthreads=threads, keep_records=False)
+    vals = []
+    n = 0
+    for _ in range(max(1, steps)):
+        t0 = time.perf_counter()
+        e = O.enumerate_sets(prob, k_max=CPU_SAMPLE_KMAX, nthreads=threads, keep_records=False)
+        dt = time.perf_counter() - t0
+        vals.append(e.n_cand / dt)
+        n = e.n_cand
+    return {"value": statistics.median(vals), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"C oracle, main instance n=12 m=62 p=6, all {n} candidate sets with |S|<={CPU_SAMPLE_KMAX}",
+            "seconds_per_step": n / statistics.median(vals)}
+
+
+def run_reference(args):
+    world, rank, local, dist = dist_setup(args.gpus)
+    if rank != 0:
+        return 0
+    cb = cpu_baseline(steps=args.steps, warmup=args.warmup)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["seconds_per_step"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config_dict("fp64 (CPU)"),
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    from mpqpcudasolver_gb300 import solver
+
+    world, rank, local, dist = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    probs, kmax, budget = workload()
+    prec = solver.MIXED if args.precision == "mixed" else solver.FP64
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    plan = solver.Plan(probs, precision=prec, k_max=kmax, budget=budget, mem_fraction=0.85)
+    for _ in range(args.warmup):
+        plan.run(stream.cuda_stream)
+    res = plan.results()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for s in range(args.steps):
+            if s:
+                flush.zero_()
+            plan.run_timed(stream.cuda_stream)
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+    # kernel times of the last timed step (events on the launching stream)
+    kt = plan.kernel_times()
+    res = plan.results()
+    elapsed = ev0.elapsed_time(ev1)
+    ms_step = max_over_ranks(elapsed / args.steps, dist)
+    if dist is not None:
+        dist.barrier()
+    assert res.status == 0, res.status
+    cand = res.candidates
+    value = cand * world / (ms_step / 1e3)
+    launches = plan.launches
+    plan.close()
+    del plan
+    torch.cuda.synchronize(dev)
+
+    # plain FP64 path on the same workload: speed-up and identical regions
+    fp64 = None
+    if prec == solver.MIXED and not args.skip_fp64:
+        p64 = solver.Plan(probs, precision=solver.FP64, k_max=kmax, budget=budget, mem_fraction=0.85)
+        p64.run(stream.cuda_stream)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        p64.run(stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        r64 = p64.results()
+        fp64 = {"ms_per_step": e0.elapsed_time(e1), "candidates": r64.candidates}
+        fp64["value"] = r64.candidates / (fp64["ms_per_step"] / 1e3)
+        fp64["regions_identical"] = same_regions(res, r64)
+        fp64["regions"] = r64.total("regions")
+        fp64["optimal"] = r64.total("optimal")
+        fp64["feasible_identical"] = r64.total("feasible") == res.total("feasible")
+        p64.close()
+        del p64
+
+    # end to end through the C ABI: host problem arrays in, host results out
+    e2e_vals, h2d, d2h = [], 0, 0
+    for _ in range(max(1, args.e2e_steps)):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        r = solver.solve(probs, precision=prec, k_max=kmax, budget=budget, mem_fraction=0.85)
+        dt = time.perf_counter() - t0
+        e2e_vals.append(r.candidates / dt)
+        h2d, d2h = r.h2d_bytes, r.d2h_bytes
+    # slowest rank's end-to-end rate, times the replicas
+    e2e_val = -max_over_ranks(-statistics.median(e2e_vals), dist) * world
+
+    if rank != 0:
+        return 0
+    # roofline of the LP1 kernel (HBM-facing) and the kernel list
+    elem = 4 if prec == solver.MIXED else 8
+    feas_name = "k_feasibility<float>" if prec == solver.MIXED else "k_feasibility<double>"
+    feas_ms, feas_n = kt.get(feas_name, (0.0, 0))
+    step_kernel_ms = sum(v[0] for v in kt.values())
+    dominant = max(kt.items(), key=lambda kv: kv[1][0])[0] if kt else None
+    bytes_lp1 = lp1_hbm_bytes(probs, kmax, res, elem)
+    peaks = measured_peaks()
+    achieved = bytes_lp1 / (feas_ms / 1e3) / 1e9 if feas_ms > 0 else None
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "lp1_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            with open(tpath) as f:
+                tj = json.load(f)
+            traffic = tj.get("dram_bytes_per_candidate", 0) * (res.candidates - len(probs)) / max(feas_n, 1)
+        except Exception:
+            traffic = None
+    roof = {"bound": "hbm", "kernel": feas_name, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
+            "traffic": traffic, "algorithmic_bytes_per_launch": bytes_lp1 / max(feas_n, 1),
+            "avg_launch_ms": feas_ms / max(feas_n, 1), "peak_source": peaks["source"] + " (MEASURED_PEAKS.json hbm_gbs)",
+            "note": "achieved = LP1 tableau/record bytes per launch / mean launch time; the kernel is bound by "
+                    "shared-memory pivots and FP32 issue, not HBM"}
+    cb = cpu_baseline(steps=1)
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64cert" if prec == solver.MIXED else "f64",
+        "data": "synthetic (seeded generators)", "config": config_dict(args.precision),
+        "candidates_per_step": cand,
+        "pivots_per_s": (res.total("lp1_pivots") + res.total("lp2_pivots") + res.total("cheb_pivots"))
+        * world / (ms_step / 1e3),
+        "regions_per_step": res.total("regions"), "feasible_per_step": res.total("feasible"),
+        "fp64_fallbacks": {"lp1": res.total("fallback_lp1"), "optimality": res.total("fallback_opt")},
+        "fp64_path": fp64,
+        "speedup_vs_fp64": (value / world / fp64["value"]) if fp64 else None,
+        "roofline": roof,
+        "model_bytes_touched_per_s": model_bytes_touched(probs, res, elem) / (ms_step / 1e3),
+        "kernels_ms_per_step": {k: round(v[0], 3) for k, v in sorted(kt.items(), key=lambda kv: -kv[1][0])},
+        "dominant_kernel": dominant,
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "path": "mpqp_solve_batch (C ABI): host arrays in, plan + upload + run + download + free"},
+        "clocks": clocks,
+        "gpu_launches": launches * args.steps,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--skip-fp64", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

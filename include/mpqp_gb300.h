@@ -137,6 +137,7 @@ typedef struct {
 typedef struct {
     long long candidates, pruned, feasible, optimal, regions;
     long long lp1_pivots, lp2_pivots, cheb_pivots, fallback_lp1, fallback_opt;
+    long long stored;             /* LP1 tableaus kept for warm starts      */
     int last_level, truncated;
 } mpqp_inst_stats;
 
@@ -151,6 +152,8 @@ typedef struct {
     mpqp_opt_set *opt;            /* n_opt, sorted (inst, level, mask)      */
     long long n_rec;
     void *rec;                    /* n_rec records (96 bytes each) or NULL  */
+    long long h2d_bytes;          /* problem data uploaded by the plan      */
+    long long d2h_bytes;          /* result bytes copied back               */
 } mpqp_batch_result;
 
 void mpqp_default_options(mpqp_options *opt);
@@ -168,6 +171,12 @@ int mpqp_plan_run(mpqp_plan *plan, void *stream);
 int mpqp_plan_results(mpqp_plan *plan, mpqp_batch_result **out);
 /* Number of kernel launches one run enqueues. */
 int mpqp_plan_launches(const mpqp_plan *plan);
+/* Like mpqp_plan_run, without the graph and with a CUDA event before every
+ * launch; mpqp_plan_kernel_times then returns, per kernel name (64-byte
+ * slots), the summed milliseconds and the launch count.  Returns the number
+ * of distinct kernels (or an error code). */
+int mpqp_plan_run_timed(mpqp_plan *plan, void *stream);
+int mpqp_plan_kernel_times(mpqp_plan *plan, int max_kernels, char *names, double *ms, int *count);
 void mpqp_plan_destroy(mpqp_plan *plan);
 
 /* Region laws of optimal sets, computed in FP64 on the device:

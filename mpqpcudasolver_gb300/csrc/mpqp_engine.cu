@@ -198,8 +198,13 @@ struct mpqp_plan {
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_mid = nullptr;
     bool ran = false;
+    // timed runs: one event before every launch and one after the last
+    std::vector<cudaEvent_t> kev;
+    std::vector<const char *> kname;
+    bool timed = false;
     double last_ms = 0;
     double feas_ms = 0, opt_ms = 0;
+    long long h2d_bytes = 0;
 };
 
 extern "C" void mpqp_default_options(mpqp_options *o)
@@ -258,6 +263,8 @@ static void free_plan_mem(mpqp_plan *P)
     if (P->ev0) cudaEventDestroy(P->ev0);
     if (P->ev1) cudaEventDestroy(P->ev1);
     if (P->ev_mid) cudaEventDestroy(P->ev_mid);
+    for (cudaEvent_t e : P->kev) cudaEventDestroy(e);
+    P->kev.clear();
     P->ev0 = P->ev1 = P->ev_mid = nullptr;
 }
 
@@ -276,32 +283,56 @@ static int grid_for(const void *fn, size_t smem, int *grid)
     return MPQP_OK;
 }
 
-static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed_phases)
+// The fixed launch sequence of one enumeration.  timed: record an event
+// before every launch (and one after the last) on the same stream.
+static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
 {
     const DevBuffers &B = P->B;
     const bool mixed = P->prec == PREC_MIXED;
+    const char *feas = mixed ? "k_feasibility<float>" : "k_feasibility<double>";
+    const char *opt = mixed ? "k_optimality<float>" : "k_optimality<double>";
     int nl = 0;
-    auto chk = [&](cudaError_t e) -> int {
-        nl++;
+    if (timed) P->kname.clear();
+    auto chk = [&](const char *name, cudaError_t e) -> int {
         if (e != cudaSuccess) { set_err(std::string("launch: ") + cudaGetErrorString(e)); return MPQP_ECUDA; }
         return MPQP_OK;
     };
-#define L(x) do { int _r = chk(x); if (_r) return _r; } while (0)
-    L(launch_reset(B, s));
-    L(launch_level0(B, P->prec, s));
-    L(launch_optimality(B, P->tol, P->sd, 0, P->prec, P->grid_opt, P->smem_opt, s));
-    if (mixed) L(launch_optimality_fp64(B, P->tol, P->sd, 0, P->grid_optfb, P->smem_optfb, s));
-    L(launch_finalize(B, 0, s));
+    auto pre = [&](const char *name) -> int {
+        if (timed) {
+            if ((int)P->kev.size() <= nl) {
+                cudaEvent_t e;
+                if (cudaEventCreate(&e) != cudaSuccess) { set_err("cudaEventCreate"); return MPQP_ECUDA; }
+                P->kev.push_back(e);
+            }
+            if (cudaEventRecord(P->kev[nl], s) != cudaSuccess) { set_err("cudaEventRecord"); return MPQP_ECUDA; }
+            P->kname.push_back(name);
+        }
+        nl++;
+        return MPQP_OK;
+    };
+#define L(name, x) do { int _r = pre(name); if (_r) return _r; _r = chk(name, x); if (_r) return _r; } while (0)
+    L("k_reset", launch_reset(B, s));
+    L("k_level0", launch_level0(B, P->prec, s));
+    L(opt, launch_optimality(B, P->tol, P->sd, 0, P->prec, P->grid_opt, P->smem_opt, s));
+    if (mixed) L("k_optimality_fp64", launch_optimality_fp64(B, P->tol, P->sd, 0, P->grid_optfb, P->smem_optfb, s));
+    L("k_finalize", launch_finalize(B, 0, s));
     for (int k = 1; k <= P->kmax; k++) {
-        L(launch_enumerate(B, k, P->grid_enum, s));
-        L(launch_feasibility(B, P->tol, P->sd, k, P->prec, P->grid_feas, P->smem_feas, s));
-        if (mixed) L(launch_lp1_fp64(B, P->tol, P->sd, k, P->grid_lp1fb, P->smem_lp1fb, s));
-        L(launch_optimality(B, P->tol, P->sd, k, P->prec, P->grid_opt, P->smem_opt, s));
-        if (mixed) L(launch_optimality_fp64(B, P->tol, P->sd, k, P->grid_optfb, P->smem_optfb, s));
-        L(launch_finalize(B, k, s));
+        L("k_enumerate", launch_enumerate(B, k, P->grid_enum, s));
+        L(feas, launch_feasibility(B, P->tol, P->sd, k, P->prec, P->grid_feas, P->smem_feas, s));
+        if (mixed) L("k_lp1_fp64", launch_lp1_fp64(B, P->tol, P->sd, k, P->grid_lp1fb, P->smem_lp1fb, s));
+        L(opt, launch_optimality(B, P->tol, P->sd, k, P->prec, P->grid_opt, P->smem_opt, s));
+        if (mixed) L("k_optimality_fp64", launch_optimality_fp64(B, P->tol, P->sd, k, P->grid_optfb, P->smem_optfb, s));
+        L("k_finalize", launch_finalize(B, k, s));
     }
 #undef L
-    (void)timed_phases;
+    if (timed) {
+        if ((int)P->kev.size() <= nl) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) { set_err("cudaEventCreate"); return MPQP_ECUDA; }
+            P->kev.push_back(e);
+        }
+        if (cudaEventRecord(P->kev[nl], s) != cudaSuccess) { set_err("cudaEventRecord"); return MPQP_ECUDA; }
+    }
     P->n_launches = nl;
     return MPQP_OK;
 }
@@ -468,6 +499,7 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
     CK(cudaMemcpy((void *)B.inst, P->desc.data(), sizeof(InstDesc) * n_inst, cudaMemcpyHostToDevice));
     CK(cudaMemcpy((void *)B.dpool, dp.data(), sizeof(double) * dp.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy((void *)B.fpool, fp.data(), sizeof(float) * fp.size(), cudaMemcpyHostToDevice));
+    P->h2d_bytes = (long long)(sizeof(InstDesc) * n_inst + sizeof(double) * dp.size() + sizeof(float) * fp.size());
     CK(cudaMemset(B.hash[0], 0xff, sizeof(HashSlot) * hash_cap));
     CK(cudaMemset(B.hash[1], 0xff, sizeof(HashSlot) * hash_cap));
     CK(cudaMemset(B.ctl, 0, sizeof(Ctl)));
@@ -528,6 +560,45 @@ extern "C" int mpqp_plan_run(mpqp_plan *P, void *stream)
 
 extern "C" int mpqp_plan_launches(const mpqp_plan *P) { return P ? P->n_launches : 0; }
 
+extern "C" int mpqp_plan_run_timed(mpqp_plan *P, void *stream)
+{
+    if (!P) return MPQP_EINVAL;
+    cudaStream_t s = (cudaStream_t)stream;
+    CK(cudaEventRecord(P->ev0, s));
+    int rc = enqueue(P, s, true);
+    if (rc) return rc;
+    CK(cudaEventRecord(P->ev1, s));
+    P->ran = true;
+    P->timed = true;
+    return MPQP_OK;
+}
+
+extern "C" int mpqp_plan_kernel_times(mpqp_plan *P, int max_kernels, char *names, double *ms, int *count)
+{
+    if (!P || !P->timed) { set_err("no timed run"); return MPQP_EINVAL; }
+    CK(cudaEventSynchronize(P->ev1));
+    std::vector<std::string> nm;
+    std::vector<double> t;
+    std::vector<int> c;
+    for (size_t i = 0; i < P->kname.size(); i++) {
+        float e = 0;
+        CK(cudaEventElapsedTime(&e, P->kev[i], P->kev[i + 1]));
+        size_t j = 0;
+        while (j < nm.size() && nm[j] != P->kname[i]) j++;
+        if (j == nm.size()) { nm.push_back(P->kname[i]); t.push_back(0); c.push_back(0); }
+        t[j] += e;
+        c[j] += 1;
+    }
+    const int n = std::min((int)nm.size(), max_kernels);
+    for (int i = 0; i < n; i++) {
+        strncpy(names + 64 * i, nm[i].c_str(), 63);
+        names[64 * i + 63] = 0;
+        ms[i] = t[i];
+        count[i] = c[i];
+    }
+    return n;
+}
+
 static bool set_less(uint64_t alo, uint64_t ahi, uint64_t blo, uint64_t bhi)
 {
     // lexicographic order of the sorted element lists of two equal-size sets
@@ -562,7 +633,8 @@ extern "C" int mpqp_plan_results(mpqp_plan *P, mpqp_batch_result **out)
         s.candidates = ic[i].cum_cand; s.pruned = ic[i].pruned; s.feasible = ic[i].feasible;
         s.optimal = ic[i].optimal; s.regions = ic[i].region; s.lp1_pivots = ic[i].lp1_piv;
         s.lp2_pivots = ic[i].lp2_piv; s.cheb_pivots = ic[i].cheb_piv; s.fallback_lp1 = ic[i].fb_lp1;
-        s.fallback_opt = ic[i].fb_opt; s.last_level = ic[i].last_level; s.truncated = ic[i].truncated;
+        s.fallback_opt = ic[i].fb_opt; s.stored = ic[i].stored;
+        s.last_level = ic[i].last_level; s.truncated = ic[i].truncated;
         nlev = std::max(nlev, ic[i].last_level + 1);
     }
     R->n_levels = nlev;
@@ -581,8 +653,11 @@ extern "C" int mpqp_plan_results(mpqp_plan *P, mpqp_batch_result **out)
         o.mask_lo = ov[i].lo; o.mask_hi = ov[i].hi; o.inst = ov[i].inst; o.level = ov[i].level;
         o.t = ov[i].t; o.r = ov[i].r; o.region = ov[i].region; o.fp64 = ov[i].fp64; o.rec = ov[i].rec;
     }
+    R->h2d_bytes = P->h2d_bytes;
+    R->d2h_bytes = (long long)(sizeof(Ctl) + sizeof(InstCtl) * P->n_inst + sizeof(OptRec) * nopt);
     if (P->B.rec) {
         long long nrec = std::min(ctl.rec_base, P->B.rec_cap);
+        R->d2h_bytes += (long long)sizeof(CandRec) * nrec;
         R->n_rec = nrec;
         R->rec = malloc(sizeof(CandRec) * (nrec ? nrec : 1));
         if (nrec) CK(cudaMemcpy(R->rec, P->B.rec, sizeof(CandRec) * nrec, cudaMemcpyDeviceToHost));

@@ -103,6 +103,7 @@ struct InstCtl {
     long long feasible, optimal, region;
     long long lp1_piv, lp2_piv, cheb_piv;
     long long fb_lp1, fb_opt;   // FP64 fallbacks (mixed precision)
+    long long stored;           // LP1 tableaus written for the next level
     int stopped;                // budget exhausted or max level reached
     int truncated;              // stopped by the budget
     int last_level;

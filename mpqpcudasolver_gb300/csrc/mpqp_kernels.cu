@@ -371,6 +371,7 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
     ioff = __shfl_sync(FULLMASK, ioff, 0);
     if (idx < 0) return -1;
     if (need_tab) {
+        if (lane == 0) atomicAdd((unsigned long long *)&B.ictl[inst].stored, 1ull);
         TT *dst = (TT *)B.tab[side] + toff;
         warp_copy<TS, TT>(dst, tab, (I.M1 + 1) * I.ld1);
         uint8_t *di = B.ids[side] + ioff;

@@ -51,7 +51,7 @@ class OptSet(ctypes.Structure):
 class InstStats(ctypes.Structure):
     _fields_ = [(nm, ctypes.c_longlong) for nm in ("candidates", "pruned", "feasible", "optimal", "regions",
                                                     "lp1_pivots", "lp2_pivots", "cheb_pivots", "fallback_lp1",
-                                                    "fallback_opt")] + \
+                                                    "fallback_opt", "stored")] + \
         [("last_level", ctypes.c_int), ("truncated", ctypes.c_int)]
 
 
@@ -59,7 +59,8 @@ class BatchResult(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("n_inst", ctypes.c_int), ("n_levels", ctypes.c_int),
                 ("overflow", ctypes.c_int), ("device_ms", ctypes.c_double),
                 ("inst", ctypes.POINTER(InstStats)), ("n_opt", ctypes.c_longlong), ("opt", ctypes.POINTER(OptSet)),
-                ("n_rec", ctypes.c_longlong), ("rec", ctypes.c_void_p)]
+                ("n_rec", ctypes.c_longlong), ("rec", ctypes.c_void_p), ("h2d_bytes", ctypes.c_longlong),
+                ("d2h_bytes", ctypes.c_longlong)]
 
 
 class GPUResults(ctypes.Structure):
@@ -81,6 +82,7 @@ REC_DTYPE = np.dtype([("mask_lo", "<u8"), ("mask_hi", "<u8"), ("level", "<i4"), 
 
 EXPORTS = ("mpqp", "warm_up", "mpqp_free", "mpqp_default_options", "mpqp_solve_batch", "mpqp_batch_free",
            "mpqp_plan_create", "mpqp_plan_run", "mpqp_plan_results", "mpqp_plan_launches", "mpqp_plan_destroy",
+           "mpqp_plan_run_timed", "mpqp_plan_kernel_times",
            "mpqp_region_laws_stride", "mpqp_region_laws", "mpqp_version", "mpqp_last_error")
 
 _lib = None
@@ -122,6 +124,11 @@ def load(build_if_missing: bool = False):
     lib.mpqp_plan_launches.argtypes = [ctypes.c_void_p]
     lib.mpqp_plan_launches.restype = ctypes.c_int
     lib.mpqp_plan_destroy.argtypes = [ctypes.c_void_p]
+    lib.mpqp_plan_run_timed.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.mpqp_plan_run_timed.restype = ctypes.c_int
+    lib.mpqp_plan_kernel_times.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, P(ctypes.c_double),
+                                           P(ctypes.c_int)]
+    lib.mpqp_plan_kernel_times.restype = ctypes.c_int
     lib.mpqp_region_laws_stride.argtypes = [P(Problem)]
     lib.mpqp_region_laws_stride.restype = ctypes.c_longlong
     lib.mpqp_region_laws.argtypes = [P(Problem), ctypes.c_longlong, P(ctypes.c_uint64), P(ctypes.c_double),
@@ -180,6 +187,8 @@ class Result:
     inst: np.ndarray          # structured per-instance counters
     opt: np.ndarray           # structured optimal sets
     rec: np.ndarray | None    # structured records (record=1)
+    h2d_bytes: int = 0
+    d2h_bytes: int = 0
 
     @property
     def candidates(self) -> int:
@@ -189,7 +198,7 @@ class Result:
         return int(self.inst[field].sum())
 
 
-_INST_DTYPE = np.dtype([(f[0], "<i8") for f in InstStats._fields_[:10]] + [("last_level", "<i4"),
+_INST_DTYPE = np.dtype([(f[0], "<i8") for f in InstStats._fields_[:11]] + [("last_level", "<i4"),
                                                                             ("truncated", "<i4")])
 _OPT_DTYPE = np.dtype([("mask_lo", "<u8"), ("mask_hi", "<u8"), ("inst", "<i4"), ("level", "<i4"), ("t", "<f8"),
                        ("r", "<f8"), ("region", "<i4"), ("fp64", "<i4"), ("rec", "<i8")])
@@ -209,7 +218,7 @@ def _convert(rp) -> Result:
         nrec = r.n_rec
         buf = (ctypes.c_char * (nrec * REC_DTYPE.itemsize)).from_address(r.rec)
         rec = np.frombuffer(buf, dtype=REC_DTYPE).copy()
-    return Result(r.status, r.device_ms, r.n_levels, r.overflow, inst, opt, rec)
+    return Result(r.status, r.device_ms, r.n_levels, r.overflow, inst, opt, rec, r.h2d_bytes, r.d2h_bytes)
 
 
 def solve(probs, precision: int = FP64, k_min: int = 0, k_max=None, budget=0, **opts) -> Result:
@@ -249,6 +258,21 @@ class Plan:
         self.lib.mpqp_batch_free(out)
         _check(rc)
         return res
+
+    def run_timed(self, stream: int = 0):
+        """One run without the graph, with a CUDA event around every launch."""
+        _check(self.lib.mpqp_plan_run_timed(self.h, ctypes.c_void_p(stream)))
+
+    def kernel_times(self) -> dict:
+        """{kernel name: (total ms, launches)} of the last timed run."""
+        nmax = 32
+        names = ctypes.create_string_buffer(64 * nmax)
+        ms = (ctypes.c_double * nmax)()
+        cnt = (ctypes.c_int * nmax)()
+        n = self.lib.mpqp_plan_kernel_times(self.h, nmax, names, ms, cnt)
+        if n < 0:
+            _check(n)
+        return {names.raw[64 * i:64 * i + 64].split(b"\0")[0].decode(): (ms[i], cnt[i]) for i in range(n)}
 
     @property
     def launches(self) -> int:
