@@ -121,6 +121,7 @@ typedef struct {
     double tol_feas, tol_opt, tol_licq, r_min, tol_piv, tol_dj;
     int max_pivots, degen_switch;
     double tol_piv32, tol_dj32, margin_z, margin_beta, margin_t, margin_licq;
+    double tol_zero_row;     /* region row zero when max|g| <= tol * max(1,|h|) */
 } mpqp_options;
 
 /* One optimal active set */

@@ -227,6 +227,7 @@ extern "C" void mpqp_default_options(mpqp_options *o)
     o->margin_beta = 1e-3;
     o->margin_t = 3e-5;   // x (row magnitude / pivot ratio) x (1 + p |theta|max)
     o->margin_licq = 1e-3;
+    o->tol_zero_row = 1e-12;
 }
 
 static void fill_defaults(mpqp_options &o)
@@ -236,7 +237,7 @@ static void fill_defaults(mpqp_options &o)
 #define DEF(f) if (o.f == 0) o.f = d.f
     DEF(mem_fraction); DEF(tol_feas); DEF(tol_opt); DEF(tol_licq); DEF(r_min); DEF(tol_piv); DEF(tol_dj);
     DEF(max_pivots); DEF(degen_switch); DEF(tol_piv32); DEF(tol_dj32); DEF(margin_z); DEF(margin_beta);
-    DEF(margin_t); DEF(margin_licq);
+    DEF(margin_t); DEF(margin_licq); DEF(tol_zero_row);
 #undef DEF
 }
 
@@ -354,6 +355,7 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
     t.tol_piv = o.tol_piv; t.tol_dj = o.tol_dj; t.max_pivots = o.max_pivots; t.degen_switch = o.degen_switch;
     t.tol_piv32 = (float)o.tol_piv32; t.tol_dj32 = (float)o.tol_dj32;
     t.margin_z = o.margin_z; t.margin_beta = o.margin_beta; t.margin_t = o.margin_t; t.margin_licq = o.margin_licq;
+    t.tol_zero_row = o.tol_zero_row;
     // host precompute
     std::vector<Prepared> prep(n_inst);
     for (int i = 0; i < n_inst; i++) {

@@ -45,6 +45,7 @@ struct Tol {
     double margin_beta; // FP32 basic slacks above this certify feasibility
     double margin_t;    // FP32 LP2 t below -margin_t * error scale -> not optimal without FP64
     double margin_licq; // FP32 Cholesky pivot ratio below this -> FP64
+    double tol_zero_row;// region row is zero when max|g| <= tol_zero_row * max(1, |h|)
 };
 
 struct InstDesc {

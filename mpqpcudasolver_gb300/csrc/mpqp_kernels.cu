@@ -597,6 +597,18 @@ template <> __device__ __forceinline__ KktData<float> kkt_data<float>(const DevB
     return {B.fpool + I.f_Wm, B.fpool + I.f_Wh, B.fpool + I.f_wc, B.fpool + I.f_At, B.fpool + I.f_bt};
 }
 
+// A region row [g | h] counts as zero (and is dropped before the Chebyshev
+// LP, as utils.py:46-47 does for exact zeros) when max|g| <= tz * max(1,|h|):
+// rows that vanish in exact arithmetic come out as rounding noise.
+template <typename T>
+__device__ __forceinline__ bool nonzero_row(const T *g, int p, double tz)
+{
+    T gmax = T(0);
+    for (int cc = 0; cc < p; cc++) { const T a = xabs(g[cc]); if (a > gmax) gmax = a; }
+    const T ah = xabs(g[p]);
+    return gmax > (T)tz * (ah > T(1) ? ah : T(1));
+}
+
 struct OptResult {
     int licq, lp2_status, lp2_piv, cheb_status, cheb_piv, optimal, region;
     double t, r;
@@ -818,9 +830,7 @@ __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const 
         bool keep = false;
         if (r < R2) {
             if (r >= m) keep = true;
-            else {
-                for (int cc = 0; cc < p; cc++) if (G[r * P1 + cc] != T(0)) { keep = true; break; }
-            }
+            else keep = nonzero_row<T>(G + (size_t)r * P1, p, tol.tol_zero_row);
         }
         const unsigned km = __ballot_sync(FULLMASK, keep);
         if (keep) {
@@ -1134,7 +1144,7 @@ __global__ void __launch_bounds__(128) k_region_laws(DevBuffers B, Tol tol, Slot
             bool keep = false;
             if (r < R2) {
                 if (r >= m) keep = true;
-                else for (int cc = 0; cc < p; cc++) if (G[r * P1 + cc] != 0.0) { keep = true; break; }
+                else keep = nonzero_row<double>(G + (size_t)r * P1, p, tol.tol_zero_row);
             }
             const unsigned km = __ballot_sync(FULLMASK, keep);
             if (keep) {

@@ -39,7 +39,8 @@ class Options(ctypes.Structure):
                 ("r_min", ctypes.c_double), ("tol_piv", ctypes.c_double), ("tol_dj", ctypes.c_double),
                 ("max_pivots", ctypes.c_int), ("degen_switch", ctypes.c_int),
                 ("tol_piv32", ctypes.c_double), ("tol_dj32", ctypes.c_double), ("margin_z", ctypes.c_double),
-                ("margin_beta", ctypes.c_double), ("margin_t", ctypes.c_double), ("margin_licq", ctypes.c_double)]
+                ("margin_beta", ctypes.c_double), ("margin_t", ctypes.c_double), ("margin_licq", ctypes.c_double),
+                ("tol_zero_row", ctypes.c_double)]
 
 
 class OptSet(ctypes.Structure):

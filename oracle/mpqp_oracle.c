@@ -45,6 +45,7 @@ void orc_default_tol(orc_tol *t)
     t->tol_dj = 1e-9;
     t->max_pivots = 256;
     t->degen_switch = 8;
+    t->tol_zero_row = 1e-12;
 }
 
 static void free_data(orc_data *d)
@@ -418,9 +419,13 @@ static void optimality(const orc_data *d, const int *S, int k, const orc_tol *to
     for (int r = 0; r < nrows; r++) {
         const double *g = G + (size_t)r * P1;
         if (r < m) {
-            int nz = 0;
-            for (int c = 0; c < p; c++) if (g[c] != 0.0) { nz = 1; break; }
-            if (!nz) continue;
+            /* utils.py:46-47 drops rows whose theta part is exactly zero; rows
+             * that are zero in exact arithmetic come out as rounding noise,
+             * so the test is relative: max|g| <= tol_zero_row * max(1, |h|) */
+            double gmax = 0.0;
+            for (int c = 0; c < p; c++) if (fabs(g[c]) > gmax) gmax = fabs(g[c]);
+            const double ah = fabs(g[p]);
+            if (!(gmax > tol->tol_zero_row * (ah > 1.0 ? ah : 1.0))) continue;
         }
         double acc = 0.0;
         for (int c = 0; c < p; c++) acc = fma(g[c], g[c], acc);

@@ -51,6 +51,7 @@ typedef struct {
     double tol_dj;     /* pricing: |reduced cost| must exceed this           */
     int max_pivots;    /* per LP */
     int degen_switch;  /* consecutive degenerate pivots before Bland's rule */
+    double tol_zero_row; /* region row counts as zero when max|g| <= this * max(1,|h|) */
 } orc_tol;
 
 /* LP status codes (shared with the device code) */

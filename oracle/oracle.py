@@ -44,7 +44,7 @@ class OrcTol(ctypes.Structure):
     _fields_ = [("tol_feas", ctypes.c_double), ("tol_opt", ctypes.c_double),
                 ("tol_licq", ctypes.c_double), ("r_min", ctypes.c_double),
                 ("tol_piv", ctypes.c_double), ("tol_dj", ctypes.c_double),
-                ("max_pivots", ctypes.c_int), ("degen_switch", ctypes.c_int)]
+                ("max_pivots", ctypes.c_int), ("degen_switch", ctypes.c_int), ("tol_zero_row", ctypes.c_double)]
 
 
 class OrcCand(ctypes.Structure):

@@ -104,8 +104,11 @@ def scale_constraint(A, b):
     return [A * norm_val, b * norm_val]
 
 
-def compute_critical_region(A, b, c, H, inv_Q, F, CRA, CRb, active_set):
-    """``utils.py:23-97`` with HiGHS in place of Gurobi; also returns r*."""
+def compute_critical_region(A, b, c, H, inv_Q, F, CRA, CRb, active_set, zero_tol=None):
+    """``utils.py:23-97`` with HiGHS in place of Gurobi; also returns r*.
+
+    zero_tol=None keeps the reference's exact zero-row test; a number uses the
+    relative test max|row| <= zero_tol * max(1, |rhs|) instead."""
     num_t = CRA.shape[1]
     active_set = list(active_set)
     aux = A[active_set] @ inv_Q
@@ -119,8 +122,14 @@ def compute_critical_region(A, b, c, H, inv_Q, F, CRA, CRb, active_set):
     lambda_A, lambda_b = -lagrange_A[0:], lagrange_b[0:]
     inactive_A = A[inactive] @ parameter_A - F[inactive]
     inactive_b = b[inactive] - A[inactive] @ parameter_b
-    lamba_nonzeros = [i for i, t in enumerate(lambda_A) if np.nonzero(t)[0].shape[0] > 0]
-    ineq_nonzeros = [i for i, t in enumerate(inactive_A) if np.nonzero(t)[0].shape[0] > 0]
+    if zero_tol is None:
+        lamba_nonzeros = [i for i, t in enumerate(lambda_A) if np.nonzero(t)[0].shape[0] > 0]
+        ineq_nonzeros = [i for i, t in enumerate(inactive_A) if np.nonzero(t)[0].shape[0] > 0]
+    else:
+        lamba_nonzeros = [i for i, t in enumerate(lambda_A)
+                          if np.max(np.abs(t)) > zero_tol * max(1.0, abs(float(np.ravel(lambda_b[i])[0])))]
+        ineq_nonzeros = [i for i, t in enumerate(inactive_A)
+                         if np.max(np.abs(t)) > zero_tol * max(1.0, abs(float(np.ravel(inactive_b[i])[0])))]
     CR_A = np.vstack((lambda_A[lamba_nonzeros], inactive_A[ineq_nonzeros], CRA))
     CR_b = np.vstack((lambda_b[lamba_nonzeros], inactive_b[ineq_nonzeros], CRb))
     CR_As, CR_bs = scale_constraint(CR_A, CR_b)
@@ -140,8 +149,8 @@ def compute_critical_region(A, b, c, H, inv_Q, F, CRA, CRb, active_set):
     return region, r
 
 
-def region_for(prob, S):
+def region_for(prob, S, zero_tol=None):
     """Region of S on an MPQP problem (b, c, CRb as column vectors, utils.py:128-144)."""
     inv_Q = np.linalg.pinv(prob.Q)
     return compute_critical_region(prob.A, prob.b.reshape(-1, 1), prob.c.reshape(-1, 1), prob.H,
-                                   inv_Q, prob.F, prob.CRA, prob.CRb.reshape(-1, 1), list(S))
+                                   inv_Q, prob.F, prob.CRA, prob.CRb.reshape(-1, 1), list(S), zero_tol=zero_tol)

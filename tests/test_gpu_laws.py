@@ -1,0 +1,68 @@
+"""Region laws on the device (FP64) against the oracle and the reference math.
+
+The affine laws lambda(theta), x(theta) and the normalised region rows of
+every region found are compared with
+* the C oracle (same operation order: identical to 1e-12 relative), and
+* a line-by-line restatement of ``compute_critical_region`` (numpy pinv,
+  utils.py:23-97): within 1e-8 relative, as the target requires.  Rows whose
+  theta part vanishes up to rounding are dropped by the relative test both
+  sides use (max|g| <= 1e-12 max(1,|h|)) instead of the exact-zero test.
+"""
+import numpy as np
+import pytest
+
+from mpqpcudasolver_gb300 import problems as P
+from mpqpcudasolver_gb300 import solver
+from oracle import oracle as O
+from oracle import reference_lp as R
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "config1": (lambda: P.config1(), 4),
+    "config2-k3": (lambda: P.config2(), 3),
+    "config3main-k2": (lambda: P.config3_main(), 2),
+    "config5-k3": (lambda: P.mpc_mpqp(0), 3),
+}
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    if a.shape != b.shape:
+        return np.inf
+    if a.size == 0:
+        return 0.0
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_region_laws_match_oracle_and_reference(gpu_lib, case):
+    make, kmax = CASES[case]
+    prob = P.scale_problem(make())
+    res = solver.solve([prob], precision=solver.FP64, k_max=kmax, cand_cap=1 << 18, arena_bytes=1 << 28)
+    regions = [solver.mask_to_set(o["mask_lo"], o["mask_hi"]) for o in res.opt if o["region"]]
+    assert regions, "no region found"
+    sets = regions[:200]
+    laws = solver.region_laws(prob, sets)
+    worst_ref = 0.0
+    for S, law in zip(sets, laws):
+        assert law is not None
+        rec, ol = O.check_set(prob, S, want_laws=True)
+        assert rec["region"] == 1
+        for key in ("lagrange_A", "lagrange_b", "parameter_A", "parameter_b", "CR_As", "CR_bs"):
+            assert _rel(law[key], ol[key]) <= 1e-12, (S, key)
+        reg, r = R.region_for(prob, S, zero_tol=1e-12)
+        assert reg is not None
+        for key in ("lagrange_A", "parameter_A", "CR_As"):
+            worst_ref = max(worst_ref, _rel(law[key], reg[key]))
+        for key in ("lagrange_b", "parameter_b", "CR_bs"):
+            worst_ref = max(worst_ref, _rel(law[key], np.asarray(reg[key]).ravel()))
+    assert worst_ref <= 1e-8, worst_ref
+
+
+def test_region_laws_reject_bad_sets(gpu_lib):
+    prob = P.scale_problem(P.config1())
+    with pytest.raises(solver.MpqpError):
+        solver.region_laws(prob, [[0, 1, 2, 3, 4]])        # |S| > n
+    with pytest.raises(solver.MpqpError):
+        solver.region_laws(prob, [[prob.m]])               # index out of range
