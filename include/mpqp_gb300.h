@@ -190,6 +190,24 @@ long long mpqp_region_laws_stride(const mpqp_problem *prob);
 int mpqp_region_laws(const mpqp_problem *prob, long long n_sets, const uint64_t *masks /* 2 per set */,
                      double *laws, int *sizes);
 
+/* Region laws without any device allocation.  No counterpart in the
+ * reference: its region laws are computed on the host (utils.py:23-97).
+ * For callers that may not call cudaMalloc -- a control loop past its
+ * start-up, where an allocation can stall or fail, or a host application
+ * that owns the device memory through its own allocator.  Same results as
+ * mpqp_region_laws, but `masks` (2 per set) stays on the host while `laws`
+ * (n_sets * mpqp_region_laws_stride doubles) and `sizes` (4 ints per set)
+ * are device buffers the caller allocated.  The work is queued on `stream`
+ * (a cudaStream_t, NULL = default stream); synchronise it before reading.
+ * Scratch: a fixed MPQP_NOALLOC_SCRATCH_BYTES (1 MiB) device array holds the
+ * instance's FP64 KKT blocks plus 16 bytes per set; larger calls return
+ * MPQP_ECAPACITY.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress), so make it before any stream capture.
+ * All calls share the array: calls whose work overlaps on the GPU race. */
+#define MPQP_NOALLOC_SCRATCH_BYTES (1 << 20)
+int mpqp_region_laws_noalloc(const mpqp_problem *prob, long long n_sets, const uint64_t *masks, double *laws,
+                             int *sizes, void *stream);
+
 const char *mpqp_version(void);
 const char *mpqp_last_error(void);
 

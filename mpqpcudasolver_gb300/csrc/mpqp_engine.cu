@@ -50,6 +50,10 @@ static std::mutex g_mu;
 
 static void set_err(const std::string &s) { g_err = s; }
 
+namespace mq {
+void set_error_text(const char *msg) { set_err(msg ? msg : ""); }
+}  // namespace mq
+
 #define CK(call)                                                                                       \
     do {                                                                                               \
         cudaError_t _e = (call);                                                                       \
