@@ -179,13 +179,20 @@ def dist_setup(n_gpus: int):
     return world, rank, local, dist
 
 
-def max_over_ranks(x: float, dist) -> float:
+def max_over_ranks(x: float, dist, device: str = "cuda") -> float:
+    """Largest value over all ranks (the slowest replica's step time)."""
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, ms_per_step: float, world: int) -> float:
+    """Replicas only: every rank runs the full workload, so the job checks
+    world x units per (slowest) step."""
+    return units_per_rank * world / (ms_per_step / 1e3)
 
 
 def cpu_baseline(steps: int = 1, warmup: int = 0) -> dict:
@@ -261,7 +268,7 @@ def run_ours(args):
         dist.barrier()
     assert res.status == 0, res.status
     cand = res.candidates
-    value = cand * world / (ms_step / 1e3)
+    value = whole_job_rate(cand, ms_step, world)
     launches = plan.launches
     plan.close()
     del plan

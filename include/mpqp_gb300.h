@@ -80,6 +80,14 @@ void warm_up(void);
 /* Releases a result of mpqp() (the reference never frees; this is optional). */
 void mpqp_free(GPUResults *res);
 
+/* The problem mpqp() reads back from the reference's LP matrices, without
+ * touching the GPU: Q (n_x^2), c (n_x), H (n_x*n_t), A (n_c*n_x), b (n_c),
+ * F (n_c*n_t), At (n_cp*n_t), bt (n_cp), row-major; *n_cp = M1 - n_c.
+ * Pass NULL for outputs you do not need.  Returns MPQP_OK or MPQP_ELAYOUT. */
+int mpqp_unpack_lp(const double *AxT, int n_c, int n_x, int n_t, const double *A1, const double *xb1, int M1,
+                   int N1, const double *A2, const double *xb2, int M2, int N2, int n_eqs, double *Q, double *c,
+                   double *H, double *A, double *b, double *F, double *At, double *bt, int *n_cp);
+
 /* ------------------------------------------------------------------ */
 /* Native interface                                                      */
 /* ------------------------------------------------------------------ */

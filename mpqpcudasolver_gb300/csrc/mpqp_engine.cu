@@ -832,6 +832,22 @@ static int unpack_lp(const double *AxT, int n_c, int n_x, int n_t, const double 
     return MPQP_OK;
 }
 
+extern "C" int mpqp_unpack_lp(const double *AxT, int n_c, int n_x, int n_t, const double *A1, const double *xb1,
+                              int M1, int N1, const double *A2, const double *xb2, int M2, int N2, int n_eqs,
+                              double *Q, double *c, double *H, double *A, double *b, double *F, double *At,
+                              double *bt, int *n_cp)
+{
+    std::vector<double> q, cc, h, a, bb, f, at, btv;
+    int ncp = 0;
+    const int rc = unpack_lp(AxT, n_c, n_x, n_t, A1, xb1, M1, N1, A2, xb2, M2, N2, n_eqs, q, cc, h, a, bb, f, at,
+                             btv, ncp);
+    if (n_cp) *n_cp = ncp;
+    if (rc) return rc;
+    auto out = [](double *dst, const std::vector<double> &v) { if (dst) memcpy(dst, v.data(), sizeof(double) * v.size()); };
+    out(Q, q); out(c, cc); out(H, h); out(A, a); out(b, bb); out(F, f); out(At, at); out(bt, btv);
+    return MPQP_OK;
+}
+
 extern "C" GPUResults *mpqp(const double *AxT, int n_c, int n_x, int n_t, int k_min, int k_max, int extra_batches,
                             const double *A1, const double *xb1, const int *b1, int M1, int N1, const double *A2,
                             const double *xb2, const int *b2, const int *non_b2, int M2, int N2, int n_eqs,

@@ -81,7 +81,7 @@ REC_DTYPE = np.dtype([("mask_lo", "<u8"), ("mask_hi", "<u8"), ("level", "<i4"), 
                       ("lp2_status", "<i4"), ("lp2_pivots", "<i4"), ("cheb_status", "<i4"),
                       ("cheb_pivots", "<i4"), ("t", "<f8"), ("r", "<f8"), ("inst", "<i4"), ("fp64", "<i4")])
 
-EXPORTS = ("mpqp", "warm_up", "mpqp_free", "mpqp_default_options", "mpqp_solve_batch", "mpqp_batch_free",
+EXPORTS = ("mpqp", "warm_up", "mpqp_free", "mpqp_unpack_lp", "mpqp_default_options", "mpqp_solve_batch", "mpqp_batch_free",
            "mpqp_plan_create", "mpqp_plan_run", "mpqp_plan_results", "mpqp_plan_launches", "mpqp_plan_destroy",
            "mpqp_plan_run_timed", "mpqp_plan_kernel_times",
            "mpqp_region_laws_stride", "mpqp_region_laws", "mpqp_version", "mpqp_last_error")
@@ -112,6 +112,10 @@ def load(build_if_missing: bool = False):
                          ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.mpqp.restype = P(GPUResults)
     lib.mpqp_free.argtypes = [P(GPUResults)]
+    dp = P(ctypes.c_double)
+    lib.mpqp_unpack_lp.argtypes = [dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, ctypes.c_int, ctypes.c_int,
+                                   dp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int] + [dp] * 8 + [P(ctypes.c_int)]
+    lib.mpqp_unpack_lp.restype = ctypes.c_int
     lib.mpqp_default_options.argtypes = [P(Options)]
     lib.mpqp_solve_batch.argtypes = [ctypes.c_int, P(Problem), P(Options), PP]
     lib.mpqp_solve_batch.restype = ctypes.c_int
@@ -319,6 +323,24 @@ def region_laws(prob, sets):
         out.append(dict(lagrange_A=lag[:, :p].copy(), lagrange_b=lag[:, p].copy(), parameter_A=par[:, :p].copy(),
                         parameter_b=par[:, p].copy(), CR_As=cr[:, :p].copy(), CR_bs=cr[:, p].copy(),
                         active_set=list(sets[i])))
+    return out
+
+
+def unpack_lp(d: dict):
+    """Problem arrays that ``mpqp()`` reads back from the LP matrices of
+    ``host.build_lp_data`` (host only, no GPU work)."""
+    lib = load()
+    n_c, n_x, n_t, M1 = d["num_c"], d["num_x"], d["num_t"], d["M1"]
+    n_cp = M1 - n_c
+    out = {k: np.zeros(sz) for k, sz in (("Q", (n_x, n_x)), ("c", n_x), ("H", (n_x, n_t)), ("A", (n_c, n_x)),
+                                           ("b", n_c), ("F", (n_c, n_t)), ("At", (n_cp, n_t)), ("bt", n_cp))}
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    ncp = ctypes.c_int(0)
+    rc = lib.mpqp_unpack_lp(dp(d["A0"]), n_c, n_x, n_t, dp(d["A1"]), dp(d["xb1"]), d["M1"], d["N1"], dp(d["A2"]),
+                            dp(d["xb2"]), d["M2"], d["N2"], d["n_eqs"], *(dp(out[k]) for k in
+                                                                        ("Q", "c", "H", "A", "b", "F", "At", "bt")),
+                            ctypes.byref(ncp))
+    _check(rc)
     return out
 
 

@@ -1,0 +1,84 @@
+"""The C-ABI library on the CPU: it builds, loads, exports every symbol the
+public header declares, and rebuilds the problem from the reference's LP
+matrices exactly (host-only entry point; nothing here launches a kernel)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from mpqpcudasolver_gb300 import build as B
+from mpqpcudasolver_gb300 import host
+from mpqpcudasolver_gb300 import problems as P
+from mpqpcudasolver_gb300 import solver
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "mpqp_gb300.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    B.build()
+    return solver.load()
+
+
+def header_functions():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    names = set(re.findall(r"\b([a-z_][a-z0-9_]*)\s*\([^;{]*\)\s*;", txt))
+    return sorted(n for n in names if n not in {"if", "while", "sizeof"})
+
+
+def test_header_declares_the_reference_entry_points():
+    fns = header_functions()
+    assert "mpqp" in fns and "warm_up" in fns
+    assert len(fns) >= 15
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in header_functions():
+        assert hasattr(lib, name), name
+    for name in solver.EXPORTS:
+        assert hasattr(lib, name), name
+    assert lib.mpqp_version().startswith(b"mpqp_gb300")
+
+
+def test_gpu_results_prefix_matches_reference_layout():
+    # main.py:12-22: four ints, three doubles, one pointer
+    class Ref(ctypes.Structure):
+        _fields_ = [('n_batches', ctypes.c_int), ('n_splits', ctypes.c_int), ('n_feasible_lps', ctypes.c_int),
+                    ('n_final_lps', ctypes.c_int), ('time_feas', ctypes.c_double), ('time_opti', ctypes.c_double),
+                    ('time_GPU', ctypes.c_double), ('active_sets', ctypes.POINTER(ctypes.c_int))]
+    for f, _ in Ref._fields_:
+        assert getattr(Ref, f).offset == getattr(solver.GPUResults, f).offset, f
+
+
+@pytest.mark.parametrize("make", [P.config1, P.config2, P.config4, lambda: P.mpc_mpqp(3),
+                                  lambda: P.config3_extra(5)])
+def test_unpack_lp_recovers_the_problem(lib, make):
+    prog = host.MPQPProb.from_mpqp(make())
+    prog.process_constraints(scale_method=1)
+    d = host.build_lp_data(prog)
+    out = solver.unpack_lp(d)
+    assert np.array_equal(out["A"], prog.A)
+    assert np.array_equal(out["F"], prog.F)
+    assert np.array_equal(out["b"], prog.b.ravel())
+    assert np.array_equal(out["At"], prog.A_t)
+    assert np.array_equal(out["bt"], prog.b_t.ravel())
+    assert np.array_equal(out["Q"], prog.Q)
+    assert np.array_equal(out["H"], prog.H)
+    assert np.array_equal(out["c"], prog.c.ravel())
+
+
+def test_unpack_lp_rejects_other_layouts(lib):
+    prog = host.MPQPProb.from_mpqp(P.config1())
+    prog.process_constraints(scale_method=1)
+    d = host.build_lp_data(prog)
+    bad = dict(d, N1=d["N1"] + 1)
+    with pytest.raises(solver.MpqpError) as e:
+        solver.unpack_lp(bad)
+    assert e.value.code == solver.ELAYOUT
+    bad = dict(d, A0=np.asfortranarray(d["A0"] + 1.0))
+    with pytest.raises(solver.MpqpError) as e:
+        solver.unpack_lp(bad)
+    assert e.value.code == solver.ELAYOUT
