@@ -147,6 +147,10 @@ typedef struct {
     long long candidates, pruned, feasible, optimal, regions;
     long long lp1_pivots, lp2_pivots, cheb_pivots, fallback_lp1, fallback_opt;
     long long stored;             /* LP1 tableaus kept for warm starts      */
+    /* order-independent digests of the feasible / optimal / region sets:
+     * sum mod 2^64 of a 64-bit hash of each set's mask (equal digests =
+     * equal sets, up to hash collisions) */
+    unsigned long long feasible_digest, optimal_digest, region_digest;
     int last_level, truncated;
 } mpqp_inst_stats;
 
@@ -160,7 +164,7 @@ typedef struct {
     long long n_opt;
     mpqp_opt_set *opt;            /* n_opt, sorted (inst, level, mask)      */
     long long n_rec;
-    void *rec;                    /* n_rec records (96 bytes each) or NULL  */
+    void *rec;                    /* n_rec records (104 bytes each) or NULL */
     long long h2d_bytes;          /* problem data uploaded by the plan      */
     long long d2h_bytes;          /* result bytes copied back               */
 } mpqp_batch_result;

@@ -68,10 +68,15 @@ void set_error_text(const char *msg) { set_err(msg ? msg : ""); }
 // ---------------------------------------------------------------------
 struct Prepared {
     InstDesc d;
-    std::vector<double> Wm, Wh, wc, At, bt, QiAT, QiH, Qic, root;
+    std::vector<double> Wm, Wh, wc, At, bt, QiAT, QiH, Qic;
+    std::vector<double> root;    // LP1 root tableau, FP64 stride ld1d
+    std::vector<double> root_f;  // the same values at the plan's stride ld1 (FP32 copy)
 };
 
 static inline int odd_up(int x) { return (x & 1) ? x : x + 1; }
+// smallest y >= x with y = 4 (mod 8): FP32 rows 16-byte aligned and
+// conflict-free for 128-bit shared-memory accesses
+static inline int four_mod8_up(int x) { int y = (x + 3) & ~3; return (y & 4) ? y : y + 4; }
 
 static void fwd_sub(const double *L, int n, const double *rhs, int rs, double *y, int ys)
 {
@@ -91,7 +96,7 @@ static void bwd_sub(const double *L, int n, const double *y, int ysd, double *x,
     }
 }
 
-static int prepare_instance(const mpqp_problem &P, Prepared &out)
+static int prepare_instance(const mpqp_problem &P, Prepared &out, int prec)
 {
     const int n = P.n, m = P.m, p = P.p, ncp = P.ncp;
     if (n < 1 || m < 1 || p < 1 || ncp < 1 || m > kMaxM || p > kMaxP) {
@@ -118,8 +123,10 @@ static int prepare_instance(const mpqp_problem &P, Prepared &out)
     memset(&d, 0, sizeof(d));
     d.n = n; d.m = m; d.p = p; d.ncp = ncp;
     d.M1 = m + ncp; d.nv = n + p;
-    d.ld1 = odd_up(d.nv + 1);
-    d.ld2 = odd_up(p + 2);
+    d.ld1d = odd_up(d.nv + 1);
+    d.ld2d = odd_up(p + 2);
+    d.ld1 = prec == PREC_MIXED ? four_mod8_up(d.nv + 1) : d.ld1d;
+    d.ld2 = prec == PREC_MIXED ? four_mod8_up(p + 2) : d.ld2d;
     d.k_min = P.k_min < 0 ? 0 : P.k_min;
     d.k_max = kmax;
     d.tab_elems = ((d.M1 + 1) * d.ld1 + 3) & ~3;
@@ -167,17 +174,20 @@ static int prepare_instance(const mpqp_problem &P, Prepared &out)
     bwd_sub(L.data(), n, u.data(), 1, out.Qic.data(), 1);
     out.At.assign(P.At, P.At + (size_t)ncp * p);
     out.bt.assign(P.bt, P.bt + ncp);
-    const int ld = d.ld1;
-    out.root.assign((size_t)d.tab_elems, 0.0);
-    for (int i = 0; i < m; i++) {
-        for (int j = 0; j < n; j++) out.root[i * ld + j] = P.A[i * n + j];
-        for (int j = 0; j < p; j++) out.root[i * ld + n + j] = -P.F[i * p + j];
-        out.root[i * ld + d.nv] = P.b[i];
-    }
-    for (int i = 0; i < ncp; i++) {
-        for (int j = 0; j < p; j++) out.root[(m + i) * ld + n + j] = P.At[i * p + j];
-        out.root[(m + i) * ld + d.nv] = P.bt[i];
-    }
+    auto fill_root = [&](std::vector<double> &root, int ld) {
+        root.assign(((size_t)(d.M1 + 1) * ld + 3) & ~(size_t)3, 0.0);
+        for (int i = 0; i < m; i++) {
+            for (int j = 0; j < n; j++) root[i * ld + j] = P.A[i * n + j];
+            for (int j = 0; j < p; j++) root[i * ld + n + j] = -P.F[i * p + j];
+            root[i * ld + d.nv] = P.b[i];
+        }
+        for (int i = 0; i < ncp; i++) {
+            for (int j = 0; j < p; j++) root[(m + i) * ld + n + j] = P.At[i * p + j];
+            root[(m + i) * ld + d.nv] = P.bt[i];
+        }
+    };
+    fill_root(out.root, d.ld1d);
+    fill_root(out.root_f, d.ld1);
     return MPQP_OK;
 }
 
@@ -228,8 +238,8 @@ extern "C" void mpqp_default_options(mpqp_options *o)
     o->tol_piv32 = 1e-6;
     o->tol_dj32 = 1e-6;
     o->margin_z = 1e-3;
-    o->margin_beta = 1e-3;
-    o->margin_t = 3e-5;   // x (row magnitude / pivot ratio) x (1 + p |theta|max)
+    o->margin_beta = 3e-5;   // x max(1, max |T_ij|) of the final FP32 LP1 tableau
+    o->margin_t = 1e-5;   // x (row magnitude / pivot ratio) x (1 + p |theta|max)
     o->margin_licq = 1e-3;
     o->tol_zero_row = 1e-12;
 }
@@ -363,7 +373,7 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
     // host precompute
     std::vector<Prepared> prep(n_inst);
     for (int i = 0; i < n_inst; i++) {
-        int rc = prepare_instance(probs[i], prep[i]);
+        int rc = prepare_instance(probs[i], prep[i], P->prec);
         if (rc) { set_err("instance " + std::to_string(i) + ": " + g_err); delete P; return rc; }
     }
     // pools
@@ -376,7 +386,7 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
         return off;
     };
     SlotDims &sd = P->sd;
-    sd = SlotDims{0, 0, 0, 1, 0, 0, 0};
+    sd = SlotDims{0, 0, 0, 1, 0, 0, 0, 0, 0};
     long long tab_tot0 = 0, ids_tot0 = 0;
     size_t max_tab_bytes = 0;
     for (int i = 0; i < n_inst; i++) {
@@ -386,7 +396,7 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
         d.o_At = put(dp, pr.At); d.o_bt = put(dp, pr.bt); d.o_QiAT = put(dp, pr.QiAT);
         d.o_QiH = put(dp, pr.QiH); d.o_Qic = put(dp, pr.Qic); d.o_root = put(dp, pr.root);
         d.f_Wm = put(fp, pr.Wm); d.f_Wh = put(fp, pr.Wh); d.f_wc = put(fp, pr.wc);
-        d.f_At = put(fp, pr.At); d.f_bt = put(fp, pr.bt); d.f_root = put(fp, pr.root);
+        d.f_At = put(fp, pr.At); d.f_bt = put(fp, pr.bt); d.f_root = put(fp, pr.root_f);
         P->desc.push_back(d);
         P->kmax = std::max(P->kmax, d.k_max);
         sd.maxM1 = std::max(sd.maxM1, d.M1);
@@ -396,6 +406,8 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
         sd.maxP1 = std::max(sd.maxP1, d.p + 1);
         sd.maxR2 = std::max(sd.maxR2, d.m + d.ncp);
         sd.maxLD2 = std::max(sd.maxLD2, d.ld2);
+        sd.maxLD1d = std::max(sd.maxLD1d, d.ld1d);
+        sd.maxLD2d = std::max(sd.maxLD2d, d.ld2d);
         tab_tot0 += d.tab_elems;
         ids_tot0 += d.ids_bytes;
         max_tab_bytes = std::max(max_tab_bytes, (size_t)d.tab_elems * (P->prec == PREC_MIXED ? 4 : 8));
@@ -640,6 +652,8 @@ extern "C" int mpqp_plan_results(mpqp_plan *P, mpqp_batch_result **out)
         s.optimal = ic[i].optimal; s.regions = ic[i].region; s.lp1_pivots = ic[i].lp1_piv;
         s.lp2_pivots = ic[i].lp2_piv; s.cheb_pivots = ic[i].cheb_piv; s.fallback_lp1 = ic[i].fb_lp1;
         s.fallback_opt = ic[i].fb_opt; s.stored = ic[i].stored;
+        s.feasible_digest = ic[i].feas_digest; s.optimal_digest = ic[i].opt_digest;
+        s.region_digest = ic[i].reg_digest;
         s.last_level = ic[i].last_level; s.truncated = ic[i].truncated;
         nlev = std::max(nlev, ic[i].last_level + 1);
     }

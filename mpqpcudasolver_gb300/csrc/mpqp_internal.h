@@ -42,7 +42,7 @@ struct Tol {
     float tol_piv32;
     float tol_dj32;
     double margin_z;    // FP32 LP1 z above this -> infeasible without FP64
-    double margin_beta; // FP32 basic slacks above this certify feasibility
+    double margin_beta; // FP32 basic slacks above margin_beta * max(1, tableau growth) certify feasibility
     double margin_t;    // FP32 LP2 t below -margin_t * error scale -> not optimal without FP64
     double margin_licq; // FP32 Cholesky pivot ratio below this -> FP64
     double tol_zero_row;// region row is zero when max|g| <= tol_zero_row * max(1, |h|)
@@ -50,7 +50,9 @@ struct Tol {
 
 struct InstDesc {
     int n, m, p, ncp;
-    int M1, nv, ld1, ld2;       // LP1 rows, LP1 free vars, tableau strides (odd)
+    int M1, nv;                 // LP1 rows, LP1 free variables
+    int ld1, ld2;               // strides of the plan's LP1 / LP2 tableaus (FP32: = 4 mod 8, FP64: odd)
+    int ld1d, ld2d;             // strides of the FP64 re-solve tableaus (odd)
     int k_min, k_max;
     int tab_elems;              // (M1+1)*ld1 rounded up to a multiple of 4
     int ids_bytes;              // M1 + nv rounded up to 16
@@ -92,6 +94,8 @@ struct CandRec {                // identical field layout to the oracle's record
     int32_t lp2_status, lp2_pivots, cheb_status, cheb_pivots;
     double t, r;
     int32_t inst, fp64;         // instance; bit0 LP1 / bit1 LP2 decided in FP64
+    float lp1_growth;           // FP32 LP1: max |T_ij| of the final tableau (mixed precision)
+    float lp1_minbeta;          // FP32 LP1: smallest basic slack value
 };
 
 struct HashSlot { uint64_t lo, hi; int inst; int tag; int val; int pad; };
@@ -105,6 +109,8 @@ struct InstCtl {
     long long lp1_piv, lp2_piv, cheb_piv;
     long long fb_lp1, fb_opt;   // FP64 fallbacks (mixed precision)
     long long stored;           // LP1 tableaus written for the next level
+    // order-independent digests (sum mod 2^64 of a 64-bit hash of each mask)
+    unsigned long long feas_digest, opt_digest, reg_digest;
     int stopped;                // budget exhausted or max level reached
     int truncated;              // stopped by the budget
     int last_level;
@@ -133,6 +139,7 @@ enum Overflow : int { OV_CAND = 1, OV_NODE = 2, OV_TAB = 4, OV_IDS = 8, OV_OPT =
 struct SlotDims {
     int maxM1, maxLD1, maxNv;       // LP1 tableau
     int maxK, maxP1, maxR2, maxLD2; // KKT factor and LP2 / Chebyshev tableau
+    int maxLD1d, maxLD2d;           // strides of the FP64 re-solve tableaus
 };
 
 struct DevBuffers {

@@ -73,6 +73,12 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x)
     return x;
 }
 
+// hash summed into the per-instance set digests
+__device__ __forceinline__ unsigned long long mask_digest(uint64_t lo, uint64_t hi)
+{
+    return mix64(lo ^ mix64(hi ^ 0x5bd1e9955bd1e995ULL));
+}
+
 __device__ __forceinline__ uint64_t hash_key(int inst, uint64_t lo, uint64_t hi)
 {
     return mix64(lo ^ mix64(hi ^ ((uint64_t)(uint32_t)inst * 0x9e3779b97f4a7c15ULL)));
@@ -118,6 +124,66 @@ struct Lp {
     uint8_t *bid, *nid;
 };
 
+// Order-preserving unsigned images of non-negative values (min over the
+// keys = min over the values); all-ones marks "no candidate".
+__device__ __forceinline__ unsigned key_of(float v) { return __float_as_uint(v); }
+__device__ __forceinline__ unsigned long long key_of(double v) { return (unsigned long long)__double_as_longlong(v); }
+__device__ __forceinline__ unsigned key_none(float) { return 0xffffffffu; }
+__device__ __forceinline__ unsigned long long key_none(double) { return ~0ull; }
+
+// Warp-wide smallest (key, id); returns the winning lane's idx, or -1.  Ids
+// are unique across the warp, so the result does not depend on lane order.
+__device__ __forceinline__ int warp_argmin(unsigned key, unsigned id, int idx)
+{
+    const unsigned kmin = __reduce_min_sync(FULLMASK, key);
+    if (kmin == 0xffffffffu) return -1;
+    const bool m = key == kmin;
+    const unsigned idm = __reduce_min_sync(FULLMASK, m ? id : 0xffffffffu);
+    const unsigned win = __ballot_sync(FULLMASK, m && id == idm);
+    return __shfl_sync(FULLMASK, idx, __ffs(win) - 1);
+}
+
+__device__ __forceinline__ int warp_argmin(unsigned long long key, unsigned id, int idx)
+{
+    const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
+    const unsigned hmin = __reduce_min_sync(FULLMASK, hi);
+    if (hmin == 0xffffffffu) return -1;
+    const unsigned lmin = __reduce_min_sync(FULLMASK, hi == hmin ? lo : 0xffffffffu);
+    const bool m = hi == hmin && lo == lmin;
+    const unsigned idm = __reduce_min_sync(FULLMASK, m ? id : 0xffffffffu);
+    const unsigned win = __ballot_sync(FULLMASK, m && id == idm);
+    return __shfl_sync(FULLMASK, idx, __ffs(win) - 1);
+}
+
+// ratio of the ratio test: IEEE division in FP64 (the oracle's operation);
+// the FP32 pass only needs an ordering, so it takes the fast division.
+__device__ __forceinline__ double ratio_div(double b, double a) { return __ddiv_rn(b, a); }
+__device__ __forceinline__ float ratio_div(float b, float a) { return __fdividef(b, a); }
+
+// T[i][*] -= f * R[*] over columns 0..ncols (the pivot row R is in shared
+// memory); FP32 rows are 16-byte aligned (stride = 4 mod 8) and go four
+// elements per access.
+__device__ __forceinline__ void row_update(double *Ti, const double *R, double nf, int ncols)
+{
+    for (int j = 0; j <= ncols; j++) Ti[j] = xfma(nf, R[j], Ti[j]);
+}
+
+__device__ __forceinline__ void row_update(float *Ti, const float *R, float nf, int ncols)
+{
+    float4 *t4 = reinterpret_cast<float4 *>(Ti);
+    const float4 *r4 = reinterpret_cast<const float4 *>(R);
+    const int nch = (ncols + 4) >> 2;
+    for (int c = 0; c < nch; c++) {
+        float4 t = t4[c];
+        const float4 r = r4[c];
+        t.x = __fmaf_rn(nf, r.x, t.x);
+        t.y = __fmaf_rn(nf, r.y, t.y);
+        t.z = __fmaf_rn(nf, r.z, t.z);
+        t.w = __fmaf_rn(nf, r.w, t.w);
+        t4[c] = t;
+    }
+}
+
 template <typename T>
 __device__ int warp_simplex(const Lp<T> &L, T tol_piv, T tol_dj, int max_piv, int degen_switch, int *piv_out)
 {
@@ -127,30 +193,25 @@ __device__ int warp_simplex(const Lp<T> &L, T tol_piv, T tol_dj, int max_piv, in
     T *obj = L.tab + (size_t)L.nrows * L.ld;
     for (;;) {
         // pricing: largest |reduced cost|, smallest id on ties (Bland: smallest id)
-        T bs = T(0);
-        int bidv = 0x7fffffff, bq = -1;
+        auto bkey = key_none(T(0));
+        unsigned bid_ = 0xffffffffu;
+        int bq = -1;
         for (int j = lane; j < L.ncols; j += 32) {
             const T g = obj[j];
             const int id = L.nid[j];
-            const T s = (id < L.nfree) ? xabs(g) : g;
-            if (!(s > tol_dj)) continue;
-            const bool better = (bq < 0) || (bland ? id < bidv : (s > bs || (s == bs && id < bidv)));
-            if (better) { bs = s; bidv = id; bq = j; }
+            const T sc = (id < L.nfree) ? xabs(g) : g;
+            if (!(sc > tol_dj)) continue;
+            const auto k = bland ? decltype(bkey)(0) : ~key_of(sc);
+            if (bq < 0 || k < bkey || (k == bkey && (unsigned)id < bid_)) { bkey = k; bid_ = id; bq = j; }
         }
-#pragma unroll
-        for (int off = 16; off; off >>= 1) {
-            const T os = __shfl_xor_sync(FULLMASK, bs, off);
-            const int oid = __shfl_xor_sync(FULLMASK, bidv, off);
-            const int oq = __shfl_xor_sync(FULLMASK, bq, off);
-            const bool better = (oq >= 0) && ((bq < 0) || (bland ? oid < bidv : (os > bs || (os == bs && oid < bidv))));
-            if (better) { bs = os; bidv = oid; bq = oq; }
-        }
-        if (bq < 0) { status = LP_OPTIMAL; break; }
-        const int q = bq;
+        const int q = warp_argmin(bkey, bid_, bq);
+        if (q < 0) { status = LP_OPTIMAL; break; }
         const T sg = obj[q] > T(0) ? T(1) : T(-1);
         // ratio test: smallest max(beta,0)/a over a > tol_piv, smallest id on ties
-        T br = T(0);
-        int brid = 0x7fffffff, bri = -1;
+        auto rkey = key_none(T(0));
+        unsigned rid = 0xffffffffu;
+        int bri = -1;
+        T rval = T(0);
         for (int i = lane; i < L.nrows; i += 32) {
             const int id = L.bid[i];
             if (id < L.nfree) continue;
@@ -158,21 +219,17 @@ __device__ int warp_simplex(const Lp<T> &L, T tol_piv, T tol_dj, int max_piv, in
             if (!(a > tol_piv)) continue;
             T beta = L.tab[(size_t)i * L.ld + L.ncols];
             if (!(beta > T(0))) beta = T(0);
-            const T ratio = xdiv(beta, a);
-            const bool better = (bri < 0) || ratio < br || (ratio == br && id < brid);
-            if (better) { br = ratio; brid = id; bri = i; }
+            const T ratio = ratio_div(beta, a);
+            const auto k = key_of(ratio);
+            if (bri < 0 || k < rkey || (k == rkey && (unsigned)id < rid)) { rkey = k; rid = id; bri = i; rval = ratio; }
         }
-#pragma unroll
-        for (int off = 16; off; off >>= 1) {
-            const T orr = __shfl_xor_sync(FULLMASK, br, off);
-            const int oid = __shfl_xor_sync(FULLMASK, brid, off);
-            const int oi = __shfl_xor_sync(FULLMASK, bri, off);
-            const bool better = (oi >= 0) && ((bri < 0) || orr < br || (orr == br && oid < brid));
-            if (better) { br = orr; brid = oid; bri = oi; }
-        }
-        if (bri < 0) { status = LP_UNBOUNDED; break; }
+        const int r = warp_argmin(rkey, rid, bri);
+        if (r < 0) { status = LP_UNBOUNDED; break; }
         if (piv >= max_piv) { status = LP_ITER_LIMIT; break; }
-        const int r = bri;
+        // the chosen ratio, recomputed identically in every lane (degeneracy test)
+        T br = L.tab[(size_t)r * L.ld + L.ncols];
+        if (!(br > T(0))) br = T(0);
+        const T rr = ratio_div(br, sg * L.tab[(size_t)r * L.ld + q]);
         T *R = L.tab + (size_t)r * L.ld;
         const T inv = xdiv(T(1), R[q]);
         __syncwarp();
@@ -181,9 +238,8 @@ __device__ int warp_simplex(const Lp<T> &L, T tol_piv, T tol_dj, int max_piv, in
         for (int i = lane; i <= L.nrows; i += 32) {
             if (i == r) continue;
             T *Ti = L.tab + (size_t)i * L.ld;
-            const T f = Ti[q];
-            const T nf = -f;
-            for (int j = 0; j <= L.ncols; j++) Ti[j] = xfma(nf, R[j], Ti[j]);
+            const T nf = -Ti[q];
+            row_update(Ti, R, nf, L.ncols);
             Ti[q] = xmul(nf, inv);
         }
         __syncwarp();
@@ -194,7 +250,8 @@ __device__ int warp_simplex(const Lp<T> &L, T tol_piv, T tol_dj, int max_piv, in
         }
         __syncwarp();
         piv++;
-        degen = (br == T(0)) ? degen + 1 : 0;
+        (void)rval;
+        degen = (rr == T(0)) ? degen + 1 : 0;
         bland = degen >= degen_switch;
     }
     *piv_out = piv;
@@ -210,7 +267,7 @@ __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t
 template <typename T>
 __host__ __device__ inline size_t lp1_slot_bytes(int maxM1, int maxLD1, int maxNv)
 {
-    return align16((size_t)(maxM1 + 1) * maxLD1 * sizeof(T)) + align16((size_t)maxM1 + maxNv);
+    return align16((((size_t)(maxM1 + 1) * maxLD1 + 3) & ~(size_t)3) * sizeof(T)) + align16((size_t)maxM1 + maxNv);
 }
 
 // optimality slot: R (kmax^2), Y and Lambda (kmax x P1), G (R2 x P1),
@@ -333,12 +390,24 @@ __device__ __forceinline__ void warp_copy(TD *dst, const TS *src, int n)
     for (int e = lane_id(); e < n; e += 32) dst[e] = (TD)src[e];
 }
 
+// 16-byte vector copy of n elements (n a multiple of 4 elements, both ends
+// 16-byte aligned: tableau offsets are multiples of 4 elements).
+template <typename T>
+__device__ __forceinline__ void warp_copy_v(T *dst, const T *src, int n)
+{
+    const int n4 = n * (int)sizeof(T) / 16;
+    const int4 *s4 = reinterpret_cast<const int4 *>(src);
+    int4 *d4 = reinterpret_cast<int4 *>(dst);
+    for (int e = lane_id(); e < n4; e += 32) d4[e] = s4[e];
+}
+
 // Append a feasible (or, exhaustive, any) candidate as a node of `side`;
 // stores its tableau when it can have children.  Returns the node index or -1.
+// src_ld: row stride of `tab` (0: the plan's stride, copied as is).
 template <typename TT, typename TS>
 __device__ long long store_node(const DevBuffers &B, int side, int level, const InstDesc &I, int inst,
                                 uint64_t lo, uint64_t hi, bool feasible, const TS *tab, const uint8_t *ids,
-                                long long rec)
+                                long long rec, int src_ld = 0)
 {
     const int lane = lane_id();
     Ctl *ctl = B.ctl;
@@ -373,7 +442,16 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
     if (need_tab) {
         if (lane == 0) atomicAdd((unsigned long long *)&B.ictl[inst].stored, 1ull);
         TT *dst = (TT *)B.tab[side] + toff;
-        warp_copy<TS, TT>(dst, tab, (I.M1 + 1) * I.ld1);
+        if (src_ld == 0) {
+            warp_copy_v<TT>(dst, (const TT *)tab, I.tab_elems);
+        } else {
+            // re-stride (and convert) row by row; padding columns become 0
+            const int ncol = I.nv + 1;
+            for (int e = lane; e < I.tab_elems; e += 32) {
+                const int i = e / I.ld1, j = e - i * I.ld1;
+                dst[e] = (i <= I.M1 && j < ncol) ? (TT)tab[(size_t)i * src_ld + j] : TT(0);
+            }
+        }
         uint8_t *di = B.ids[side] + ioff;
         for (int e = lane; e < I.M1 + I.nv; e += 32) di[e] = ids[e];
     }
@@ -402,10 +480,11 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
-    const size_t slot = lp1_slot_bytes<T>(sd.maxM1, sd.maxLD1, sd.maxNv);
+    const int mld = sizeof(T) == 4 ? sd.maxLD1 : sd.maxLD1d;
+    const size_t slot = lp1_slot_bytes<T>(sd.maxM1, mld, sd.maxNv);
     unsigned char *base = smem + wib * slot;
     T *tab = (T *)base;
-    uint8_t *ids = base + align16((size_t)(sd.maxM1 + 1) * sd.maxLD1 * sizeof(T));
+    uint8_t *ids = base + align16((((size_t)(sd.maxM1 + 1) * mld + 3) & ~(size_t)3) * sizeof(T));
     const int side = level & 1, pside = side ^ 1;
     Ctl *ctl = B.ctl;
     const long long ncand = ctl->n_cand;
@@ -434,12 +513,13 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
             if (lc.inst >= 0 && lane == 0) {
                 atomicAdd((unsigned long long *)&B.ictl[lc.inst].feasible, (unsigned long long)lc.a);
                 atomicAdd((unsigned long long *)&B.ictl[lc.inst].lp1_piv, (unsigned long long)lc.b);
+                atomicAdd(&B.ictl[lc.inst].feas_digest, (unsigned long long)lc.c);
             }
             lc.reset(inst);
         }
         const int M1 = I.M1, nv = I.nv, ld = I.ld1;
-        // stage the parent tableau and basis
-        warp_copy<T, T>(tab, (const T *)B.tab[pside] + par.tab_off, (M1 + 1) * ld);
+        // stage the parent tableau and basis (16-byte vector loads)
+        warp_copy_v<T>(tab, (const T *)B.tab[pside] + par.tab_off, I.tab_elems);
         const uint8_t *sid = B.ids[pside] + par.ids_off;
         for (int e = lane; e < M1 + nv; e += 32) ids[e] = sid[e];
         __syncwarp();
@@ -464,6 +544,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         uint64_t lo = par.lo, hi = par.hi;
         if (c.j < 64) lo |= 1ull << c.j; else hi |= 1ull << (c.j - 64);
         bool feasible = false, decided = true;
+        float lp1_growth = 0.0f, lp1_minbeta = 0.0f;
         if (!mixed) {
             feasible = (st == LP_OPTIMAL) && ((double)z <= tol.tol_feas);
         } else {
@@ -473,20 +554,29 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
                 // certificate: every slack of S nonbasic and every basic slack
                 // clearly positive -> the basic solution is a feasible point
                 // with all rows of S tight.
+                // The FP32 errors of the basic values grow with the tableau's
+                // element growth (max |T_ij| ~ |B^-1 N|), so the margin does too.
                 bool s_basic = false;
-                T minb = pos_inf<T>();
+                T minb = pos_inf<T>(), gmax = T(1);
                 for (int i = lane; i < M1; i += 32) {
+                    const T *Ti = tab + (size_t)i * ld;
+                    for (int j = 0; j < nv; j++) { const T a = xabs(Ti[j]); if (a > gmax) gmax = a; }
                     const int id = bid[i];
                     if (id < nv) continue;
                     const int ci = id - nv;
                     if (ci < I.m && mask_has(lo, hi, ci)) s_basic = true;
-                    const T bb = tab[(size_t)i * ld + nv];
+                    const T bb = Ti[nv];
                     if (bb < minb) minb = bb;
                 }
                 s_basic = __any_sync(FULLMASK, s_basic);
 #pragma unroll
-                for (int off = 16; off; off >>= 1) { const T o = __shfl_xor_sync(FULLMASK, minb, off); if (o < minb) minb = o; }
-                if (!s_basic && (double)minb > tol.margin_beta) feasible = true;
+                for (int off = 16; off; off >>= 1) {
+                    const T o = __shfl_xor_sync(FULLMASK, minb, off); if (o < minb) minb = o;
+                    const T g = __shfl_xor_sync(FULLMASK, gmax, off); if (g > gmax) gmax = g;
+                }
+                lp1_growth = (float)gmax;
+                lp1_minbeta = (float)minb;
+                if (!s_basic && (double)minb > tol.margin_beta * (double)gmax) feasible = true;
                 else decided = false;
             }
         }
@@ -499,6 +589,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
             R.lp2_status = LP_SKIPPED; R.lp2_pivots = 0; R.cheb_status = LP_SKIPPED; R.cheb_pivots = 0;
             R.t = __longlong_as_double(0x7ff8000000000000LL); R.r = R.t;
             R.inst = inst; R.fp64 = decided ? (mixed ? 0 : 1) : 0;
+            R.lp1_growth = lp1_growth; R.lp1_minbeta = lp1_minbeta;
         }
         if (!decided) {
             if (lane == 0) {
@@ -507,13 +598,14 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
             }
             continue;
         }
-        if (feasible) lc.a++;
+        if (feasible) { lc.a++; lc.c += (long long)mask_digest(lo, hi); }
         if (feasible || B.exhaustive)
             store_node<T, T>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec);
     }
     if (lc.inst >= 0 && lane == 0) {
         atomicAdd((unsigned long long *)&B.ictl[lc.inst].feasible, (unsigned long long)lc.a);
         atomicAdd((unsigned long long *)&B.ictl[lc.inst].lp1_piv, (unsigned long long)lc.b);
+        atomicAdd(&B.ictl[lc.inst].feas_digest, (unsigned long long)lc.c);
     }
 }
 
@@ -524,10 +616,10 @@ __global__ void __launch_bounds__(128) k_lp1_fp64(DevBuffers B, Tol tol, SlotDim
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
-    const size_t slot = lp1_slot_bytes<double>(sd.maxM1, sd.maxLD1, sd.maxNv);
+    const size_t slot = lp1_slot_bytes<double>(sd.maxM1, sd.maxLD1d, sd.maxNv);
     unsigned char *base = smem + wib * slot;
     double *tab = (double *)base;
-    uint8_t *ids = base + align16((size_t)(sd.maxM1 + 1) * sd.maxLD1 * sizeof(double));
+    uint8_t *ids = base + align16((((size_t)(sd.maxM1 + 1) * sd.maxLD1d + 3) & ~(size_t)3) * sizeof(double));
     const int side = level & 1, pside = side ^ 1;
     Ctl *ctl = B.ctl;
     const long long nq = ctl->n_q_lp1 < B.q_cap ? ctl->n_q_lp1 : B.q_cap;
@@ -541,7 +633,7 @@ __global__ void __launch_bounds__(128) k_lp1_fp64(DevBuffers B, Tol tol, SlotDim
         const Node par = B.node[pside][c.parent];
         const int inst = par.inst;
         const InstDesc &I = B.inst[inst];
-        const int M1 = I.M1, nv = I.nv, ld = I.ld1;
+        const int M1 = I.M1, nv = I.nv, ld = I.ld1d;
         uint64_t lo = par.lo, hi = par.hi;
         if (c.j < 64) lo |= 1ull << c.j; else hi |= 1ull << (c.j - 64);
         const double *root = B.dpool + I.o_root;
@@ -567,14 +659,17 @@ __global__ void __launch_bounds__(128) k_lp1_fp64(DevBuffers B, Tol tol, SlotDim
         if (lane == 0) {
             atomicAdd((unsigned long long *)&B.ictl[inst].fb_lp1, 1ull);
             atomicAdd((unsigned long long *)&B.ictl[inst].lp1_piv, (unsigned long long)piv);
-            if (feasible) atomicAdd((unsigned long long *)&B.ictl[inst].feasible, 1ull);
+            if (feasible) {
+                atomicAdd((unsigned long long *)&B.ictl[inst].feasible, 1ull);
+                atomicAdd(&B.ictl[inst].feas_digest, mask_digest(lo, hi));
+            }
             if (rec >= 0) {
                 CandRec &R = B.rec[rec];
                 R.lp1_status = st; R.lp1_pivots += piv; R.z = z; R.feasible = feasible; R.fp64 |= 1;
             }
         }
         if (feasible || B.exhaustive)
-            store_node<float, double>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec);
+            store_node<float, double>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, I.ld1d);
     }
 }
 
@@ -628,7 +723,7 @@ struct OptWs {
         Y = (T *)(base + o); o += align16((size_t)sd.maxK * sd.maxP1 * sizeof(T));
         Lam = (T *)(base + o); o += align16((size_t)sd.maxK * sd.maxP1 * sizeof(T));
         G = (T *)(base + o); o += align16((size_t)sd.maxR2 * sd.maxP1 * sizeof(T));
-        Tb = (T *)(base + o); o += align16((size_t)(sd.maxR2 + 1) * sd.maxLD2 * sizeof(T));
+        Tb = (T *)(base + o); o += align16((size_t)(sd.maxR2 + 1) * (sizeof(T) == 4 ? sd.maxLD2 : sd.maxLD2d) * sizeof(T));
         ids = base + o; o += align16((size_t)sd.maxR2 + sd.maxP1);
         S = (int *)(base + o);
     }
@@ -693,24 +788,26 @@ __device__ int kkt_factor(const KktData<T> &D, const InstDesc &I, uint64_t lo, u
 // Region rows in the reference order (utils.py:39-57): lambda rows (S
 // order), inactive rows (ascending), parameter box rows.  G is R2 x (p+1),
 // each row [g | h] meaning g theta <= h.
-// track = true also returns the largest absolute row sum
-// |h| + sum_c (|Wh_ic| + sum_l |Wm_i,S_l| |Lambda_l,c|), the scale of the
-// rounding error of the FP32 rows (warp-uniform result).
+// track = true also returns a bound on the magnitude of the terms summed
+// into any row, max_i (sum_c |Wh_ic| + |wc_i| + sum_l |Wm_i,S_l| |Lambda_l|_1),
+// the scale of the FP32 rounding error of the rows (warp-uniform result).
 template <typename T, bool track = false>
 __device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, uint64_t hi, int k, OptWs<T> &ws)
 {
-    T amax = T(0);
     const int lane = lane_id();
     const int m = I.m, p = I.p, ncp = I.ncp, P1 = p + 1;
     const int *S = ws.S;
     const T *Lam = ws.Lam;
     T *G = ws.G;
+    T amax = T(0);
+    T *labs = ws.Y;   // |Lambda_l|_1, Y is free once Lambda is known
     for (int a = lane; a < k; a += 32) {
         T rs = T(0);
         for (int cc = 0; cc < p; cc++) { G[a * P1 + cc] = Lam[a * P1 + cc]; if (track) rs += xabs(Lam[a * P1 + cc]); }
         G[a * P1 + p] = -Lam[a * P1 + p];
-        if (track) { rs += xabs(Lam[a * P1 + p]); if (rs > amax) amax = rs; }
+        if (track) { rs += xabs(Lam[a * P1 + p]); labs[a] = rs; if (rs > amax) amax = rs; }
     }
+    if (track) __syncwarp();
     for (int i = lane; i < m; i += 32) {
         if (mask_has(lo, hi, i)) continue;
         const int pos = k + i - mask_rank(lo, hi, i);
@@ -718,22 +815,18 @@ __device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, ui
         T rs = T(0);
         for (int cc = 0; cc < p; cc++) {
             T acc = -D.Wh[(size_t)i * p + cc];
-            T ab = xabs(acc);
-            for (int l = 0; l < k; l++) {
-                acc = xfma(wmi[S[l]], Lam[l * P1 + cc], acc);
-                if (track) ab += xabs(wmi[S[l]] * Lam[l * P1 + cc]);
-            }
+            if (track) rs += xabs(acc);
+            for (int l = 0; l < k; l++) acc = xfma(wmi[S[l]], Lam[l * P1 + cc], acc);
             G[pos * P1 + cc] = acc;
-            rs += ab;
         }
         T acc = D.wc[i];
-        T ab = xabs(acc);
-        for (int l = 0; l < k; l++) {
-            acc = xfma(-wmi[S[l]], Lam[l * P1 + p], acc);
-            if (track) ab += xabs(wmi[S[l]] * Lam[l * P1 + p]);
+        if (track) {
+            rs += xabs(acc);
+            for (int l = 0; l < k; l++) rs = xfma(xabs(wmi[S[l]]), labs[l], rs);
+            if (rs > amax) amax = rs;
         }
+        for (int l = 0; l < k; l++) acc = xfma(-wmi[S[l]], Lam[l * P1 + p], acc);
         G[pos * P1 + p] = acc;
-        if (track) { rs += ab; if (rs > amax) amax = rs; }
     }
     for (int ii = lane; ii < ncp; ii += 32) {
         for (int cc = 0; cc < p; cc++) G[(m + ii) * P1 + cc] = D.At[ii * p + cc];
@@ -754,7 +847,8 @@ __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const 
                                      OptWs<T> &ws)
 {
     const int lane = lane_id();
-    const int m = I.m, p = I.p, ncp = I.ncp, P1 = p + 1, R2 = m + ncp, ld2 = I.ld2;
+    const int m = I.m, p = I.p, ncp = I.ncp, P1 = p + 1, R2 = m + ncp;
+    const int ld2 = sizeof(T) == 4 ? I.ld2 : I.ld2d;
     const KktData<T> D = kkt_data<T>(B, I);
     OptResult res;
     res.licq = 1; res.lp2_status = LP_SKIPPED; res.lp2_piv = 0; res.cheb_status = LP_SKIPPED; res.cheb_piv = 0;
@@ -779,10 +873,11 @@ __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const 
     for (int off = 16; off; off >>= 1) { const T o = __shfl_xor_sync(FULLMASK, t0, off); if (o < t0) t0 = o; }
     T *Tb = ws.Tb;
     uint8_t *bid = ws.ids, *nid = ws.ids + R2;
+    T g0 = T(1);   // largest initial |entry| (growth reference of the FP32 screen)
     for (int r = lane; r < R2; r += 32) {
         T *tr = Tb + (size_t)r * ld2;
         const T *g = G + (size_t)r * P1;
-        for (int cc = 0; cc < p; cc++) tr[cc] = g[cc];
+        for (int cc = 0; cc < p; cc++) { tr[cc] = g[cc]; if (screen) { const T a = xabs(g[cc]); if (a > g0) g0 = a; } }
         const T cf = (r < m) ? T(1) : T(0);
         tr[p] = cf;
         T beta = xfma(-cf, t0, g[p]);
@@ -812,7 +907,17 @@ __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const 
             for (int ii = lane; ii < ncp; ii += 32) { const T v = xabs(D.bt[ii]); if (v > bmax) bmax = v; }
 #pragma unroll
             for (int off = 16; off; off >>= 1) { const T o = __shfl_xor_sync(FULLMASK, bmax, off); if (o > bmax) bmax = o; }
-            const double scale = (double)amax / (double)rho * (1.0 + (double)p * (double)bmax);
+            // element growth of the FP32 LP2 tableau: max |final| / max |initial|
+            T g2 = T(0);
+            for (int r = lane; r < R2; r += 32)
+                for (int cc = 0; cc < P1; cc++) { const T a = xabs(Tb[(size_t)r * ld2 + cc]); if (a > g2) g2 = a; }
+#pragma unroll
+            for (int off = 16; off; off >>= 1) {
+                const T o = __shfl_xor_sync(FULLMASK, g2, off); if (o > g2) g2 = o;
+                const T q0 = __shfl_xor_sync(FULLMASK, g0, off); if (q0 > g0) g0 = q0;
+            }
+            const double growth = (double)g2 > (double)g0 ? (double)g2 / (double)g0 : 1.0;
+            const double scale = (double)amax / (double)rho * (1.0 + (double)p * (double)bmax) * growth;
             if (res.t < -tol.margin_t * scale) return res;      // clearly not optimal
             res.decided = false;
             return res;
@@ -886,6 +991,8 @@ __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const 
 __device__ void write_opt(const DevBuffers &B, const Node &nd, int level, const OptResult &res, bool fp64)
 {
     Ctl *ctl = B.ctl;
+    if (res.optimal) atomicAdd(&B.ictl[nd.inst].opt_digest, mask_digest(nd.lo, nd.hi));
+    if (res.region) atomicAdd(&B.ictl[nd.inst].reg_digest, mask_digest(nd.lo, nd.hi));
     if (res.optimal) {
         const long long oi = (long long)atomicAdd((unsigned long long *)&ctl->n_opt, 1ull);
         if (oi < B.opt_cap) {
@@ -914,7 +1021,7 @@ __global__ void __launch_bounds__(128) k_optimality(DevBuffers B, Tol tol, SlotD
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
-    const size_t slot = opt_slot_bytes<T>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2);
+    const size_t slot = opt_slot_bytes<T>(sd.maxK, sd.maxP1, sd.maxR2, sizeof(T) == 4 ? sd.maxLD2 : sd.maxLD2d);
     OptWs<T> ws(smem + wib * slot, sd);
     const int side = level & 1;
     Ctl *ctl = B.ctl;
@@ -967,7 +1074,7 @@ __global__ void __launch_bounds__(128) k_optimality_fp64(DevBuffers B, Tol tol, 
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
-    const size_t slot = opt_slot_bytes<double>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2);
+    const size_t slot = opt_slot_bytes<double>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2d);
     OptWs<double> ws(smem + wib * slot, sd);
     const int side = level & 1;
     Ctl *ctl = B.ctl;
@@ -1009,7 +1116,7 @@ __global__ void k_level0(DevBuffers B)
     for (int i = 0; i < inst; i++) { toff += B.inst[i].tab_elems; ioff += B.inst[i].ids_bytes; }
     T *dst = (T *)B.tab[0] + toff;
     const T *src = pool_of<T>(B) + root_off<T>(I);
-    for (int e = lane; e < (I.M1 + 1) * I.ld1; e += 32) dst[e] = src[e];
+    warp_copy_v<T>(dst, src, I.tab_elems);
     uint8_t *ids = B.ids[0] + ioff;
     for (int i = lane; i < I.M1; i += 32) ids[i] = (uint8_t)(I.nv + i);
     for (int j = lane; j < I.nv; j += 32) ids[I.M1 + j] = (uint8_t)j;
@@ -1027,10 +1134,12 @@ __global__ void k_level0(DevBuffers B)
             R.lp2_status = LP_SKIPPED; R.lp2_pivots = 0; R.cheb_status = LP_SKIPPED; R.cheb_pivots = 0;
             R.t = __longlong_as_double(0x7ff8000000000000LL); R.r = R.t;
             R.inst = inst; R.fp64 = 1;
+            R.lp1_growth = 0.0f; R.lp1_minbeta = 0.0f;
         }
         InstCtl *ic = &B.ictl[inst];
         ic->lvl_cand = 1;
         ic->feasible = 1;
+        ic->feas_digest = mask_digest(0, 0);
         if (inst == 0) {
             long long tt = 0, it = 0;
             for (int i = 0; i < B.n_inst; i++) { tt += B.inst[i].tab_elems; it += B.inst[i].ids_bytes; }
@@ -1107,7 +1216,7 @@ __global__ void __launch_bounds__(128) k_region_laws(DevBuffers B, Tol tol, Slot
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
-    const size_t slot = opt_slot_bytes<double>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2);
+    const size_t slot = opt_slot_bytes<double>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2d);
     OptWs<double> ws(smem + wib * slot, sd);
     const InstDesc &I = B.inst[0];
     const KktData<double> D = kkt_data<double>(B, I);
@@ -1163,7 +1272,7 @@ __global__ void __launch_bounds__(128) k_region_laws(DevBuffers B, Tol tol, Slot
     }
 }
 
-size_t laws_smem_per_warp(const SlotDims &sd) { return opt_slot_bytes<double>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2); }
+size_t laws_smem_per_warp(const SlotDims &sd) { return opt_slot_bytes<double>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2d); }
 
 cudaError_t launch_region_laws(const DevBuffers &B, const Tol &tol, const SlotDims &sd, const uint64_t *masks,
                                long long n_sets, double *laws, int *sizes, long long stride, int grid, size_t smem,
@@ -1178,13 +1287,13 @@ cudaError_t launch_region_laws(const DevBuffers &B, const Tol &tol, const SlotDi
 // ---------------------------------------------------------------------
 size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd)
 {
-    return prec_bytes == 8 ? lp1_slot_bytes<double>(sd.maxM1, sd.maxLD1, sd.maxNv)
+    return prec_bytes == 8 ? lp1_slot_bytes<double>(sd.maxM1, sd.maxLD1d, sd.maxNv)
                            : lp1_slot_bytes<float>(sd.maxM1, sd.maxLD1, sd.maxNv);
 }
 
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd)
 {
-    return prec_bytes == 8 ? opt_slot_bytes<double>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2)
+    return prec_bytes == 8 ? opt_slot_bytes<double>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2d)
                            : opt_slot_bytes<float>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2);
 }
 

@@ -62,6 +62,7 @@ int precompute(const mpqp_problem &P, InstDesc &d, double *pool, size_t pool_cap
     memset(&d, 0, sizeof(d));
     d.n = n; d.m = m; d.p = p; d.ncp = ncp;
     d.M1 = m + ncp; d.nv = n + p; d.ld1 = odd_up(d.nv + 1); d.ld2 = odd_up(p + 2);
+    d.ld1d = d.ld1; d.ld2d = d.ld2;
     size_t o = 0;
     auto take = [&](size_t cnt) { const size_t at = o; o += (cnt + 3) & ~(size_t)3; return (long long)at; };
     d.o_Wm = take((size_t)m * m); d.o_Wh = take((size_t)m * p); d.o_wc = take(m);
@@ -182,6 +183,7 @@ extern "C" int mpqp_region_laws_noalloc(const mpqp_problem *prob, long long n_se
     sd.maxM1 = d.M1; sd.maxLD1 = d.ld1; sd.maxNv = d.nv;
     sd.maxK = kcap < 1 ? 1 : kcap;
     sd.maxP1 = p + 1; sd.maxR2 = m + ncp; sd.maxLD2 = d.ld2;
+    sd.maxLD1d = d.ld1d; sd.maxLD2d = d.ld2d;
     const size_t smem = 4 * laws_smem_per_warp(sd);
     const void *fn = kernel_ptr("laws");
     int sms = 0, nb = 0;

@@ -53,6 +53,7 @@ class InstStats(ctypes.Structure):
     _fields_ = [(nm, ctypes.c_longlong) for nm in ("candidates", "pruned", "feasible", "optimal", "regions",
                                                     "lp1_pivots", "lp2_pivots", "cheb_pivots", "fallback_lp1",
                                                     "fallback_opt", "stored")] + \
+        [(nm, ctypes.c_ulonglong) for nm in ("feasible_digest", "optimal_digest", "region_digest")] + \
         [("last_level", ctypes.c_int), ("truncated", ctypes.c_int)]
 
 
@@ -79,7 +80,8 @@ REC_DTYPE = np.dtype([("mask_lo", "<u8"), ("mask_hi", "<u8"), ("level", "<i4"), 
                       ("lp1_status", "<i4"), ("lp1_pivots", "<i4"), ("z", "<f8"),
                       ("feasible", "<i4"), ("licq", "<i4"), ("optimal", "<i4"), ("region", "<i4"),
                       ("lp2_status", "<i4"), ("lp2_pivots", "<i4"), ("cheb_status", "<i4"),
-                      ("cheb_pivots", "<i4"), ("t", "<f8"), ("r", "<f8"), ("inst", "<i4"), ("fp64", "<i4")])
+                      ("cheb_pivots", "<i4"), ("t", "<f8"), ("r", "<f8"), ("inst", "<i4"), ("fp64", "<i4"),
+                      ("lp1_growth", "<f4"), ("lp1_minbeta", "<f4")])
 
 EXPORTS = ("mpqp", "warm_up", "mpqp_free", "mpqp_unpack_lp", "mpqp_default_options", "mpqp_solve_batch", "mpqp_batch_free",
            "mpqp_plan_create", "mpqp_plan_run", "mpqp_plan_results", "mpqp_plan_launches", "mpqp_plan_destroy",
@@ -203,8 +205,9 @@ class Result:
         return int(self.inst[field].sum())
 
 
-_INST_DTYPE = np.dtype([(f[0], "<i8") for f in InstStats._fields_[:11]] + [("last_level", "<i4"),
-                                                                            ("truncated", "<i4")])
+_INST_DTYPE = np.dtype([(f[0], "<i8") for f in InstStats._fields_[:11]] +
+                       [("feasible_digest", "<u8"), ("optimal_digest", "<u8"), ("region_digest", "<u8"),
+                        ("last_level", "<i4"), ("truncated", "<i4")])
 _OPT_DTYPE = np.dtype([("mask_lo", "<u8"), ("mask_hi", "<u8"), ("inst", "<i4"), ("level", "<i4"), ("t", "<f8"),
                        ("r", "<f8"), ("region", "<i4"), ("fp64", "<i4"), ("rec", "<i8")])
 assert _INST_DTYPE.itemsize == ctypes.sizeof(InstStats)
@@ -342,6 +345,20 @@ def unpack_lp(d: dict):
                             ctypes.byref(ncp))
     _check(rc)
     return out
+
+
+def mask_digest(lo, hi) -> int:
+    """The 64-bit hash the device sums into the set digests."""
+    M = (1 << 64) - 1
+
+    def mix(x):
+        x ^= x >> 33
+        x = (x * 0xff51afd7ed558ccd) & M
+        x ^= x >> 33
+        x = (x * 0xc4ceb9fe1a85ec53) & M
+        x ^= x >> 33
+        return x
+    return mix((int(lo) ^ mix((int(hi) ^ 0x5bd1e9955bd1e995) & M)) & M)
 
 
 def mask_to_set(lo, hi) -> list[int]:

@@ -109,3 +109,35 @@ def test_budget_truncation_matches_oracle(gpu_lib, budget):
         assert int(res.inst["truncated"][0]) == ref.truncated
         assert res.total("feasible") == ref.n_feasible
         assert res.total("regions") == ref.n_region
+
+
+def _digest(sets_lo_hi):
+    return sum(solver.mask_digest(lo, hi) for lo, hi in sets_lo_hi) % (1 << 64)
+
+
+def test_set_digests_match_oracle(gpu_lib):
+    prob = P.scale_problem(P.config2())
+    ref = O.enumerate_sets(prob, k_max=3)
+    for prec in (solver.FP64, solver.MIXED):
+        res = solver.solve([prob], precision=prec, k_max=3, cand_cap=1 << 18, arena_bytes=1 << 28)
+        c = ref.cand
+        for field, dig in (("feasible", "feasible_digest"), ("optimal", "optimal_digest"),
+                           ("region", "region_digest")):
+            want = _digest(zip(c["mask_lo"][c[field] == 1], c["mask_hi"][c[field] == 1]))
+            assert int(res.inst[dig][0]) == want, (prec, field)
+
+
+def test_mixed_equals_fp64_on_the_full_bench_batch(gpu_lib):
+    """Size-independent check at the bench's full size (60.8M candidates,
+    33 instances): identical feasible / optimal / region sets per instance
+    (order-independent 64-bit digests) and identical counts."""
+    probs = [P.scale_problem(p) for p in P.config3(n_extra=32)]
+    kmax = [6] + [p.n for p in probs[1:]]
+    budget = [0] + [1 << 19] * 32
+    r32 = solver.solve(probs, precision=solver.MIXED, k_max=kmax, budget=budget, mem_fraction=0.8)
+    r64 = solver.solve(probs, precision=solver.FP64, k_max=kmax, budget=budget, mem_fraction=0.8)
+    assert r32.status == 0 and r64.status == 0
+    for f in ("candidates", "feasible", "optimal", "regions", "feasible_digest", "optimal_digest", "region_digest",
+              "truncated", "last_level"):
+        assert np.array_equal(r32.inst[f], r64.inst[f]), f
+    assert r32.candidates == 60802277
