@@ -2,7 +2,7 @@
 """Benchmark: candidate active sets checked per second at m = 62.
 
 Workload (one "step" = one full enumeration of it, all levels, one launch
-sequence): the config-3 batch -- a random mpQP with n=12, m=62, p=6 whose
+sequence): the m = 62 batch -- a random mpQP with n=12, m=62, p=6 whose
 candidate active sets of cardinality 0..6 are all checked (54.3M candidates),
 plus 32 random instances (seeds 1..32, n~U{5..15}, m~U{20..80}, p~U{2..6})
 enumerated up to |S| = n under a budget of 2^19 candidates each.  Inputs are
@@ -40,14 +40,14 @@ CPU_SAMPLE_KMAX = 4
 
 def workload():
     from mpqpcudasolver_gb300 import problems as P
-    probs = [P.scale_problem(p) for p in P.config3(n_extra=32)]
+    probs = [P.scale_problem(p) for p in P.m62_batch(n_extra=32)]
     kmax = [MAIN_KMAX] + [p.n for p in probs[1:]]
     budget = [0] + [EXTRA_BUDGET] * (len(probs) - 1)
     return probs, kmax, budget
 
 
 def config_dict(precision: str) -> dict:
-    return {"workload": f"config3: random mpQP n=12 m=62 p=6, all active sets |S|<=6, plus 32 random mpQPs "
+    return {"workload": f"m62 batch: random mpQP n=12 m=62 p=6, all active sets |S|<=6, plus 32 random mpQPs "
                         f"(seeds 1..32, n~U{{5..15}}, m~U{{20..80}}, p~U{{2..6}}) up to |S|=n, budget "
                         f"{EXTRA_BUDGET} candidates each; one launch sequence per step",
             "precision": precision, "instances": 33, "m": 62, "n": 12, "p": 6,
@@ -200,7 +200,7 @@ def cpu_baseline(steps: int = 1, warmup: int = 0) -> dict:
     the main m=62 instance, all candidates with |S| <= 4, every host thread."""
     from mpqpcudasolver_gb300 import problems as P
     from oracle import oracle as O
-    prob = P.scale_problem(P.config3_main())
+    prob = P.scale_problem(P.random_n12_m62_p6())
     threads = os.cpu_count() or 1
     for _ in range(warmup):
         O.enumerate_sets(prob, k_max=CPU_SAMPLE_KMAX, nthreads=threads, keep_records=False)

@@ -1,4 +1,4 @@
-"""Seeded synthetic mpQP generators for the five benchmark workloads.
+"""Seeded synthetic mpQP generators for the benchmark and test workloads.
 
 Every problem has the form used throughout the reference (``main.py:71-80``,
 ``utils.py:147-161``)::
@@ -13,15 +13,17 @@ so a seed fixes the problem bit for bit on every machine.
 
 Workloads (n = #variables, m = #constraints, p = #parameters):
 
-* ``config1``  n=4,  m=10, p=2, seed 0 -- small enough for exhaustive checks.
-* ``config2``  n=10, m=43, p=4.
-* ``config3``  n=12, m=62, p=6 (main instance) plus 32 independent instances
-  (seeds 1..32) with n~U{5..15}, m~U{20..80}, p~U{2..6}.
-* ``config4``  n=16, m=62, p=8, Q = U diag(lambda) U^T with U Haar-random and
-  lambda log-uniform in [1e-2, 1e2]; 20 % of the constraint rows duplicate
-  other rows up to N(0, 1e-12) noise on A, F and b.
-* ``config5``  64 condensed linear-MPC problems (seeds 0..63), horizon 6:
-  n=12, m=72, p=4.
+* ``random_n4_m10_p2``    n=4,  m=10, p=2, seed 0 -- small enough for
+  exhaustive checks (386 active sets with |S| <= 4).
+* ``random_n10_m43_p4``   n=10, m=43, p=4.
+* ``m62_batch``           ``random_n12_m62_p6`` (n=12, m=62, p=6) plus 32
+  ``batch_member`` instances (seeds 1..32) with n~U{5..15}, m~U{20..80},
+  p~U{2..6}: the benchmark batch.
+* ``illcond_n16_m62_p8``  n=16, m=62, p=8, Q = U diag(lambda) U^T with U
+  Haar-random and lambda log-uniform in [1e-2, 1e2]; 20 % of the constraint
+  rows duplicate other rows up to N(0, 1e-12) noise on A, F and b.
+* ``mpc_batch``           64 condensed linear-MPC problems (seeds 0..63),
+  horizon 6: n=12, m=72, p=4.
 """
 from __future__ import annotations
 
@@ -78,7 +80,7 @@ def _box(p: int, half_width: float):
 
 def random_mpqp(n: int, m: int, p: int, seed: int, box: float = 1.0,
                 rng: np.random.Generator | None = None) -> MPQP:
-    """Plain random mpQP (the config-1 generator, reused at other sizes).
+    """Plain random mpQP (the generator of every ``random_*`` workload).
 
     Draw order: M (n x n) N(0,1); c N(0,1); H (n x p) N(0,1); A (m x n) N(0,1)
     with unit-norm rows; b U[1,2] (so the origin is strictly feasible);
@@ -99,34 +101,35 @@ def random_mpqp(n: int, m: int, p: int, seed: int, box: float = 1.0,
     return MPQP(Q, c, H, A, b, F, CRA, CRb, name=f"random(n={n},m={m},p={p},seed={seed})")
 
 
-def config1() -> MPQP:
+def random_n4_m10_p2() -> MPQP:
     return random_mpqp(4, 10, 2, seed=0)
 
 
-def config2() -> MPQP:
+def random_n10_m43_p4() -> MPQP:
     return random_mpqp(10, 43, 4, seed=0)
 
 
-def config3_main() -> MPQP:
+def random_n12_m62_p6() -> MPQP:
     return random_mpqp(12, 62, 6, seed=0)
 
 
-def config3_extra(seed: int) -> MPQP:
-    """Extra config-3 instance: sizes drawn first from the same stream."""
+def batch_member(seed: int) -> MPQP:
+    """One extra instance of the m = 62 batch; its sizes are drawn first from
+    the same stream (n~U{5..15}, m~U{20..80}, p~U{2..6})."""
     rng = np.random.default_rng(seed)
     n = int(rng.integers(5, 16))
     m = int(rng.integers(20, 81))
     p = int(rng.integers(2, 7))
     prob = random_mpqp(n, m, p, seed=seed, rng=rng)
-    prob.name = f"config3-extra(seed={seed},n={n},m={m},p={p})"
+    prob.name = f"batch_member(seed={seed},n={n},m={m},p={p})"
     return prob
 
 
-def config3(n_extra: int = 32) -> list[MPQP]:
-    return [config3_main()] + [config3_extra(s) for s in range(1, n_extra + 1)]
+def m62_batch(n_extra: int = 32) -> list[MPQP]:
+    return [random_n12_m62_p6()] + [batch_member(s) for s in range(1, n_extra + 1)]
 
 
-def config4(seed: int = 0) -> MPQP:
+def illcond_n16_m62_p8(seed: int = 0) -> MPQP:
     """Ill-conditioned Q and near-duplicate constraint rows.
 
     Draw order: Gaussian G (n x n) -> U = QR(G) with the sign fix
@@ -158,7 +161,7 @@ def config4(seed: int = 0) -> MPQP:
     F[dup_rows] = F[src] + rng.normal(0.0, 1e-12, (n_dup, p))
     b[dup_rows] = b[src] + rng.normal(0.0, 1e-12, n_dup)
     CRA, CRb = _box(p, 1.0)
-    return MPQP(Q, c, H, A, b, F, CRA, CRb, name=f"config4(seed={seed})",
+    return MPQP(Q, c, H, A, b, F, CRA, CRb, name=f"illcond_n16_m62_p8(seed={seed})",
                 meta={"dup_rows": dup_rows.tolist(), "dup_src": src.tolist()})
 
 
@@ -208,7 +211,7 @@ def mpc_mpqp(seed: int, horizon: int = 6) -> MPQP:
     return MPQP(Q, c, H, A, b, F, CRA, CRb, name=f"mpc(seed={seed})")
 
 
-def config5(n_instances: int = 64) -> list[MPQP]:
+def mpc_batch(n_instances: int = 64) -> list[MPQP]:
     return [mpc_mpqp(s) for s in range(n_instances)]
 
 
@@ -249,10 +252,10 @@ def scale_problem(prob: MPQP) -> MPQP:
 
 
 WORKLOADS = {
-    "config1": lambda: [config1()],
-    "config2": lambda: [config2()],
-    "config3": config3,
-    "config3_main": lambda: [config3_main()],
-    "config4": lambda: [config4()],
-    "config5": config5,
+    "n4-m10-p2": lambda: [random_n4_m10_p2()],
+    "n10-m43-p4": lambda: [random_n10_m43_p4()],
+    "m62-batch": m62_batch,
+    "n12-m62-p6": lambda: [random_n12_m62_p6()],
+    "illcond-n16-m62-p8": lambda: [illcond_n16_m62_p8()],
+    "mpc-batch": mpc_batch,
 }

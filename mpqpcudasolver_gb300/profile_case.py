@@ -2,8 +2,9 @@
 
     python -m mpqpcudasolver_gb300.profile_case CASE [--precision mixed|fp64] [--runs R]
 
-CASE: config3main-k3 | config3main-k4 | config3main-k5 | config3 (the bench
-batch) | config2-k4 | config4-k3 | config5 (64 MPC instances, |S| <= 3).
+CASE: m62-k3 | m62-k4 | m62-k5 (the n=12, m=62, p=6 instance up to |S| = k)
+| m62-batch (the bench batch) | n10m43p4-k4 | illcond-k3 | mpc-batch (64 MPC
+instances, |S| <= 3).
 Prints one JSON line with the candidates, the device time of the last run
 and the per-kernel times of a timed run.
 """
@@ -18,17 +19,17 @@ from . import solver
 
 
 def workload(case: str):
-    if case.startswith("config3main-k"):
-        return [P.scale_problem(P.config3_main())], int(case.rsplit("k", 1)[1]), 0
-    if case == "config3":
-        probs = [P.scale_problem(p) for p in P.config3(n_extra=32)]
+    if case.startswith("m62-k"):
+        return [P.scale_problem(P.random_n12_m62_p6())], int(case.rsplit("k", 1)[1]), 0
+    if case == "m62-batch":
+        probs = [P.scale_problem(p) for p in P.m62_batch(n_extra=32)]
         return probs, [6] + [p.n for p in probs[1:]], [0] + [1 << 19] * 32
-    if case == "config2-k4":
-        return [P.scale_problem(P.config2())], 4, 0
-    if case == "config4-k3":
-        return [P.scale_problem(P.config4())], 3, 0
-    if case == "config5":
-        return [P.scale_problem(p) for p in P.config5(64)], 3, 0
+    if case == "n10m43p4-k4":
+        return [P.scale_problem(P.random_n10_m43_p4())], 4, 0
+    if case == "illcond-k3":
+        return [P.scale_problem(P.illcond_n16_m62_p8())], 3, 0
+    if case == "mpc-batch":
+        return [P.scale_problem(p) for p in P.mpc_batch(64)], 3, 0
     raise SystemExit(f"unknown case {case}")
 
 

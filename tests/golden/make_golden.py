@@ -41,7 +41,7 @@ from oracle import oracle as O  # noqa: E402
 
 # problems of the fixtures: (label, generator)
 PROBLEMS = [
-    ("config1", lambda: P.config1()),
+    ("n4m10p2", lambda: P.random_n4_m10_p2()),
     ("rand-n3-m8-p2-s11", lambda: P.random_mpqp(3, 8, 2, seed=11)),
     ("rand-n4-m12-p3-s12", lambda: P.random_mpqp(4, 12, 3, seed=12)),
     ("rand-n5-m14-p2-s13", lambda: P.random_mpqp(5, 14, 2, seed=13)),

@@ -53,8 +53,8 @@ def test_gpu_results_prefix_matches_reference_layout():
         assert getattr(Ref, f).offset == getattr(solver.GPUResults, f).offset, f
 
 
-@pytest.mark.parametrize("make", [P.config1, P.config2, P.config4, lambda: P.mpc_mpqp(3),
-                                  lambda: P.config3_extra(5)])
+@pytest.mark.parametrize("make", [P.random_n4_m10_p2, P.random_n10_m43_p4, P.illcond_n16_m62_p8, lambda: P.mpc_mpqp(3),
+                                  lambda: P.batch_member(5)])
 def test_unpack_lp_recovers_the_problem(lib, make):
     prog = host.MPQPProb.from_mpqp(make())
     prog.process_constraints(scale_method=1)
@@ -71,7 +71,7 @@ def test_unpack_lp_recovers_the_problem(lib, make):
 
 
 def test_unpack_lp_rejects_other_layouts(lib):
-    prog = host.MPQPProb.from_mpqp(P.config1())
+    prog = host.MPQPProb.from_mpqp(P.random_n4_m10_p2())
     prog.process_constraints(scale_method=1)
     d = host.build_lp_data(prog)
     bad = dict(d, N1=d["N1"] + 1)

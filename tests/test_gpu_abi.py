@@ -16,7 +16,7 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 GEN = {
-    "config1": lambda: P.config1(),
+    "n4m10p2": lambda: P.random_n4_m10_p2(),
     "rand-n3-m8-p2-s11": lambda: P.random_mpqp(3, 8, 2, seed=11),
     "rand-n4-m12-p3-s12": lambda: P.random_mpqp(4, 12, 3, seed=12),
     "rand-n5-m14-p2-s13": lambda: P.random_mpqp(5, 14, 2, seed=13),
@@ -53,7 +53,7 @@ def test_mpqp_drop_in_matches_oracle_and_reference(gpu_lib, ref, label, precisio
 
 def test_mpqp_reports_malformed_layout_without_gpu_work(gpu_lib):
     lib = host.load_mpqp_cuda()
-    prog = host.MPQPProb.from_mpqp(P.config1())
+    prog = host.MPQPProb.from_mpqp(P.random_n4_m10_p2())
     prog.process_constraints(scale_method=1)
     d = host.build_lp_data(prog)
     d = dict(d, M2=d["M2"] - 1)

@@ -19,10 +19,10 @@ from oracle import reference_lp as R
 pytestmark = pytest.mark.gpu
 
 CASES = {
-    "config1": (lambda: P.config1(), 4),
-    "config2-k3": (lambda: P.config2(), 3),
-    "config3main-k2": (lambda: P.config3_main(), 2),
-    "config5-k3": (lambda: P.mpc_mpqp(0), 3),
+    "n4m10p2": (lambda: P.random_n4_m10_p2(), 4),
+    "n10m43p4-k3": (lambda: P.random_n10_m43_p4(), 3),
+    "m62-k2": (lambda: P.random_n12_m62_p6(), 2),
+    "mpc-k3": (lambda: P.mpc_mpqp(0), 3),
 }
 
 
@@ -62,7 +62,7 @@ def test_region_laws_match_oracle_and_reference(gpu_lib, case):
 
 
 def test_region_laws_reject_bad_sets(gpu_lib):
-    prob = P.scale_problem(P.config1())
+    prob = P.scale_problem(P.random_n4_m10_p2())
     with pytest.raises(solver.MpqpError):
         solver.region_laws(prob, [[0, 1, 2, 3, 4]])        # |S| > n
     with pytest.raises(solver.MpqpError):

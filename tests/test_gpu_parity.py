@@ -15,12 +15,12 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 CASES = {
-    "config1": (lambda: P.config1(), 4, False),
-    "config1-exhaustive": (lambda: P.config1(), 4, True),
-    "config2-k3": (lambda: P.config2(), 3, False),
-    "config3main-k3": (lambda: P.config3_main(), 3, False),
-    "config4-k3": (lambda: P.config4(), 3, False),
-    "config5-k3": (lambda: P.mpc_mpqp(0), 3, False),
+    "n4m10p2": (lambda: P.random_n4_m10_p2(), 4, False),
+    "n4m10p2-exhaustive": (lambda: P.random_n4_m10_p2(), 4, True),
+    "n10m43p4-k3": (lambda: P.random_n10_m43_p4(), 3, False),
+    "m62-k3": (lambda: P.random_n12_m62_p6(), 3, False),
+    "illcond-k3": (lambda: P.illcond_n16_m62_p8(), 3, False),
+    "mpc-k3": (lambda: P.mpc_mpqp(0), 3, False),
 }
 
 
@@ -82,7 +82,7 @@ def test_mixed_verdicts_equal_fp64(gpu_lib, case):
 
 
 def test_batch_of_instances_matches_per_instance_oracle(gpu_lib):
-    probs = [P.scale_problem(p) for p in P.config3(n_extra=6)]
+    probs = [P.scale_problem(p) for p in P.m62_batch(n_extra=6)]
     kmax = 2
     res = solver.solve(probs, precision=solver.FP64, k_max=kmax, record=1, rec_cap=1 << 20, cand_cap=1 << 18,
                        arena_bytes=1 << 28)
@@ -100,7 +100,7 @@ def test_batch_of_instances_matches_per_instance_oracle(gpu_lib):
 
 @pytest.mark.parametrize("budget", [50, 1000, 5000])
 def test_budget_truncation_matches_oracle(gpu_lib, budget):
-    prob = P.scale_problem(P.config2())
+    prob = P.scale_problem(P.random_n10_m43_p4())
     ref = O.enumerate_sets(prob, k_max=6, budget=budget, keep_records=False)
     for prec in (solver.FP64, solver.MIXED):
         res = solver.solve([prob], precision=prec, k_max=6, budget=budget, cand_cap=1 << 18, arena_bytes=1 << 28)
@@ -116,7 +116,7 @@ def _digest(sets_lo_hi):
 
 
 def test_set_digests_match_oracle(gpu_lib):
-    prob = P.scale_problem(P.config2())
+    prob = P.scale_problem(P.random_n10_m43_p4())
     ref = O.enumerate_sets(prob, k_max=3)
     for prec in (solver.FP64, solver.MIXED):
         res = solver.solve([prob], precision=prec, k_max=3, cand_cap=1 << 18, arena_bytes=1 << 28)
@@ -131,7 +131,7 @@ def test_mixed_equals_fp64_on_the_full_bench_batch(gpu_lib):
     """Size-independent check at the bench's full size (60.8M candidates,
     33 instances): identical feasible / optimal / region sets per instance
     (order-independent 64-bit digests) and identical counts."""
-    probs = [P.scale_problem(p) for p in P.config3(n_extra=32)]
+    probs = [P.scale_problem(p) for p in P.m62_batch(n_extra=32)]
     kmax = [6] + [p.n for p in probs[1:]]
     budget = [0] + [1 << 19] * 32
     r32 = solver.solve(probs, precision=solver.MIXED, k_max=kmax, budget=budget, mem_fraction=0.8)

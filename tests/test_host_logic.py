@@ -14,17 +14,17 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def test_generators_are_deterministic_and_shaped():
-    a, b = P.config1(), P.config1()
+    a, b = P.random_n4_m10_p2(), P.random_n4_m10_p2()
     for k in ("Q", "c", "H", "A", "b", "F", "CRA", "CRb"):
         assert np.array_equal(getattr(a, k), getattr(b, k))
     assert (a.n, a.m, a.p) == (4, 10, 2)
     assert np.allclose(np.linalg.norm(a.A, axis=1), 1.0)
     assert a.b.min() >= 1.0 and a.b.max() <= 2.0
-    c3 = P.config3(n_extra=32)
+    c3 = P.m62_batch(n_extra=32)
     assert len(c3) == 33 and (c3[0].n, c3[0].m, c3[0].p) == (12, 62, 6)
     for pr in c3[1:]:
         assert 5 <= pr.n <= 15 and 20 <= pr.m <= 80 and 2 <= pr.p <= 6
-    c4 = P.config4()
+    c4 = P.illcond_n16_m62_p8()
     assert (c4.n, c4.m, c4.p) == (16, 62, 8)
     ev = np.linalg.eigvalsh(c4.Q)
     assert ev.min() > 0 and 5e3 < ev.max() / ev.min() < 1e4 + 1
@@ -37,7 +37,7 @@ def test_generators_are_deterministic_and_shaped():
 
 
 def test_scaling_restates_the_reference_and_is_idempotent():
-    raw = P.config2()
+    raw = P.random_n10_m43_p4()
     s1 = P.scale_problem(raw)
     assert np.allclose(np.max(np.abs(np.hstack([s1.A, s1.F])), axis=1), 1.0)
     assert np.isclose(np.max(np.abs(np.hstack([s1.Q, s1.H, s1.c[:, None]]))), 8.0)
@@ -47,7 +47,7 @@ def test_scaling_restates_the_reference_and_is_idempotent():
 
 
 def test_lp_builders_agree():
-    prog = host.MPQPProb.from_mpqp(P.config2())
+    prog = host.MPQPProb.from_mpqp(P.random_n10_m43_p4())
     prog.process_constraints(scale_method=1)
     d = host.build_lp_data(prog)
     r = R.build_lp_matrices(prog.to_mpqp())

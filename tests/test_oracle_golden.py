@@ -19,7 +19,7 @@ from oracle import reference_lp as R
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 GEN = {
-    "config1": lambda: P.config1(),
+    "n4m10p2": lambda: P.random_n4_m10_p2(),
     "rand-n3-m8-p2-s11": lambda: P.random_mpqp(3, 8, 2, seed=11),
     "rand-n4-m12-p3-s12": lambda: P.random_mpqp(4, 12, 3, seed=12),
     "rand-n5-m14-p2-s13": lambda: P.random_mpqp(5, 14, 2, seed=13),
@@ -42,7 +42,7 @@ def _sets(cand, field):
     return sorted(tuple(O.mask_to_set(c["mask_lo"], c["mask_hi"])) for c in cand if c[field])
 
 
-@pytest.mark.parametrize("label", ["config1", "rand-n3-m8-p2-s11", "rand-n4-m12-p3-s12", "rand-n5-m14-p2-s13"])
+@pytest.mark.parametrize("label", ["n4m10p2", "rand-n3-m8-p2-s11", "rand-n4-m12-p3-s12", "rand-n5-m14-p2-s13"])
 def test_oracle_matches_exact_rational_verdicts(exact, label):
     fx = exact[label]
     prob = P.scale_problem(GEN[label]())

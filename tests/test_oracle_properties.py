@@ -12,7 +12,7 @@ def _set(c):
     return tuple(O.mask_to_set(c["mask_lo"], c["mask_hi"]))
 
 
-@pytest.mark.parametrize("make,kmax", [(P.config2, 3), (lambda: P.mpc_mpqp(1), 3), (P.config4, 2)])
+@pytest.mark.parametrize("make,kmax", [(P.random_n10_m43_p4, 3), (lambda: P.mpc_mpqp(1), 3), (P.illcond_n16_m62_p8, 2)])
 def test_pruning_keeps_every_feasible_set(make, kmax):
     prob = P.scale_problem(make())
     ep = O.enumerate_sets(prob, k_max=kmax, nthreads=4)
@@ -34,7 +34,7 @@ def test_supersets_of_infeasible_sets_are_never_checked():
 
 
 def test_warm_start_chain_equals_enumeration_records():
-    prob = P.scale_problem(P.config2())
+    prob = P.scale_problem(P.random_n10_m43_p4())
     e = O.enumerate_sets(prob, k_max=3)
     rng = np.random.default_rng(3)
     for i in rng.choice(len(e.cand), 40, replace=False):
@@ -46,7 +46,7 @@ def test_warm_start_chain_equals_enumeration_records():
 
 
 def test_budget_stops_at_the_first_level_that_does_not_fit():
-    prob = P.scale_problem(P.config2())
+    prob = P.scale_problem(P.random_n10_m43_p4())
     full = O.enumerate_sets(prob, k_max=3, keep_records=True)
     per_level = np.bincount(full.cand["level"])
     cum = np.cumsum(per_level)
@@ -55,8 +55,8 @@ def test_budget_stops_at_the_first_level_that_does_not_fit():
     assert e.truncated == 1 and e.n_cand == cum[2]
 
 
-@pytest.mark.parametrize("make,kmax,n", [(P.config3_main, 2, 120), (lambda: P.mpc_mpqp(4), 3, 120),
-                                         (lambda: P.config3_extra(9), 2, 120)])
+@pytest.mark.parametrize("make,kmax,n", [(P.random_n12_m62_p6, 2, 120), (lambda: P.mpc_mpqp(4), 3, 120),
+                                         (lambda: P.batch_member(9), 2, 120)])
 def test_verdicts_match_highs_on_reference_formulation(make, kmax, n):
     prob = P.scale_problem(make())
     mats = R.build_lp_matrices(prob)

@@ -84,10 +84,10 @@ def test_noalloc_matches_allocating_entry_point_two_calls(gpu_lib):
     import torch
     assert torch.cuda.is_available()
     lib = solver.load()
-    # first call: config 1 regions; second call: a different, larger problem
-    p1 = P.scale_problem(P.config1())
+    # first call: the n=4, m=10 problem; second call: a different, larger problem
+    p1 = P.scale_problem(P.random_n4_m10_p2())
     s1 = _regions(p1, 4)
-    p2 = P.scale_problem(P.config3_main())
+    p2 = P.scale_problem(P.random_n12_m62_p6())
     s2 = _regions(p2, 2)[:300]
     assert s1 and s2
     laws1, sizes1 = _call_noalloc(lib, p1, s1)
@@ -100,7 +100,7 @@ def test_noalloc_rejects_calls_beyond_the_scratch(gpu_lib):
     import torch
     lib = solver.load()
     f = _bind(lib)
-    prob = P.scale_problem(P.config1())
+    prob = P.scale_problem(P.random_n4_m10_p2())
     ps = solver._ProblemSet([prob], 0, 0, 0)
     n_sets = SCRATCH_BYTES // 16 + 1          # masks alone exceed the scratch
     masks = np.zeros((n_sets, 2), dtype=np.uint64)
