@@ -132,15 +132,50 @@ def lp1_hbm_bytes(probs, kmax, res, elem: int) -> float:
     total = 0.0
     for i, pr in enumerate(probs):
         M1, nv = pr.m + pr.CRA.shape[0], pr.n + pr.p
-        ld1 = (nv + 1) | 1
-        tab = (M1 + 1) * ld1 * elem
-        ids = M1 + nv
+        if elem == 4:   # FP32 rows: smallest stride >= nv+1 that is 4 (mod 8)
+            ld1 = (nv + 1 + 3) & ~3
+            ld1 = ld1 if ld1 & 4 else ld1 + 4
+        else:           # FP64 rows: odd stride
+            ld1 = (nv + 1) | 1
+        tab = (((M1 + 1) * ld1 + 3) & ~3) * elem
+        ids = (M1 + nv + 15) & ~15
         st = res.inst[i]
         cand = int(st["candidates"]) - 1          # level 0 (empty set) has no parent
         feas = int(st["feasible"]) - 1
         stored = int(st["stored"])
         total += cand * (8 + 48 + tab + ids) + feas * (48 + 32) + stored * (tab + ids)
     return total
+
+
+def opt_algorithmic_bytes(probs, res, elem: int) -> float:
+    """Algorithmic bytes of all optimality (k_optimality) launches of one step.
+
+    Per evaluated set (every feasible set, the empty set included): the
+    shared-data gather for the KKT rows 8*m*(n+p+1), the region tableau
+    written once 8*R*(p+2) (R = m + rows of the parameter box) and the 16 B
+    mask and verdict; per LP2 / Chebyshev pivot one read and one write of the
+    (R+1) x (p+2) tableau at the pivot element size.
+    """
+    total = 0.0
+    for i, pr in enumerate(probs):
+        st = res.inst[i]
+        m, n, p = pr.m, pr.n, pr.p
+        R = m + pr.CRA.shape[0]
+        total += int(st["feasible"]) * (8 * m * (n + p + 1) + 8 * R * (p + 2) + 16)
+        total += 2 * elem * (int(st["lp2_pivots"]) + int(st["cheb_pivots"])) * (R + 1) * (p + 2)
+    return float(total)
+
+
+def traffic_per_launch(name: str, units_per_launch: float):
+    """DRAM bytes per launch, scaled from an ncu capture of a smaller case
+    (bytes per unit, recorded under profiles/) to this launch's units."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        with open(path) as f:
+            per_unit = float(json.load(f)["dram_bytes_per_unit"])
+    except Exception:
+        return None
+    return per_unit * units_per_launch
 
 
 def model_bytes_touched(probs, res, elem: int) -> float:
@@ -309,30 +344,33 @@ def run_ours(args):
 
     if rank != 0:
         return 0
-    # roofline of the LP1 kernel (HBM-facing) and the kernel list
+    # rooflines: the dominant (optimality) kernel, and the LP1 kernel beside it
     elem = 4 if prec == solver.MIXED else 8
-    feas_name = "k_feasibility<float>" if prec == solver.MIXED else "k_feasibility<double>"
-    feas_ms, feas_n = kt.get(feas_name, (0.0, 0))
-    step_kernel_ms = sum(v[0] for v in kt.values())
+    tname = "float" if prec == solver.MIXED else "double"
     dominant = max(kt.items(), key=lambda kv: kv[1][0])[0] if kt else None
-    bytes_lp1 = lp1_hbm_bytes(probs, kmax, res, elem)
     peaks = measured_peaks()
-    achieved = bytes_lp1 / (feas_ms / 1e3) / 1e9 if feas_ms > 0 else None
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "lp1_traffic.json")
-    if os.path.exists(tpath):
-        try:
-            with open(tpath) as f:
-                tj = json.load(f)
-            traffic = tj.get("dram_bytes_per_candidate", 0) * (res.candidates - len(probs)) / max(feas_n, 1)
-        except Exception:
-            traffic = None
-    roof = {"bound": "hbm", "kernel": feas_name, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-            "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
-            "traffic": traffic, "algorithmic_bytes_per_launch": bytes_lp1 / max(feas_n, 1),
-            "avg_launch_ms": feas_ms / max(feas_n, 1), "peak_source": peaks["source"] + " (MEASURED_PEAKS.json hbm_gbs)",
-            "note": "achieved = LP1 tableau/record bytes per launch / mean launch time; the kernel is bound by "
-                    "shared-memory pivots and FP32 issue, not HBM"}
+    peak_src = peaks["source"] + " (MEASURED_PEAKS.json hbm_gbs)"
+
+    def roofline(kname, step_bytes, units, traffic_file, per_unit_text):
+        ms, nl = kt.get(kname, (0.0, 0))
+        nl = max(nl, 1)
+        achieved = step_bytes / (ms / 1e3) / 1e9 if ms > 0 else None
+        return {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
+                "traffic": traffic_per_launch(traffic_file, units / nl),
+                "algorithmic_bytes_per_launch": step_bytes / nl, "units_per_launch": units / nl,
+                "avg_launch_ms": ms / nl, "launches_per_step": nl, "peak_source": peak_src,
+                "per_unit": per_unit_text}
+
+    n_eval = res.total("feasible")
+    roof = roofline(f"k_optimality<{tname}>", opt_algorithmic_bytes(probs, res, elem), n_eval,
+                    "opt_traffic.json",
+                    "per evaluated (feasible) set: 8*m*(n+p+1) KKT gather + 8*R*(p+2) region tableau + 16 B "
+                    "mask/verdict, plus 2*(R+1)*(p+2)*s per LP2/Chebyshev pivot (s = 4 B FP32)")
+    roof_lp1 = roofline(f"k_feasibility<{tname}>", lp1_hbm_bytes(probs, kmax, res, elem),
+                        res.candidates - len(probs), "lp1_traffic.json",
+                        "per candidate (levels >= 1): 8 B record + 48 B parent node + parent LP1 tableau "
+                        "(M1+1)*ld1*s + basis ids; per feasible child 80 B; per stored child its tableau and ids")
     cb = cpu_baseline(steps=1)
     clocks = clk.summary()
     line = {
@@ -348,6 +386,7 @@ def run_ours(args):
         "fp64_path": fp64,
         "speedup_vs_fp64": (value / world / fp64["value"]) if fp64 else None,
         "roofline": roof,
+        "roofline_lp1": roof_lp1,
         "model_bytes_touched_per_s": model_bytes_touched(probs, res, elem) / (ms_step / 1e3),
         "kernels_ms_per_step": {k: round(v[0], 3) for k, v in sorted(kt.items(), key=lambda kv: -kv[1][0])},
         "dominant_kernel": dominant,

@@ -38,10 +38,13 @@ def main(argv=None):
     ap.add_argument("case")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--runs", type=int, default=1)
+    ap.add_argument("--mem-fraction", type=float, default=0.85,
+                    help="share of free device memory the plan may take (arenas are also capped by the "
+                         "combinatorial size of the workload)")
     args = ap.parse_args(argv)
     probs, kmax, budget = workload(args.case)
     prec = solver.MIXED if args.precision == "mixed" else solver.FP64
-    plan = solver.Plan(probs, precision=prec, k_max=kmax, budget=budget, mem_fraction=0.85)
+    plan = solver.Plan(probs, precision=prec, k_max=kmax, budget=budget, mem_fraction=args.mem_fraction)
     for _ in range(args.runs):
         plan.run()
     r = plan.results()
@@ -55,6 +58,9 @@ def main(argv=None):
                       "kernels": {k: [round(v[0], 3), v[1]] for k, v in kt.items()},
                       "fallbacks": [r.total("fallback_lp1"), r.total("fallback_opt")]}))
     plan.close()
+    if r.status != 0 or r2.status != 0:
+        print(f"status {r.status} / {r2.status}: {solver.last_error()}", file=sys.stderr)
+        return 1
     return 0
 
 
