@@ -363,7 +363,8 @@ def run_ours(args):
                 "per_unit": per_unit_text}
 
     n_eval = res.total("feasible")
-    roof = roofline(f"k_optimality<{tname}>", opt_algorithmic_bytes(probs, res, elem), n_eval,
+    opt_name = next((k for k in kt if k.startswith("k_opt_screen")), f"k_optimality<{tname}>")
+    roof = roofline(opt_name, opt_algorithmic_bytes(probs, res, elem), n_eval,
                     "opt_traffic.json",
                     "per evaluated (feasible) set: 8*m*(n+p+1) KKT gather + 8*R*(p+2) region tableau + 16 B "
                     "mask/verdict, plus 2*(R+1)*(p+2)*s per LP2/Chebyshev pivot (s = 4 B FP32)")

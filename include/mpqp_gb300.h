@@ -130,6 +130,8 @@ typedef struct {
     int max_pivots, degen_switch;
     double tol_piv32, tol_dj32, margin_z, margin_beta, margin_t, margin_licq;
     double tol_zero_row;     /* region row zero when max|g| <= tol * max(1,|h|) */
+    int screen_lanes;        /* MPQP_MIXED: lanes per LP2 of the FP32 screen,
+                                8, 16 or 32 (0 selects the default)        */
 } mpqp_options;
 
 /* One optimal active set */

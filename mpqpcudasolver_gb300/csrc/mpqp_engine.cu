@@ -24,6 +24,7 @@
 namespace mq {
 size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd);
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd);
+size_t screen_smem_per_warp(int lanes, const SlotDims &sd);
 size_t laws_smem_per_warp(const SlotDims &sd);
 const void *kernel_ptr(const char *name);
 cudaError_t launch_enumerate(const DevBuffers &B, int level, int grid, cudaStream_t s);
@@ -33,6 +34,8 @@ cudaError_t launch_lp1_fp64(const DevBuffers &B, const Tol &tol, const SlotDims 
                             size_t smem, cudaStream_t s);
 cudaError_t launch_optimality(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int prec,
                               int grid, size_t smem, cudaStream_t s);
+cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int lanes, int grid,
+                              size_t smem, cudaStream_t s);
 cudaError_t launch_optimality_fp64(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int grid,
                                    size_t smem, cudaStream_t s);
 cudaError_t launch_level0(const DevBuffers &B, int prec, cudaStream_t s);
@@ -205,6 +208,7 @@ struct mpqp_plan {
     std::vector<void *> allocs;
     int kmax = 0;
     int prec = PREC_FP64;
+    int screen_lanes = 32;      // mixed precision: lanes per LP2 of the FP32 screen
     int grid_enum = 0, grid_feas = 0, grid_lp1fb = 0, grid_opt = 0, grid_optfb = 0;
     size_t smem_feas = 0, smem_lp1fb = 0, smem_opt = 0, smem_optfb = 0;
     int n_launches = 0;
@@ -242,6 +246,7 @@ extern "C" void mpqp_default_options(mpqp_options *o)
     o->margin_t = 1e-5;   // x (row magnitude / pivot ratio) x (1 + p |theta|max)
     o->margin_licq = 1e-3;
     o->tol_zero_row = 1e-12;
+    o->screen_lanes = 32;
 }
 
 static void fill_defaults(mpqp_options &o)
@@ -251,7 +256,7 @@ static void fill_defaults(mpqp_options &o)
 #define DEF(f) if (o.f == 0) o.f = d.f
     DEF(mem_fraction); DEF(tol_feas); DEF(tol_opt); DEF(tol_licq); DEF(r_min); DEF(tol_piv); DEF(tol_dj);
     DEF(max_pivots); DEF(degen_switch); DEF(tol_piv32); DEF(tol_dj32); DEF(margin_z); DEF(margin_beta);
-    DEF(margin_t); DEF(margin_licq); DEF(tol_zero_row);
+    DEF(margin_t); DEF(margin_licq); DEF(tol_zero_row); DEF(screen_lanes);
 #undef DEF
 }
 
@@ -283,13 +288,13 @@ static void free_plan_mem(mpqp_plan *P)
     P->ev0 = P->ev1 = P->ev_mid = nullptr;
 }
 
-static int grid_for(const void *fn, size_t smem, int *grid)
+static int grid_for(const void *fn, size_t smem, int *grid, int block = 128)
 {
     int dev = 0, sms = 0, nb = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     if (smem > 48 * 1024) CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, smem));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, block, smem));
     if (nb < 1) {
         set_err("kernel does not fit on an SM (shared memory " + std::to_string(smem) + " bytes)");
         return MPQP_EINVAL;
@@ -305,7 +310,12 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
     const DevBuffers &B = P->B;
     const bool mixed = P->prec == PREC_MIXED;
     const char *feas = mixed ? "k_feasibility<float>" : "k_feasibility<double>";
-    const char *opt = mixed ? "k_optimality<float>" : "k_optimality<double>";
+    const char *opt = !mixed ? "k_optimality<double>"
+                      : P->screen_lanes == 8 ? "k_opt_screen<8>" : P->screen_lanes == 16 ? "k_opt_screen<16>" : "k_opt_screen<32>";
+    auto launch_opt = [&](int level) {
+        return mixed ? launch_opt_screen(B, P->tol, P->sd, level, P->screen_lanes, P->grid_opt, P->smem_opt, s)
+                     : launch_optimality(B, P->tol, P->sd, level, P->prec, P->grid_opt, P->smem_opt, s);
+    };
     int nl = 0;
     if (timed) P->kname.clear();
     auto chk = [&](const char *name, cudaError_t e) -> int {
@@ -328,14 +338,14 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
 #define L(name, x) do { int _r = pre(name); if (_r) return _r; _r = chk(name, x); if (_r) return _r; } while (0)
     L("k_reset", launch_reset(B, s));
     L("k_level0", launch_level0(B, P->prec, s));
-    L(opt, launch_optimality(B, P->tol, P->sd, 0, P->prec, P->grid_opt, P->smem_opt, s));
+    L(opt, launch_opt(0));
     if (mixed) L("k_optimality_fp64", launch_optimality_fp64(B, P->tol, P->sd, 0, P->grid_optfb, P->smem_optfb, s));
     L("k_finalize", launch_finalize(B, 0, s));
     for (int k = 1; k <= P->kmax; k++) {
         L("k_enumerate", launch_enumerate(B, k, P->grid_enum, s));
         L(feas, launch_feasibility(B, P->tol, P->sd, k, P->prec, P->grid_feas, P->smem_feas, s));
         if (mixed) L("k_lp1_fp64", launch_lp1_fp64(B, P->tol, P->sd, k, P->grid_lp1fb, P->smem_lp1fb, s));
-        L(opt, launch_optimality(B, P->tol, P->sd, k, P->prec, P->grid_opt, P->smem_opt, s));
+        L(opt, launch_opt(k));
         if (mixed) L("k_optimality_fp64", launch_optimality_fp64(B, P->tol, P->sd, k, P->grid_optfb, P->smem_optfb, s));
         L("k_finalize", launch_finalize(B, k, s));
     }
@@ -362,6 +372,12 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
     fill_defaults(P->opt);
     const mpqp_options &o = P->opt;
     P->prec = o.precision == MPQP_MIXED ? PREC_MIXED : PREC_FP64;
+    if (o.screen_lanes != 8 && o.screen_lanes != 16 && o.screen_lanes != 32) {
+        set_err("screen_lanes must be 8, 16 or 32");
+        delete P;
+        return MPQP_EINVAL;
+    }
+    P->screen_lanes = o.screen_lanes;
     P->n_inst = n_inst;
     P->probs.assign(probs, probs + n_inst);
     Tol &t = P->tol;
@@ -369,6 +385,8 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
     t.tol_piv = o.tol_piv; t.tol_dj = o.tol_dj; t.max_pivots = o.max_pivots; t.degen_switch = o.degen_switch;
     t.tol_piv32 = (float)o.tol_piv32; t.tol_dj32 = (float)o.tol_dj32;
     t.margin_z = o.margin_z; t.margin_beta = o.margin_beta; t.margin_t = o.margin_t; t.margin_licq = o.margin_licq;
+    t.margin_z32 = (float)o.margin_z; t.margin_beta32 = (float)o.margin_beta;
+    t.margin_t32 = (float)o.margin_t; t.margin_licq32 = (float)o.margin_licq;
     t.tol_zero_row = o.tol_zero_row;
     // host precompute
     std::vector<Prepared> prep(n_inst);
@@ -524,12 +542,16 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
     // kernel geometry
     P->smem_feas = 4 * lp1_smem_per_warp(P->prec == PREC_MIXED ? 4 : 8, sd);
     P->smem_lp1fb = 4 * lp1_smem_per_warp(8, sd);
-    P->smem_opt = 4 * opt_smem_per_warp(P->prec == PREC_MIXED ? 4 : 8, sd);
+    // mixed precision: the grouped FP32 screen, one warp per block
+    P->smem_opt = P->prec == PREC_MIXED ? screen_smem_per_warp(P->screen_lanes, sd) : 4 * opt_smem_per_warp(8, sd);
     P->smem_optfb = 4 * opt_smem_per_warp(8, sd);
     if ((rc = grid_for(kernel_ptr("enumerate"), 0, &P->grid_enum)) ||
         (rc = grid_for(kernel_ptr(P->prec == PREC_MIXED ? "feas32" : "feas64"), P->smem_feas, &P->grid_feas)) ||
         (rc = grid_for(kernel_ptr("lp1_fp64"), P->smem_lp1fb, &P->grid_lp1fb)) ||
-        (rc = grid_for(kernel_ptr(P->prec == PREC_MIXED ? "opt32" : "opt64"), P->smem_opt, &P->grid_opt)) ||
+        (rc = P->prec == PREC_MIXED
+                  ? grid_for(kernel_ptr(P->screen_lanes == 8 ? "screen8" : P->screen_lanes == 16 ? "screen16" : "screen32"),
+                             P->smem_opt, &P->grid_opt, 32)
+                  : grid_for(kernel_ptr("opt64"), P->smem_opt, &P->grid_opt)) ||
         (rc = grid_for(kernel_ptr("opt_fp64"), P->smem_optfb, &P->grid_optfb))) {
         free_plan_mem(P);
         delete P;

@@ -46,6 +46,9 @@ struct Tol {
     double margin_t;    // FP32 LP2 t below -margin_t * error scale -> not optimal without FP64
     double margin_licq; // FP32 Cholesky pivot ratio below this -> FP64
     double tol_zero_row;// region row is zero when max|g| <= tol_zero_row * max(1, |h|)
+    // FP32 copies of the margins: the FP32 kernels decide without FP64
+    // arithmetic (GB300's FP64 pipe is a small fraction of its FP32 rate)
+    float margin_z32, margin_beta32, margin_t32, margin_licq32;
 };
 
 struct InstDesc {

@@ -549,7 +549,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
             feasible = (st == LP_OPTIMAL) && ((double)z <= tol.tol_feas);
         } else {
             if (st != LP_OPTIMAL) decided = false;
-            else if ((double)z > tol.margin_z) feasible = false;
+            else if (z > (T)tol.margin_z32) feasible = false;
             else {
                 // certificate: every slack of S nonbasic and every basic slack
                 // clearly positive -> the basic solution is a feasible point
@@ -576,7 +576,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
                 }
                 lp1_growth = (float)gmax;
                 lp1_minbeta = (float)minb;
-                if (!s_basic && (double)minb > tol.margin_beta * (double)gmax) feasible = true;
+                if (!s_basic && minb > (T)tol.margin_beta32 * gmax) feasible = true;
                 else decided = false;
             }
         }
@@ -716,6 +716,7 @@ struct OptWs {
     T *R, *Y, *Lam, *G, *Tb;
     uint8_t *ids;
     int *S;
+    __device__ OptWs() {}
     __device__ OptWs(unsigned char *base, const SlotDims &sd)
     {
         size_t o = 0;
@@ -734,7 +735,7 @@ struct OptWs {
 // Returns 0 on success, 1 when a pivot fails the threshold thr (relative to
 // the diagonal).  Fills ws.S with the sorted active set.
 template <typename T>
-__device__ int kkt_factor(const KktData<T> &D, const InstDesc &I, uint64_t lo, uint64_t hi, double thr,
+__device__ int kkt_factor(const KktData<T> &D, const InstDesc &I, uint64_t lo, uint64_t hi, T thr,
                           OptWs<T> &ws, int *k_out, T *rho_out = nullptr)
 {
     const int lane = lane_id();
@@ -753,7 +754,7 @@ __device__ int kkt_factor(const KktData<T> &D, const InstDesc &I, uint64_t lo, u
             const T d0 = D.Wm[(size_t)S[a] * m + S[a]];
             T acc = d0;
             for (int l = 0; l < a; l++) acc = xfma(-R[l * k + a], R[l * k + a], acc);
-            if (!(acc > (T)thr * d0)) fail = 1;
+            if (!(acc > thr * d0)) fail = 1;
             else R[a * k + a] = xsqrt(acc);
             if (rho_out && !fail) { const T rr = acc / d0; if (rr < rho) rho = rr; }
         }
@@ -791,46 +792,63 @@ __device__ int kkt_factor(const KktData<T> &D, const InstDesc &I, uint64_t lo, u
 // track = true also returns a bound on the magnitude of the terms summed
 // into any row, max_i (sum_c |Wh_ic| + |wc_i| + sum_l |Wm_i,S_l| |Lambda_l|_1),
 // the scale of the FP32 rounding error of the rows (warp-uniform result).
+// out = nullptr writes ws.G (row stride p+1, h in column p); otherwise the
+// rows go to out with row stride ldo and h in column hcol.
 template <typename T, bool track = false>
-__device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, uint64_t hi, int k, OptWs<T> &ws)
+__device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, uint64_t hi, int k, OptWs<T> &ws,
+                         T *out = nullptr, int ldo = 0, int hcol = 0)
 {
     const int lane = lane_id();
     const int m = I.m, p = I.p, ncp = I.ncp, P1 = p + 1;
     const int *S = ws.S;
     const T *Lam = ws.Lam;
-    T *G = ws.G;
+    T *G = out ? out : ws.G;
+    const int ldg = out ? ldo : P1, hc = out ? hcol : p;
     T amax = T(0);
     T *labs = ws.Y;   // |Lambda_l|_1, Y is free once Lambda is known
     for (int a = lane; a < k; a += 32) {
         T rs = T(0);
-        for (int cc = 0; cc < p; cc++) { G[a * P1 + cc] = Lam[a * P1 + cc]; if (track) rs += xabs(Lam[a * P1 + cc]); }
-        G[a * P1 + p] = -Lam[a * P1 + p];
+        for (int cc = 0; cc < p; cc++) { G[a * ldg + cc] = Lam[a * P1 + cc]; if (track) rs += xabs(Lam[a * P1 + cc]); }
+        G[a * ldg + hc] = -Lam[a * P1 + p];
         if (track) { rs += xabs(Lam[a * P1 + p]); labs[a] = rs; if (rs > amax) amax = rs; }
     }
     if (track) __syncwarp();
+    // inactive rows: g_c = -Wh_ic + sum_l Wm_i,S_l Lambda_lc (c < p) and
+    // h = wc_i - sum_l Wm_i,S_l Lambda_lp, each summed in ascending l; the
+    // columns go in register blocks of 8 so that Wm_i,S_l is read once per block
+    constexpr int CB = 8;
     for (int i = lane; i < m; i += 32) {
         if (mask_has(lo, hi, i)) continue;
         const int pos = k + i - mask_rank(lo, hi, i);
         const T *wmi = D.Wm + (size_t)i * m;
         T rs = T(0);
-        for (int cc = 0; cc < p; cc++) {
-            T acc = -D.Wh[(size_t)i * p + cc];
-            if (track) rs += xabs(acc);
-            for (int l = 0; l < k; l++) acc = xfma(wmi[S[l]], Lam[l * P1 + cc], acc);
-            G[pos * P1 + cc] = acc;
+        for (int c0 = 0; c0 < P1; c0 += CB) {
+            T acc[CB];
+#pragma unroll
+            for (int j = 0; j < CB; j++) {
+                const int cc = c0 + j;
+                acc[j] = cc < p ? -D.Wh[(size_t)i * p + cc] : (cc == p ? D.wc[i] : T(0));
+                if (track && cc <= p) rs += xabs(acc[j]);
+            }
+            for (int l = 0; l < k; l++) {
+                const T w = wmi[S[l]];
+                const T *lam = Lam + l * P1;
+                if (track && c0 == 0) rs = xfma(xabs(w), labs[l], rs);
+#pragma unroll
+                for (int j = 0; j < CB; j++) {
+                    const int cc = c0 + j;
+                    if (cc < p) acc[j] = xfma(w, lam[cc], acc[j]);
+                    else if (cc == p) acc[j] = xfma(-w, lam[cc], acc[j]);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < CB; j++) if (c0 + j <= p) G[pos * ldg + (c0 + j < p ? c0 + j : hc)] = acc[j];
         }
-        T acc = D.wc[i];
-        if (track) {
-            rs += xabs(acc);
-            for (int l = 0; l < k; l++) rs = xfma(xabs(wmi[S[l]]), labs[l], rs);
-            if (rs > amax) amax = rs;
-        }
-        for (int l = 0; l < k; l++) acc = xfma(-wmi[S[l]], Lam[l * P1 + p], acc);
-        G[pos * P1 + p] = acc;
+        if (track && rs > amax) amax = rs;
     }
     for (int ii = lane; ii < ncp; ii += 32) {
-        for (int cc = 0; cc < p; cc++) G[(m + ii) * P1 + cc] = D.At[ii * p + cc];
-        G[(m + ii) * P1 + p] = D.bt[ii];
+        for (int cc = 0; cc < p; cc++) G[(m + ii) * ldg + cc] = D.At[ii * p + cc];
+        G[(m + ii) * ldg + hc] = D.bt[ii];
     }
     if (track) {
 #pragma unroll
@@ -840,9 +858,9 @@ __device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, ui
     return amax;
 }
 
-// screen = true (T = float): the FP32 screening pass of the mixed path; only
-// a clear "not optimal" is final, everything else returns decided = false.
-template <typename T, bool screen>
+// Optimality and region verdict of one feasible set (the FP64 path; the FP32
+// screen of the mixed path is k_opt_screen).
+template <typename T>
 __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const InstDesc &I, uint64_t lo, uint64_t hi,
                                      OptWs<T> &ws)
 {
@@ -855,16 +873,14 @@ __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const 
     res.optimal = 0; res.region = 0;
     res.t = __longlong_as_double(0x7ff8000000000000LL); res.r = res.t;
     res.decided = true;
-    const T tpiv = screen ? (T)tol.tol_piv32 : (T)tol.tol_piv;
-    const T tdj = screen ? (T)tol.tol_dj32 : (T)tol.tol_dj;
+    const T tpiv = (T)tol.tol_piv;
+    const T tdj = (T)tol.tol_dj;
     int k = 0;
-    T rho = T(1);
-    if (kkt_factor<T>(D, I, lo, hi, screen ? tol.margin_licq : tol.tol_licq, ws, &k, screen ? &rho : nullptr)) {
-        if (screen) { res.decided = false; return res; }
+    if (kkt_factor<T>(D, I, lo, hi, (T)tol.tol_licq, ws, &k)) {
         res.licq = 0; res.lp2_status = LP_LICQ_FAIL;
         return res;
     }
-    const T amax = region_rows<T, screen>(D, I, lo, hi, k, ws);
+    region_rows<T>(D, I, lo, hi, k, ws);
     const T *G = ws.G;
     // LP2: max t  s.t.  g theta + t <= h (constraint rows), At theta <= bt
     T t0 = pos_inf<T>();
@@ -873,11 +889,10 @@ __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const 
     for (int off = 16; off; off >>= 1) { const T o = __shfl_xor_sync(FULLMASK, t0, off); if (o < t0) t0 = o; }
     T *Tb = ws.Tb;
     uint8_t *bid = ws.ids, *nid = ws.ids + R2;
-    T g0 = T(1);   // largest initial |entry| (growth reference of the FP32 screen)
     for (int r = lane; r < R2; r += 32) {
         T *tr = Tb + (size_t)r * ld2;
         const T *g = G + (size_t)r * P1;
-        for (int cc = 0; cc < p; cc++) { tr[cc] = g[cc]; if (screen) { const T a = xabs(g[cc]); if (a > g0) g0 = a; } }
+        for (int cc = 0; cc < p; cc++) tr[cc] = g[cc];
         const T cf = (r < m) ? T(1) : T(0);
         tr[p] = cf;
         T beta = xfma(-cf, t0, g[p]);
@@ -900,31 +915,8 @@ __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const 
     if (res.lp2_status == LP_OPTIMAL) {
         const T t = -Tb[(size_t)R2 * ld2 + P1];
         res.t = (double)t;
-        if (screen) {
-            // error scale of the FP32 margin: row magnitude / pivot ratio,
-            // times the reach of theta inside the box
-            T bmax = T(0);
-            for (int ii = lane; ii < ncp; ii += 32) { const T v = xabs(D.bt[ii]); if (v > bmax) bmax = v; }
-#pragma unroll
-            for (int off = 16; off; off >>= 1) { const T o = __shfl_xor_sync(FULLMASK, bmax, off); if (o > bmax) bmax = o; }
-            // element growth of the FP32 LP2 tableau: max |final| / max |initial|
-            T g2 = T(0);
-            for (int r = lane; r < R2; r += 32)
-                for (int cc = 0; cc < P1; cc++) { const T a = xabs(Tb[(size_t)r * ld2 + cc]); if (a > g2) g2 = a; }
-#pragma unroll
-            for (int off = 16; off; off >>= 1) {
-                const T o = __shfl_xor_sync(FULLMASK, g2, off); if (o > g2) g2 = o;
-                const T q0 = __shfl_xor_sync(FULLMASK, g0, off); if (q0 > g0) g0 = q0;
-            }
-            const double growth = (double)g2 > (double)g0 ? (double)g2 / (double)g0 : 1.0;
-            const double scale = (double)amax / (double)rho * (1.0 + (double)p * (double)bmax) * growth;
-            if (res.t < -tol.margin_t * scale) return res;      // clearly not optimal
-            res.decided = false;
-            return res;
-        }
         res.optimal = res.t > tol.tol_opt;
     } else {
-        if (screen) { res.decided = false; return res; }
         if (res.lp2_status == LP_UNBOUNDED) res.t = pos_inf<double>();
     }
     if (!res.optimal) return res;
@@ -1014,8 +1006,8 @@ __device__ void write_opt(const DevBuffers &B, const Node &nd, int level, const 
     }
 }
 
-// mode: T = double -> final FP64 verdicts; T = float -> FP32 screen that
-// queues undecided nodes for k_optimality_fp64.
+// Final FP64 verdicts of every feasible set of a level (the FP64 path;
+// instantiated for T = double only).
 template <typename T>
 __global__ void __launch_bounds__(128) k_optimality(DevBuffers B, Tol tol, SlotDims sd, int level)
 {
@@ -1026,7 +1018,7 @@ __global__ void __launch_bounds__(128) k_optimality(DevBuffers B, Tol tol, SlotD
     const int side = level & 1;
     Ctl *ctl = B.ctl;
     const long long nn = ctl->n_node[side] < B.node_cap ? ctl->n_node[side] : B.node_cap;
-    constexpr bool screen = sizeof(T) == 4;
+    static_assert(sizeof(T) == 8, "the FP32 screen is k_opt_screen");
     LocalInstCounters lc;
     lc.reset(-1);
     for (;;) {
@@ -1047,19 +1039,12 @@ __global__ void __launch_bounds__(128) k_optimality(DevBuffers B, Tol tol, SlotD
             }
             lc.reset(nd.inst);
         }
-        const OptResult res = eval_optimality<T, screen>(B, tol, I, nd.lo, nd.hi, ws);
+        const OptResult res = eval_optimality<T>(B, tol, I, nd.lo, nd.hi, ws);
         lc.c += res.lp2_piv;
         lc.d += res.cheb_piv;
-        if (!res.decided) {
-            if (lane == 0) {
-                const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_opt, 1ull);
-                if (qi < B.q_cap) B.q_opt[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
-            }
-            continue;
-        }
         lc.a += res.optimal;
         lc.b += res.region;
-        if (lane == 0) write_opt(B, nd, level, res, !screen);
+        if (lane == 0) write_opt(B, nd, level, res, true);
         __syncwarp();
     }
     if (lc.inst >= 0 && lane == 0) {
@@ -1086,7 +1071,7 @@ __global__ void __launch_bounds__(128) k_optimality_fp64(DevBuffers B, Tol tol, 
         if (x >= nq) break;
         const Node nd = B.node[side][B.q_opt[x]];
         const InstDesc &I = B.inst[nd.inst];
-        const OptResult res = eval_optimality<double, false>(B, tol, I, nd.lo, nd.hi, ws);
+        const OptResult res = eval_optimality<double>(B, tol, I, nd.lo, nd.hi, ws);
         if (lane == 0) {
             InstCtl *ic = &B.ictl[nd.inst];
             atomicAdd((unsigned long long *)&ic->fb_opt, 1ull);
@@ -1104,6 +1089,328 @@ __global__ void __launch_bounds__(128) k_optimality_fp64(DevBuffers B, Tol tol, 
 // level 0, finalisation and reset
 // ---------------------------------------------------------------------
 // One warp per instance: the empty set with the root LP1 tableau.
+// ---------------------------------------------------------------------
+// FP32 LP2 screen, several sets per warp
+// ---------------------------------------------------------------------
+// A warp takes NG = 32/GL feasible sets at once.  The KKT factorisation and
+// the region rows of each set run on the whole warp, one set after the
+// other, straight into that set's LP2 tableau; then NG groups of GL lanes
+// run the NG LP2s in lock step: every lane executes every instruction of the
+// simplex loop and a group that has finished only stops writing, so one
+// shared-memory instruction serves NG tableaus and the arg-min reductions
+// take log2(GL) shuffle steps.  The pivoting rules and roundings are those of
+// warp_simplex; the verdict is that of the FP32 screen in eval_optimality.
+
+template <int GL>
+__device__ __forceinline__ int group_argmin(unsigned key, unsigned id, int idx)
+{
+    if constexpr (GL == 32) {
+        return warp_argmin(key, id, idx);
+    } else {
+#pragma unroll
+        for (int off = GL / 2; off; off >>= 1) {
+            const unsigned k2 = __shfl_xor_sync(FULLMASK, key, off);
+            const unsigned i2 = __shfl_xor_sync(FULLMASK, id, off);
+            const int x2 = __shfl_xor_sync(FULLMASK, idx, off);
+            if (k2 < key || (k2 == key && i2 < id)) { key = k2; id = i2; idx = x2; }
+        }
+        return idx;
+    }
+}
+
+template <int GL>
+__device__ __forceinline__ float group_max(float v)
+{
+#pragma unroll
+    for (int off = GL / 2; off; off >>= 1) { const float o = __shfl_xor_sync(FULLMASK, v, off); if (o > v) v = o; }
+    return v;
+}
+
+// Lock-step simplex of the lane groups (run: this group has an LP to solve;
+// a group without one returns LP_SKIPPED).  All 32 lanes must call it.
+template <int GL>
+__device__ int group_simplex(const Lp<float> &L, bool run, float tol_piv, float tol_dj, int max_piv, int degen_switch,
+                             int *piv_out)
+{
+    const int sub = lane_id() & (GL - 1);
+    int piv = 0, degen = 0, status = run ? -1 : LP_SKIPPED;
+    bool bland = false;
+    float *obj = L.tab + (size_t)L.nrows * L.ld;
+    for (;;) {
+        if (!__any_sync(FULLMASK, status < 0)) break;
+        bool act = status < 0;
+        // pricing: largest |reduced cost|, smallest id on ties (Bland: smallest id)
+        unsigned bkey = 0xffffffffu, bid_ = 0xffffffffu;
+        int bq = -1;
+        if (act) {
+            for (int j = sub; j < L.ncols; j += GL) {
+                const float g = obj[j];
+                const int id = L.nid[j];
+                const float sc = (id < L.nfree) ? fabsf(g) : g;
+                if (!(sc > tol_dj)) continue;
+                const unsigned k = bland ? 0u : ~key_of(sc);
+                if (bq < 0 || k < bkey || (k == bkey && (unsigned)id < bid_)) { bkey = k; bid_ = id; bq = j; }
+            }
+        }
+        const int q = group_argmin<GL>(bkey, bid_, bq);
+        if (act && q < 0) { status = LP_OPTIMAL; act = false; }
+        // ratio test: smallest max(beta,0)/a over a > tol_piv, smallest id on ties
+        float sg = 1.0f;
+        unsigned rkey = 0xffffffffu, rid = 0xffffffffu;
+        int bri = -1;
+        if (act) {
+            sg = obj[q] > 0.0f ? 1.0f : -1.0f;
+            for (int i = sub; i < L.nrows; i += GL) {
+                const int id = L.bid[i];
+                if (id < L.nfree) continue;
+                const float a = sg * L.tab[(size_t)i * L.ld + q];
+                if (!(a > tol_piv)) continue;
+                float beta = L.tab[(size_t)i * L.ld + L.ncols];
+                if (!(beta > 0.0f)) beta = 0.0f;
+                const unsigned k = key_of(ratio_div(beta, a));
+                if (bri < 0 || k < rkey || (k == rkey && (unsigned)id < rid)) { rkey = k; rid = id; bri = i; }
+            }
+        }
+        const int r = group_argmin<GL>(rkey, rid, bri);
+        if (act && r < 0) { status = LP_UNBOUNDED; act = false; }
+        if (act && piv >= max_piv) { status = LP_ITER_LIMIT; act = false; }
+        float rr = 0.0f, inv = 0.0f;
+        float *R = L.tab;
+        if (act) {
+            R = L.tab + (size_t)r * L.ld;
+            float br = R[L.ncols];
+            if (!(br > 0.0f)) br = 0.0f;
+            rr = ratio_div(br, sg * R[q]);
+            inv = xdiv(1.0f, R[q]);
+        }
+        __syncwarp();
+        if (act)
+            for (int j = sub; j <= L.ncols; j += GL) R[j] = (j == q) ? inv : xmul(R[j], inv);
+        __syncwarp();
+        if (act) {
+            for (int i = sub; i <= L.nrows; i += GL) {
+                if (i == r) continue;
+                float *Ti = L.tab + (size_t)i * L.ld;
+                const float nf = -Ti[q];
+                row_update(Ti, R, nf, L.ncols);
+                Ti[q] = xmul(nf, inv);
+            }
+        }
+        __syncwarp();
+        if (act && sub == 0) {
+            const uint8_t t = L.bid[r];
+            L.bid[r] = L.nid[q];
+            L.nid[q] = t;
+        }
+        __syncwarp();
+        if (act) {
+            piv++;
+            degen = (rr == 0.0f) ? degen + 1 : 0;
+            bland = degen >= degen_switch;
+        }
+    }
+    *piv_out = piv;
+    return status;
+}
+
+struct ScreenSlot {             // one set of the grouped FP32 screen
+    Node nd;
+    long long x;                // node index
+    int state;                  // SLOT_*
+    int m, R2, p, ld2;
+    int status, piv;            // LP2 result
+    float t0, amax, rho, g0, bmax, t, g2;
+};
+enum : int { SLOT_EMPTY = 0, SLOT_LP2 = 1, SLOT_UNDECIDED = 2 };
+
+// per-warp layout: KKT workspace (R, Y, Lambda, S), then per group the LP2
+// tableau (R2+1) x ld2, its ids (R2 + P1) and the slot record
+__host__ __device__ inline size_t screen_kkt_bytes(const SlotDims &sd)
+{
+    return align16((size_t)sd.maxK * sd.maxK * 4) + 2 * align16((size_t)sd.maxK * sd.maxP1 * 4) +
+           align16((size_t)sd.maxK * sizeof(int));
+}
+__host__ __device__ inline size_t screen_group_bytes(const SlotDims &sd)
+{
+    return align16((size_t)(sd.maxR2 + 1) * sd.maxLD2 * 4) + align16((size_t)sd.maxR2 + sd.maxP1) +
+           align16(sizeof(ScreenSlot));
+}
+__host__ __device__ inline size_t screen_warp_bytes(int gl, const SlotDims &sd)
+{
+    return screen_kkt_bytes(sd) + (size_t)(32 / gl) * screen_group_bytes(sd);
+}
+
+template <int GL>
+__global__ void __launch_bounds__(32) k_opt_screen(DevBuffers B, Tol tol, SlotDims sd, int level)
+{
+    constexpr int NG = 32 / GL;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = lane_id(), grp = lane / GL, sub = lane & (GL - 1);
+    OptWs<float> ws;
+    {
+        size_t o = 0;
+        ws.R = (float *)(smem + o); o += align16((size_t)sd.maxK * sd.maxK * 4);
+        ws.Y = (float *)(smem + o); o += align16((size_t)sd.maxK * sd.maxP1 * 4);
+        ws.Lam = (float *)(smem + o); o += align16((size_t)sd.maxK * sd.maxP1 * 4);
+        ws.S = (int *)(smem + o);
+        ws.G = nullptr; ws.Tb = nullptr; ws.ids = nullptr;
+    }
+    unsigned char *gbase = smem + screen_kkt_bytes(sd);
+    const size_t gbytes = screen_group_bytes(sd);
+    const size_t tab_bytes = align16((size_t)(sd.maxR2 + 1) * sd.maxLD2 * 4);
+    const size_t ids_bytes = align16((size_t)sd.maxR2 + sd.maxP1);
+    auto tab_of = [&](int g) { return (float *)(gbase + g * gbytes); };
+    auto ids_of = [&](int g) { return (uint8_t *)(gbase + g * gbytes + tab_bytes); };
+    auto slot_of = [&](int g) { return (ScreenSlot *)(gbase + g * gbytes + tab_bytes + ids_bytes); };
+
+    const int side = level & 1;
+    Ctl *ctl = B.ctl;
+    const long long nn = ctl->n_node[side] < B.node_cap ? ctl->n_node[side] : B.node_cap;
+    LocalInstCounters lc;
+    lc.reset(-1);
+    for (;;) {
+        long long x0;
+        if (lane == 0) x0 = (long long)atomicAdd(&ctl->ctr[3], (unsigned long long)NG);
+        x0 = __shfl_sync(FULLMASK, x0, 0);
+        if (x0 >= nn) break;
+        // phase A: KKT and region rows of each set, the whole warp per set
+        for (int g = 0; g < NG; g++) {
+            ScreenSlot *sl = slot_of(g);
+            const long long x = x0 + g;
+            int state = SLOT_EMPTY;
+            Node nd;
+            if (x < nn) {
+                nd = B.node[side][x];
+                if ((nd.flags & (NODE_VALID | NODE_FEASIBLE)) == (NODE_VALID | NODE_FEASIBLE) &&
+                    level >= B.inst[nd.inst].k_min)
+                    state = SLOT_LP2;
+            }
+            if (state == SLOT_LP2) {
+                const InstDesc &I = B.inst[nd.inst];
+                const KktData<float> D = kkt_data<float>(B, I);
+                const int m = I.m, p = I.p, ncp = I.ncp, P1 = p + 1, R2 = m + ncp, ld2 = I.ld2;
+                int k = 0;
+                float rho = 1.0f;
+                if (kkt_factor<float>(D, I, nd.lo, nd.hi, tol.margin_licq32, ws, &k, &rho)) {
+                    state = SLOT_UNDECIDED;
+                } else {
+                    float *Tb = tab_of(g);
+                    uint8_t *bid = ids_of(g), *nid = bid + R2;
+                    const float amax = region_rows<float, true>(D, I, nd.lo, nd.hi, k, ws, Tb, ld2, P1);
+                    // LP2: max t  s.t.  g theta + t <= h (constraint rows), At theta <= bt
+                    float t0 = pos_inf<float>();
+                    for (int r = lane; r < m; r += 32) { const float h = Tb[(size_t)r * ld2 + P1]; if (h < t0) t0 = h; }
+#pragma unroll
+                    for (int off = 16; off; off >>= 1) { const float o = __shfl_xor_sync(FULLMASK, t0, off); if (o < t0) t0 = o; }
+                    float g0 = 1.0f;
+                    for (int r = lane; r < R2; r += 32) {
+                        float *tr = Tb + (size_t)r * ld2;
+                        for (int cc = 0; cc < p; cc++) { const float a = fabsf(tr[cc]); if (a > g0) g0 = a; }
+                        const float cf = (r < m) ? 1.0f : 0.0f;
+                        float beta = __fmaf_rn(-cf, t0, tr[P1]);
+                        if (!(beta > 0.0f)) beta = 0.0f;
+                        tr[p] = cf;
+                        tr[P1] = beta;
+                        bid[r] = (uint8_t)(P1 + r);
+                    }
+                    for (int cc = lane; cc <= P1; cc += 32) {
+                        float *ob = Tb + (size_t)R2 * ld2;
+                        ob[cc] = (cc == p) ? 1.0f : (cc == P1 ? -t0 : 0.0f);
+                        if (cc < P1) nid[cc] = (uint8_t)cc;
+                    }
+                    float bmax = 0.0f;
+                    for (int ii = lane; ii < ncp; ii += 32) { const float v = fabsf(D.bt[ii]); if (v > bmax) bmax = v; }
+                    g0 = group_max<32>(g0);
+                    bmax = group_max<32>(bmax);
+                    if (lane == 0) {
+                        sl->m = m; sl->R2 = R2; sl->p = p; sl->ld2 = ld2;
+                        sl->t0 = t0; sl->amax = amax; sl->rho = rho; sl->g0 = g0; sl->bmax = bmax;
+                    }
+                }
+            }
+            if (lane == 0) {
+                sl->state = state;
+                sl->x = x;
+                if (state != SLOT_EMPTY) sl->nd = nd;
+                sl->piv = 0;
+                sl->status = LP_SKIPPED;
+            }
+            __syncwarp();
+        }
+        // phase B: the NG LP2s in lock step, one lane group each
+        {
+            ScreenSlot *sl = slot_of(grp);
+            const bool run = sl->state == SLOT_LP2;
+            const int R2 = run ? sl->R2 : 0, p = run ? sl->p : 0, ld2 = run ? sl->ld2 : 4;
+            const int P1 = p + 1;
+            float *Tb = tab_of(grp);
+            uint8_t *bid = ids_of(grp);
+            Lp<float> L{Tb, ld2, R2, P1, P1, bid, bid + R2};
+            int piv = 0;
+            const int st = group_simplex<GL>(L, run, tol.tol_piv32, tol.tol_dj32, tol.max_pivots, tol.degen_switch, &piv);
+            float g2 = 0.0f;
+            if (run && st == LP_OPTIMAL)
+                for (int r = sub; r < R2; r += GL)
+                    for (int cc = 0; cc < P1; cc++) { const float a = fabsf(Tb[(size_t)r * ld2 + cc]); if (a > g2) g2 = a; }
+            g2 = group_max<GL>(g2);
+            const float t = run ? -Tb[(size_t)R2 * ld2 + P1] : 0.0f;
+            __syncwarp();
+            if (run && sub == 0) { sl->status = st; sl->piv = piv; sl->t = t; sl->g2 = g2; }
+            __syncwarp();
+        }
+        // phase C: verdicts, records, queue and counters
+        for (int g = 0; g < NG; g++) {
+            const ScreenSlot *sl = slot_of(g);
+            const int state = sl->state;
+            if (state == SLOT_EMPTY) continue;
+            const Node nd = sl->nd;
+            if (nd.inst != lc.inst) {
+                if (lc.inst >= 0 && lane == 0) {
+                    atomicAdd((unsigned long long *)&B.ictl[lc.inst].optimal, (unsigned long long)lc.a);
+                    atomicAdd((unsigned long long *)&B.ictl[lc.inst].region, (unsigned long long)lc.b);
+                    atomicAdd((unsigned long long *)&B.ictl[lc.inst].lp2_piv, (unsigned long long)lc.c);
+                    atomicAdd((unsigned long long *)&B.ictl[lc.inst].cheb_piv, (unsigned long long)lc.d);
+                }
+                lc.reset(nd.inst);
+            }
+            lc.c += sl->piv;
+            // "not optimal" is final when t < -margin_t * scale, scale = (row
+            // magnitude / smallest Cholesky pivot ratio) * (reach of theta in
+            // the box) * (relative element growth of the LP2 tableau); all in
+            // FP32 (rho > margin_licq and g0 >= 1, so the quotients are tame)
+            bool decided = false;
+            if (state == SLOT_LP2 && sl->status == LP_OPTIMAL) {
+                const float growth = sl->g2 > sl->g0 ? __fdividef(sl->g2, sl->g0) : 1.0f;
+                const float scale = __fdividef(sl->amax, sl->rho) * (1.0f + (float)sl->p * sl->bmax) * growth;
+                decided = sl->t < -tol.margin_t32 * scale;
+            }
+            if (!decided) {
+                if (lane == 0) {
+                    const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_opt, 1ull);
+                    if (qi < B.q_cap) B.q_opt[qi] = (int)sl->x; else atomicOr(&ctl->overflow, OV_QUEUE);
+                }
+                continue;
+            }
+            // a final "not optimal" only leaves a diagnostic record
+            if (lane == 0 && nd.rec >= 0 && B.rec) {
+                OptResult res;
+                res.licq = 1; res.lp2_status = sl->status; res.lp2_piv = sl->piv;
+                res.cheb_status = LP_SKIPPED; res.cheb_piv = 0; res.optimal = 0; res.region = 0;
+                res.t = (double)sl->t; res.r = __longlong_as_double(0x7ff8000000000000LL);
+                res.decided = true;
+                write_opt(B, nd, level, res, false);
+            }
+        }
+        __syncwarp();
+    }
+    if (lc.inst >= 0 && lane == 0) {
+        atomicAdd((unsigned long long *)&B.ictl[lc.inst].optimal, (unsigned long long)lc.a);
+        atomicAdd((unsigned long long *)&B.ictl[lc.inst].region, (unsigned long long)lc.b);
+        atomicAdd((unsigned long long *)&B.ictl[lc.inst].lp2_piv, (unsigned long long)lc.c);
+        atomicAdd((unsigned long long *)&B.ictl[lc.inst].cheb_piv, (unsigned long long)lc.d);
+    }
+}
+
 template <typename T>
 __global__ void k_level0(DevBuffers B)
 {
@@ -1291,6 +1598,8 @@ size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd)
                            : lp1_slot_bytes<float>(sd.maxM1, sd.maxLD1, sd.maxNv);
 }
 
+size_t screen_smem_per_warp(int lanes, const SlotDims &sd) { return screen_warp_bytes(lanes, sd); }
+
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd)
 {
     return prec_bytes == 8 ? opt_slot_bytes<double>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2d)
@@ -1313,8 +1622,10 @@ const void *kernel_ptr(const char *name)
         {"feas32", (const void *)k_feasibility<float>},
         {"lp1_fp64", (const void *)k_lp1_fp64},
         {"opt64", (const void *)k_optimality<double>},
-        {"opt32", (const void *)k_optimality<float>},
         {"opt_fp64", (const void *)k_optimality_fp64},
+        {"screen8", (const void *)k_opt_screen<8>},
+        {"screen16", (const void *)k_opt_screen<16>},
+        {"screen32", (const void *)k_opt_screen<32>},
         {"level0_64", (const void *)k_level0<double>},
         {"level0_32", (const void *)k_level0<float>},
         {"reset", (const void *)k_reset},
@@ -1353,8 +1664,17 @@ cudaError_t launch_lp1_fp64(const DevBuffers &B, const Tol &tol, const SlotDims 
 cudaError_t launch_optimality(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int prec,
                               int grid, size_t smem, cudaStream_t s)
 {
-    if (prec == PREC_FP64) k_optimality<double><<<grid, 128, smem, s>>>(B, tol, sd, level);
-    else k_optimality<float><<<grid, 128, smem, s>>>(B, tol, sd, level);
+    (void)prec;   // the FP32 screen of the mixed path is launch_opt_screen
+    k_optimality<double><<<grid, 128, smem, s>>>(B, tol, sd, level);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int lanes, int grid,
+                              size_t smem, cudaStream_t s)
+{
+    if (lanes == 8) k_opt_screen<8><<<grid, 32, smem, s>>>(B, tol, sd, level);
+    else if (lanes == 16) k_opt_screen<16><<<grid, 32, smem, s>>>(B, tol, sd, level);
+    else k_opt_screen<32><<<grid, 32, smem, s>>>(B, tol, sd, level);
     return cudaGetLastError();
 }
 

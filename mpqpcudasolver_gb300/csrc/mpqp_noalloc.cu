@@ -202,7 +202,7 @@ extern "C" int mpqp_region_laws_noalloc(const mpqp_problem *prob, long long n_se
     B.inst = (const InstDesc *)scratch;
     B.dpool = (const double *)(scratch + kDescBytes);
     B.n_inst = 1;
-    Tol tol;
+    Tol tol{};
     memset(&tol, 0, sizeof(tol));
     mpqp_options o;
     mpqp_default_options(&o);

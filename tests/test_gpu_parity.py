@@ -141,3 +141,23 @@ def test_mixed_equals_fp64_on_the_full_bench_batch(gpu_lib):
               "truncated", "last_level"):
         assert np.array_equal(r32.inst[f], r64.inst[f]), f
     assert r32.candidates == 60802277
+
+
+@pytest.mark.parametrize("lanes", [8, 16])
+def test_screen_lane_groups_match_full_warp_screen(gpu_lib, lanes):
+    """The FP32 LP2 screen run by groups of 8 or 16 lanes (4 or 2 sets per
+    warp, in lock step) takes the pivots of the full-warp screen with the same
+    roundings: every record, FP32 t included, and the fallback counts agree."""
+    probs = [P.scale_problem(P.random_n10_m43_p4()), P.scale_problem(P.illcond_n16_m62_p8()),
+             P.scale_problem(P.mpc_mpqp(0))]
+    kw = dict(precision=solver.MIXED, k_max=3, record=1, rec_cap=1 << 20, cand_cap=1 << 20, arena_bytes=1 << 28)
+    a = solver.solve(probs, screen_lanes=32, **kw)
+    b = solver.solve(probs, screen_lanes=lanes, **kw)
+    assert a.status == 0 and b.status == 0
+    ra, rb = _sorted(a.rec, key_inst=True), _sorted(b.rec, key_inst=True)
+    assert len(ra) == len(rb) == a.candidates
+    for f in ("inst", "mask_lo", "mask_hi", "feasible", "optimal", "region", "lp2_status", "lp2_pivots", "fp64"):
+        assert np.array_equal(ra[f], rb[f]), f
+    assert _same(ra["t"], rb["t"])
+    for f in ("fallback_lp1", "fallback_opt", "optimal", "regions"):
+        assert a.total(f) == b.total(f), f
