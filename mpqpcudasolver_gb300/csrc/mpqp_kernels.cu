@@ -1213,6 +1213,122 @@ __device__ int group_simplex(const Lp<float> &L, bool run, float tol_piv, float 
     return status;
 }
 
+// The full-warp FP32 LP2 of the screen for p + 1 <= 7 and R2 <= 96: the
+// pivoting rules, operations and their order are those of warp_simplex on
+// the same tableau, with the bookkeeping moved to registers: each lane keeps
+// the offsets and basic ids of its rows lane, lane+32, lane+64; lanes
+// 0..P1 hold the objective row (lane j: column j, lane P1: right-hand side)
+// and lanes 0..P1-1 the nonbasic ids; the constraint rows stay in shared
+// memory (row stride ld, NCH = (P1+4)/4 float4 chunks per row).
+template <int NCH>
+__device__ int lp2_screen_simplex(float *tab, int ld, int R2, int P1, float tol_piv, float tol_dj, int max_piv,
+                                  int degen_switch, int *piv_out, float *t_out)
+{
+    constexpr int NR = 3;
+    const int lane = lane_id();
+    const int nfree = P1, ncols = P1;
+    int rowoff[NR], bidr[NR];
+    bool valid[NR];
+#pragma unroll
+    for (int s = 0; s < NR; s++) {
+        const int i = lane + 32 * s;
+        valid[s] = i < R2;
+        rowoff[s] = i * ld;
+        bidr[s] = P1 + i;
+    }
+    float ob = lane <= ncols ? tab[R2 * ld + lane] : 0.0f;
+    int nidl = lane < ncols ? lane : 255;
+    int piv = 0, degen = 0, status;
+    bool bland = false;
+    for (;;) {
+        // pricing: largest |reduced cost|, smallest id on ties (Bland: smallest id)
+        unsigned key = 0xffffffffu, kid = 0xffffffffu;
+        int kidx = -1;
+        if (lane < ncols) {
+            const float sc = nidl < nfree ? fabsf(ob) : ob;
+            if (sc > tol_dj) { key = bland ? 0u : ~key_of(sc); kid = (unsigned)nidl; kidx = lane; }
+        }
+        const int q = warp_argmin(key, kid, kidx);
+        if (q < 0) { status = LP_OPTIMAL; break; }
+        const float obq = __shfl_sync(FULLMASK, ob, q);
+        const float sg = obq > 0.0f ? 1.0f : -1.0f;
+        // ratio test: smallest max(beta,0)/a over a > tol_piv, smallest id on ties
+        unsigned rkey = 0xffffffffu, rid = 0xffffffffu;
+        int bri = -1;
+        float aq[NR];
+#pragma unroll
+        for (int s = 0; s < NR; s++) {
+            aq[s] = 0.0f;
+            if (valid[s]) {
+                aq[s] = tab[rowoff[s] + q];
+                if (bidr[s] >= nfree) {
+                    const float a = sg * aq[s];
+                    if (a > tol_piv) {
+                        float beta = tab[rowoff[s] + ncols];
+                        if (!(beta > 0.0f)) beta = 0.0f;
+                        const unsigned k = key_of(ratio_div(beta, a));
+                        if (bri < 0 || k < rkey || (k == rkey && (unsigned)bidr[s] < rid)) {
+                            rkey = k; rid = (unsigned)bidr[s]; bri = lane + 32 * s;
+                        }
+                    }
+                }
+            }
+        }
+        const int r = warp_argmin(rkey, rid, bri);
+        if (r < 0) { status = LP_UNBOUNDED; break; }
+        if (piv >= max_piv) { status = LP_ITER_LIMIT; break; }
+        float *Rp = tab + r * ld;
+        float br = Rp[ncols];
+        if (!(br > 0.0f)) br = 0.0f;
+        const float prq = Rp[q];
+        const float rr = ratio_div(br, sg * prq);
+        const float inv = xdiv(1.0f, prq);
+        const int owner = r & 31, oslot = r >> 5;
+        const int lid = __shfl_sync(FULLMASK, (int)rid, owner);   // the owner's best row is r
+        const int eid = __shfl_sync(FULLMASK, nidl, q);
+        __syncwarp();
+        if (lane <= ncols) Rp[lane] = (lane == q) ? inv : xmul(Rp[lane], inv);
+        __syncwarp();
+        float4 Rv[NCH];
+#pragma unroll
+        for (int c = 0; c < NCH; c++) Rv[c] = reinterpret_cast<const float4 *>(Rp)[c];
+        const float rl = lane <= ncols ? Rp[lane] : 0.0f;
+#pragma unroll
+        for (int s = 0; s < NR; s++) {
+            if (valid[s] && lane + 32 * s != r) {
+                float *Ti = tab + rowoff[s];
+                const float nf = -aq[s];
+#pragma unroll
+                for (int c = 0; c < NCH; c++) {
+                    float4 t = reinterpret_cast<float4 *>(Ti)[c];
+                    t.x = __fmaf_rn(nf, Rv[c].x, t.x);
+                    t.y = __fmaf_rn(nf, Rv[c].y, t.y);
+                    t.z = __fmaf_rn(nf, Rv[c].z, t.z);
+                    t.w = __fmaf_rn(nf, Rv[c].w, t.w);
+                    reinterpret_cast<float4 *>(Ti)[c] = t;
+                }
+                Ti[q] = xmul(nf, inv);
+            }
+        }
+        if (lane <= ncols) {
+            const float nfo = -obq;
+            ob = (lane == q) ? xmul(nfo, inv) : __fmaf_rn(nfo, rl, ob);
+        }
+        if (lane == owner) {
+#pragma unroll
+            for (int s = 0; s < NR; s++) if (s == oslot) bidr[s] = eid;
+        }
+        if (lane == q) nidl = lid;
+        __syncwarp();
+        piv++;
+        degen = (rr == 0.0f) ? degen + 1 : 0;
+        bland = degen >= degen_switch;
+    }
+    *piv_out = piv;
+    *t_out = -__shfl_sync(FULLMASK, ob, ncols);
+    return status;
+}
+
 struct ScreenSlot {             // one set of the grouped FP32 screen
     Node nd;
     long long x;                // node index
@@ -1338,7 +1454,35 @@ __global__ void __launch_bounds__(32) k_opt_screen(DevBuffers B, Tol tol, SlotDi
             __syncwarp();
         }
         // phase B: the NG LP2s in lock step, one lane group each
-        {
+        if constexpr (GL == 32) {
+            ScreenSlot *sl = slot_of(0);
+            if (sl->state == SLOT_LP2) {
+                const int R2 = sl->R2, P1 = sl->p + 1, ld2 = sl->ld2;
+                float *Tb = tab_of(0);
+                int piv = 0, st;
+                float t;
+                if (P1 <= 7 && R2 <= 96) {
+                    st = (P1 + 4) / 4 == 1
+                             ? lp2_screen_simplex<1>(Tb, ld2, R2, P1, tol.tol_piv32, tol.tol_dj32, tol.max_pivots,
+                                                     tol.degen_switch, &piv, &t)
+                             : lp2_screen_simplex<2>(Tb, ld2, R2, P1, tol.tol_piv32, tol.tol_dj32, tol.max_pivots,
+                                                     tol.degen_switch, &piv, &t);
+                } else {
+                    uint8_t *bid = ids_of(0);
+                    Lp<float> L{Tb, ld2, R2, P1, P1, bid, bid + R2};
+                    st = group_simplex<32>(L, true, tol.tol_piv32, tol.tol_dj32, tol.max_pivots, tol.degen_switch, &piv);
+                    t = -Tb[(size_t)R2 * ld2 + P1];
+                }
+                float g2 = 0.0f;
+                if (st == LP_OPTIMAL)
+                    for (int r = lane; r < R2; r += 32)
+                        for (int cc = 0; cc < P1; cc++) { const float a = fabsf(Tb[(size_t)r * ld2 + cc]); if (a > g2) g2 = a; }
+                g2 = group_max<32>(g2);
+                __syncwarp();
+                if (lane == 0) { sl->status = st; sl->piv = piv; sl->t = t; sl->g2 = g2; }
+            }
+            __syncwarp();
+        } else {
             ScreenSlot *sl = slot_of(grp);
             const bool run = sl->state == SLOT_LP2;
             const int R2 = run ? sl->R2 : 0, p = run ? sl->p : 0, ld2 = run ? sl->ld2 : 4;

@@ -496,13 +496,15 @@ static inline uint64_t mix64(uint64_t x)
     return x;
 }
 
-static void mh_init(mhash *h, int64_t n)
+static int mh_init(mhash *h, int64_t n)
 {
     uint64_t cap = 16;
     while (cap < (uint64_t)(2 * n + 1)) cap <<= 1;
     h->cap = cap;
     h->lo = calloc(cap, 8); h->hi = calloc(cap, 8); h->val = malloc(cap * 4);
+    if (!h->lo || !h->hi || !h->val) return ORC_ENOMEM;
     for (uint64_t i = 0; i < cap; i++) h->val[i] = -1;
+    return 0;
 }
 
 static void mh_free(mhash *h) { free(h->lo); free(h->hi); free(h->val); }
@@ -601,6 +603,39 @@ static void rec_init(orc_cand *r)
     r->lp2_status = ORC_SKIPPED; r->cheb_status = ORC_SKIPPED;
 }
 
+/* LP1 tableaus computed per pass of the level loop (candidates) */
+#define ORC_CHUNK 65536
+
+/* parents of one level: tableaus, basis ids and masks, grown on demand */
+typedef struct {
+    double *T; uint8_t *B, *N; uint64_t *lo, *hi;
+    int64_t n, cap;
+} parent_list;
+
+static void pl_free(parent_list *l)
+{
+    free(l->T); free(l->B); free(l->N); free(l->lo); free(l->hi);
+    memset(l, 0, sizeof(*l));
+}
+
+static int pl_reserve(parent_list *l, int64_t cap, size_t tsz, int M1, int nv)
+{
+    if (cap <= l->cap) return 0;
+    double *T = realloc(l->T, (size_t)cap * tsz * sizeof(double));
+    if (T) l->T = T;
+    uint8_t *B = realloc(l->B, (size_t)cap * M1);
+    if (B) l->B = B;
+    uint8_t *N = realloc(l->N, (size_t)cap * nv);
+    if (N) l->N = N;
+    uint64_t *lo = realloc(l->lo, (size_t)cap * 8);
+    if (lo) l->lo = lo;
+    uint64_t *hi = realloc(l->hi, (size_t)cap * 8);
+    if (hi) l->hi = hi;
+    if (!T || !B || !N || !lo || !hi) return ORC_ENOMEM;
+    l->cap = cap;
+    return 0;
+}
+
 int orc_enumerate(const orc_problem *pr, const orc_tol *tol, int k_min, int k_max,
                   int64_t budget, int exhaustive, int nthreads, int keep_records, orc_result *out)
 {
@@ -611,18 +646,23 @@ int orc_enumerate(const orc_problem *pr, const orc_tol *tol, int k_min, int k_ma
     if (k_max > d.m) k_max = d.m;
     if (k_min < 0) k_min = 0;
     const size_t tsz = (size_t)(d.M1 + 1) * d.ld1;
-    /* level 0: the empty set */
-    int64_t nF = 1;
-    double *FT = malloc(tsz * sizeof(double));
-    uint8_t *FB = malloc(d.M1), *FN = malloc(d.nv);
-    uint64_t *Flo = malloc(8), *Fhi = malloc(8);
-    {
-        lp1_state s = { FT, FB, FN };
-        lp1_init_root(&d, &s);
-        Flo[0] = 0; Fhi[0] = 0;
-    }
+    /* everything the level loop owns, freed on every exit */
+    parent_list F = {0}, NF = {0};
     int64_t cap_rec = 1024, n_rec = 0;
-    orc_cand *recs = keep_records ? malloc(cap_rec * sizeof(orc_cand)) : NULL;
+    orc_cand *recs = NULL, *crec = NULL;
+    int32_t *cpar = NULL, *cj = NULL;
+    double *CT = NULL;
+    uint8_t *CB = NULL, *CN = NULL;
+    int64_t *fidx = NULL;
+    mhash h = {0};
+    /* level 0: the empty set */
+    if ((rc = pl_reserve(&F, 1, tsz, d.M1, d.nv))) goto done;
+    {
+        lp1_state s = { F.T, F.B, F.N };
+        lp1_init_root(&d, &s);
+        F.lo[0] = 0; F.hi[0] = 0; F.n = 1;
+    }
+    if (keep_records && !(recs = malloc(cap_rec * sizeof(orc_cand)))) { rc = ORC_ENOMEM; goto done; }
     {
         orc_cand r0;
         rec_init(&r0);
@@ -641,75 +681,88 @@ int orc_enumerate(const orc_problem *pr, const orc_tol *tol, int k_min, int k_ma
     }
     out->n_levels = 1;
     int S[128];
-    for (int k = 1; k <= k_max && nF > 0; k++) {
-        mhash h;
-        mh_init(&h, nF);
-        for (int64_t i = 0; i < nF; i++) mh_insert(&h, Flo[i], Fhi[i], (int32_t)i);
+    for (int k = 1; k <= k_max && F.n > 0; k++) {
+        if ((rc = mh_init(&h, F.n))) goto done;
+        for (int64_t i = 0; i < F.n; i++) mh_insert(&h, F.lo[i], F.hi[i], (int32_t)i);
         /* candidates */
         int64_t ccap = 1024, nc = 0;
-        int32_t *cpar = malloc(ccap * 4), *cj = malloc(ccap * 4);
-        for (int64_t pi = 0; pi < nF; pi++) {
-            const int kp = mask_to_set(Flo[pi], Fhi[pi], S);
+        cpar = malloc(ccap * 4); cj = malloc(ccap * 4);
+        if (!cpar || !cj) { rc = ORC_ENOMEM; goto done; }
+        for (int64_t pi = 0; pi < F.n; pi++) {
+            const int kp = mask_to_set(F.lo[pi], F.hi[pi], S);
             const int jmin = kp ? S[kp - 1] + 1 : 0;
             for (int j = jmin; j < d.m; j++) {
                 int ok = 1;
                 for (int a = 0; a < kp && ok && !exhaustive; a++) {
-                    uint64_t lo = Flo[pi], hi = Fhi[pi];
+                    uint64_t lo = F.lo[pi], hi = F.hi[pi];
                     /* S + {j} - {S[a]} */
                     if (S[a] < 64) lo &= ~((uint64_t)1 << S[a]); else hi &= ~((uint64_t)1 << (S[a] - 64));
                     mask_set(&lo, &hi, j);
                     if (mh_find(&h, lo, hi) < 0) ok = 0;
                 }
                 if (!ok) { out->n_pruned++; continue; }
-                if (nc == ccap) { ccap *= 2; cpar = realloc(cpar, ccap * 4); cj = realloc(cj, ccap * 4); }
+                if (nc == ccap) {
+                    ccap *= 2;
+                    int32_t *a = realloc(cpar, ccap * 4);
+                    if (a) cpar = a;
+                    int32_t *b = realloc(cj, ccap * 4);
+                    if (b) cj = b;
+                    if (!a || !b) { rc = ORC_ENOMEM; goto done; }
+                }
                 cpar[nc] = (int32_t)pi; cj[nc] = j; nc++;
             }
         }
         mh_free(&h);
-        if (nc == 0) { free(cpar); free(cj); break; }
+        memset(&h, 0, sizeof(h));
+        if (nc == 0) break;
         if (budget > 0 && out->n_cand + nc > budget) {
             out->truncated = 1;
-            free(cpar); free(cj);
             break;
         }
         out->n_levels = k + 1;
-        double *CT = malloc(nc * tsz * sizeof(double));
-        uint8_t *CB = malloc(nc * d.M1), *CN = malloc(nc * d.nv);
-        orc_cand *crec = malloc(nc * sizeof(orc_cand));
+        /* children of the deepest level are nobody's parents */
+        const int keep_children = exhaustive || k < k_max;
+        const int64_t chunk = nc < ORC_CHUNK ? nc : ORC_CHUNK;
+        crec = malloc(nc * sizeof(orc_cand));
+        CT = malloc(chunk * tsz * sizeof(double));
+        CB = malloc(chunk * d.M1); CN = malloc(chunk * d.nv);
+        if (!crec || !CT || !CB || !CN) { rc = ORC_ENOMEM; goto done; }
         for (int64_t i = 0; i < nc; i++) {
             rec_init(&crec[i]);
-            crec[i].mask_lo = Flo[cpar[i]]; crec[i].mask_hi = Fhi[cpar[i]];
+            crec[i].mask_lo = F.lo[cpar[i]]; crec[i].mask_hi = F.hi[cpar[i]];
             mask_set(&crec[i].mask_lo, &crec[i].mask_hi, cj[i]);
             crec[i].level = k; crec[i].parent = cpar[i];
         }
         job_t jb;
         memset(&jb, 0, sizeof(jb));
         jb.d = &d; jb.tol = tol; jb.k = k;
-        jb.parT = FT; jb.parB = FB; jb.parN = FN; jb.cpar = cpar; jb.cj = cj;
-        jb.candT = CT; jb.candB = CB; jb.candN = CN; jb.rec = crec; jb.ncand = nc;
-        run_pool(lp1_worker, &jb, nthreads);
-        /* new feasible list (candidate order = lexicographic) */
-        int64_t nfn = 0;
-        for (int64_t i = 0; i < nc; i++) nfn += crec[i].feasible;
-        int64_t npar_new = exhaustive ? nc : nfn;
-        int64_t *fidx = malloc((nfn ? nfn : 1) * sizeof(int64_t));
-        double *NT = malloc((npar_new ? npar_new : 1) * tsz * sizeof(double));
-        uint8_t *NB = malloc((npar_new ? npar_new : 1) * d.M1), *NN = malloc((npar_new ? npar_new : 1) * d.nv);
-        uint64_t *Nlo = malloc((npar_new ? npar_new : 1) * 8), *Nhi = malloc((npar_new ? npar_new : 1) * 8);
-        int64_t f = 0, g = 0;
-        for (int64_t i = 0; i < nc; i++) {
-            out->n_lp1_pivots += crec[i].lp1_pivots;
-            if (crec[i].feasible) fidx[f++] = i;
-            if (!crec[i].feasible && !exhaustive) continue;
-            memcpy(NT + g * tsz, CT + i * tsz, tsz * sizeof(double));
-            memcpy(NB + g * d.M1, CB + i * d.M1, d.M1);
-            memcpy(NN + g * d.nv, CN + i * d.nv, d.nv);
-            Nlo[g] = crec[i].mask_lo; Nhi[g] = crec[i].mask_hi;
-            g++;
+        jb.parT = F.T; jb.parB = F.B; jb.parN = F.N;
+        jb.candT = CT; jb.candB = CB; jb.candN = CN;
+        /* LP1 chunk by chunk; the kept children in candidate (lexicographic) order */
+        for (int64_t c0 = 0; c0 < nc; c0 += chunk) {
+            const int64_t n = nc - c0 < chunk ? nc - c0 : chunk;
+            jb.cpar = cpar + c0; jb.cj = cj + c0; jb.rec = crec + c0; jb.ncand = n;
+            run_pool(lp1_worker, &jb, nthreads);
+            if (!keep_children) continue;
+            for (int64_t i = 0; i < n; i++) {
+                const orc_cand *r = &crec[c0 + i];
+                if (!r->feasible && !exhaustive) continue;
+                if (NF.n == NF.cap && (rc = pl_reserve(&NF, NF.cap ? 2 * NF.cap : 1024, tsz, d.M1, d.nv))) goto done;
+                memcpy(NF.T + NF.n * tsz, CT + i * tsz, tsz * sizeof(double));
+                memcpy(NF.B + NF.n * d.M1, CB + i * d.M1, d.M1);
+                memcpy(NF.N + NF.n * d.nv, CN + i * d.nv, d.nv);
+                NF.lo[NF.n] = r->mask_lo; NF.hi[NF.n] = r->mask_hi;
+                NF.n++;
+            }
         }
         free(CT); free(CB); free(CN);
+        CT = NULL; CB = NULL; CN = NULL;
+        int64_t nfn = 0;
+        for (int64_t i = 0; i < nc; i++) { nfn += crec[i].feasible; out->n_lp1_pivots += crec[i].lp1_pivots; }
+        if (!(fidx = malloc((nfn ? nfn : 1) * sizeof(int64_t)))) { rc = ORC_ENOMEM; goto done; }
+        for (int64_t i = 0, f = 0; i < nc; i++) if (crec[i].feasible) fidx[f++] = i;
         if (k >= k_min && nfn > 0) {
-            jb.feas_idx = fidx; jb.nfeas = nfn;
+            jb.rec = crec; jb.feas_idx = fidx; jb.nfeas = nfn;
             run_pool(opt_worker, &jb, nthreads);
         }
         for (int64_t i = 0; i < nc; i++) {
@@ -723,18 +776,30 @@ int orc_enumerate(const orc_problem *pr, const orc_tol *tol, int k_min, int k_ma
         if (keep_records) {
             if (n_rec + nc > cap_rec) {
                 while (n_rec + nc > cap_rec) cap_rec *= 2;
-                recs = realloc(recs, cap_rec * sizeof(orc_cand));
+                orc_cand *rr = realloc(recs, cap_rec * sizeof(orc_cand));
+                if (!rr) { rc = ORC_ENOMEM; goto done; }
+                recs = rr;
             }
             memcpy(recs + n_rec, crec, nc * sizeof(orc_cand));
             n_rec += nc;
         }
         free(crec); free(cpar); free(cj); free(fidx);
-        free(FT); free(FB); free(FN); free(Flo); free(Fhi);
-        FT = NT; FB = NB; FN = NN; Flo = Nlo; Fhi = Nhi; nF = npar_new;
+        crec = NULL; cpar = NULL; cj = NULL; fidx = NULL;
+        pl_free(&F);
+        F = NF;
+        memset(&NF, 0, sizeof(NF));
     }
-    free(FT); free(FB); free(FN); free(Flo); free(Fhi);
-    out->cand = recs;
+done:
+    mh_free(&h);
+    free(crec); free(cpar); free(cj); free(fidx); free(CT); free(CB); free(CN);
+    pl_free(&F); pl_free(&NF);
     free_data(&d);
+    if (rc) {
+        free(recs);
+        memset(out, 0, sizeof(*out));
+        return rc;
+    }
+    out->cand = recs;
     return 0;
 }
 

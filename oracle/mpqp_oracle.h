@@ -56,6 +56,7 @@ typedef struct {
 
 /* LP status codes (shared with the device code) */
 enum { ORC_OPTIMAL = 0, ORC_UNBOUNDED = 1, ORC_ITER_LIMIT = 2, ORC_SKIPPED = 3, ORC_LICQ_FAIL = 4 };
+#define ORC_ENOMEM (-5)   /* host memory exhausted */
 
 typedef struct {
     uint64_t mask_lo, mask_hi;
@@ -87,7 +88,11 @@ void orc_default_tol(orc_tol *tol);
  * plus the whole level fit in the budget; otherwise the enumeration stops
  * there (out->truncated = 1).  exhaustive = 1: every combination is a
  * candidate (children of all candidates, no subset test).
- * nthreads <= 1 runs serially.  Returns 0 on success, negative on error. */
+ * nthreads <= 1 runs serially.  The LP1 tableaus of a level are computed in
+ * chunks of ORC_CHUNK candidates; only children that become parents of the
+ * next level are kept (none at k_max unless exhaustive), so host memory
+ * grows with the feasible sets, not with the candidates.
+ * Returns 0 on success, negative on error (ORC_ENOMEM: out of memory). */
 int orc_enumerate(const orc_problem *pr, const orc_tol *tol, int k_min, int k_max,
                   int64_t budget, int exhaustive, int nthreads, int keep_records, orc_result *out);
 void orc_free_result(orc_result *res);
