@@ -258,6 +258,159 @@ __device__ int warp_simplex(const Lp<T> &L, T tol_piv, T tol_dj, int max_piv, in
     return status;
 }
 
+// Full-warp FP32 simplex with register bookkeeping, for tableaus of at most
+// 96 rows and NCH float4 chunks per row (NCH = (ncols+4)/4, the row stride a
+// multiple of 4): the pivoting rules, operations and their order are those of
+// warp_simplex on the same tableau (so the same pivots and bit-identical
+// values), with the bookkeeping moved to registers: each lane keeps the
+// offsets and basic ids of its rows lane, lane+32, lane+64; lanes 0..ncols
+// hold the objective row (lane j: column j; lane ncols: right-hand side) and
+// lanes 0..ncols-1 the nonbasic ids.  The constraint rows stay in shared
+// memory; the objective row and the ids are written back on return.  Ids
+// below ncols are free variables (nfree = ncols in both LPs).
+constexpr int kFastRows = 96;
+constexpr int kFastChunks = 6;
+
+template <int NCH>
+__device__ int simplex_fast32(float *tab, int ld, int nrows, int ncols, uint8_t *bid, uint8_t *nid, float tol_piv,
+                              float tol_dj, int max_piv, int degen_switch, int *piv_out)
+{
+    constexpr int NR = kFastRows / 32;
+    const int lane = lane_id();
+    const int nfree = ncols;
+    int rowoff[NR], bidr[NR];
+    bool valid[NR];
+#pragma unroll
+    for (int s = 0; s < NR; s++) {
+        const int i = lane + 32 * s;
+        valid[s] = i < nrows;
+        rowoff[s] = i * ld;
+        bidr[s] = valid[s] ? bid[i] : 255;
+    }
+    float *obj = tab + nrows * ld;
+    float ob = lane <= ncols ? obj[lane] : 0.0f;
+    int nidl = lane < ncols ? nid[lane] : 255;
+    int piv = 0, degen = 0, status;
+    bool bland = false;
+    for (;;) {
+        // pricing: largest |reduced cost|, smallest id on ties (Bland: smallest id)
+        unsigned key = 0xffffffffu, kid = 0xffffffffu;
+        int kidx = -1;
+        if (lane < ncols) {
+            const float sc = nidl < nfree ? fabsf(ob) : ob;
+            if (sc > tol_dj) { key = bland ? 0u : ~key_of(sc); kid = (unsigned)nidl; kidx = lane; }
+        }
+        const int q = warp_argmin(key, kid, kidx);
+        if (q < 0) { status = LP_OPTIMAL; break; }
+        const float obq = __shfl_sync(FULLMASK, ob, q);
+        const float sg = obq > 0.0f ? 1.0f : -1.0f;
+        // ratio test: smallest max(beta,0)/a over a > tol_piv, smallest id on ties
+        unsigned rkey = 0xffffffffu, rid = 0xffffffffu;
+        int bri = -1;
+        float aq[NR];
+#pragma unroll
+        for (int s = 0; s < NR; s++) {
+            aq[s] = 0.0f;
+            if (valid[s]) {
+                aq[s] = tab[rowoff[s] + q];
+                if (bidr[s] >= nfree) {
+                    const float a = sg * aq[s];
+                    if (a > tol_piv) {
+                        float beta = tab[rowoff[s] + ncols];
+                        if (!(beta > 0.0f)) beta = 0.0f;
+                        const unsigned k = key_of(ratio_div(beta, a));
+                        if (bri < 0 || k < rkey || (k == rkey && (unsigned)bidr[s] < rid)) {
+                            rkey = k; rid = (unsigned)bidr[s]; bri = lane + 32 * s;
+                        }
+                    }
+                }
+            }
+        }
+        const int r = warp_argmin(rkey, rid, bri);
+        if (r < 0) { status = LP_UNBOUNDED; break; }
+        if (piv >= max_piv) { status = LP_ITER_LIMIT; break; }
+        float *Rp = tab + r * ld;
+        float br = Rp[ncols];
+        if (!(br > 0.0f)) br = 0.0f;
+        const float prq = Rp[q];
+        const float rr = ratio_div(br, sg * prq);
+        const float inv = xdiv(1.0f, prq);
+        const int owner = r & 31, oslot = r >> 5;
+        const int lid = __shfl_sync(FULLMASK, (int)rid, owner);   // the owner's best row is r
+        const int eid = __shfl_sync(FULLMASK, nidl, q);
+        __syncwarp();
+        if (lane <= ncols) Rp[lane] = (lane == q) ? inv : xmul(Rp[lane], inv);
+        __syncwarp();
+        const float rl = lane <= ncols ? Rp[lane] : 0.0f;
+        bool upd[NR];
+#pragma unroll
+        for (int s = 0; s < NR; s++) upd[s] = valid[s] && lane + 32 * s != r;
+        // chunk by chunk (one float4 of the pivot row live), then column q
+#pragma unroll
+        for (int c = 0; c < NCH; c++) {
+            const float4 Rc = reinterpret_cast<const float4 *>(Rp)[c];
+#pragma unroll
+            for (int s = 0; s < NR; s++) {
+                if (upd[s]) {
+                    float4 *Tc = reinterpret_cast<float4 *>(tab + rowoff[s]) + c;
+                    const float nf = -aq[s];
+                    float4 t = *Tc;
+                    t.x = __fmaf_rn(nf, Rc.x, t.x);
+                    t.y = __fmaf_rn(nf, Rc.y, t.y);
+                    t.z = __fmaf_rn(nf, Rc.z, t.z);
+                    t.w = __fmaf_rn(nf, Rc.w, t.w);
+                    *Tc = t;
+                }
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < NR; s++) if (upd[s]) tab[rowoff[s] + q] = xmul(-aq[s], inv);
+        if (lane <= ncols) {
+            const float nfo = -obq;
+            ob = (lane == q) ? xmul(nfo, inv) : __fmaf_rn(nfo, rl, ob);
+        }
+        if (lane == owner) {
+#pragma unroll
+            for (int s = 0; s < NR; s++) if (s == oslot) bidr[s] = eid;
+        }
+        if (lane == q) nidl = lid;
+        __syncwarp();
+        piv++;
+        degen = (rr == 0.0f) ? degen + 1 : 0;
+        bland = degen >= degen_switch;
+    }
+    // write the bookkeeping back
+    if (lane <= ncols) obj[lane] = ob;
+    if (lane < ncols) nid[lane] = (uint8_t)nidl;
+#pragma unroll
+    for (int s = 0; s < NR; s++) if (valid[s]) bid[lane + 32 * s] = (uint8_t)bidr[s];
+    __syncwarp();
+    *piv_out = piv;
+    return status;
+}
+
+// warp_simplex for an FP32 tableau: simplex_fast32 when it fits (rows of at
+// most MAXCH chunks), else the generic loop (the same pivots either way)
+template <int MAXCH>
+__device__ __forceinline__ int warp_simplex_f32(const Lp<float> &L, float tol_piv, float tol_dj, int max_piv,
+                                                int degen_switch, int *piv_out)
+{
+    static_assert(MAXCH >= 1 && MAXCH <= kFastChunks, "chunk count");
+    const int nch = (L.ncols + 4) >> 2;
+    if (L.nrows <= kFastRows && L.nfree == L.ncols && (L.ld & 3) == 0 && nch <= MAXCH) {
+        switch (nch) {
+        case 1: return simplex_fast32<1>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out);
+        case 2: return simplex_fast32<2>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out);
+        case 3: if constexpr (MAXCH >= 3) return simplex_fast32<3>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out);
+        case 4: if constexpr (MAXCH >= 4) return simplex_fast32<4>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out);
+        case 5: if constexpr (MAXCH >= 5) return simplex_fast32<5>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out);
+        case 6: if constexpr (MAXCH >= 6) return simplex_fast32<6>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out);
+        default: break;
+        }
+    }
+    return warp_simplex<float>(L, tol_piv, tol_dj, max_piv, degen_switch, piv_out);
+}
+
 // ---------------------------------------------------------------------
 // shared-memory slot sizes
 // ---------------------------------------------------------------------
@@ -539,7 +692,9 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         __syncwarp();
         Lp<T> L{tab, ld, M1, nv, nv, bid, nid};
         int piv = 0;
-        const int st = warp_simplex<T>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv);
+        int st;
+        if constexpr (sizeof(T) == 4) st = warp_simplex_f32<kFastChunks>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv);
+        else st = warp_simplex<T>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv);
         const T z = obj[nv];
         uint64_t lo = par.lo, hi = par.hi;
         if (c.j < 64) lo |= 1ull << c.j; else hi |= 1ull << (c.j - 64);
@@ -1213,122 +1368,6 @@ __device__ int group_simplex(const Lp<float> &L, bool run, float tol_piv, float 
     return status;
 }
 
-// The full-warp FP32 LP2 of the screen for p + 1 <= 7 and R2 <= 96: the
-// pivoting rules, operations and their order are those of warp_simplex on
-// the same tableau, with the bookkeeping moved to registers: each lane keeps
-// the offsets and basic ids of its rows lane, lane+32, lane+64; lanes
-// 0..P1 hold the objective row (lane j: column j, lane P1: right-hand side)
-// and lanes 0..P1-1 the nonbasic ids; the constraint rows stay in shared
-// memory (row stride ld, NCH = (P1+4)/4 float4 chunks per row).
-template <int NCH>
-__device__ int lp2_screen_simplex(float *tab, int ld, int R2, int P1, float tol_piv, float tol_dj, int max_piv,
-                                  int degen_switch, int *piv_out, float *t_out)
-{
-    constexpr int NR = 3;
-    const int lane = lane_id();
-    const int nfree = P1, ncols = P1;
-    int rowoff[NR], bidr[NR];
-    bool valid[NR];
-#pragma unroll
-    for (int s = 0; s < NR; s++) {
-        const int i = lane + 32 * s;
-        valid[s] = i < R2;
-        rowoff[s] = i * ld;
-        bidr[s] = P1 + i;
-    }
-    float ob = lane <= ncols ? tab[R2 * ld + lane] : 0.0f;
-    int nidl = lane < ncols ? lane : 255;
-    int piv = 0, degen = 0, status;
-    bool bland = false;
-    for (;;) {
-        // pricing: largest |reduced cost|, smallest id on ties (Bland: smallest id)
-        unsigned key = 0xffffffffu, kid = 0xffffffffu;
-        int kidx = -1;
-        if (lane < ncols) {
-            const float sc = nidl < nfree ? fabsf(ob) : ob;
-            if (sc > tol_dj) { key = bland ? 0u : ~key_of(sc); kid = (unsigned)nidl; kidx = lane; }
-        }
-        const int q = warp_argmin(key, kid, kidx);
-        if (q < 0) { status = LP_OPTIMAL; break; }
-        const float obq = __shfl_sync(FULLMASK, ob, q);
-        const float sg = obq > 0.0f ? 1.0f : -1.0f;
-        // ratio test: smallest max(beta,0)/a over a > tol_piv, smallest id on ties
-        unsigned rkey = 0xffffffffu, rid = 0xffffffffu;
-        int bri = -1;
-        float aq[NR];
-#pragma unroll
-        for (int s = 0; s < NR; s++) {
-            aq[s] = 0.0f;
-            if (valid[s]) {
-                aq[s] = tab[rowoff[s] + q];
-                if (bidr[s] >= nfree) {
-                    const float a = sg * aq[s];
-                    if (a > tol_piv) {
-                        float beta = tab[rowoff[s] + ncols];
-                        if (!(beta > 0.0f)) beta = 0.0f;
-                        const unsigned k = key_of(ratio_div(beta, a));
-                        if (bri < 0 || k < rkey || (k == rkey && (unsigned)bidr[s] < rid)) {
-                            rkey = k; rid = (unsigned)bidr[s]; bri = lane + 32 * s;
-                        }
-                    }
-                }
-            }
-        }
-        const int r = warp_argmin(rkey, rid, bri);
-        if (r < 0) { status = LP_UNBOUNDED; break; }
-        if (piv >= max_piv) { status = LP_ITER_LIMIT; break; }
-        float *Rp = tab + r * ld;
-        float br = Rp[ncols];
-        if (!(br > 0.0f)) br = 0.0f;
-        const float prq = Rp[q];
-        const float rr = ratio_div(br, sg * prq);
-        const float inv = xdiv(1.0f, prq);
-        const int owner = r & 31, oslot = r >> 5;
-        const int lid = __shfl_sync(FULLMASK, (int)rid, owner);   // the owner's best row is r
-        const int eid = __shfl_sync(FULLMASK, nidl, q);
-        __syncwarp();
-        if (lane <= ncols) Rp[lane] = (lane == q) ? inv : xmul(Rp[lane], inv);
-        __syncwarp();
-        float4 Rv[NCH];
-#pragma unroll
-        for (int c = 0; c < NCH; c++) Rv[c] = reinterpret_cast<const float4 *>(Rp)[c];
-        const float rl = lane <= ncols ? Rp[lane] : 0.0f;
-#pragma unroll
-        for (int s = 0; s < NR; s++) {
-            if (valid[s] && lane + 32 * s != r) {
-                float *Ti = tab + rowoff[s];
-                const float nf = -aq[s];
-#pragma unroll
-                for (int c = 0; c < NCH; c++) {
-                    float4 t = reinterpret_cast<float4 *>(Ti)[c];
-                    t.x = __fmaf_rn(nf, Rv[c].x, t.x);
-                    t.y = __fmaf_rn(nf, Rv[c].y, t.y);
-                    t.z = __fmaf_rn(nf, Rv[c].z, t.z);
-                    t.w = __fmaf_rn(nf, Rv[c].w, t.w);
-                    reinterpret_cast<float4 *>(Ti)[c] = t;
-                }
-                Ti[q] = xmul(nf, inv);
-            }
-        }
-        if (lane <= ncols) {
-            const float nfo = -obq;
-            ob = (lane == q) ? xmul(nfo, inv) : __fmaf_rn(nfo, rl, ob);
-        }
-        if (lane == owner) {
-#pragma unroll
-            for (int s = 0; s < NR; s++) if (s == oslot) bidr[s] = eid;
-        }
-        if (lane == q) nidl = lid;
-        __syncwarp();
-        piv++;
-        degen = (rr == 0.0f) ? degen + 1 : 0;
-        bland = degen >= degen_switch;
-    }
-    *piv_out = piv;
-    *t_out = -__shfl_sync(FULLMASK, ob, ncols);
-    return status;
-}
-
 struct ScreenSlot {             // one set of the grouped FP32 screen
     Node nd;
     long long x;                // node index
@@ -1459,20 +1498,11 @@ __global__ void __launch_bounds__(32) k_opt_screen(DevBuffers B, Tol tol, SlotDi
             if (sl->state == SLOT_LP2) {
                 const int R2 = sl->R2, P1 = sl->p + 1, ld2 = sl->ld2;
                 float *Tb = tab_of(0);
-                int piv = 0, st;
-                float t;
-                if (P1 <= 7 && R2 <= 96) {
-                    st = (P1 + 4) / 4 == 1
-                             ? lp2_screen_simplex<1>(Tb, ld2, R2, P1, tol.tol_piv32, tol.tol_dj32, tol.max_pivots,
-                                                     tol.degen_switch, &piv, &t)
-                             : lp2_screen_simplex<2>(Tb, ld2, R2, P1, tol.tol_piv32, tol.tol_dj32, tol.max_pivots,
-                                                     tol.degen_switch, &piv, &t);
-                } else {
-                    uint8_t *bid = ids_of(0);
-                    Lp<float> L{Tb, ld2, R2, P1, P1, bid, bid + R2};
-                    st = group_simplex<32>(L, true, tol.tol_piv32, tol.tol_dj32, tol.max_pivots, tol.degen_switch, &piv);
-                    t = -Tb[(size_t)R2 * ld2 + P1];
-                }
+                uint8_t *bid = ids_of(0);
+                Lp<float> L{Tb, ld2, R2, P1, P1, bid, bid + R2};
+                int piv = 0;
+                const int st = warp_simplex_f32<2>(L, tol.tol_piv32, tol.tol_dj32, tol.max_pivots, tol.degen_switch, &piv);
+                const float t = -Tb[(size_t)R2 * ld2 + P1];
                 float g2 = 0.0f;
                 if (st == LP_OPTIMAL)
                     for (int r = lane; r < R2; r += 32)
