@@ -715,7 +715,15 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
                 T minb = pos_inf<T>(), gmax = T(1);
                 for (int i = lane; i < M1; i += 32) {
                     const T *Ti = tab + (size_t)i * ld;
-                    for (int j = 0; j < nv; j++) { const T a = xabs(Ti[j]); if (a > gmax) gmax = a; }
+                    int j = 0;
+                    if constexpr (sizeof(T) == 4) {
+                        // FP32 rows are 16-byte aligned: four entries per access
+                        for (; j + 4 <= nv; j += 4) {
+                            const float4 v = reinterpret_cast<const float4 *>(Ti)[j >> 2];
+                            gmax = fmaxf(gmax, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
+                        }
+                    }
+                    for (; j < nv; j++) { const T a = xabs(Ti[j]); if (a > gmax) gmax = a; }
                     const int id = bid[i];
                     if (id < nv) continue;
                     const int ci = id - nv;
@@ -948,10 +956,12 @@ __device__ int kkt_factor(const KktData<T> &D, const InstDesc &I, uint64_t lo, u
 // into any row, max_i (sum_c |Wh_ic| + |wc_i| + sum_l |Wm_i,S_l| |Lambda_l|_1),
 // the scale of the FP32 rounding error of the rows (warp-uniform result).
 // out = nullptr writes ws.G (row stride p+1, h in column p); otherwise the
-// rows go to out with row stride ldo and h in column hcol.
+// rows go to out with row stride ldo and h in column hcol.  t0_out / g0_out
+// (optional, warp-uniform results): min h over the constraint rows and
+// max(1, max |g|) over all rows, the start value and growth reference of LP2.
 template <typename T, bool track = false>
 __device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, uint64_t hi, int k, OptWs<T> &ws,
-                         T *out = nullptr, int ldo = 0, int hcol = 0)
+                         T *out = nullptr, int ldo = 0, int hcol = 0, T *t0_out = nullptr, T *g0_out = nullptr)
 {
     const int lane = lane_id();
     const int m = I.m, p = I.p, ncp = I.ncp, P1 = p + 1;
@@ -960,11 +970,20 @@ __device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, ui
     T *G = out ? out : ws.G;
     const int ldg = out ? ldo : P1, hc = out ? hcol : p;
     T amax = T(0);
+    T tmin = pos_inf<T>(), gmax = T(1);
+    const bool want_t0 = t0_out != nullptr;
     T *labs = ws.Y;   // |Lambda_l|_1, Y is free once Lambda is known
     for (int a = lane; a < k; a += 32) {
         T rs = T(0);
-        for (int cc = 0; cc < p; cc++) { G[a * ldg + cc] = Lam[a * P1 + cc]; if (track) rs += xabs(Lam[a * P1 + cc]); }
-        G[a * ldg + hc] = -Lam[a * P1 + p];
+        for (int cc = 0; cc < p; cc++) {
+            const T v = Lam[a * P1 + cc];
+            G[a * ldg + cc] = v;
+            if (track) rs += xabs(v);
+            if (want_t0 && xabs(v) > gmax) gmax = xabs(v);
+        }
+        const T h = -Lam[a * P1 + p];
+        G[a * ldg + hc] = h;
+        if (want_t0 && h < tmin) tmin = h;
         if (track) { rs += xabs(Lam[a * P1 + p]); labs[a] = rs; if (rs > amax) amax = rs; }
     }
     if (track) __syncwarp();
@@ -997,13 +1016,34 @@ __device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, ui
                 }
             }
 #pragma unroll
-            for (int j = 0; j < CB; j++) if (c0 + j <= p) G[pos * ldg + (c0 + j < p ? c0 + j : hc)] = acc[j];
+            for (int j = 0; j < CB; j++) {
+                if (c0 + j < p) {
+                    G[pos * ldg + c0 + j] = acc[j];
+                    if (want_t0 && xabs(acc[j]) > gmax) gmax = xabs(acc[j]);
+                } else if (c0 + j == p) {
+                    G[pos * ldg + hc] = acc[j];
+                    if (want_t0 && acc[j] < tmin) tmin = acc[j];
+                }
+            }
         }
         if (track && rs > amax) amax = rs;
     }
     for (int ii = lane; ii < ncp; ii += 32) {
-        for (int cc = 0; cc < p; cc++) G[(m + ii) * ldg + cc] = D.At[ii * p + cc];
+        for (int cc = 0; cc < p; cc++) {
+            const T v = D.At[ii * p + cc];
+            G[(m + ii) * ldg + cc] = v;
+            if (want_t0 && xabs(v) > gmax) gmax = xabs(v);
+        }
         G[(m + ii) * ldg + hc] = D.bt[ii];
+    }
+    if (want_t0) {
+#pragma unroll
+        for (int off = 16; off; off >>= 1) {
+            const T o = __shfl_xor_sync(FULLMASK, tmin, off); if (o < tmin) tmin = o;
+            const T g = __shfl_xor_sync(FULLMASK, gmax, off); if (g > gmax) gmax = g;
+        }
+        *t0_out = tmin;
+        *g0_out = gmax;
     }
     if (track) {
 #pragma unroll
@@ -1396,7 +1436,7 @@ __host__ __device__ inline size_t screen_warp_bytes(int gl, const SlotDims &sd)
 }
 
 template <int GL>
-__global__ void __launch_bounds__(32) k_opt_screen(DevBuffers B, Tol tol, SlotDims sd, int level)
+__global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, SlotDims sd, int level)
 {
     constexpr int NG = 32 / GL;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1451,16 +1491,12 @@ __global__ void __launch_bounds__(32) k_opt_screen(DevBuffers B, Tol tol, SlotDi
                 } else {
                     float *Tb = tab_of(g);
                     uint8_t *bid = ids_of(g), *nid = bid + R2;
-                    const float amax = region_rows<float, true>(D, I, nd.lo, nd.hi, k, ws, Tb, ld2, P1);
                     // LP2: max t  s.t.  g theta + t <= h (constraint rows), At theta <= bt
-                    float t0 = pos_inf<float>();
-                    for (int r = lane; r < m; r += 32) { const float h = Tb[(size_t)r * ld2 + P1]; if (h < t0) t0 = h; }
-#pragma unroll
-                    for (int off = 16; off; off >>= 1) { const float o = __shfl_xor_sync(FULLMASK, t0, off); if (o < t0) t0 = o; }
-                    float g0 = 1.0f;
+                    float t0, g0;
+                    const float amax = region_rows<float, true>(D, I, nd.lo, nd.hi, k, ws, Tb, ld2, P1, &t0, &g0);
+                    __syncwarp();
                     for (int r = lane; r < R2; r += 32) {
                         float *tr = Tb + (size_t)r * ld2;
-                        for (int cc = 0; cc < p; cc++) { const float a = fabsf(tr[cc]); if (a > g0) g0 = a; }
                         const float cf = (r < m) ? 1.0f : 0.0f;
                         float beta = __fmaf_rn(-cf, t0, tr[P1]);
                         if (!(beta > 0.0f)) beta = 0.0f;
@@ -1475,7 +1511,6 @@ __global__ void __launch_bounds__(32) k_opt_screen(DevBuffers B, Tol tol, SlotDi
                     }
                     float bmax = 0.0f;
                     for (int ii = lane; ii < ncp; ii += 32) { const float v = fabsf(D.bt[ii]); if (v > bmax) bmax = v; }
-                    g0 = group_max<32>(g0);
                     bmax = group_max<32>(bmax);
                     if (lane == 0) {
                         sl->m = m; sl->R2 = R2; sl->p = p; sl->ld2 = ld2;
