@@ -130,8 +130,10 @@ typedef struct {
     int max_pivots, degen_switch;
     double tol_piv32, tol_dj32, margin_z, margin_beta, margin_t, margin_licq;
     double tol_zero_row;     /* region row zero when max|g| <= tol * max(1,|h|) */
-    int screen_lanes;        /* MPQP_MIXED: lanes per LP2 of the FP32 screen,
-                                8, 16 or 32 (0 selects the default)        */
+    int lp2_screen;          /* MPQP_MIXED, FP32 optimality screen: 0 the dual
+                                bound on instances whose parameter set is a
+                                box (the primal tableau screen elsewhere),
+                                1 the primal tableau screen everywhere      */
 } mpqp_options;
 
 /* One optimal active set */

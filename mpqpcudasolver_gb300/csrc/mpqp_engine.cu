@@ -24,7 +24,7 @@
 namespace mq {
 size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd);
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd);
-size_t screen_smem_per_warp(int lanes, const SlotDims &sd);
+size_t screen_smem_per_warp(const SlotDims &sd);
 size_t laws_smem_per_warp(const SlotDims &sd);
 const void *kernel_ptr(const char *name);
 cudaError_t launch_enumerate(const DevBuffers &B, int level, int grid, cudaStream_t s);
@@ -34,7 +34,7 @@ cudaError_t launch_lp1_fp64(const DevBuffers &B, const Tol &tol, const SlotDims 
                             size_t smem, cudaStream_t s);
 cudaError_t launch_optimality(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int prec,
                               int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int lanes, int grid,
+cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode, int grid,
                               size_t smem, cudaStream_t s);
 cudaError_t launch_optimality_fp64(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int grid,
                                    size_t smem, cudaStream_t s);
@@ -72,6 +72,7 @@ void set_error_text(const char *msg) { set_err(msg ? msg : ""); }
 struct Prepared {
     InstDesc d;
     std::vector<double> Wm, Wh, wc, At, bt, QiAT, QiH, Qic;
+    std::vector<double> blo, bhi;   // parameter box, when At is [diag(+); diag(-)]
     std::vector<double> root;    // LP1 root tableau, FP64 stride ld1d
     std::vector<double> root_f;  // the same values at the plan's stride ld1 (FP32 copy)
 };
@@ -191,6 +192,21 @@ static int prepare_instance(const mpqp_problem &P, Prepared &out, int prec)
     };
     fill_root(out.root, d.ld1d);
     fill_root(out.root_f, d.ld1);
+    // parameter box: row c reads s theta_c <= bt_c (s > 0), row p + c reads
+    // s' theta_c <= bt_{p+c} (s' < 0), nothing else nonzero
+    d.box = ncp == 2 * p;
+    out.blo.assign(p, 0.0);
+    out.bhi.assign(p, 0.0);
+    for (int c = 0; c < p && d.box; c++) {
+        for (int j = 0; j < p; j++) {
+            const double up = P.At[c * p + j], dn = P.At[(p + c) * p + j];
+            if (j == c ? !(up > 0.0 && dn < 0.0) : (up != 0.0 || dn != 0.0)) { d.box = 0; break; }
+        }
+        if (!d.box) break;
+        out.bhi[c] = P.bt[c] / P.At[c * p + c];
+        out.blo[c] = P.bt[p + c] / P.At[(p + c) * p + c];
+        if (!(out.blo[c] <= out.bhi[c])) d.box = 0;
+    }
     return MPQP_OK;
 }
 
@@ -208,7 +224,7 @@ struct mpqp_plan {
     std::vector<void *> allocs;
     int kmax = 0;
     int prec = PREC_FP64;
-    int screen_lanes = 32;      // mixed precision: lanes per LP2 of the FP32 screen
+    int lp2_screen = 0;         // mixed precision: 0 dual bound on box instances, 1 primal tableau screen
     int grid_enum = 0, grid_feas = 0, grid_lp1fb = 0, grid_opt = 0, grid_optfb = 0;
     size_t smem_feas = 0, smem_lp1fb = 0, smem_opt = 0, smem_optfb = 0;
     int n_launches = 0;
@@ -246,7 +262,7 @@ extern "C" void mpqp_default_options(mpqp_options *o)
     o->margin_t = 1e-5;   // x (row magnitude / pivot ratio) x (1 + p |theta|max)
     o->margin_licq = 1e-3;
     o->tol_zero_row = 1e-12;
-    o->screen_lanes = 32;
+    o->lp2_screen = 0;
 }
 
 static void fill_defaults(mpqp_options &o)
@@ -256,7 +272,7 @@ static void fill_defaults(mpqp_options &o)
 #define DEF(f) if (o.f == 0) o.f = d.f
     DEF(mem_fraction); DEF(tol_feas); DEF(tol_opt); DEF(tol_licq); DEF(r_min); DEF(tol_piv); DEF(tol_dj);
     DEF(max_pivots); DEF(degen_switch); DEF(tol_piv32); DEF(tol_dj32); DEF(margin_z); DEF(margin_beta);
-    DEF(margin_t); DEF(margin_licq); DEF(tol_zero_row); DEF(screen_lanes);
+    DEF(margin_t); DEF(margin_licq); DEF(tol_zero_row);
 #undef DEF
 }
 
@@ -310,10 +326,9 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
     const DevBuffers &B = P->B;
     const bool mixed = P->prec == PREC_MIXED;
     const char *feas = mixed ? "k_feasibility<float>" : "k_feasibility<double>";
-    const char *opt = !mixed ? "k_optimality<double>"
-                      : P->screen_lanes == 8 ? "k_opt_screen<8>" : P->screen_lanes == 16 ? "k_opt_screen<16>" : "k_opt_screen<32>";
+    const char *opt = mixed ? "k_opt_screen" : "k_optimality<double>";
     auto launch_opt = [&](int level) {
-        return mixed ? launch_opt_screen(B, P->tol, P->sd, level, P->screen_lanes, P->grid_opt, P->smem_opt, s)
+        return mixed ? launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, P->grid_opt, P->smem_opt, s)
                      : launch_optimality(B, P->tol, P->sd, level, P->prec, P->grid_opt, P->smem_opt, s);
     };
     int nl = 0;
@@ -372,12 +387,12 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
     fill_defaults(P->opt);
     const mpqp_options &o = P->opt;
     P->prec = o.precision == MPQP_MIXED ? PREC_MIXED : PREC_FP64;
-    if (o.screen_lanes != 8 && o.screen_lanes != 16 && o.screen_lanes != 32) {
-        set_err("screen_lanes must be 8, 16 or 32");
+    if (o.lp2_screen != 0 && o.lp2_screen != 1) {
+        set_err("lp2_screen must be 0 or 1");
         delete P;
         return MPQP_EINVAL;
     }
-    P->screen_lanes = o.screen_lanes;
+    P->lp2_screen = o.lp2_screen;
     P->n_inst = n_inst;
     P->probs.assign(probs, probs + n_inst);
     Tol &t = P->tol;
@@ -415,6 +430,7 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
         d.o_QiH = put(dp, pr.QiH); d.o_Qic = put(dp, pr.Qic); d.o_root = put(dp, pr.root);
         d.f_Wm = put(fp, pr.Wm); d.f_Wh = put(fp, pr.Wh); d.f_wc = put(fp, pr.wc);
         d.f_At = put(fp, pr.At); d.f_bt = put(fp, pr.bt); d.f_root = put(fp, pr.root_f);
+        d.f_blo = put(fp, pr.blo); d.f_bhi = put(fp, pr.bhi);
         P->desc.push_back(d);
         P->kmax = std::max(P->kmax, d.k_max);
         sd.maxM1 = std::max(sd.maxM1, d.M1);
@@ -543,14 +559,13 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
     P->smem_feas = 4 * lp1_smem_per_warp(P->prec == PREC_MIXED ? 4 : 8, sd);
     P->smem_lp1fb = 4 * lp1_smem_per_warp(8, sd);
     // mixed precision: the grouped FP32 screen, one warp per block
-    P->smem_opt = P->prec == PREC_MIXED ? screen_smem_per_warp(P->screen_lanes, sd) : 4 * opt_smem_per_warp(8, sd);
+    P->smem_opt = P->prec == PREC_MIXED ? screen_smem_per_warp(sd) : 4 * opt_smem_per_warp(8, sd);
     P->smem_optfb = 4 * opt_smem_per_warp(8, sd);
     if ((rc = grid_for(kernel_ptr("enumerate"), 0, &P->grid_enum)) ||
         (rc = grid_for(kernel_ptr(P->prec == PREC_MIXED ? "feas32" : "feas64"), P->smem_feas, &P->grid_feas)) ||
         (rc = grid_for(kernel_ptr("lp1_fp64"), P->smem_lp1fb, &P->grid_lp1fb)) ||
         (rc = P->prec == PREC_MIXED
-                  ? grid_for(kernel_ptr(P->screen_lanes == 8 ? "screen8" : P->screen_lanes == 16 ? "screen16" : "screen32"),
-                             P->smem_opt, &P->grid_opt, 32)
+                  ? grid_for(kernel_ptr("screen"), P->smem_opt, &P->grid_opt, 32)
                   : grid_for(kernel_ptr("opt64"), P->smem_opt, &P->grid_opt)) ||
         (rc = grid_for(kernel_ptr("opt_fp64"), P->smem_optfb, &P->grid_optfb))) {
         free_plan_mem(P);

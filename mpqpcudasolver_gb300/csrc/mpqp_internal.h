@@ -64,6 +64,9 @@ struct InstDesc {
     long long o_Wm, o_Wh, o_wc, o_At, o_bt, o_QiAT, o_QiH, o_Qic, o_root;
     // offsets (elements) into the FP32 pool
     long long f_Wm, f_Wh, f_wc, f_At, f_bt, f_root;
+    long long f_blo, f_bhi;     // parameter box lo <= theta <= hi (FP32), valid when box
+    int box;                    // 1: At = [diag(+); diag(-)] (rows c, then p + c), a box
+    int pad_box;
 };
 
 struct Node {                   // a feasible (or, when exhaustive, any) active set

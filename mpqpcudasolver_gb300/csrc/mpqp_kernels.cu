@@ -1285,330 +1285,351 @@ __global__ void __launch_bounds__(128) k_optimality_fp64(DevBuffers B, Tol tol, 
 // ---------------------------------------------------------------------
 // One warp per instance: the empty set with the root LP1 tableau.
 // ---------------------------------------------------------------------
-// FP32 LP2 screen, several sets per warp
+// FP32 LP2 screen of the mixed path
 // ---------------------------------------------------------------------
-// A warp takes NG = 32/GL feasible sets at once.  The KKT factorisation and
-// the region rows of each set run on the whole warp, one set after the
-// other, straight into that set's LP2 tableau; then NG groups of GL lanes
-// run the NG LP2s in lock step: every lane executes every instruction of the
-// simplex loop and a group that has finished only stops writing, so one
-// shared-memory instruction serves NG tableaus and the arg-min reductions
-// take log2(GL) shuffle steps.  The pivoting rules and roundings are those of
-// warp_simplex; the verdict is that of the FP32 screen in eval_optimality.
-
-template <int GL>
-__device__ __forceinline__ int group_argmin(unsigned key, unsigned id, int idx)
+// Order-preserving unsigned image of any non-NaN float (negative included).
+__device__ __forceinline__ unsigned key_signed(float v)
 {
-    if constexpr (GL == 32) {
-        return warp_argmin(key, id, idx);
-    } else {
-#pragma unroll
-        for (int off = GL / 2; off; off >>= 1) {
-            const unsigned k2 = __shfl_xor_sync(FULLMASK, key, off);
-            const unsigned i2 = __shfl_xor_sync(FULLMASK, id, off);
-            const int x2 = __shfl_xor_sync(FULLMASK, idx, off);
-            if (k2 < key || (k2 == key && i2 < id)) { key = k2; id = i2; idx = x2; }
-        }
-        return idx;
-    }
+    const unsigned u = __float_as_uint(v);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
-template <int GL>
-__device__ __forceinline__ float group_max(float v)
+__device__ __forceinline__ float warp_max(float v)
 {
 #pragma unroll
-    for (int off = GL / 2; off; off >>= 1) { const float o = __shfl_xor_sync(FULLMASK, v, off); if (o > v) v = o; }
+    for (int off = 16; off; off >>= 1) { const float o = __shfl_xor_sync(FULLMASK, v, off); if (o > v) v = o; }
     return v;
 }
 
-// Lock-step simplex of the lane groups (run: this group has an LP to solve;
-// a group without one returns LP_SKIPPED).  All 32 lanes must call it.
-template <int GL>
-__device__ int group_simplex(const Lp<float> &L, bool run, float tol_piv, float tol_dj, int max_piv, int degen_switch,
-                             int *piv_out)
+__device__ __forceinline__ float warp_sum(float v)
 {
-    const int sub = lane_id() & (GL - 1);
-    int piv = 0, degen = 0, status = run ? -1 : LP_SKIPPED;
-    bool bland = false;
-    float *obj = L.tab + (size_t)L.nrows * L.ld;
-    for (;;) {
-        if (!__any_sync(FULLMASK, status < 0)) break;
-        bool act = status < 0;
-        // pricing: largest |reduced cost|, smallest id on ties (Bland: smallest id)
-        unsigned bkey = 0xffffffffu, bid_ = 0xffffffffu;
-        int bq = -1;
-        if (act) {
-            for (int j = sub; j < L.ncols; j += GL) {
-                const float g = obj[j];
-                const int id = L.nid[j];
-                const float sc = (id < L.nfree) ? fabsf(g) : g;
-                if (!(sc > tol_dj)) continue;
-                const unsigned k = bland ? 0u : ~key_of(sc);
-                if (bq < 0 || k < bkey || (k == bkey && (unsigned)id < bid_)) { bkey = k; bid_ = id; bq = j; }
-            }
-        }
-        const int q = group_argmin<GL>(bkey, bid_, bq);
-        if (act && q < 0) { status = LP_OPTIMAL; act = false; }
-        // ratio test: smallest max(beta,0)/a over a > tol_piv, smallest id on ties
-        float sg = 1.0f;
-        unsigned rkey = 0xffffffffu, rid = 0xffffffffu;
-        int bri = -1;
-        if (act) {
-            sg = obj[q] > 0.0f ? 1.0f : -1.0f;
-            for (int i = sub; i < L.nrows; i += GL) {
-                const int id = L.bid[i];
-                if (id < L.nfree) continue;
-                const float a = sg * L.tab[(size_t)i * L.ld + q];
-                if (!(a > tol_piv)) continue;
-                float beta = L.tab[(size_t)i * L.ld + L.ncols];
-                if (!(beta > 0.0f)) beta = 0.0f;
-                const unsigned k = key_of(ratio_div(beta, a));
-                if (bri < 0 || k < rkey || (k == rkey && (unsigned)id < rid)) { rkey = k; rid = id; bri = i; }
-            }
-        }
-        const int r = group_argmin<GL>(rkey, rid, bri);
-        if (act && r < 0) { status = LP_UNBOUNDED; act = false; }
-        if (act && piv >= max_piv) { status = LP_ITER_LIMIT; act = false; }
-        float rr = 0.0f, inv = 0.0f;
-        float *R = L.tab;
-        if (act) {
-            R = L.tab + (size_t)r * L.ld;
-            float br = R[L.ncols];
-            if (!(br > 0.0f)) br = 0.0f;
-            rr = ratio_div(br, sg * R[q]);
-            inv = xdiv(1.0f, R[q]);
-        }
-        __syncwarp();
-        if (act)
-            for (int j = sub; j <= L.ncols; j += GL) R[j] = (j == q) ? inv : xmul(R[j], inv);
-        __syncwarp();
-        if (act) {
-            for (int i = sub; i <= L.nrows; i += GL) {
-                if (i == r) continue;
-                float *Ti = L.tab + (size_t)i * L.ld;
-                const float nf = -Ti[q];
-                row_update(Ti, R, nf, L.ncols);
-                Ti[q] = xmul(nf, inv);
-            }
-        }
-        __syncwarp();
-        if (act && sub == 0) {
-            const uint8_t t = L.bid[r];
-            L.bid[r] = L.nid[q];
-            L.nid[q] = t;
-        }
-        __syncwarp();
-        if (act) {
-            piv++;
-            degen = (rr == 0.0f) ? degen + 1 : 0;
-            bland = degen >= degen_switch;
+#pragma unroll
+    for (int off = 16; off; off >>= 1) v += __shfl_xor_sync(FULLMASK, v, off);
+    return v;
+}
+
+constexpr int kDualMaxP = 6;      // p <= 6
+constexpr int kDualMaxRows = 96;
+constexpr int kDualLd = 12;       // row stride of the dual layout (conflict-free 128-bit loads)
+enum : int { LP_BOUND = 5 };      // record status: "not optimal" proven by a dual bound (t = the bound)
+
+// Dual bound of LP2 for an instance whose parameter set is a box
+// lo <= theta <= hi (constraint rows m..m+2p-1: theta_c <= hi_c scaled, then
+// -theta_c <= -lo_c scaled).  LP2 is
+//     max t  s.t.  g_r theta + c_r t <= h_r   (c_r = 1 for r < m, 0 for box rows).
+// For every y >= 0 with c.y > 0 and every feasible (theta, t),
+//     t <= (h.y + sum_c |(G^T y)_c| reach_c) / (c.y),   reach_c = max(|lo_c|, |hi_c|),
+// so a y whose bound is below -thr proves "not optimal".  The y are the basic
+// solutions of a revised primal simplex on the dual LP
+//     min h.y  s.t.  G^T y = 0,  c.y = 1,  y >= 0,
+// started at the best single-row bound (row i* and, per parameter, the box
+// row that cancels g_{i*,c}) and stopped as soon as its objective is below
+// -thr; the bound is then recomputed from max(y, 0) and the rows, so FP32
+// drift in the basis inverse cannot make a "not optimal" verdict unsound.
+// Lanes 0..p hold one basic variable each (row index, value, row of B^-1:
+// binv[0..p-1] for the theta equations, binvp for c.y = 1); every lane holds
+// the prices (pi[0..p-1]: a vertex theta; pip: the objective).
+// Row layout (stride kDualLd): columns 0..5 g_r (zero beyond p), 6 c_r, 7 h_r.
+// Returns 1 when "not optimal" is proven; *it_out iterations, *bound_out the
+// last verified bound (+inf when none was computed).
+__device__ int lp2_dual_screen(const float *T, int m, int R2, int p, const float *blo, const float *bhi, float thr,
+                               float tol_piv, float tol_dj, int max_it, int degen_switch, int *it_out,
+                               float *bound_out)
+{
+    constexpr int NR = kDualMaxRows / 32;
+    constexpr int MP = kDualMaxP;
+    constexpr int LD = kDualLd;
+    const int lane = lane_id();
+    const int P1 = p + 1;
+    auto row8 = [&](int r, float *a) {
+        const float4 v0 = reinterpret_cast<const float4 *>(T + r * LD)[0];
+        const float4 v1 = reinterpret_cast<const float4 *>(T + r * LD)[1];
+        a[0] = v0.x; a[1] = v0.y; a[2] = v0.z; a[3] = v0.w; a[4] = v1.x; a[5] = v1.y; a[6] = v1.z; a[7] = v1.w;
+    };
+    float lo[MP], hi[MP];
+#pragma unroll
+    for (int c = 0; c < MP; c++) { lo[c] = c < p ? blo[c] : 0.0f; hi[c] = c < p ? bhi[c] : 0.0f; }
+    // best single-row bound b_r = h_r - min over the box of g_r theta (r < m)
+    unsigned bkey = 0xffffffffu;
+    int bi = -1;
+    for (int r = lane; r < m; r += 32) {
+        float a[8];
+        row8(r, a);
+        float b = a[7];
+#pragma unroll
+        for (int c = 0; c < MP; c++) b -= a[c] > 0.0f ? a[c] * lo[c] : a[c] * hi[c];
+        const unsigned k = key_signed(b);
+        if (bi < 0 || k < bkey) { bkey = k; bi = r; }
+    }
+    const int istar = warp_argmin(bkey, (unsigned)bi, bi);
+    // start basis: lane 0 row i*, lane 1+c the box row of parameter c that
+    // cancels g_{i*,c} (the upper row when g <= 0); pi = (box corner, b*)
+    float gi[8];
+    row8(istar, gi);
+    float binv[MP], pi[MP], binvp = 0.0f, y = 0.0f;
+    float pip = gi[7];
+    int bidx = -1;
+#pragma unroll
+    for (int c = 0; c < MP; c++) {
+        binv[c] = 0.0f;
+        pi[c] = 0.0f;
+        if (c < p) {
+            const bool upper = !(gi[c] > 0.0f);
+            const int row = m + (upper ? c : p + c);
+            const float sc = T[row * LD + c];                 // the box row's coefficient
+            pi[c] = upper ? hi[c] : lo[c];
+            const float yc = __fdividef(-gi[c], sc);          // >= 0
+            pip = __fmaf_rn(yc, T[row * LD + 7], pip);
+            if (lane == 1 + c) { bidx = row; y = yc; binv[c] = __fdividef(1.0f, sc); binvp = yc; }
         }
     }
-    *piv_out = piv;
-    return status;
+    if (lane == 0) { bidx = istar; y = 1.0f; binvp = 1.0f; }
+    // basic flags of the own rows lane, lane+32, lane+64
+    unsigned basic = 0;
+#pragma unroll
+    for (int s = 0; s < NR; s++) {
+        const int r = lane + 32 * s;
+        bool b = r == istar;
+        if (r >= m && r < m + p) b = !(T[istar * LD + (r - m)] > 0.0f);
+        else if (r >= m + p && r < m + 2 * p) b = T[istar * LD + (r - m - p)] > 0.0f;
+        if (b) basic |= 1u << s;
+    }
+    float reach = 0.0f;
+#pragma unroll
+    for (int c = 0; c < MP; c++) if (lane == c) reach = fmaxf(fabsf(lo[c]), fabsf(hi[c]));
+    // verified bound from max(y, 0): lane c < p sums (G^T y)_c, lane p c.y, lane p+1 h.y
+    const int vcol = lane < p ? lane : (lane == p ? 6 : 7);
+    auto verify = [&]() -> float {
+        float acc = 0.0f;
+#pragma unroll
+        for (int i = 0; i <= MP; i++) {
+            if (i < P1) {
+                const float yi = __shfl_sync(FULLMASK, fmaxf(y, 0.0f), i);
+                const int ri = __shfl_sync(FULLMASK, bidx, i);
+                if (lane <= P1) acc = __fmaf_rn(yi, T[ri * LD + vcol], acc);
+            }
+        }
+        const float cy = __shfl_sync(FULLMASK, acc, p);
+        const float num = warp_sum(lane < p ? fabsf(acc) * reach : (lane == P1 ? acc : 0.0f));
+        return cy > 0.0f ? __fdividef(num, cy) : pos_inf<float>();
+    };
+
+    int it = 0, degen = 0, proven = 0;
+    bool bland = false;
+    float bound = pos_inf<float>();
+    for (;;) {
+        if (pip < -thr) {
+            bound = verify();
+            if (bound < -thr) { proven = 1; break; }
+        }
+        if (it >= max_it) break;
+        // pricing: most negative reduced cost d_r = h_r - pi.a_r (Bland: smallest r)
+        unsigned key = 0xffffffffu, kid = 0xffffffffu;
+        int kq = -1;
+        float dbest = 0.0f;
+#pragma unroll
+        for (int s = 0; s < NR; s++) {
+            const int r = lane + 32 * s;
+            if (r < R2 && !((basic >> s) & 1u)) {
+                float a[8];
+                row8(r, a);
+                float d = __fmaf_rn(-pip, a[6], a[7]);
+#pragma unroll
+                for (int c = 0; c < MP; c++) d = __fmaf_rn(-pi[c], a[c], d);
+                if (d < -tol_dj) {
+                    const unsigned k = bland ? 0u : ~key_of(-d);
+                    if (kq < 0 || k < key || (k == key && (unsigned)r < kid)) { key = k; kid = r; kq = r; dbest = d; }
+                }
+            }
+        }
+        const int q = warp_argmin(key, kid, kq);
+        if (q < 0) {                       // dual optimum: pip is the LP2 optimum t*
+            bound = verify();
+            proven = bound < -thr;
+            break;
+        }
+        const float dq = __shfl_sync(FULLMASK, dbest, q & 31);
+        // entering column u = B^-1 a_q; ratio test over the basic positions
+        float aq[8];
+        row8(q, aq);
+        float u = binvp * aq[6];
+#pragma unroll
+        for (int c = 0; c < MP; c++) u = __fmaf_rn(binv[c], aq[c], u);
+        unsigned rk = 0xffffffffu, rid = 0xffffffffu;
+        int rl = -1;
+        if (lane < P1 && u > tol_piv) { rk = key_of(__fdividef(fmaxf(y, 0.0f), u)); rid = (unsigned)bidx; rl = lane; }
+        const int l = warp_argmin(rk, rid, rl);
+        if (l < 0) break;                  // unbounded dual: not possible for LP2 in exact arithmetic
+        const float ul = __shfl_sync(FULLMASK, u, l);
+        const float yl = __shfl_sync(FULLMASK, fmaxf(y, 0.0f), l);
+        const int oldb = __shfl_sync(FULLMASK, bidx, l);
+        const float inv = __fdividef(1.0f, ul);
+        const float theta = yl * inv;
+        const float f = u * inv, fp = dq * inv;
+        // the pivot on row l of B^-1 (its old values, one element at a time)
+        const bool own = lane == l, other = lane < P1 && lane != l;
+#pragma unroll
+        for (int c = 0; c < MP; c++) {
+            const float rj = __shfl_sync(FULLMASK, binv[c], l);
+            binv[c] = own ? rj * inv : (other ? __fmaf_rn(-f, rj, binv[c]) : binv[c]);
+            pi[c] = __fmaf_rn(fp, rj, pi[c]);
+        }
+        {
+            const float rj = __shfl_sync(FULLMASK, binvp, l);
+            binvp = own ? rj * inv : (other ? __fmaf_rn(-f, rj, binvp) : binvp);
+            pip = __fmaf_rn(fp, rj, pip);
+        }
+        if (own) { y = theta; bidx = q; }
+        else if (other) y = __fmaf_rn(-theta, u, y);
+        if (lane == (q & 31)) basic |= 1u << (q >> 5);
+        if (lane == (oldb & 31)) basic &= ~(1u << (oldb >> 5));
+        it++;
+        degen = (theta == 0.0f) ? degen + 1 : 0;
+        bland = degen >= degen_switch;
+    }
+    *it_out = it;
+    *bound_out = bound;
+    return proven;
 }
 
-struct ScreenSlot {             // one set of the grouped FP32 screen
-    Node nd;
-    long long x;                // node index
-    int state;                  // SLOT_*
-    int m, R2, p, ld2;
-    int status, piv;            // LP2 result
-    float t0, amax, rho, g0, bmax, t, g2;
-};
-enum : int { SLOT_EMPTY = 0, SLOT_LP2 = 1, SLOT_UNDECIDED = 2 };
-
-// per-warp layout: KKT workspace (R, Y, Lambda, S), then per group the LP2
-// tableau (R2+1) x ld2, its ids (R2 + P1) and the slot record
-__host__ __device__ inline size_t screen_kkt_bytes(const SlotDims &sd)
+// per-warp shared memory of the screen: KKT workspace (R, Y, Lambda, S),
+// the LP2 tableau (R2+1) x ld2 and its basis ids (R2 + P1)
+__host__ __device__ inline size_t screen_warp_bytes(const SlotDims &sd)
 {
     return align16((size_t)sd.maxK * sd.maxK * 4) + 2 * align16((size_t)sd.maxK * sd.maxP1 * 4) +
-           align16((size_t)sd.maxK * sizeof(int));
-}
-__host__ __device__ inline size_t screen_group_bytes(const SlotDims &sd)
-{
-    return align16((size_t)(sd.maxR2 + 1) * sd.maxLD2 * 4) + align16((size_t)sd.maxR2 + sd.maxP1) +
-           align16(sizeof(ScreenSlot));
-}
-__host__ __device__ inline size_t screen_warp_bytes(int gl, const SlotDims &sd)
-{
-    return screen_kkt_bytes(sd) + (size_t)(32 / gl) * screen_group_bytes(sd);
+           align16((size_t)sd.maxK * sizeof(int)) + align16((size_t)(sd.maxR2 + 1) * sd.maxLD2 * 4) +
+           align16((size_t)sd.maxR2 + sd.maxP1);
 }
 
-template <int GL>
-__global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, SlotDims sd, int level)
+// The FP32 screen of every feasible set of a level, one warp per set.  Only a
+// clear "not optimal" is final; every other set is queued for
+// k_optimality_fp64.  mode 0: the dual bound where the parameter set is a box
+// (p <= 6, at most 96 rows), the primal tableau screen elsewhere; mode 1:
+// the primal tableau screen everywhere.
+__global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, SlotDims sd, int level, int mode)
 {
-    constexpr int NG = 32 / GL;
     extern __shared__ __align__(16) unsigned char smem[];
-    const int lane = lane_id(), grp = lane / GL, sub = lane & (GL - 1);
+    const int lane = lane_id();
     OptWs<float> ws;
+    float *Tb;
+    uint8_t *ids;
     {
         size_t o = 0;
         ws.R = (float *)(smem + o); o += align16((size_t)sd.maxK * sd.maxK * 4);
         ws.Y = (float *)(smem + o); o += align16((size_t)sd.maxK * sd.maxP1 * 4);
         ws.Lam = (float *)(smem + o); o += align16((size_t)sd.maxK * sd.maxP1 * 4);
-        ws.S = (int *)(smem + o);
+        ws.S = (int *)(smem + o); o += align16((size_t)sd.maxK * sizeof(int));
+        Tb = (float *)(smem + o); o += align16((size_t)(sd.maxR2 + 1) * sd.maxLD2 * 4);
+        ids = smem + o;
         ws.G = nullptr; ws.Tb = nullptr; ws.ids = nullptr;
     }
-    unsigned char *gbase = smem + screen_kkt_bytes(sd);
-    const size_t gbytes = screen_group_bytes(sd);
-    const size_t tab_bytes = align16((size_t)(sd.maxR2 + 1) * sd.maxLD2 * 4);
-    const size_t ids_bytes = align16((size_t)sd.maxR2 + sd.maxP1);
-    auto tab_of = [&](int g) { return (float *)(gbase + g * gbytes); };
-    auto ids_of = [&](int g) { return (uint8_t *)(gbase + g * gbytes + tab_bytes); };
-    auto slot_of = [&](int g) { return (ScreenSlot *)(gbase + g * gbytes + tab_bytes + ids_bytes); };
-
     const int side = level & 1;
     Ctl *ctl = B.ctl;
     const long long nn = ctl->n_node[side] < B.node_cap ? ctl->n_node[side] : B.node_cap;
     LocalInstCounters lc;
     lc.reset(-1);
     for (;;) {
-        long long x0;
-        if (lane == 0) x0 = (long long)atomicAdd(&ctl->ctr[3], (unsigned long long)NG);
-        x0 = __shfl_sync(FULLMASK, x0, 0);
-        if (x0 >= nn) break;
-        // phase A: KKT and region rows of each set, the whole warp per set
-        for (int g = 0; g < NG; g++) {
-            ScreenSlot *sl = slot_of(g);
-            const long long x = x0 + g;
-            int state = SLOT_EMPTY;
-            Node nd;
-            if (x < nn) {
-                nd = B.node[side][x];
-                if ((nd.flags & (NODE_VALID | NODE_FEASIBLE)) == (NODE_VALID | NODE_FEASIBLE) &&
-                    level >= B.inst[nd.inst].k_min)
-                    state = SLOT_LP2;
+        long long x;
+        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[3], 1ull);
+        x = __shfl_sync(FULLMASK, x, 0);
+        if (x >= nn) break;
+        const Node nd = B.node[side][x];
+        if ((nd.flags & (NODE_VALID | NODE_FEASIBLE)) != (NODE_VALID | NODE_FEASIBLE)) continue;
+        const InstDesc &I = B.inst[nd.inst];
+        if (level < I.k_min) continue;
+        if (nd.inst != lc.inst) {
+            if (lc.inst >= 0 && lane == 0) {
+                atomicAdd((unsigned long long *)&B.ictl[lc.inst].optimal, (unsigned long long)lc.a);
+                atomicAdd((unsigned long long *)&B.ictl[lc.inst].region, (unsigned long long)lc.b);
+                atomicAdd((unsigned long long *)&B.ictl[lc.inst].lp2_piv, (unsigned long long)lc.c);
+                atomicAdd((unsigned long long *)&B.ictl[lc.inst].cheb_piv, (unsigned long long)lc.d);
             }
-            if (state == SLOT_LP2) {
-                const InstDesc &I = B.inst[nd.inst];
-                const KktData<float> D = kkt_data<float>(B, I);
-                const int m = I.m, p = I.p, ncp = I.ncp, P1 = p + 1, R2 = m + ncp, ld2 = I.ld2;
-                int k = 0;
-                float rho = 1.0f;
-                if (kkt_factor<float>(D, I, nd.lo, nd.hi, tol.margin_licq32, ws, &k, &rho)) {
-                    state = SLOT_UNDECIDED;
-                } else {
-                    float *Tb = tab_of(g);
-                    uint8_t *bid = ids_of(g), *nid = bid + R2;
-                    // LP2: max t  s.t.  g theta + t <= h (constraint rows), At theta <= bt
-                    float t0, g0;
-                    const float amax = region_rows<float, true>(D, I, nd.lo, nd.hi, k, ws, Tb, ld2, P1, &t0, &g0);
-                    __syncwarp();
-                    for (int r = lane; r < R2; r += 32) {
-                        float *tr = Tb + (size_t)r * ld2;
-                        const float cf = (r < m) ? 1.0f : 0.0f;
-                        float beta = __fmaf_rn(-cf, t0, tr[P1]);
-                        if (!(beta > 0.0f)) beta = 0.0f;
-                        tr[p] = cf;
-                        tr[P1] = beta;
-                        bid[r] = (uint8_t)(P1 + r);
-                    }
-                    for (int cc = lane; cc <= P1; cc += 32) {
-                        float *ob = Tb + (size_t)R2 * ld2;
-                        ob[cc] = (cc == p) ? 1.0f : (cc == P1 ? -t0 : 0.0f);
-                        if (cc < P1) nid[cc] = (uint8_t)cc;
-                    }
-                    float bmax = 0.0f;
-                    for (int ii = lane; ii < ncp; ii += 32) { const float v = fabsf(D.bt[ii]); if (v > bmax) bmax = v; }
-                    bmax = group_max<32>(bmax);
-                    if (lane == 0) {
-                        sl->m = m; sl->R2 = R2; sl->p = p; sl->ld2 = ld2;
-                        sl->t0 = t0; sl->amax = amax; sl->rho = rho; sl->g0 = g0; sl->bmax = bmax;
-                    }
-                }
-            }
-            if (lane == 0) {
-                sl->state = state;
-                sl->x = x;
-                if (state != SLOT_EMPTY) sl->nd = nd;
-                sl->piv = 0;
-                sl->status = LP_SKIPPED;
-            }
-            __syncwarp();
+            lc.reset(nd.inst);
         }
-        // phase B: the NG LP2s in lock step, one lane group each
-        if constexpr (GL == 32) {
-            ScreenSlot *sl = slot_of(0);
-            if (sl->state == SLOT_LP2) {
-                const int R2 = sl->R2, P1 = sl->p + 1, ld2 = sl->ld2;
-                float *Tb = tab_of(0);
-                uint8_t *bid = ids_of(0);
-                Lp<float> L{Tb, ld2, R2, P1, P1, bid, bid + R2};
-                int piv = 0;
-                const int st = warp_simplex_f32<2>(L, tol.tol_piv32, tol.tol_dj32, tol.max_pivots, tol.degen_switch, &piv);
-                const float t = -Tb[(size_t)R2 * ld2 + P1];
-                float g2 = 0.0f;
-                if (st == LP_OPTIMAL)
+        const KktData<float> D = kkt_data<float>(B, I);
+        const int m = I.m, p = I.p, ncp = I.ncp, P1 = p + 1, R2 = m + ncp, ld2 = I.ld2;
+        int k = 0;
+        float rho = 1.0f;
+        bool decided = false;
+        int status = LP_SKIPPED, piv = 0;
+        float t = 0.0f;
+        if (!kkt_factor<float>(D, I, nd.lo, nd.hi, tol.margin_licq32, ws, &k, &rho)) {
+            // LP2: max t  s.t.  g theta + t <= h (constraint rows), At theta <= bt
+            // the dual screen (mode 0, a box, p <= 6, at most 96 rows; its layout
+            // needs rows of kDualLd floats in the slot) or the primal tableau
+            const bool dual = mode == 0 && I.box && p <= kDualMaxP && R2 <= kDualMaxRows && sd.maxLD2 >= kDualLd;
+            float t0, g0;
+            const float amax = dual ? region_rows<float, true>(D, I, nd.lo, nd.hi, k, ws, Tb, kDualLd, 7, &t0, &g0)
+                                    : region_rows<float, true>(D, I, nd.lo, nd.hi, k, ws, Tb, ld2, P1, &t0, &g0);
+            float bmax = 0.0f;
+            for (int ii = lane; ii < ncp; ii += 32) { const float v = fabsf(D.bt[ii]); if (v > bmax) bmax = v; }
+            bmax = warp_max(bmax);
+            // error scale of the FP32 rows: row magnitude / smallest Cholesky
+            // pivot ratio, times the reach of theta inside the box (rho >
+            // margin_licq, so the quotient is tame)
+            const float scale = __fdividef(amax, rho) * (1.0f + (float)p * bmax);
+            __syncwarp();
+            if (dual) {
+                // dual layout: g beyond p zero, column 6 c_r (h is in column 7)
+                for (int r = lane; r < R2; r += 32) {
+                    float *tr = Tb + (size_t)r * kDualLd;
+                    for (int cc = p; cc < kDualMaxP; cc++) tr[cc] = 0.0f;
+                    tr[6] = (r < m) ? 1.0f : 0.0f;
+                }
+                __syncwarp();
+                float bound;
+                decided = lp2_dual_screen(Tb, m, R2, p, B.fpool + I.f_blo, B.fpool + I.f_bhi, tol.margin_t32 * scale,
+                                          tol.tol_piv32, tol.tol_dj32, tol.max_pivots, tol.degen_switch, &piv, &bound);
+                status = LP_BOUND;
+                t = bound;
+            } else {
+                uint8_t *bid = ids, *nid = ids + R2;
+                for (int r = lane; r < R2; r += 32) {
+                    float *tr = Tb + (size_t)r * ld2;
+                    const float cf = (r < m) ? 1.0f : 0.0f;
+                    float beta = __fmaf_rn(-cf, t0, tr[P1]);
+                    if (!(beta > 0.0f)) beta = 0.0f;
+                    tr[p] = cf;
+                    tr[P1] = beta;
+                    bid[r] = (uint8_t)(P1 + r);
+                }
+                for (int cc = lane; cc <= P1; cc += 32) {
+                    float *ob = Tb + (size_t)R2 * ld2;
+                    ob[cc] = (cc == p) ? 1.0f : (cc == P1 ? -t0 : 0.0f);
+                    if (cc < P1) nid[cc] = (uint8_t)cc;
+                }
+                __syncwarp();
+                Lp<float> L{Tb, ld2, R2, P1, P1, bid, nid};
+                status = warp_simplex_f32<2>(L, tol.tol_piv32, tol.tol_dj32, tol.max_pivots, tol.degen_switch, &piv);
+                t = -Tb[(size_t)R2 * ld2 + P1];
+                if (status == LP_OPTIMAL) {
+                    // "not optimal" when t < -margin_t * scale * (relative element growth of the tableau)
+                    float g2 = 0.0f;
                     for (int r = lane; r < R2; r += 32)
                         for (int cc = 0; cc < P1; cc++) { const float a = fabsf(Tb[(size_t)r * ld2 + cc]); if (a > g2) g2 = a; }
-                g2 = group_max<32>(g2);
-                __syncwarp();
-                if (lane == 0) { sl->status = st; sl->piv = piv; sl->t = t; sl->g2 = g2; }
+                    g2 = warp_max(g2);
+                    const float growth = g2 > g0 ? __fdividef(g2, g0) : 1.0f;
+                    decided = t < -tol.margin_t32 * scale * growth;
+                }
             }
-            __syncwarp();
-        } else {
-            ScreenSlot *sl = slot_of(grp);
-            const bool run = sl->state == SLOT_LP2;
-            const int R2 = run ? sl->R2 : 0, p = run ? sl->p : 0, ld2 = run ? sl->ld2 : 4;
-            const int P1 = p + 1;
-            float *Tb = tab_of(grp);
-            uint8_t *bid = ids_of(grp);
-            Lp<float> L{Tb, ld2, R2, P1, P1, bid, bid + R2};
-            int piv = 0;
-            const int st = group_simplex<GL>(L, run, tol.tol_piv32, tol.tol_dj32, tol.max_pivots, tol.degen_switch, &piv);
-            float g2 = 0.0f;
-            if (run && st == LP_OPTIMAL)
-                for (int r = sub; r < R2; r += GL)
-                    for (int cc = 0; cc < P1; cc++) { const float a = fabsf(Tb[(size_t)r * ld2 + cc]); if (a > g2) g2 = a; }
-            g2 = group_max<GL>(g2);
-            const float t = run ? -Tb[(size_t)R2 * ld2 + P1] : 0.0f;
-            __syncwarp();
-            if (run && sub == 0) { sl->status = st; sl->piv = piv; sl->t = t; sl->g2 = g2; }
-            __syncwarp();
         }
-        // phase C: verdicts, records, queue and counters
-        for (int g = 0; g < NG; g++) {
-            const ScreenSlot *sl = slot_of(g);
-            const int state = sl->state;
-            if (state == SLOT_EMPTY) continue;
-            const Node nd = sl->nd;
-            if (nd.inst != lc.inst) {
-                if (lc.inst >= 0 && lane == 0) {
-                    atomicAdd((unsigned long long *)&B.ictl[lc.inst].optimal, (unsigned long long)lc.a);
-                    atomicAdd((unsigned long long *)&B.ictl[lc.inst].region, (unsigned long long)lc.b);
-                    atomicAdd((unsigned long long *)&B.ictl[lc.inst].lp2_piv, (unsigned long long)lc.c);
-                    atomicAdd((unsigned long long *)&B.ictl[lc.inst].cheb_piv, (unsigned long long)lc.d);
-                }
-                lc.reset(nd.inst);
+        lc.c += piv;
+        if (!decided) {
+            if (lane == 0) {
+                const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_opt, 1ull);
+                if (qi < B.q_cap) B.q_opt[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
             }
-            lc.c += sl->piv;
-            // "not optimal" is final when t < -margin_t * scale, scale = (row
-            // magnitude / smallest Cholesky pivot ratio) * (reach of theta in
-            // the box) * (relative element growth of the LP2 tableau); all in
-            // FP32 (rho > margin_licq and g0 >= 1, so the quotients are tame)
-            bool decided = false;
-            if (state == SLOT_LP2 && sl->status == LP_OPTIMAL) {
-                const float growth = sl->g2 > sl->g0 ? __fdividef(sl->g2, sl->g0) : 1.0f;
-                const float scale = __fdividef(sl->amax, sl->rho) * (1.0f + (float)sl->p * sl->bmax) * growth;
-                decided = sl->t < -tol.margin_t32 * scale;
-            }
-            if (!decided) {
-                if (lane == 0) {
-                    const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_opt, 1ull);
-                    if (qi < B.q_cap) B.q_opt[qi] = (int)sl->x; else atomicOr(&ctl->overflow, OV_QUEUE);
-                }
-                continue;
-            }
-            // a final "not optimal" only leaves a diagnostic record
-            if (lane == 0 && nd.rec >= 0 && B.rec) {
-                OptResult res;
-                res.licq = 1; res.lp2_status = sl->status; res.lp2_piv = sl->piv;
-                res.cheb_status = LP_SKIPPED; res.cheb_piv = 0; res.optimal = 0; res.region = 0;
-                res.t = (double)sl->t; res.r = __longlong_as_double(0x7ff8000000000000LL);
-                res.decided = true;
-                write_opt(B, nd, level, res, false);
-            }
+            __syncwarp();
+            continue;
+        }
+        // a final "not optimal" only leaves a diagnostic record
+        if (lane == 0 && nd.rec >= 0 && B.rec) {
+            OptResult res;
+            res.licq = 1; res.lp2_status = status; res.lp2_piv = piv;
+            res.cheb_status = LP_SKIPPED; res.cheb_piv = 0; res.optimal = 0; res.region = 0;
+            res.t = (double)t; res.r = __longlong_as_double(0x7ff8000000000000LL);
+            res.decided = true;
+            write_opt(B, nd, level, res, false);
         }
         __syncwarp();
     }
@@ -1807,7 +1828,7 @@ size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd)
                            : lp1_slot_bytes<float>(sd.maxM1, sd.maxLD1, sd.maxNv);
 }
 
-size_t screen_smem_per_warp(int lanes, const SlotDims &sd) { return screen_warp_bytes(lanes, sd); }
+size_t screen_smem_per_warp(const SlotDims &sd) { return screen_warp_bytes(sd); }
 
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd)
 {
@@ -1832,9 +1853,7 @@ const void *kernel_ptr(const char *name)
         {"lp1_fp64", (const void *)k_lp1_fp64},
         {"opt64", (const void *)k_optimality<double>},
         {"opt_fp64", (const void *)k_optimality_fp64},
-        {"screen8", (const void *)k_opt_screen<8>},
-        {"screen16", (const void *)k_opt_screen<16>},
-        {"screen32", (const void *)k_opt_screen<32>},
+        {"screen", (const void *)k_opt_screen},
         {"level0_64", (const void *)k_level0<double>},
         {"level0_32", (const void *)k_level0<float>},
         {"reset", (const void *)k_reset},
@@ -1878,12 +1897,10 @@ cudaError_t launch_optimality(const DevBuffers &B, const Tol &tol, const SlotDim
     return cudaGetLastError();
 }
 
-cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int lanes, int grid,
+cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode, int grid,
                               size_t smem, cudaStream_t s)
 {
-    if (lanes == 8) k_opt_screen<8><<<grid, 32, smem, s>>>(B, tol, sd, level);
-    else if (lanes == 16) k_opt_screen<16><<<grid, 32, smem, s>>>(B, tol, sd, level);
-    else k_opt_screen<32><<<grid, 32, smem, s>>>(B, tol, sd, level);
+    k_opt_screen<<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
     return cudaGetLastError();
 }
 

@@ -43,6 +43,7 @@ namespace {
 
 constexpr size_t kScratchBytes = (size_t)MPQP_NOALLOC_SCRATCH_BYTES;
 constexpr size_t kDescBytes = 256;           // InstDesc slot at the start
+static_assert(sizeof(InstDesc) <= kDescBytes, "InstDesc outgrew its scratch slot");
 constexpr int kMaxDevices = 64;
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];

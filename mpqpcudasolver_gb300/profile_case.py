@@ -41,11 +41,12 @@ def main(argv=None):
     ap.add_argument("--mem-fraction", type=float, default=0.85,
                     help="share of free device memory the plan may take (arenas are also capped by the "
                          "combinatorial size of the workload)")
-    ap.add_argument("--screen-lanes", type=int, default=0, help="lanes per LP2 of the FP32 screen (8, 16, 32)")
+    ap.add_argument("--lp2-screen", type=int, default=0,
+                    help="FP32 optimality screen: 0 dual bound on box instances, 1 primal tableau screen")
     args = ap.parse_args(argv)
     probs, kmax, budget = workload(args.case)
     prec = solver.MIXED if args.precision == "mixed" else solver.FP64
-    extra = {"screen_lanes": args.screen_lanes} if args.screen_lanes else {}
+    extra = {"lp2_screen": args.lp2_screen}
     plan = solver.Plan(probs, precision=prec, k_max=kmax, budget=budget, mem_fraction=args.mem_fraction, **extra)
     for _ in range(args.runs):
         plan.run()

@@ -40,7 +40,7 @@ class Options(ctypes.Structure):
                 ("max_pivots", ctypes.c_int), ("degen_switch", ctypes.c_int),
                 ("tol_piv32", ctypes.c_double), ("tol_dj32", ctypes.c_double), ("margin_z", ctypes.c_double),
                 ("margin_beta", ctypes.c_double), ("margin_t", ctypes.c_double), ("margin_licq", ctypes.c_double),
-                ("tol_zero_row", ctypes.c_double), ("screen_lanes", ctypes.c_int)]
+                ("tol_zero_row", ctypes.c_double), ("lp2_screen", ctypes.c_int)]
 
 
 class OptSet(ctypes.Structure):

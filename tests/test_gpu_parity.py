@@ -143,21 +143,28 @@ def test_mixed_equals_fp64_on_the_full_bench_batch(gpu_lib):
     assert r32.candidates == 60802277
 
 
-@pytest.mark.parametrize("lanes", [8, 16])
-def test_screen_lane_groups_match_full_warp_screen(gpu_lib, lanes):
-    """The FP32 LP2 screen run by groups of 8 or 16 lanes (4 or 2 sets per
-    warp, in lock step) takes the pivots of the full-warp screen with the same
-    roundings: every record, FP32 t included, and the fallback counts agree."""
+def test_dual_and_primal_screens_give_the_same_verdicts(gpu_lib):
+    """The FP32 optimality screen proves "not optimal" either with a dual
+    bound (instances whose parameter set is a box, the default) or with the
+    primal LP2 tableau; everything it cannot prove goes to the FP64 kernel.
+    Both routes must end in the same feasible, optimal and region sets, with
+    the same FP64 t* and r* for every optimal set.  The illcond instance has
+    p = 8 and takes the primal route in both modes."""
     probs = [P.scale_problem(P.random_n10_m43_p4()), P.scale_problem(P.illcond_n16_m62_p8()),
-             P.scale_problem(P.mpc_mpqp(0))]
+             P.scale_problem(P.mpc_mpqp(0)), P.scale_problem(P.random_n12_m62_p6())]
     kw = dict(precision=solver.MIXED, k_max=3, record=1, rec_cap=1 << 20, cand_cap=1 << 20, arena_bytes=1 << 28)
-    a = solver.solve(probs, screen_lanes=32, **kw)
-    b = solver.solve(probs, screen_lanes=lanes, **kw)
+    a = solver.solve(probs, lp2_screen=0, **kw)
+    b = solver.solve(probs, lp2_screen=1, **kw)
     assert a.status == 0 and b.status == 0
     ra, rb = _sorted(a.rec, key_inst=True), _sorted(b.rec, key_inst=True)
     assert len(ra) == len(rb) == a.candidates
-    for f in ("inst", "mask_lo", "mask_hi", "feasible", "optimal", "region", "lp2_status", "lp2_pivots", "fp64"):
+    for f in ("inst", "mask_lo", "mask_hi", "feasible", "optimal", "region"):
         assert np.array_equal(ra[f], rb[f]), f
-    assert _same(ra["t"], rb["t"])
-    for f in ("fallback_lp1", "fallback_opt", "optimal", "regions"):
+    opt = ra["optimal"] == 1
+    assert _same(ra["t"][opt], rb["t"][opt]) and _same(ra["r"][opt], rb["r"][opt])
+    for f in ("feasible", "optimal", "regions", "fallback_lp1"):
         assert a.total(f) == b.total(f), f
+    # the illcond instance (p = 8) is screened the same way in both modes
+    ill = ra["inst"] == 1
+    assert np.array_equal(ra["lp2_status"][ill], rb["lp2_status"][ill])
+    print("optimality fallbacks: dual", a.total("fallback_opt"), "primal", b.total("fallback_opt"))
