@@ -613,7 +613,8 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
         nd.lo = lo; nd.hi = hi; nd.inst = inst; nd.flags = NODE_VALID | (feasible ? NODE_FEASIBLE : 0);
         nd.tab_off = toff; nd.ids_off = ioff; nd.rec = rec;
         B.node[side][idx] = nd;
-        if (feasible && !B.exhaustive) {
+        // the hash serves the subset test of the next level only
+        if (feasible && !B.exhaustive && need_tab) {
             if (!hash_insert(B.hash[side], B.hash_cap, (ctl->epoch << 8) | level, inst, lo, hi, (int)idx))
                 atomicOr(&ctl->overflow, OV_HASH);
         }
