@@ -224,6 +224,31 @@ int mpqp_region_laws(const mpqp_problem *prob, long long n_sets, const uint64_t 
 int mpqp_region_laws_noalloc(const mpqp_problem *prob, long long n_sets, const uint64_t *masks, double *laws,
                              int *sizes, void *stream);
 
+/* Constraint reduction before the enumeration.  Replaces the ppopt steps of
+ * MPQPProb.process_constraints (utils.py:163-190: process_program_constraints,
+ * find_implicit_equalities, find_redundant_constraints of ppopt 1.5.1) on the
+ * rows of [A -F; 0 At] u <= [b; bt], u = (x, theta):
+ *   1. a row whose x- and theta-parts are zero is dropped (MPQP_ROW_ZERO);
+ *   2. rows are compared after dividing each by the 2-norm of its [A -F]
+ *      (or At) part; a row equal to an earlier one of the same block, within
+ *      a squared distance of 1e-16, is dropped (MPQP_ROW_DUPLICATE);
+ *   3. a row of A that is the negation of an earlier one (b included) is
+ *      dropped (MPQP_ROW_EQUALITY_PAIR) and the earlier one is kept as an
+ *      implicit equality (MPQP_ROW_EQUALITY);
+ *   4. every other row is redundant (MPQP_ROW_REDUNDANT) when max a_i u over
+ *      all remaining rows, row i relaxed by 1, is at most its right-hand side
+ *      + 1e-9 (normalised rows): one FP64 LP per row on the device, all rows
+ *      against the same row set.
+ * row_status: m + ncp ints, A's rows then At's rows.  Requires b >= 0 and
+ * bt >= 0 (the origin feasible), m + ncp + n + p <= 255. */
+#define MPQP_ROW_KEPT 0
+#define MPQP_ROW_ZERO 1
+#define MPQP_ROW_DUPLICATE 2
+#define MPQP_ROW_EQUALITY_PAIR 3
+#define MPQP_ROW_REDUNDANT 4
+#define MPQP_ROW_EQUALITY 5
+int mpqp_reduce_constraints(const mpqp_problem *prob, int *row_status);
+
 const char *mpqp_version(void);
 const char *mpqp_last_error(void);
 

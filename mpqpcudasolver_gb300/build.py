@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmpqp_gb300.so")
-SOURCES = ["mpqp_kernels.cu", "mpqp_engine.cu", "mpqp_noalloc.cu"]
+SOURCES = ["mpqp_kernels.cu", "mpqp_engine.cu", "mpqp_noalloc.cu", "mpqp_preprocess.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -1642,6 +1642,49 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
     }
 }
 
+// ---------------------------------------------------------------------
+// Constraint reduction: one FP64 LP per row (redundancy test)
+// ---------------------------------------------------------------------
+// The LP rows are M u <= d (u = (x, theta) free, nv columns, row-major M).
+// For each row i of `check`: max a_i u over all rows, with row i relaxed to
+// d_i + 1 so that the maximum stays finite; row i is redundant when that
+// maximum is at most d_i + tol.  One warp per row, the FP64 warp simplex from
+// the slack basis (u = 0 is feasible: d >= 0).  out[c] = 1 redundant, 0 not
+// (an iteration limit keeps the row).
+__global__ void __launch_bounds__(32) k_redundancy(const double *M, const double *d, int nrows, int nv, int ld,
+                                                   const int *check, int n_check, double tol, Tol lt, int max_piv,
+                                                   int *out)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = lane_id();
+    double *T = (double *)smem;
+    uint8_t *bid = smem + align16((size_t)(nrows + 1) * ld * sizeof(double));
+    uint8_t *nid = bid + nrows;
+    for (int c = blockIdx.x; c < n_check; c += gridDim.x) {
+        const int i = check[c];
+        for (int e = lane; e < nrows * nv; e += 32) {
+            const int r = e / nv, j = e - r * nv;
+            T[(size_t)r * ld + j] = M[e];
+        }
+        for (int r = lane; r < nrows; r += 32) {
+            T[(size_t)r * ld + nv] = d[r] + (r == i ? 1.0 : 0.0);
+            bid[r] = (uint8_t)(nv + r);
+        }
+        // objective: minimise -a_i u  (z = 0 - sum_j a_ij u_j)
+        for (int j = lane; j <= nv; j += 32) {
+            T[(size_t)nrows * ld + j] = j < nv ? M[(size_t)i * nv + j] : 0.0;
+            if (j < nv) nid[j] = (uint8_t)j;
+        }
+        __syncwarp();
+        Lp<double> L{T, ld, nrows, nv, nv, bid, nid};
+        int piv = 0;
+        const int st = warp_simplex<double>(L, lt.tol_piv, lt.tol_dj, max_piv, lt.degen_switch, &piv);
+        const double maxval = -T[(size_t)nrows * ld + nv];
+        if (lane == 0) out[c] = (st == LP_OPTIMAL && maxval <= d[i] + tol) ? 1 : 0;
+        __syncwarp();
+    }
+}
+
 template <typename T>
 __global__ void k_level0(DevBuffers B)
 {
@@ -1902,6 +1945,22 @@ cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDim
                               size_t smem, cudaStream_t s)
 {
     k_opt_screen<<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
+    return cudaGetLastError();
+}
+
+size_t redundancy_smem_bytes(int nrows, int ld)
+{
+    return align16((size_t)(nrows + 1) * ld * sizeof(double)) + align16((size_t)nrows + 64);
+}
+
+cudaError_t launch_redundancy(const double *M, const double *d, int nrows, int nv, int ld, const int *check, int n_check,
+                              double tol, const Tol &lt, int max_piv, int *out, int grid, size_t smem, cudaStream_t s)
+{
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_redundancy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_redundancy<<<grid, 32, smem, s>>>(M, d, nrows, nv, ld, check, n_check, tol, lt, max_piv, out);
     return cudaGetLastError();
 }
 

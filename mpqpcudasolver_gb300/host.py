@@ -29,9 +29,11 @@ class MPQPProb:
     """Problem holder of ``utils.py:147-161``.
 
     ``process_constraints`` applies the reference's numerical scaling
-    (``utils.py:192-229``); its ppopt calls -- zero/duplicate row removal,
-    implicit equalities and redundancy removal (``utils.py:165-190``) -- are
-    outside the accelerated path and are not performed.
+    (``utils.py:192-229``).  With ``reduce=True`` it first runs the row
+    reduction that the reference takes from ppopt (zero and duplicate rows,
+    implicit equalities, redundant rows; ``utils.py:165-190``) on the device
+    (``mpqp_reduce_constraints``); the default keeps every row, as the golden
+    fixtures of the reference's own driver were made without ppopt.
     """
 
     def __init__(self, A, b, c, H, Q, CRa, CRb, F):
@@ -56,7 +58,13 @@ class MPQPProb:
         return MPQP(self.Q.copy(), self.c.ravel().copy(), self.H.copy(), self.A.copy(), self.b.ravel().copy(),
                     self.F.copy(), self.A_t.copy(), self.b_t.ravel().copy())
 
-    def process_constraints(self, scale_method: int = 1):
+    def process_constraints(self, scale_method: int = 1, reduce: bool = False):
+        if reduce:
+            from .solver import reduce_constraints
+            _, red = reduce_constraints(self.to_mpqp())
+            self.A, self.F, self.b = red.A, red.F, red.b.reshape(-1, 1)
+            self.A_t, self.b_t = red.CRA, red.CRb.reshape(-1, 1)
+            self.equality_indices = list(red.meta["equality_rows"])
         if scale_method == 2:
             H = np.block([self.A, -self.F])
             norm = np.linalg.norm(H, axis=1, keepdims=True)

@@ -86,7 +86,8 @@ REC_DTYPE = np.dtype([("mask_lo", "<u8"), ("mask_hi", "<u8"), ("level", "<i4"), 
 EXPORTS = ("mpqp", "warm_up", "mpqp_free", "mpqp_unpack_lp", "mpqp_default_options", "mpqp_solve_batch", "mpqp_batch_free",
            "mpqp_plan_create", "mpqp_plan_run", "mpqp_plan_results", "mpqp_plan_launches", "mpqp_plan_destroy",
            "mpqp_plan_run_timed", "mpqp_plan_kernel_times",
-           "mpqp_region_laws_stride", "mpqp_region_laws", "mpqp_version", "mpqp_last_error")
+           "mpqp_region_laws_stride", "mpqp_region_laws", "mpqp_reduce_constraints", "mpqp_version",
+           "mpqp_last_error")
 
 _lib = None
 
@@ -141,6 +142,8 @@ def load(build_if_missing: bool = False):
     lib.mpqp_region_laws.argtypes = [P(Problem), ctypes.c_longlong, P(ctypes.c_uint64), P(ctypes.c_double),
                                      P(ctypes.c_int)]
     lib.mpqp_region_laws.restype = ctypes.c_int
+    lib.mpqp_reduce_constraints.argtypes = [P(Problem), P(ctypes.c_int)]
+    lib.mpqp_reduce_constraints.restype = ctypes.c_int
     lib.mpqp_version.restype = ctypes.c_char_p
     lib.mpqp_last_error.restype = ctypes.c_char_p
     _lib = lib
@@ -296,6 +299,40 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+# row status codes of mpqp_reduce_constraints
+ROW_KEPT, ROW_ZERO, ROW_DUPLICATE, ROW_EQUALITY_PAIR, ROW_REDUNDANT, ROW_EQUALITY = range(6)
+
+
+def reduce_constraints(prob):
+    """Constraint reduction on the device (zero, duplicate, implicit-equality
+    and redundant rows; the ppopt steps of utils.py:163-190).
+
+    Returns (status, reduced): ``status`` holds one code per row of A, then
+    per row of CRA; ``reduced`` is a copy of ``prob`` with the removed rows
+    dropped (row order kept) and ``meta["kept_rows"]`` / ``meta["kept_param_rows"]``
+    / ``meta["equality_rows"]`` (indices into the reduced A) recorded."""
+    lib = load()
+    ps = _ProblemSet([prob], 0, 0, 0)
+    status = np.zeros(prob.m + prob.ncp, dtype=np.intc)
+    _check(lib.mpqp_reduce_constraints(ps.arr, status.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+    return status, apply_row_status(prob, status)
+
+
+def apply_row_status(prob, status):
+    """The problem with the rows that ``status`` marks as removed dropped."""
+    m = prob.m
+    keep = [i for i in range(m) if status[i] in (ROW_KEPT, ROW_EQUALITY)]
+    keep_t = [i for i in range(prob.ncp) if status[m + i] in (ROW_KEPT, ROW_EQUALITY)]
+    out = prob.copy()
+    out.A, out.b, out.F = prob.A[keep], prob.b[keep], prob.F[keep]
+    out.CRA, out.CRb = prob.CRA[keep_t], prob.CRb[keep_t]
+    for name in ("A", "b", "F", "CRA", "CRb"):
+        setattr(out, name, np.ascontiguousarray(getattr(out, name), dtype=np.float64))
+    out.meta = dict(prob.meta, kept_rows=keep, kept_param_rows=keep_t,
+                    equality_rows=[j for j, i in enumerate(keep) if status[i] == ROW_EQUALITY])
+    return out
 
 
 def region_laws(prob, sets):
