@@ -169,12 +169,15 @@ def active_sets_to_regions(prog: MPQPProb, all_active_sets) -> list[dict]:
     return out
 
 
-def calculate_mpqp_with_CUDA(problems, precision: str = "fp64"):
-    """``main.py:11-173`` over a list of ``MPQP`` problems.
+def calculate_mpqp_with_CUDA(problems, precision: str = "fp64", reduce: bool = False, reserved_memory: int = 0):
+    """``main.py:11-173`` over a list of ``MPQP`` problems, one call each.
 
     Returns rows (index, n_regions, total_time, time_GPU) like the reference,
     plus the raw results.  ``precision`` selects the plain FP64 kernels or the
-    FP32 kernels with FP64 certificates (environment variable MPQP_PRECISION).
+    FP32 kernels with FP64 certificates (environment variable MPQP_PRECISION);
+    ``reduce`` runs the device row reduction first (the ppopt steps of
+    ``utils.py:165-190``); ``reserved_memory`` (MiB) is the argument of
+    ``main.py:144``: device memory left free when the call sizes its buffers.
     """
     import os
     os.environ["MPQP_PRECISION"] = "mixed" if precision == "mixed" else "fp64"
@@ -184,10 +187,10 @@ def calculate_mpqp_with_CUDA(problems, precision: str = "fp64"):
     raw = []
     for idx, prob in enumerate(problems):
         prog = MPQPProb.from_mpqp(prob)
-        prog.process_constraints(scale_method=1)
+        prog.process_constraints(scale_method=1, reduce=reduce)
         d = build_lp_data(prog)
         t0 = time.time()
-        r = call_mpqp(lib, d)
+        r = call_mpqp(lib, d, reserved_memory=reserved_memory)
         g = r.contents
         if g.status != 0:
             raise solver.MpqpError(g.status, solver.last_error())
@@ -199,3 +202,53 @@ def calculate_mpqp_with_CUDA(problems, precision: str = "fp64"):
                         radius=[g.radius[i] for i in range(n_final)], n_candidates=g.n_candidates))
         results[idx] = (idx, n_regions, total, g.time_GPU)
     return results, raw
+
+
+def calculate_mpqp_batched(problems, precision: str = "mixed", reduce: bool = False, reserved_memory: int = 0,
+                           max_batch: int = 64):
+    """The driver loop of ``main.py:52-173`` for many problems at once.
+
+    Each problem is reduced (``reduce``) and scaled as in
+    ``MPQPProb.process_constraints``; then up to ``max_batch`` problems share one
+    launch sequence (``mpqp_solve_batch``), every active set up to |S| = n.  A
+    batch may use the free device memory minus ``reserved_memory`` MiB; a batch
+    whose buffers overflow (MPQP_ECAPACITY) is split in half and run again, down
+    to single problems (which then raise).
+
+    Returns rows (index, n_regions, time, n_candidates): the time of a batch is
+    shared among its problems in proportion to their candidates.
+    """
+    import torch
+    prec = solver.MIXED if precision == "mixed" else solver.FP64
+    progs = []
+    for prob in problems:
+        prog = MPQPProb.from_mpqp(prob)
+        prog.process_constraints(scale_method=1, reduce=reduce)
+        progs.append(prog.to_mpqp())
+    free = torch.cuda.mem_get_info()[0]
+    frac = max(0.02, min(0.9, (free - reserved_memory * (1 << 20)) / free))
+    results = np.zeros((len(problems), 4))
+    batches = []
+
+    def run(idx):
+        t0 = time.time()
+        try:
+            r = solver.solve([progs[i] for i in idx], precision=prec, k_max=[progs[i].n for i in idx],
+                             mem_fraction=frac)
+        except solver.MpqpError as e:
+            if e.code == solver.ECAPACITY and len(idx) > 1:
+                half = len(idx) // 2
+                run(idx[:half])
+                run(idx[half:])
+                return
+            raise
+        dt = time.time() - t0
+        cand = np.array([r.inst[j]["candidates"] for j in range(len(idx))], dtype=np.float64)
+        share = cand / max(cand.sum(), 1.0)
+        for j, i in enumerate(idx):
+            results[i] = (i, r.inst[j]["regions"], dt * share[j], cand[j])
+        batches.append(len(idx))
+
+    for b0 in range(0, len(problems), max_batch):
+        run(list(range(b0, min(b0 + max_batch, len(problems)))))
+    return results, batches

@@ -251,6 +251,25 @@ def scale_problem(prob: MPQP) -> MPQP:
     return out
 
 
+def pop_like_set(n_problems: int = 24, seed: int = 0, n_max: int = 5, m_max: int = 16) -> list[MPQP]:
+    """A seeded stand-in for a set of test problems of mixed sizes (the
+    reference's driver loops over a public test set, which is not copied
+    here).  Problem i: sizes drawn from ``default_rng(seed)`` in the order
+    n ~ U{2..n_max}, m ~ U{n+2..m_max}, p ~ U{2..4}, box ~ U[1, 3]; then
+    ``random_mpqp(n, m, p, seed=seed*1000+i, box)``."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_problems):
+        n = int(rng.integers(2, n_max + 1))
+        m = int(rng.integers(n + 2, m_max + 1))
+        p = int(rng.integers(2, 5))
+        box = float(rng.uniform(1.0, 3.0))
+        prob = random_mpqp(n, m, p, seed=seed * 1000 + i, box=box)
+        prob.name = f"pop_like(seed={seed},i={i},n={n},m={m},p={p})"
+        out.append(prob)
+    return out
+
+
 WORKLOADS = {
     "n4-m10-p2": lambda: [random_n4_m10_p2()],
     "n10-m43-p4": lambda: [random_n10_m43_p4()],
@@ -258,4 +277,5 @@ WORKLOADS = {
     "n12-m62-p6": lambda: [random_n12_m62_p6()],
     "illcond-n16-m62-p8": lambda: [illcond_n16_m62_p8()],
     "mpc-batch": mpc_batch,
+    "pop-like": pop_like_set,
 }
