@@ -25,6 +25,7 @@ namespace mq {
 size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd);
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd);
 size_t screen_smem_per_warp(const SlotDims &sd);
+bool screen_dual_route(int mode, const InstDesc &I, const SlotDims &sd);
 size_t laws_smem_per_warp(const SlotDims &sd);
 const void *kernel_ptr(const char *name);
 cudaError_t launch_enumerate(const DevBuffers &B, int level, int grid, cudaStream_t s);
@@ -34,8 +35,8 @@ cudaError_t launch_lp1_fp64(const DevBuffers &B, const Tol &tol, const SlotDims 
                             size_t smem, cudaStream_t s);
 cudaError_t launch_optimality(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int prec,
                               int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode, int grid,
-                              size_t smem, cudaStream_t s);
+cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode, int route,
+                              int grid, size_t smem, cudaStream_t s);
 cudaError_t launch_optimality_fp64(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int grid,
                                    size_t smem, cudaStream_t s);
 cudaError_t launch_level0(const DevBuffers &B, int prec, cudaStream_t s);
@@ -225,6 +226,8 @@ struct mpqp_plan {
     int kmax = 0;
     int prec = PREC_FP64;
     int lp2_screen = 0;         // mixed precision: 0 dual bound on box instances, 1 primal tableau screen
+    bool screen_dual = false, screen_primal = false;   // which FP32 screen routes the instances need
+    int grid_opt2 = 0;          // grid of the primal route (grid_opt: the dual route)
     int grid_enum = 0, grid_feas = 0, grid_lp1fb = 0, grid_opt = 0, grid_optfb = 0;
     size_t smem_feas = 0, smem_lp1fb = 0, smem_opt = 0, smem_optfb = 0;
     int n_launches = 0;
@@ -326,11 +329,6 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
     const DevBuffers &B = P->B;
     const bool mixed = P->prec == PREC_MIXED;
     const char *feas = mixed ? "k_feasibility<float>" : "k_feasibility<double>";
-    const char *opt = mixed ? "k_opt_screen" : "k_optimality<double>";
-    auto launch_opt = [&](int level) {
-        return mixed ? launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, P->grid_opt, P->smem_opt, s)
-                     : launch_optimality(B, P->tol, P->sd, level, P->prec, P->grid_opt, P->smem_opt, s);
-    };
     int nl = 0;
     if (timed) P->kname.clear();
     auto chk = [&](const char *name, cudaError_t e) -> int {
@@ -351,16 +349,29 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
         return MPQP_OK;
     };
 #define L(name, x) do { int _r = pre(name); if (_r) return _r; _r = chk(name, x); if (_r) return _r; } while (0)
+    // FP32 screen: the dual route and/or the primal route, each launched only
+    // when some instance takes it; FP64: the optimality kernel
+    auto launch_opt = [&](int level) -> int {
+        if (!mixed) {
+            L("k_optimality<double>", launch_optimality(B, P->tol, P->sd, level, P->prec, P->grid_opt, P->smem_opt, s));
+            return MPQP_OK;
+        }
+        if (P->screen_dual)
+            L("k_opt_screen<dual>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 0, P->grid_opt, P->smem_opt, s));
+        if (P->screen_primal)
+            L("k_opt_screen<primal>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 1, P->grid_opt2, P->smem_opt, s));
+        return MPQP_OK;
+    };
     L("k_reset", launch_reset(B, s));
     L("k_level0", launch_level0(B, P->prec, s));
-    L(opt, launch_opt(0));
+    { const int _o = launch_opt(0); if (_o) return _o; }
     if (mixed) L("k_optimality_fp64", launch_optimality_fp64(B, P->tol, P->sd, 0, P->grid_optfb, P->smem_optfb, s));
     L("k_finalize", launch_finalize(B, 0, s));
     for (int k = 1; k <= P->kmax; k++) {
         L("k_enumerate", launch_enumerate(B, k, P->grid_enum, s));
         L(feas, launch_feasibility(B, P->tol, P->sd, k, P->prec, P->grid_feas, P->smem_feas, s));
         if (mixed) L("k_lp1_fp64", launch_lp1_fp64(B, P->tol, P->sd, k, P->grid_lp1fb, P->smem_lp1fb, s));
-        L(opt, launch_opt(k));
+        { const int _o = launch_opt(k); if (_o) return _o; }
         if (mixed) L("k_optimality_fp64", launch_optimality_fp64(B, P->tol, P->sd, k, P->grid_optfb, P->smem_optfb, s));
         L("k_finalize", launch_finalize(B, k, s));
     }
@@ -560,13 +571,19 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
     P->smem_lp1fb = 4 * lp1_smem_per_warp(8, sd);
     // mixed precision: the grouped FP32 screen, one warp per block
     P->smem_opt = P->prec == PREC_MIXED ? screen_smem_per_warp(sd) : 4 * opt_smem_per_warp(8, sd);
+    if (P->prec == PREC_MIXED)
+        for (const InstDesc &d : P->desc) {
+            if (screen_dual_route(P->lp2_screen, d, sd)) P->screen_dual = true;
+            else P->screen_primal = true;
+        }
     P->smem_optfb = 4 * opt_smem_per_warp(8, sd);
     if ((rc = grid_for(kernel_ptr("enumerate"), 0, &P->grid_enum)) ||
         (rc = grid_for(kernel_ptr(P->prec == PREC_MIXED ? "feas32" : "feas64"), P->smem_feas, &P->grid_feas)) ||
         (rc = grid_for(kernel_ptr("lp1_fp64"), P->smem_lp1fb, &P->grid_lp1fb)) ||
         (rc = P->prec == PREC_MIXED
-                  ? grid_for(kernel_ptr("screen"), P->smem_opt, &P->grid_opt, 32)
+                  ? grid_for(kernel_ptr("screen_dual"), P->smem_opt, &P->grid_opt, 32)
                   : grid_for(kernel_ptr("opt64"), P->smem_opt, &P->grid_opt)) ||
+        (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_primal"), P->smem_opt, &P->grid_opt2, 32) : 0) ||
         (rc = grid_for(kernel_ptr("opt_fp64"), P->smem_optfb, &P->grid_optfb))) {
         free_plan_mem(P);
         delete P;

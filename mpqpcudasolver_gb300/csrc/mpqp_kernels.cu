@@ -1506,7 +1506,15 @@ __host__ __device__ inline size_t screen_warp_bytes(const SlotDims &sd)
 // clear "not optimal" is final; every other set is queued for
 // k_optimality_fp64.  mode 0: the dual bound where the parameter set is a box
 // (p <= 6, at most 96 rows), the primal tableau screen elsewhere; mode 1:
-// the primal tableau screen everywhere.
+// the primal tableau screen everywhere.  The two routes are two kernels
+// (ROUTE 0 dual, ROUTE 1 primal), each taking only its own sets, so that
+// each carries only its own code.
+__host__ __device__ __forceinline__ bool dual_route(int mode, const InstDesc &I, const SlotDims &sd)
+{
+    return mode == 0 && I.box && I.p <= kDualMaxP && I.m + I.ncp <= kDualMaxRows && sd.maxLD2 >= kDualLd;
+}
+
+template <int ROUTE>
 __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, SlotDims sd, int level, int mode)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1531,13 +1539,14 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
     lc.reset(-1);
     for (;;) {
         long long x;
-        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[3], 1ull);
+        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[ROUTE == 0 ? 3 : 5], 1ull);
         x = __shfl_sync(FULLMASK, x, 0);
         if (x >= nn) break;
         const Node nd = B.node[side][x];
         if ((nd.flags & (NODE_VALID | NODE_FEASIBLE)) != (NODE_VALID | NODE_FEASIBLE)) continue;
         const InstDesc &I = B.inst[nd.inst];
         if (level < I.k_min) continue;
+        if (dual_route(mode, I, sd) != (ROUTE == 0)) continue;
         if (nd.inst != lc.inst) {
             if (lc.inst >= 0 && lane == 0) {
                 atomicAdd((unsigned long long *)&B.ictl[lc.inst].optimal, (unsigned long long)lc.a);
@@ -1558,7 +1567,7 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
             // LP2: max t  s.t.  g theta + t <= h (constraint rows), At theta <= bt
             // the dual screen (mode 0, a box, p <= 6, at most 96 rows; its layout
             // needs rows of kDualLd floats in the slot) or the primal tableau
-            const bool dual = mode == 0 && I.box && p <= kDualMaxP && R2 <= kDualMaxRows && sd.maxLD2 >= kDualLd;
+            constexpr bool dual = ROUTE == 0;
             float t0, g0;
             const float amax = dual ? region_rows<float, true>(D, I, nd.lo, nd.hi, k, ws, Tb, kDualLd, 7, &t0, &g0)
                                     : region_rows<float, true>(D, I, nd.lo, nd.hi, k, ws, Tb, ld2, P1, &t0, &g0);
@@ -1570,7 +1579,7 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
             // margin_licq, so the quotient is tame)
             const float scale = __fdividef(amax, rho) * (1.0f + (float)p * bmax);
             __syncwarp();
-            if (dual) {
+            if constexpr (dual) {
                 // dual layout: g beyond p zero, column 6 c_r (h is in column 7)
                 for (int r = lane; r < R2; r += 32) {
                     float *tr = Tb + (size_t)r * kDualLd;
@@ -1873,6 +1882,7 @@ size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd)
 }
 
 size_t screen_smem_per_warp(const SlotDims &sd) { return screen_warp_bytes(sd); }
+bool screen_dual_route(int mode, const InstDesc &I, const SlotDims &sd) { return dual_route(mode, I, sd); }
 
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd)
 {
@@ -1897,7 +1907,8 @@ const void *kernel_ptr(const char *name)
         {"lp1_fp64", (const void *)k_lp1_fp64},
         {"opt64", (const void *)k_optimality<double>},
         {"opt_fp64", (const void *)k_optimality_fp64},
-        {"screen", (const void *)k_opt_screen},
+        {"screen_dual", (const void *)k_opt_screen<0>},
+        {"screen_primal", (const void *)k_opt_screen<1>},
         {"level0_64", (const void *)k_level0<double>},
         {"level0_32", (const void *)k_level0<float>},
         {"reset", (const void *)k_reset},
@@ -1941,10 +1952,11 @@ cudaError_t launch_optimality(const DevBuffers &B, const Tol &tol, const SlotDim
     return cudaGetLastError();
 }
 
-cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode, int grid,
-                              size_t smem, cudaStream_t s)
+cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode, int route,
+                              int grid, size_t smem, cudaStream_t s)
 {
-    k_opt_screen<<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
+    if (route == 0) k_opt_screen<0><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
+    else k_opt_screen<1><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
     return cudaGetLastError();
 }
 
