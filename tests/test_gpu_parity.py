@@ -143,6 +143,24 @@ def test_mixed_equals_fp64_on_the_full_bench_batch(gpu_lib):
     assert r32.candidates == 60802277
 
 
+def test_mixed_equals_fp64_on_mixed_size_problems_to_full_depth(gpu_lib):
+    """64 problems of mixed sizes (n <= 8, m <= 30), every active set up to
+    |S| = n (3.9M candidates): the deep levels hold near-square, badly
+    conditioned KKT systems, where the FP32 screen is most exposed; the
+    per-instance feasible / optimal / region digests must equal FP64's, in
+    both screen modes."""
+    probs = [P.scale_problem(p) for p in P.pop_like_set(64, seed=0, n_max=8, m_max=30)]
+    kmax = [p.n for p in probs]
+    r64 = solver.solve(probs, precision=solver.FP64, k_max=kmax, mem_fraction=0.5)
+    for mode in (0, 1):
+        r32 = solver.solve(probs, precision=solver.MIXED, k_max=kmax, mem_fraction=0.5, lp2_screen=mode)
+        assert r32.status == 0 and r64.status == 0
+        for f in ("candidates", "feasible", "optimal", "regions", "feasible_digest", "optimal_digest",
+                  "region_digest"):
+            assert np.array_equal(r32.inst[f], r64.inst[f]), (mode, f)
+    assert r64.candidates > 3_000_000
+
+
 def test_dual_and_primal_screens_give_the_same_verdicts(gpu_lib):
     """The FP32 optimality screen proves "not optimal" either with a dual
     bound (instances whose parameter set is a box, the default) or with the
