@@ -196,6 +196,13 @@ int mpqp_plan_run_timed(mpqp_plan *plan, void *stream);
 int mpqp_plan_kernel_times(mpqp_plan *plan, int max_kernels, char *names, double *ms, int *count);
 void mpqp_plan_destroy(mpqp_plan *plan);
 
+/* Plans take their device memory from a pool (one per device) that keeps
+ * freed memory for the next plan, so destroying a plan is cheap; the pool's
+ * idle memory counts as free when a plan sizes its buffers.  This returns the
+ * idle memory of the current device's pool to the driver.  No counterpart in
+ * the reference (its buffers live inside each mpqp() call). */
+int mpqp_release_cached_memory(void);
+
 /* Region laws of optimal sets, computed in FP64 on the device:
  *   lagrange_A (k x p), lagrange_b (k), parameter_A (n x p), parameter_b (n),
  *   CR rows (n_cr x (p+1)): [CR_As | CR_bs] normalised, reference order.

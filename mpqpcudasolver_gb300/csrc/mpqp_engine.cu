@@ -227,6 +227,7 @@ struct mpqp_plan {
     int prec = PREC_FP64;
     int lp2_screen = 0;         // mixed precision: 0 dual bound on box instances, 1 primal tableau screen
     bool screen_dual = false, screen_primal = false;   // which FP32 screen routes the instances need
+    bool pooled = false;        // allocations came from the device pool
     int grid_opt2 = 0;          // grid of the primal route (grid_opt: the dual route)
     int grid_enum = 0, grid_feas = 0, grid_lp1fb = 0, grid_opt = 0, grid_optfb = 0;
     size_t smem_feas = 0, smem_lp1fb = 0, smem_opt = 0, smem_optfb = 0;
@@ -279,10 +280,64 @@ static void fill_defaults(mpqp_options &o)
 #undef DEF
 }
 
+// Plan memory comes from one stream-ordered pool per device that keeps what
+// is freed (release threshold: everything).  Freeing the tens of GB of a
+// large plan with cudaFree unmaps them and takes over 100 ms; from the pool,
+// a plan's teardown is cheap and the next plan reuses the memory.  The idle
+// bytes of the pool count as free when a plan sizes its buffers, and
+// mpqp_release_cached_memory() hands them back to the driver.
+static std::mutex g_pool_mu;
+static cudaMemPool_t g_pools[64] = {};
+
+static cudaMemPool_t plan_pool(int dev)
+{
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (dev < 0 || dev >= 64) return nullptr;
+    if (!g_pools[dev]) {
+        cudaMemPoolProps props;
+        memset(&props, 0, sizeof(props));
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool;
+        if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+        uint64_t keep = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        g_pools[dev] = pool;
+    }
+    return g_pools[dev];
+}
+
+// bytes the pool of `dev` holds but no plan uses
+static size_t pool_idle_bytes(int dev)
+{
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (dev < 0 || dev >= 64 || !g_pools[dev]) return 0;
+    uint64_t reserved = 0, used = 0;
+    if (cudaMemPoolGetAttribute(g_pools[dev], cudaMemPoolAttrReservedMemCurrent, &reserved) != cudaSuccess ||
+        cudaMemPoolGetAttribute(g_pools[dev], cudaMemPoolAttrUsedMemCurrent, &used) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return reserved > used ? (size_t)(reserved - used) : 0;
+}
+
+static size_t free_device_bytes()
+{
+    size_t fb = 0, tb = 0;
+    int dev = 0;
+    if (cudaMemGetInfo(&fb, &tb) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return 0; }
+    return fb + pool_idle_bytes(dev);
+}
+
 static int dev_alloc(mpqp_plan *P, void **ptr, size_t bytes)
 {
     if (bytes == 0) bytes = 16;
-    cudaError_t e = cudaMalloc(ptr, bytes);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaMemPool_t pool = plan_pool(dev);
+    cudaError_t e = pool ? cudaMallocFromPoolAsync(ptr, bytes, pool, 0) : cudaMalloc(ptr, bytes);
+    if (e == cudaSuccess && pool) P->pooled = true;
     if (e != cudaSuccess) {
         set_err(std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
         cudaGetLastError();
@@ -297,7 +352,14 @@ static void free_plan_mem(mpqp_plan *P)
     if (P->exec) cudaGraphExecDestroy(P->exec);
     if (P->graph) cudaGraphDestroy(P->graph);
     P->exec = nullptr; P->graph = nullptr;
-    for (void *p : P->allocs) cudaFree(p);
+    if (P->pooled) {
+        // every run of the plan has finished before its memory goes back
+        cudaDeviceSynchronize();
+        for (void *p : P->allocs) cudaFreeAsync(p, 0);
+        cudaStreamSynchronize(0);
+    } else {
+        for (void *p : P->allocs) cudaFree(p);
+    }
     P->allocs.clear();
     if (P->ev0) cudaEventDestroy(P->ev0);
     if (P->ev1) cudaEventDestroy(P->ev1);
@@ -465,6 +527,7 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
         delete P;
         return MPQP_ECUDA;
     }
+    free_b = free_device_bytes();
     const double usable = (double)free_b * o.mem_fraction;
     long long total_budget = 0;
     bool all_budget = true;
@@ -559,6 +622,7 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
     AL(B.ictl, sizeof(InstCtl) * n_inst);
     AL(B.ctl, sizeof(Ctl));
 #undef AL
+    CK(cudaStreamSynchronize(0));   // the pool's allocations are stream-ordered on stream 0
     CK(cudaMemcpy((void *)B.inst, P->desc.data(), sizeof(InstDesc) * n_inst, cudaMemcpyHostToDevice));
     CK(cudaMemcpy((void *)B.dpool, dp.data(), sizeof(double) * dp.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy((void *)B.fpool, fp.data(), sizeof(float) * fp.size(), cudaMemcpyHostToDevice));
@@ -943,6 +1007,7 @@ extern "C" GPUResults *mpqp(const double *AxT, int n_c, int n_x, int n_t, int k_
     if (reserved_memory > 0) {
         size_t fb = 0, tb = 0;
         if (cudaMemGetInfo(&fb, &tb) == cudaSuccess) {
+            fb = free_device_bytes();
             const double keep = (double)reserved_memory * 1024.0 * 1024.0;
             o.mem_fraction = std::max(0.05, std::min(0.6, ((double)fb - keep) / std::max(1.0, (double)fb)));
         }
@@ -1010,6 +1075,21 @@ extern "C" void warm_up(void)
     mpqp_batch_result *R = nullptr;
     mpqp_solve_batch(1, &pr, &o, &R);
     mpqp_batch_free(R);
+}
+
+extern "C" int mpqp_release_cached_memory(void)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); set_err("cudaGetDevice failed"); return MPQP_ECUDA; }
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (dev >= 0 && dev < 64 && g_pools[dev]) {
+        cudaDeviceSynchronize();
+        if (cudaMemPoolTrimTo(g_pools[dev], 0) != cudaSuccess) {
+            set_err(std::string("cudaMemPoolTrimTo: ") + cudaGetErrorString(cudaGetLastError()));
+            return MPQP_ECUDA;
+        }
+    }
+    return MPQP_OK;
 }
 
 extern "C" const char *mpqp_version(void) { return "mpqp_gb300 0.1 (sm_103a)"; }

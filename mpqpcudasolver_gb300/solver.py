@@ -86,7 +86,8 @@ REC_DTYPE = np.dtype([("mask_lo", "<u8"), ("mask_hi", "<u8"), ("level", "<i4"), 
 EXPORTS = ("mpqp", "warm_up", "mpqp_free", "mpqp_unpack_lp", "mpqp_default_options", "mpqp_solve_batch", "mpqp_batch_free",
            "mpqp_plan_create", "mpqp_plan_run", "mpqp_plan_results", "mpqp_plan_launches", "mpqp_plan_destroy",
            "mpqp_plan_run_timed", "mpqp_plan_kernel_times",
-           "mpqp_region_laws_stride", "mpqp_region_laws", "mpqp_reduce_constraints", "mpqp_version",
+           "mpqp_region_laws_stride", "mpqp_region_laws", "mpqp_reduce_constraints", "mpqp_release_cached_memory",
+           "mpqp_version",
            "mpqp_last_error")
 
 _lib = None
@@ -144,6 +145,7 @@ def load(build_if_missing: bool = False):
     lib.mpqp_region_laws.restype = ctypes.c_int
     lib.mpqp_reduce_constraints.argtypes = [P(Problem), P(ctypes.c_int)]
     lib.mpqp_reduce_constraints.restype = ctypes.c_int
+    lib.mpqp_release_cached_memory.restype = ctypes.c_int
     lib.mpqp_version.restype = ctypes.c_char_p
     lib.mpqp_last_error.restype = ctypes.c_char_p
     _lib = lib
