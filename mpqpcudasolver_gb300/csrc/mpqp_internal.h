@@ -137,6 +137,7 @@ struct Ctl {
     int level;
     int epoch;                  // run counter; hash tags are (epoch << 8) | level
     int pad;
+    long long hcap[2];          // slots of the hash in use per side (a power of 2 <= hash_cap)
 };
 
 enum Overflow : int { OV_CAND = 1, OV_NODE = 2, OV_TAB = 4, OV_IDS = 8, OV_OPT = 16, OV_REC = 32, OV_QUEUE = 64, OV_HASH = 128 };

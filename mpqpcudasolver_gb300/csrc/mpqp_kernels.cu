@@ -84,6 +84,16 @@ __device__ __forceinline__ uint64_t hash_key(int inst, uint64_t lo, uint64_t hi)
     return mix64(lo ^ mix64(hi ^ ((uint64_t)(uint32_t)inst * 0x9e3779b97f4a7c15ULL)));
 }
 
+// Slots a level's hash uses: the smallest power of 2 above twice the level's
+// candidates (an upper bound on its inserts), at most the allocated table.
+// A level with few sets keeps its probes inside a small, L2-resident prefix.
+__device__ __forceinline__ long long hash_cap_for(const DevBuffers &B, long long n_sets)
+{
+    long long c = 16;
+    while (c < 2 * n_sets + 1 && c < B.hash_cap) c <<= 1;
+    return c < B.hash_cap ? c : B.hash_cap;
+}
+
 __device__ int hash_find(const HashSlot *tab, long long cap, int tag, int inst, uint64_t lo, uint64_t hi)
 {
     uint64_t s = hash_key(inst, lo, hi) & (uint64_t)(cap - 1);
@@ -449,6 +459,9 @@ __global__ void k_enumerate(DevBuffers B, int level)
     Ctl *ctl = B.ctl;
     const long long npar = ctl->n_node[pside] < B.node_cap ? ctl->n_node[pside] : B.node_cap;
     const int tag_prev = (ctl->epoch << 8) | (level - 1);  // tag of the previous level's hash entries
+    // slots the previous level's inserts used (every expandable parent was
+    // inserted, which sets it; the full table otherwise, which is always in bounds)
+    const long long hcap = ctl->hcap[pside] >= 16 && ctl->hcap[pside] <= B.hash_cap ? ctl->hcap[pside] : B.hash_cap;
     int cur_inst = -1;
     long long loc_cand = 0, loc_pruned = 0;
     for (;;) {
@@ -484,7 +497,7 @@ __global__ void k_enumerate(DevBuffers B, int level)
                     else { a = 64 + __ffsll((long long)rhi) - 1; rhi &= rhi - 1; }
                     uint64_t slo = lo, shi = hi;
                     if (a < 64) slo &= ~(1ull << a); else shi &= ~(1ull << (a - 64));
-                    if (hash_find(B.hash[pside], B.hash_cap, tag_prev, par.inst, slo, shi) < 0) ok = false;
+                    if (hash_find(B.hash[pside], hcap, tag_prev, par.inst, slo, shi) < 0) ok = false;
                 }
             }
             const unsigned okm = __ballot_sync(FULLMASK, ok);
@@ -560,7 +573,7 @@ __device__ __forceinline__ void warp_copy_v(T *dst, const T *src, int n)
 template <typename TT, typename TS>
 __device__ long long store_node(const DevBuffers &B, int side, int level, const InstDesc &I, int inst,
                                 uint64_t lo, uint64_t hi, bool feasible, const TS *tab, const uint8_t *ids,
-                                long long rec, int src_ld = 0)
+                                long long rec, long long hcap, int src_ld = 0)
 {
     const int lane = lane_id();
     Ctl *ctl = B.ctl;
@@ -615,7 +628,7 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
         B.node[side][idx] = nd;
         // the hash serves the subset test of the next level only
         if (feasible && !B.exhaustive && need_tab) {
-            if (!hash_insert(B.hash[side], B.hash_cap, (ctl->epoch << 8) | level, inst, lo, hi, (int)idx))
+            if (!hash_insert(B.hash[side], hcap, (ctl->epoch << 8) | level, inst, lo, hi, (int)idx))
                 atomicOr(&ctl->overflow, OV_HASH);
         }
     }
@@ -642,6 +655,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
     const int side = level & 1, pside = side ^ 1;
     Ctl *ctl = B.ctl;
     const long long ncand = ctl->n_cand;
+    const long long hcap = hash_cap_for(B, ncand);   // slots of this level's hash
     const bool mixed = sizeof(T) == 4;
     const T tpiv = mixed ? (T)tol.tol_piv32 : (T)tol.tol_piv;
     const T tdj = mixed ? (T)tol.tol_dj32 : (T)tol.tol_dj;
@@ -764,7 +778,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         }
         if (feasible) { lc.a++; lc.c += (long long)mask_digest(lo, hi); }
         if (feasible || B.exhaustive)
-            store_node<T, T>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec);
+            store_node<T, T>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap);
     }
     if (lc.inst >= 0 && lane == 0) {
         atomicAdd((unsigned long long *)&B.ictl[lc.inst].feasible, (unsigned long long)lc.a);
@@ -787,6 +801,7 @@ __global__ void __launch_bounds__(128) k_lp1_fp64(DevBuffers B, Tol tol, SlotDim
     const int side = level & 1, pside = side ^ 1;
     Ctl *ctl = B.ctl;
     const long long nq = ctl->n_q_lp1 < B.q_cap ? ctl->n_q_lp1 : B.q_cap;
+    const long long hcap = hash_cap_for(B, ctl->n_cand);   // slots of this level's hash
     for (;;) {
         long long x;
         if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[2], 1ull);
@@ -833,7 +848,7 @@ __global__ void __launch_bounds__(128) k_lp1_fp64(DevBuffers B, Tol tol, SlotDim
             }
         }
         if (feasible || B.exhaustive)
-            store_node<float, double>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, I.ld1d);
+            store_node<float, double>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap, I.ld1d);
     }
 }
 
@@ -1715,7 +1730,9 @@ __global__ void k_level0(DevBuffers B)
         nd.lo = 0; nd.hi = 0; nd.inst = inst; nd.flags = NODE_VALID | NODE_FEASIBLE; nd.tab_off = toff; nd.ids_off = ioff;
         nd.rec = (B.rec && inst < B.rec_cap) ? inst : -1;
         B.node[0][inst] = nd;
-        if (!B.exhaustive) hash_insert(B.hash[0], B.hash_cap, ctl->epoch << 8, inst, 0, 0, inst);
+        if (!B.exhaustive) {
+            hash_insert(B.hash[0], hash_cap_for(B, B.n_inst), ctl->epoch << 8, inst, 0, 0, inst);
+        }
         if (nd.rec >= 0) {
             CandRec &R = B.rec[nd.rec];
             R.mask_lo = 0; R.mask_hi = 0; R.level = 0; R.parent = -1;
@@ -1781,6 +1798,7 @@ __global__ void k_finalize(DevBuffers B, int level)
     if (t == 0) {
         const int pside = (level & 1) ^ 1;
         if (B.rec) ctl->rec_base += ctl->n_cand;
+        ctl->hcap[level & 1] = hash_cap_for(B, ctl->n_cand);   // what this level's inserts used
         ctl->n_cand = 0;
         if (level > 0) {
             ctl->n_node[pside] = 0;
