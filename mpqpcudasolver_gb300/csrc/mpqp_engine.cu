@@ -24,7 +24,7 @@
 namespace mq {
 size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd);
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd);
-size_t screen_smem_per_warp(const SlotDims &sd);
+size_t screen_smem_per_warp(const SlotDims &sd, int route);
 bool screen_dual_route(int mode, const InstDesc &I, const SlotDims &sd);
 size_t laws_smem_per_warp(const SlotDims &sd);
 const void *kernel_ptr(const char *name);
@@ -229,6 +229,7 @@ struct mpqp_plan {
     bool screen_dual = false, screen_primal = false;   // which FP32 screen routes the instances need
     bool pooled = false;        // allocations came from the device pool
     int grid_opt2 = 0;          // grid of the primal route (grid_opt: the dual route)
+    size_t smem_opt2 = 0;       // shared memory per block of the primal route
     int grid_enum = 0, grid_feas = 0, grid_lp1fb = 0, grid_opt = 0, grid_optfb = 0;
     size_t smem_feas = 0, smem_lp1fb = 0, smem_opt = 0, smem_optfb = 0;
     int n_launches = 0;
@@ -421,7 +422,7 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
         if (P->screen_dual)
             L("k_opt_screen<dual>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 0, P->grid_opt, P->smem_opt, s));
         if (P->screen_primal)
-            L("k_opt_screen<primal>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 1, P->grid_opt2, P->smem_opt, s));
+            L("k_opt_screen<primal>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 1, P->grid_opt2, P->smem_opt2, s));
         return MPQP_OK;
     };
     L("k_reset", launch_reset(B, s));
@@ -634,7 +635,8 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
     P->smem_feas = 4 * lp1_smem_per_warp(P->prec == PREC_MIXED ? 4 : 8, sd);
     P->smem_lp1fb = 4 * lp1_smem_per_warp(8, sd);
     // mixed precision: the grouped FP32 screen, one warp per block
-    P->smem_opt = P->prec == PREC_MIXED ? screen_smem_per_warp(sd) : 4 * opt_smem_per_warp(8, sd);
+    P->smem_opt = P->prec == PREC_MIXED ? screen_smem_per_warp(sd, 0) : 4 * opt_smem_per_warp(8, sd);
+    P->smem_opt2 = screen_smem_per_warp(sd, 1);
     if (P->prec == PREC_MIXED)
         for (const InstDesc &d : P->desc) {
             if (screen_dual_route(P->lp2_screen, d, sd)) P->screen_dual = true;
@@ -647,7 +649,7 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
         (rc = P->prec == PREC_MIXED
                   ? grid_for(kernel_ptr("screen_dual"), P->smem_opt, &P->grid_opt, 32)
                   : grid_for(kernel_ptr("opt64"), P->smem_opt, &P->grid_opt)) ||
-        (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_primal"), P->smem_opt, &P->grid_opt2, 32) : 0) ||
+        (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_primal"), P->smem_opt2, &P->grid_opt2, 32) : 0) ||
         (rc = grid_for(kernel_ptr("opt_fp64"), P->smem_optfb, &P->grid_optfb))) {
         free_plan_mem(P);
         delete P;

@@ -78,7 +78,10 @@ struct Node {                   // a feasible (or, when exhaustive, any) active 
     long long rec;              // record index (or -1)
 };
 
-enum NodeFlags : int { NODE_FEASIBLE = 1, NODE_VALID = 2 };
+// NODE_FP64CHAIN: this set, or one of the sets its LP1 warm start descends
+// from, needed the FP64 re-solve (mixed precision); FP32 "infeasible"
+// verdicts below such a node are re-solved in FP64 too.
+enum NodeFlags : int { NODE_FEASIBLE = 1, NODE_VALID = 2, NODE_FP64CHAIN = 4 };
 
 struct Cand { int parent; int j; };
 

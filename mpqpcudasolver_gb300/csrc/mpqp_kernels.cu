@@ -573,7 +573,7 @@ __device__ __forceinline__ void warp_copy_v(T *dst, const T *src, int n)
 template <typename TT, typename TS>
 __device__ long long store_node(const DevBuffers &B, int side, int level, const InstDesc &I, int inst,
                                 uint64_t lo, uint64_t hi, bool feasible, const TS *tab, const uint8_t *ids,
-                                long long rec, long long hcap, int src_ld = 0)
+                                long long rec, long long hcap, int extra_flags, int src_ld = 0)
 {
     const int lane = lane_id();
     Ctl *ctl = B.ctl;
@@ -623,7 +623,7 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
     }
     if (lane == 0) {
         Node nd;
-        nd.lo = lo; nd.hi = hi; nd.inst = inst; nd.flags = NODE_VALID | (feasible ? NODE_FEASIBLE : 0);
+        nd.lo = lo; nd.hi = hi; nd.inst = inst; nd.flags = NODE_VALID | (feasible ? NODE_FEASIBLE : 0) | extra_flags;
         nd.tab_off = toff; nd.ids_off = ioff; nd.rec = rec;
         B.node[side][idx] = nd;
         // the hash serves the subset test of the next level only
@@ -719,13 +719,10 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
             feasible = (st == LP_OPTIMAL) && ((double)z <= tol.tol_feas);
         } else {
             if (st != LP_OPTIMAL) decided = false;
-            else if (z > (T)tol.margin_z32) feasible = false;
             else {
-                // certificate: every slack of S nonbasic and every basic slack
-                // clearly positive -> the basic solution is a feasible point
-                // with all rows of S tight.
-                // The FP32 errors of the basic values grow with the tableau's
-                // element growth (max |T_ij| ~ |B^-1 N|), so the margin does too.
+                // the final tableau: whether a slack of S is basic, the
+                // smallest basic slack and the element growth max |T_ij|
+                // (~ |B^-1 N|), by which the FP32 errors of the basic values grow
                 bool s_basic = false;
                 T minb = pos_inf<T>(), gmax = T(1);
                 for (int i = lane; i < M1; i += 32) {
@@ -754,7 +751,16 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
                 }
                 lp1_growth = (float)gmax;
                 lp1_minbeta = (float)minb;
-                if (!s_basic && minb > (T)tol.margin_beta32 * gmax) feasible = true;
+                // infeasible: z clearly positive -- except in a chain that has
+                // already needed FP64 (nearly degenerate, badly conditioned
+                // bases, where the FP32 simplex can stop at a wrong optimum)
+                if (z > (T)tol.margin_z32) {
+                    if (par.flags & NODE_FP64CHAIN) decided = false;
+                    else feasible = false;
+                }
+                // feasible: every slack of S nonbasic (all rows of S tight at
+                // the basic solution) and every basic slack clearly positive
+                else if (!s_basic && minb > (T)tol.margin_beta32 * gmax) feasible = true;
                 else decided = false;
             }
         }
@@ -778,7 +784,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         }
         if (feasible) { lc.a++; lc.c += (long long)mask_digest(lo, hi); }
         if (feasible || B.exhaustive)
-            store_node<T, T>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap);
+            store_node<T, T>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap, par.flags & NODE_FP64CHAIN);
     }
     if (lc.inst >= 0 && lane == 0) {
         atomicAdd((unsigned long long *)&B.ictl[lc.inst].feasible, (unsigned long long)lc.a);
@@ -848,7 +854,8 @@ __global__ void __launch_bounds__(128) k_lp1_fp64(DevBuffers B, Tol tol, SlotDim
             }
         }
         if (feasible || B.exhaustive)
-            store_node<float, double>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap, I.ld1d);
+            store_node<float, double>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap, NODE_FP64CHAIN,
+                                      I.ld1d);
     }
 }
 
@@ -1510,11 +1517,12 @@ __device__ int lp2_dual_screen(const float *T, int m, int R2, int p, const float
 
 // per-warp shared memory of the screen: KKT workspace (R, Y, Lambda, S),
 // the LP2 tableau (R2+1) x ld2 and its basis ids (R2 + P1)
-__host__ __device__ inline size_t screen_warp_bytes(const SlotDims &sd)
+// (the primal route also keeps the unpivoted region rows G, R2 x (p+1))
+__host__ __device__ inline size_t screen_warp_bytes(const SlotDims &sd, int route)
 {
     return align16((size_t)sd.maxK * sd.maxK * 4) + 2 * align16((size_t)sd.maxK * sd.maxP1 * 4) +
            align16((size_t)sd.maxK * sizeof(int)) + align16((size_t)(sd.maxR2 + 1) * sd.maxLD2 * 4) +
-           align16((size_t)sd.maxR2 + sd.maxP1);
+           align16((size_t)sd.maxR2 + sd.maxP1) + (route == 1 ? align16((size_t)sd.maxR2 * sd.maxP1 * 4) : 0);
 }
 
 // The FP32 screen of every feasible set of a level, one warp per set.  Only a
@@ -1544,8 +1552,9 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
         ws.Lam = (float *)(smem + o); o += align16((size_t)sd.maxK * sd.maxP1 * 4);
         ws.S = (int *)(smem + o); o += align16((size_t)sd.maxK * sizeof(int));
         Tb = (float *)(smem + o); o += align16((size_t)(sd.maxR2 + 1) * sd.maxLD2 * 4);
-        ids = smem + o;
-        ws.G = nullptr; ws.Tb = nullptr; ws.ids = nullptr;
+        ids = smem + o; o += align16((size_t)sd.maxR2 + sd.maxP1);
+        ws.G = ROUTE == 1 ? (float *)(smem + o) : nullptr;
+        ws.Tb = nullptr; ws.ids = nullptr;
     }
     const int side = level & 1;
     Ctl *ctl = B.ctl;
@@ -1584,8 +1593,10 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
             // needs rows of kDualLd floats in the slot) or the primal tableau
             constexpr bool dual = ROUTE == 0;
             float t0, g0;
+            // dual: rows straight into the dual layout; primal: rows into G,
+            // kept unpivoted for the bound that verifies the verdict
             const float amax = dual ? region_rows<float, true>(D, I, nd.lo, nd.hi, k, ws, Tb, kDualLd, 7, &t0, &g0)
-                                    : region_rows<float, true>(D, I, nd.lo, nd.hi, k, ws, Tb, ld2, P1, &t0, &g0);
+                                    : region_rows<float, true>(D, I, nd.lo, nd.hi, k, ws, nullptr, 0, 0, &t0, &g0);
             float bmax = 0.0f;
             for (int ii = lane; ii < ncp; ii += 32) { const float v = fabsf(D.bt[ii]); if (v > bmax) bmax = v; }
             bmax = warp_max(bmax);
@@ -1609,10 +1620,13 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
                 t = bound;
             } else {
                 uint8_t *bid = ids, *nid = ids + R2;
+                const float *G = ws.G;
                 for (int r = lane; r < R2; r += 32) {
                     float *tr = Tb + (size_t)r * ld2;
+                    const float *g = G + (size_t)r * P1;
+                    for (int cc = 0; cc < p; cc++) tr[cc] = g[cc];
                     const float cf = (r < m) ? 1.0f : 0.0f;
-                    float beta = __fmaf_rn(-cf, t0, tr[P1]);
+                    float beta = __fmaf_rn(-cf, t0, g[p]);
                     if (!(beta > 0.0f)) beta = 0.0f;
                     tr[p] = cf;
                     tr[P1] = beta;
@@ -1627,14 +1641,39 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
                 Lp<float> L{Tb, ld2, R2, P1, P1, bid, nid};
                 status = warp_simplex_f32<2>(L, tol.tol_piv32, tol.tol_dj32, tol.max_pivots, tol.degen_switch, &piv);
                 t = -Tb[(size_t)R2 * ld2 + P1];
-                if (status == LP_OPTIMAL) {
-                    // "not optimal" when t < -margin_t * scale * (relative element growth of the tableau)
-                    float g2 = 0.0f;
-                    for (int r = lane; r < R2; r += 32)
-                        for (int cc = 0; cc < P1; cc++) { const float a = fabsf(Tb[(size_t)r * ld2 + cc]); if (a > g2) g2 = a; }
-                    g2 = warp_max(g2);
-                    const float growth = g2 > g0 ? __fdividef(g2, g0) : 1.0f;
-                    decided = t < -tol.margin_t32 * scale * growth;
+                // The FP32 primal optimum t is only a lower bound on t* when the
+                // FP32 basis is not truly optimal (degenerate, badly
+                // conditioned LPs), so it never decides alone: the duals y of
+                // the final tableau (y_r = -reduced cost of slack r, 0 when
+                // basic) give the upper bound (h.y + sum_c |(G^T y)_c| reach_c)
+                // / (c.y) of lp2_dual_screen, evaluated on the unpivoted rows;
+                // it needs a box (reach), so other parameter sets go to FP64.
+                if (status == LP_OPTIMAL && t < -tol.margin_t32 * scale && I.box) {
+                    const float *ob = Tb + (size_t)R2 * ld2;
+                    int ry = -1;
+                    float yv = 0.0f;
+                    if (lane < P1 && nid[lane] >= P1) { ry = nid[lane] - P1; yv = fmaxf(-ob[lane], 0.0f); }
+                    // lane c < p: (G^T y)_c, lane p: c.y, lane p+1: h.y
+                    float acc = 0.0f;
+                    for (int i = 0; i < P1; i++) {
+                        const int ri = __shfl_sync(FULLMASK, ry, i);
+                        const float yi = __shfl_sync(FULLMASK, yv, i);
+                        if (ri >= 0 && lane <= P1) {
+                            const float v = lane < p ? G[(size_t)ri * P1 + lane]
+                                                     : (lane == p ? (ri < m ? 1.0f : 0.0f) : G[(size_t)ri * P1 + p]);
+                            acc = __fmaf_rn(yi, v, acc);
+                        }
+                    }
+                    float reach = 0.0f;
+                    if (lane < p) {
+                        const float lo_c = B.fpool[I.f_blo + lane], hi_c = B.fpool[I.f_bhi + lane];
+                        reach = fmaxf(fabsf(lo_c), fabsf(hi_c));
+                    }
+                    const float cy = __shfl_sync(FULLMASK, acc, p);
+                    const float num = warp_sum(lane < p ? fabsf(acc) * reach : (lane == P1 ? acc : 0.0f));
+                    const float bound = cy > 0.0f ? __fdividef(num, cy) : pos_inf<float>();
+                    decided = bound < -tol.margin_t32 * scale;
+                    t = bound;
                 }
             }
         }
@@ -1899,7 +1938,7 @@ size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd)
                            : lp1_slot_bytes<float>(sd.maxM1, sd.maxLD1, sd.maxNv);
 }
 
-size_t screen_smem_per_warp(const SlotDims &sd) { return screen_warp_bytes(sd); }
+size_t screen_smem_per_warp(const SlotDims &sd, int route) { return screen_warp_bytes(sd, route); }
 bool screen_dual_route(int mode, const InstDesc &I, const SlotDims &sd) { return dual_route(mode, I, sd); }
 
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd)

@@ -161,6 +161,20 @@ def test_mixed_equals_fp64_on_mixed_size_problems_to_full_depth(gpu_lib):
     assert r64.candidates > 3_000_000
 
 
+def test_mixed_equals_fp64_on_ill_conditioned_instances(gpu_lib):
+    """Eight ill-conditioned instances (Q eigenvalues over four decades, 20 %
+    near-duplicate rows; seeds 0..7), every set up to |S| = 4: nearly singular
+    KKT systems everywhere, where an FP32 verdict is most likely to go wrong;
+    the per-instance feasible / optimal / region digests must equal FP64's."""
+    probs = [P.scale_problem(P.illcond_n16_m62_p8(seed=s)) for s in range(8)]
+    r64 = solver.solve(probs, precision=solver.FP64, k_max=4, mem_fraction=0.5)
+    r32 = solver.solve(probs, precision=solver.MIXED, k_max=4, mem_fraction=0.5)
+    assert r32.status == 0 and r64.status == 0
+    for f in ("candidates", "feasible", "optimal", "regions", "feasible_digest", "optimal_digest", "region_digest"):
+        assert np.array_equal(r32.inst[f], r64.inst[f]), f
+    print("ill-conditioned: candidates", r64.candidates, "fallbacks", r32.total("fallback_lp1"), r32.total("fallback_opt"))
+
+
 def test_dual_and_primal_screens_give_the_same_verdicts(gpu_lib):
     """The FP32 optimality screen proves "not optimal" either with a dual
     bound (instances whose parameter set is a box, the default) or with the
