@@ -95,7 +95,7 @@ int mpqp_unpack_lp(const double *AxT, int n_c, int n_x, int n_t, const double *A
 enum {
     MPQP_OK = 0,
     MPQP_EINVAL = -1,      /* bad sizes or pointers                        */
-    MPQP_ENOTSPD = -2,     /* Q is not positive definite                   */
+    MPQP_ENOTSPD = -2,     /* Q is neither positive definite nor zero      */
     MPQP_EORIGIN = -3,     /* b < 0 or CRb < 0: the origin is infeasible   */
     MPQP_ELAYOUT = -4,     /* LP matrices do not have the reference layout */
     MPQP_ECUDA = -5,       /* CUDA runtime error                           */
@@ -106,7 +106,12 @@ enum {
 enum { MPQP_FP64 = 0, MPQP_MIXED = 1 };
 
 /* One mpQP instance: min 1/2 x'Qx + (c + H theta)'x  s.t.  A x <= b + F theta,
- * At theta <= bt.  Row-major host arrays. */
+ * At theta <= bt.  Row-major host arrays.  Q positive definite, or Q = 0
+ * exactly: a multiparametric LP (the reference's README.md:5 names mpLP;
+ * its LP2 of main.py:102-108 keeps x, so Q = 0 needs no Q^-1).  For an
+ * mpLP the KKT factor is that of A_S A_S^T, a set with |S| < n keeps a
+ * null-space direction and the stationarity residual in its LP2 and is
+ * never a region (x(theta) is not unique); limits: m + ncp + 3n + p <= 252. */
 typedef struct {
     int n, m, p, ncp;
     int k_min, k_max;        /* cardinalities to check (k_max <= min(n, m))  */
@@ -206,7 +211,9 @@ int mpqp_release_cached_memory(void);
 /* Region laws of optimal sets, computed in FP64 on the device:
  *   lagrange_A (k x p), lagrange_b (k), parameter_A (n x p), parameter_b (n),
  *   CR rows (n_cr x (p+1)): [CR_As | CR_bs] normalised, reference order.
- * Sizes per set are written to `sizes` (4 ints: k, n, p, n_cr); `laws` must
+ * Sizes per set are written to `sizes` (4 ints: k, n, p, n_cr; k = -1 when
+ * the set fails the LICQ test, k = -2 for an mpLP set with |S| < n, whose
+ * law is not unique -- nothing else is written for those); `laws` must
  * hold n_sets * (mmax*(p+1) + n*(p+1) + (m+ncp)*(p+1)) doubles (see
  * mpqp_region_laws_stride). */
 long long mpqp_region_laws_stride(const mpqp_problem *prob);

@@ -33,12 +33,12 @@ cudaError_t launch_feasibility(const DevBuffers &B, const Tol &tol, const SlotDi
                                int grid, size_t smem, cudaStream_t s);
 cudaError_t launch_lp1_fp64(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int grid,
                             size_t smem, cudaStream_t s);
-cudaError_t launch_optimality(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int prec,
+cudaError_t launch_optimality(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, bool lp,
                               int grid, size_t smem, cudaStream_t s);
 cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode, int route,
                               int grid, size_t smem, cudaStream_t s);
-cudaError_t launch_optimality_fp64(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int grid,
-                                   size_t smem, cudaStream_t s);
+cudaError_t launch_optimality_fp64(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, bool lp,
+                                   int grid, size_t smem, cudaStream_t s);
 cudaError_t launch_level0(const DevBuffers &B, int prec, cudaStream_t s);
 cudaError_t launch_reset(const DevBuffers &B, cudaStream_t s);
 cudaError_t launch_finalize(const DevBuffers &B, int level, cudaStream_t s);
@@ -73,6 +73,7 @@ void set_error_text(const char *msg) { set_err(msg ? msg : ""); }
 struct Prepared {
     InstDesc d;
     std::vector<double> Wm, Wh, wc, At, bt, QiAT, QiH, Qic;
+    std::vector<double> WhL, wcL, Hm, cv;   // mpLP only: A H, A c, H, c
     std::vector<double> blo, bhi;   // parameter box, when At is [diag(+); diag(-)]
     std::vector<double> root;    // LP1 root tableau, FP64 stride ld1d
     std::vector<double> root_f;  // the same values at the plan's stride ld1 (FP32 copy)
@@ -137,19 +138,57 @@ static int prepare_instance(const mpqp_problem &P, Prepared &out, int prec)
     d.tab_elems = ((d.M1 + 1) * d.ld1 + 3) & ~3;
     d.ids_bytes = (d.M1 + d.nv + 15) & ~15;
     d.budget = P.budget;
+    d.lp = 1;
+    for (int i = 0; i < n * n && d.lp; i++) if (P.Q[i] != 0.0) d.lp = 0;
+    d.ld2lp = odd_up(p + n + 3);
+    if (d.lp) {
+        // mpLP (Q = 0): Wm = A A^T, Wh = F, wc = b, QiAT = A^T, QiH = Qic = 0,
+        // WhL = A H, wcL = A c (each sum over ascending i from 0, the oracle's order)
+        if ((p + n + 2) + (m + ncp + 2 * n + 1) > kMaxIds) {
+            set_err("mpLP instance too large for 8-bit basis ids (m + ncp + 3n + p must be <= 252)");
+            return MPQP_EINVAL;
+        }
+        out.Wm.assign((size_t)m * m, 0.0);
+        out.Wh.assign(P.F, P.F + (size_t)m * p);
+        out.wc.assign(P.b, P.b + m);
+        out.WhL.assign((size_t)m * p, 0.0);
+        out.wcL.assign(m, 0.0);
+        out.QiAT.assign((size_t)n * m, 0.0);
+        out.QiH.assign((size_t)n * p, 0.0);
+        out.Qic.assign(n, 0.0);
+        out.Hm.assign(P.H, P.H + (size_t)n * p);
+        out.cv.assign(P.c, P.c + n);
+        for (int r = 0; r < m; r++) {
+            for (int s = 0; s < m; s++) {
+                double acc = 0.0;
+                for (int i = 0; i < n; i++) acc = std::fma(P.A[(size_t)r * n + i], P.A[(size_t)s * n + i], acc);
+                out.Wm[(size_t)r * m + s] = acc;
+            }
+            for (int c = 0; c < p; c++) {
+                double acc = 0.0;
+                for (int i = 0; i < n; i++) acc = std::fma(P.A[(size_t)r * n + i], P.H[(size_t)i * p + c], acc);
+                out.WhL[(size_t)r * p + c] = acc;
+            }
+            double acc = 0.0;
+            for (int i = 0; i < n; i++) acc = std::fma(P.A[(size_t)r * n + i], P.c[i], acc);
+            out.wcL[r] = acc;
+            for (int i = 0; i < n; i++) out.QiAT[(size_t)i * m + r] = P.A[(size_t)r * n + i];
+        }
+    }
     std::vector<double> L((size_t)n * n, 0.0), V((size_t)n * m, 0.0), U((size_t)n * p, 0.0), u(n, 0.0);
-    for (int j = 0; j < n; j++) {
+    for (int j = 0; j < n && !d.lp; j++) {
         for (int i = j; i < n; i++) {
             double acc = P.Q[i * n + j];
             for (int l = 0; l < j; l++) acc = std::fma(-L[i * n + l], L[j * n + l], acc);
             if (i == j) {
-                if (!(acc > 0.0)) { set_err("Q is not positive definite"); return MPQP_ENOTSPD; }
+                if (!(acc > 0.0)) { set_err("Q is neither positive definite nor zero"); return MPQP_ENOTSPD; }
                 L[j * n + j] = std::sqrt(acc);
             } else {
                 L[i * n + j] = acc / L[j * n + j];
             }
         }
     }
+    if (!d.lp) {
     for (int r = 0; r < m; r++) fwd_sub(L.data(), n, P.A + (size_t)r * n, 1, V.data() + r, m);
     for (int c = 0; c < p; c++) fwd_sub(L.data(), n, P.H + c, p, U.data() + c, p);
     fwd_sub(L.data(), n, P.c, 1, u.data(), 1);
@@ -177,6 +216,7 @@ static int prepare_instance(const mpqp_problem &P, Prepared &out, int prec)
     for (int r = 0; r < m; r++) bwd_sub(L.data(), n, V.data() + r, m, out.QiAT.data() + r, m);
     for (int c = 0; c < p; c++) bwd_sub(L.data(), n, U.data() + c, p, out.QiH.data() + c, p);
     bwd_sub(L.data(), n, u.data(), 1, out.Qic.data(), 1);
+    }
     out.At.assign(P.At, P.At + (size_t)ncp * p);
     out.bt.assign(P.bt, P.bt + ncp);
     auto fill_root = [&](std::vector<double> &root, int ld) {
@@ -227,6 +267,8 @@ struct mpqp_plan {
     int prec = PREC_FP64;
     int lp2_screen = 0;         // mixed precision: 0 dual bound on box instances, 1 primal tableau screen
     bool screen_dual = false, screen_primal = false;   // which FP32 screen routes the instances need
+    bool has_qp = false, has_lp = false;   // mpQP / mpLP (Q = 0) instances in the batch
+    int grid_opt_lp = 0, grid_optfb_lp = 0;   // FP64 optimality kernels of the mpLP instances
     bool pooled = false;        // allocations came from the device pool
     int grid_opt2 = 0;          // grid of the primal route (grid_opt: the dual route)
     size_t smem_opt2 = 0;       // shared memory per block of the primal route
@@ -416,7 +458,11 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
     // when some instance takes it; FP64: the optimality kernel
     auto launch_opt = [&](int level) -> int {
         if (!mixed) {
-            L("k_optimality<double>", launch_optimality(B, P->tol, P->sd, level, P->prec, P->grid_opt, P->smem_opt, s));
+            if (P->has_qp)
+                L("k_optimality<double>", launch_optimality(B, P->tol, P->sd, level, false, P->grid_opt, P->smem_opt, s));
+            if (P->has_lp)
+                L("k_optimality<double,mplp>",
+                  launch_optimality(B, P->tol, P->sd, level, true, P->grid_opt_lp, P->smem_opt, s));
             return MPQP_OK;
         }
         if (P->screen_dual)
@@ -425,17 +471,28 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
             L("k_opt_screen<primal>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 1, P->grid_opt2, P->smem_opt2, s));
         return MPQP_OK;
     };
+    // FP64 re-evaluation of the sets the FP32 screen left undecided
+    auto launch_optfb = [&](int level) -> int {
+        if (!mixed) return MPQP_OK;
+        if (P->has_qp)
+            L("k_optimality_fp64",
+              launch_optimality_fp64(B, P->tol, P->sd, level, false, P->grid_optfb, P->smem_optfb, s));
+        if (P->has_lp)
+            L("k_optimality_fp64<mplp>",
+              launch_optimality_fp64(B, P->tol, P->sd, level, true, P->grid_optfb_lp, P->smem_optfb, s));
+        return MPQP_OK;
+    };
     L("k_reset", launch_reset(B, s));
     L("k_level0", launch_level0(B, P->prec, s));
     { const int _o = launch_opt(0); if (_o) return _o; }
-    if (mixed) L("k_optimality_fp64", launch_optimality_fp64(B, P->tol, P->sd, 0, P->grid_optfb, P->smem_optfb, s));
+    { const int _o = launch_optfb(0); if (_o) return _o; }
     L("k_finalize", launch_finalize(B, 0, s));
     for (int k = 1; k <= P->kmax; k++) {
         L("k_enumerate", launch_enumerate(B, k, P->grid_enum, s));
         L(feas, launch_feasibility(B, P->tol, P->sd, k, P->prec, P->grid_feas, P->smem_feas, s));
         if (mixed) L("k_lp1_fp64", launch_lp1_fp64(B, P->tol, P->sd, k, P->grid_lp1fb, P->smem_lp1fb, s));
         { const int _o = launch_opt(k); if (_o) return _o; }
-        if (mixed) L("k_optimality_fp64", launch_optimality_fp64(B, P->tol, P->sd, k, P->grid_optfb, P->smem_optfb, s));
+        { const int _o = launch_optfb(k); if (_o) return _o; }
         L("k_finalize", launch_finalize(B, k, s));
     }
 #undef L
@@ -493,7 +550,8 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
         return off;
     };
     SlotDims &sd = P->sd;
-    sd = SlotDims{0, 0, 0, 1, 0, 0, 0, 0, 0};
+    sd = SlotDims{};
+    sd.maxK = 1;
     long long tab_tot0 = 0, ids_tot0 = 0;
     size_t max_tab_bytes = 0;
     for (int i = 0; i < n_inst; i++) {
@@ -502,6 +560,7 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
         d.o_Wm = put(dp, pr.Wm); d.o_Wh = put(dp, pr.Wh); d.o_wc = put(dp, pr.wc);
         d.o_At = put(dp, pr.At); d.o_bt = put(dp, pr.bt); d.o_QiAT = put(dp, pr.QiAT);
         d.o_QiH = put(dp, pr.QiH); d.o_Qic = put(dp, pr.Qic); d.o_root = put(dp, pr.root);
+        d.o_WhL = put(dp, pr.WhL); d.o_wcL = put(dp, pr.wcL); d.o_Hm = put(dp, pr.Hm); d.o_cv = put(dp, pr.cv);
         d.f_Wm = put(fp, pr.Wm); d.f_Wh = put(fp, pr.Wh); d.f_wc = put(fp, pr.wc);
         d.f_At = put(fp, pr.At); d.f_bt = put(fp, pr.bt); d.f_root = put(fp, pr.root_f);
         d.f_blo = put(fp, pr.blo); d.f_bhi = put(fp, pr.bhi);
@@ -515,7 +574,9 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
         sd.maxR2 = std::max(sd.maxR2, d.m + d.ncp);
         sd.maxLD2 = std::max(sd.maxLD2, d.ld2);
         sd.maxLD1d = std::max(sd.maxLD1d, d.ld1d);
-        sd.maxLD2d = std::max(sd.maxLD2d, d.ld2d);
+        sd.maxLD2d = std::max(sd.maxLD2d, d.lp ? std::max(d.ld2d, d.ld2lp) : d.ld2d);
+        sd.maxR2d = std::max(sd.maxR2d, d.lp ? d.m + d.ncp + 2 * d.n + 1 : d.m + d.ncp);
+        if (d.lp) sd.maxN = std::max(sd.maxN, d.n);
         tab_tot0 += d.tab_elems;
         ids_tot0 += d.ids_bytes;
         max_tab_bytes = std::max(max_tab_bytes, (size_t)d.tab_elems * (P->prec == PREC_MIXED ? 4 : 8));
@@ -637,11 +698,12 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
     // mixed precision: the grouped FP32 screen, one warp per block
     P->smem_opt = P->prec == PREC_MIXED ? screen_smem_per_warp(sd, 0) : 4 * opt_smem_per_warp(8, sd);
     P->smem_opt2 = screen_smem_per_warp(sd, 1);
-    if (P->prec == PREC_MIXED)
-        for (const InstDesc &d : P->desc) {
-            if (screen_dual_route(P->lp2_screen, d, sd)) P->screen_dual = true;
-            else P->screen_primal = true;
-        }
+    for (const InstDesc &d : P->desc) {
+        if (d.lp) P->has_lp = true; else P->has_qp = true;
+        if (P->prec != PREC_MIXED) continue;
+        if (screen_dual_route(P->lp2_screen, d, sd)) P->screen_dual = true;
+        else P->screen_primal = true;
+    }
     P->smem_optfb = 4 * opt_smem_per_warp(8, sd);
     if ((rc = grid_for(kernel_ptr("enumerate"), 0, &P->grid_enum)) ||
         (rc = grid_for(kernel_ptr(P->prec == PREC_MIXED ? "feas32" : "feas64"), P->smem_feas, &P->grid_feas)) ||
@@ -650,7 +712,9 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
                   ? grid_for(kernel_ptr("screen_dual"), P->smem_opt, &P->grid_opt, 32)
                   : grid_for(kernel_ptr("opt64"), P->smem_opt, &P->grid_opt)) ||
         (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_primal"), P->smem_opt2, &P->grid_opt2, 32) : 0) ||
-        (rc = grid_for(kernel_ptr("opt_fp64"), P->smem_optfb, &P->grid_optfb))) {
+        (rc = grid_for(kernel_ptr("opt_fp64"), P->smem_optfb, &P->grid_optfb)) ||
+        (rc = P->has_lp && P->prec != PREC_MIXED ? grid_for(kernel_ptr("opt64_lp"), P->smem_opt, &P->grid_opt_lp) : 0) ||
+        (rc = P->has_lp ? grid_for(kernel_ptr("opt_fp64_lp"), P->smem_optfb, &P->grid_optfb_lp) : 0)) {
         free_plan_mem(P);
         delete P;
         return rc;
@@ -956,9 +1020,24 @@ static int unpack_lp(const double *AxT, int n_c, int n_x, int n_t, const double 
     const int r0 = n_c + 1 + n_cp;
     for (int i = 0; i < n_x; i++) {
         const int r = r0 + i;
+        // rows with -c_i < 0 were negated (main.py:112-114); the multiplier
+        // block of the row is s * A[:, i] (main.py:106), which fixes s; Q_ii
+        // (positive for an mpQP, zero for an mpLP) only when that column is 0
+        const double *lam = A2 + r + (size_t)(n_x + n_t) * M2;
+        int jm = -1;
+        double am = 0.0;
+        for (int j = 0; j < n_c; j++)
+            if (std::fabs(A[(size_t)j * n_x + i]) > am) { am = std::fabs(A[(size_t)j * n_x + i]); jm = j; }
         const double diag = A2[r + (size_t)i * M2];
-        if (diag == 0.0) { set_err("LP2 stationarity row has a zero diagonal"); return MPQP_ELAYOUT; }
-        const double s = diag > 0 ? 1.0 : -1.0;   // rows with -c_i < 0 were negated (main.py:112-114)
+        double s;
+        if (jm >= 0) s = (lam[(size_t)jm * M2] > 0.0) == (A[(size_t)jm * n_x + i] > 0.0) ? 1.0 : -1.0;
+        else if (diag != 0.0) s = diag > 0.0 ? 1.0 : -1.0;
+        else { set_err("LP2 stationarity row: neither A nor Q fixes its sign"); return MPQP_ELAYOUT; }
+        for (int j = 0; j < n_c; j++)
+            if (lam[(size_t)j * M2] != s * A[(size_t)j * n_x + i]) {
+                set_err("LP2 stationarity row does not hold A^T (main.py:106)");
+                return MPQP_ELAYOUT;
+            }
         for (int j = 0; j < n_x; j++) Q[i * n_x + j] = s * A2[r + (size_t)j * M2];
         for (int j = 0; j < n_t; j++) H[i * n_t + j] = s * A2[r + (size_t)(n_x + j) * M2];
         c[i] = -s * xb2[r];

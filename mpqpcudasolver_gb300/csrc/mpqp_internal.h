@@ -24,7 +24,10 @@ constexpr int kMaxIds = 255;      // ids are uint8
 constexpr int kMaxK = 32;         // largest active-set cardinality supported
 constexpr int kMaxP = 30;         // parameters
 
-enum LpStatus : int { LP_OPTIMAL = 0, LP_UNBOUNDED = 1, LP_ITER_LIMIT = 2, LP_SKIPPED = 3, LP_LICQ_FAIL = 4 };
+// LP_INFEASIBLE: an mpLP set with |S| < n whose stationarity residual cannot
+// vanish inside the parameter set (its LP2 has no feasible point)
+enum LpStatus : int { LP_OPTIMAL = 0, LP_UNBOUNDED = 1, LP_ITER_LIMIT = 2, LP_SKIPPED = 3, LP_LICQ_FAIL = 4,
+                      LP_INFEASIBLE = 5 };
 
 enum Precision : int { PREC_FP64 = 0, PREC_MIXED = 1 };
 
@@ -60,13 +63,18 @@ struct InstDesc {
     int tab_elems;              // (M1+1)*ld1 rounded up to a multiple of 4
     int ids_bytes;              // M1 + nv rounded up to 16
     long long budget;           // max candidates checked for this instance (0 = no limit)
-    // offsets (elements) into the FP64 pool
+    // offsets (elements) into the FP64 pool.  mpLP (Q = 0): Wm = A A^T,
+    // Wh = F, wc = b, QiAT = A^T, QiH = Qic = 0, and WhL = A H, wcL = A c,
+    // Hm = H, cv = c (the multiplier law and the stationarity residual)
     long long o_Wm, o_Wh, o_wc, o_At, o_bt, o_QiAT, o_QiH, o_Qic, o_root;
+    long long o_WhL, o_wcL, o_Hm, o_cv;
     // offsets (elements) into the FP32 pool
     long long f_Wm, f_Wh, f_wc, f_At, f_bt, f_root;
     long long f_blo, f_bhi;     // parameter box lo <= theta <= hi (FP32), valid when box
     int box;                    // 1: At = [diag(+); diag(-)] (rows c, then p + c), a box
-    int pad_box;
+    int lp;                     // 1: Q = 0 (mpLP)
+    int ld2lp;                  // mpLP, |S| < n: FP64 LP2 row stride (>= p + n + 3, odd)
+    int pad_lp;
 };
 
 struct Node {                   // a feasible (or, when exhaustive, any) active set
@@ -150,6 +158,8 @@ struct SlotDims {
     int maxM1, maxLD1, maxNv;       // LP1 tableau
     int maxK, maxP1, maxR2, maxLD2; // KKT factor and LP2 / Chebyshev tableau
     int maxLD1d, maxLD2d;           // strides of the FP64 re-solve tableaus
+    int maxR2d;                     // rows of the FP64 LP2 tableau (mpLP, |S| < n: m + ncp + 2n + 1)
+    int maxN;                       // mpLP instances: largest n (0: none), sizes Psi and Phi
 };
 
 struct DevBuffers {

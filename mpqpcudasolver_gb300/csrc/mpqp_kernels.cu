@@ -434,13 +434,20 @@ __host__ __device__ inline size_t lp1_slot_bytes(int maxM1, int maxLD1, int maxN
 }
 
 // optimality slot: R (kmax^2), Y and Lambda (kmax x P1), G (R2 x P1),
-// tableau (R2+1) x ld2, ids (R2 + P1), S list
+// tableau (rows+1) x ld2, ids (rows + P1, + n + 1 with mpLP instances), S
+// list; FP64 with mpLP instances also Psi (kmax x P1) and Phi (kmax x n).
+// rows = R2 (FP32) or maxR2d (FP64).
 template <typename T>
-__host__ __device__ inline size_t opt_slot_bytes(int maxK, int maxP1, int maxR2, int maxLD2)
+__host__ __device__ inline size_t opt_slot_bytes(const SlotDims &sd)
 {
-    return align16((size_t)maxK * maxK * sizeof(T)) + 2 * align16((size_t)maxK * maxP1 * sizeof(T)) +
-           align16((size_t)maxR2 * maxP1 * sizeof(T)) + align16((size_t)(maxR2 + 1) * maxLD2 * sizeof(T)) +
-           align16((size_t)maxR2 + maxP1) + align16((size_t)maxK * sizeof(int));
+    const bool d = sizeof(T) == 8;
+    const int rows = d ? sd.maxR2d : sd.maxR2, ld = d ? sd.maxLD2d : sd.maxLD2;
+    size_t b = align16((size_t)sd.maxK * sd.maxK * sizeof(T)) + 2 * align16((size_t)sd.maxK * sd.maxP1 * sizeof(T)) +
+               align16((size_t)sd.maxR2 * sd.maxP1 * sizeof(T)) + align16((size_t)(rows + 1) * ld * sizeof(T)) +
+               align16((size_t)rows + sd.maxP1 + (sd.maxN ? sd.maxN + 1 : 0)) + align16((size_t)sd.maxK * sizeof(int));
+    if (d && sd.maxN)
+        b += align16((size_t)sd.maxK * sd.maxP1 * sizeof(T)) + align16((size_t)sd.maxK * sd.maxN * sizeof(T));
+    return b;
 }
 
 // ---------------------------------------------------------------------
@@ -902,19 +909,63 @@ struct OptWs {
     T *R, *Y, *Lam, *G, *Tb;
     uint8_t *ids;
     int *S;
-    __device__ OptWs() {}
+    T *Psi, *Phi;   // mpLP (FP64 slots of batches with mpLP instances), else null
+    __device__ OptWs() : Psi(nullptr), Phi(nullptr) {}
     __device__ OptWs(unsigned char *base, const SlotDims &sd)
     {
+        const bool d = sizeof(T) == 8;
+        const int rows = d ? sd.maxR2d : sd.maxR2;
         size_t o = 0;
         R = (T *)(base + o); o += align16((size_t)sd.maxK * sd.maxK * sizeof(T));
         Y = (T *)(base + o); o += align16((size_t)sd.maxK * sd.maxP1 * sizeof(T));
         Lam = (T *)(base + o); o += align16((size_t)sd.maxK * sd.maxP1 * sizeof(T));
         G = (T *)(base + o); o += align16((size_t)sd.maxR2 * sd.maxP1 * sizeof(T));
-        Tb = (T *)(base + o); o += align16((size_t)(sd.maxR2 + 1) * (sizeof(T) == 4 ? sd.maxLD2 : sd.maxLD2d) * sizeof(T));
-        ids = base + o; o += align16((size_t)sd.maxR2 + sd.maxP1);
-        S = (int *)(base + o);
+        Tb = (T *)(base + o); o += align16((size_t)(rows + 1) * (d ? sd.maxLD2d : sd.maxLD2) * sizeof(T));
+        ids = base + o; o += align16((size_t)rows + sd.maxP1 + (sd.maxN ? sd.maxN + 1 : 0));
+        S = (int *)(base + o); o += align16((size_t)sd.maxK * sizeof(int));
+        Psi = Phi = nullptr;
+        if (d && sd.maxN) {
+            Psi = (T *)(base + o); o += align16((size_t)sd.maxK * sd.maxP1 * sizeof(T));
+            Phi = (T *)(base + o);
+        }
     }
 };
+
+// X = Wm[S,S]^-1 X in place, R the upper Cholesky factor of kkt_factor
+// (k x k); X (k rows, stride ldx) holds the right-hand sides on entry.  Lane
+// per column: a forward then a backward substitution, each accumulating in
+// ascending l (the oracle's chol_solve_inplace).
+template <typename T>
+__device__ void chol_solve_inplace(const T *R, int k, T *X, int ldx, int ncols)
+{
+    for (int cc = lane_id(); cc < ncols; cc += 32) {
+        for (int a = 0; a < k; a++) {
+            T acc = X[a * ldx + cc];
+            for (int l = 0; l < a; l++) acc = xfma(-R[l * k + a], X[l * ldx + cc], acc);
+            X[a * ldx + cc] = xdiv(acc, R[a * k + a]);
+        }
+        for (int a = k - 1; a >= 0; a--) {
+            T acc = X[a * ldx + cc];
+            for (int l = a + 1; l < k; l++) acc = xfma(-R[a * k + l], X[l * ldx + cc], acc);
+            X[a * ldx + cc] = xdiv(acc, R[a * k + a]);
+        }
+    }
+    __syncwarp();
+}
+
+// mpLP: the multiplier law Psi = Wm[S,S]^-1 [WhL_S | wcL_S] (lambda(theta) =
+// -(Psi theta + Psi_p)); Lambda of kkt_factor is then Gamma = Wm[S,S]^-1
+// [F_S | b_S], the primal law x(theta) = A_S^T Gamma(theta).
+__device__ void mplp_multipliers(const DevBuffers &B, const InstDesc &I, int k, OptWs<double> &ws)
+{
+    const int p = I.p, P1 = p + 1;
+    for (int idx = lane_id(); idx < k * P1; idx += 32) {
+        const int a = idx / P1, cc = idx - a * P1;
+        ws.Psi[idx] = cc < p ? B.dpool[I.o_WhL + (size_t)ws.S[a] * p + cc] : B.dpool[I.o_wcL + ws.S[a]];
+    }
+    __syncwarp();
+    chol_solve_inplace<double>(ws.R, k, ws.Psi, P1, P1);
+}
 
 // Cholesky of Wm[S,S] (row-oriented; each entry accumulates in ascending l),
 // then Y = R^-T [Wh_S | wc_S] and Lambda = R^-1 Y (lane per column).
@@ -982,7 +1033,7 @@ __device__ int kkt_factor(const KktData<T> &D, const InstDesc &I, uint64_t lo, u
 // rows go to out with row stride ldo and h in column hcol.  t0_out / g0_out
 // (optional, warp-uniform results): min h over the constraint rows and
 // max(1, max |g|) over all rows, the start value and growth reference of LP2.
-template <typename T, bool track = false>
+template <typename T, bool track = false, bool LP = false>
 __device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, uint64_t hi, int k, OptWs<T> &ws,
                          T *out = nullptr, int ldo = 0, int hcol = 0, T *t0_out = nullptr, T *g0_out = nullptr)
 {
@@ -990,6 +1041,10 @@ __device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, ui
     const int m = I.m, p = I.p, ncp = I.ncp, P1 = p + 1;
     const int *S = ws.S;
     const T *Lam = ws.Lam;
+    // lambda rows: Lambda (mpQP) or Psi (LP: an mpLP instance; never with
+    // track, which the FP32 screen uses and which sums |Lambda| of these rows)
+    static_assert(!(LP && track), "the FP32 screen does not take mpLP instances");
+    const T *LamL = LP ? ws.Psi : Lam;
     T *G = out ? out : ws.G;
     const int ldg = out ? ldo : P1, hc = out ? hcol : p;
     T amax = T(0);
@@ -999,15 +1054,15 @@ __device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, ui
     for (int a = lane; a < k; a += 32) {
         T rs = T(0);
         for (int cc = 0; cc < p; cc++) {
-            const T v = Lam[a * P1 + cc];
+            const T v = LamL[a * P1 + cc];
             G[a * ldg + cc] = v;
             if (track) rs += xabs(v);
             if (want_t0 && xabs(v) > gmax) gmax = xabs(v);
         }
-        const T h = -Lam[a * P1 + p];
+        const T h = -LamL[a * P1 + p];
         G[a * ldg + hc] = h;
         if (want_t0 && h < tmin) tmin = h;
-        if (track) { rs += xabs(Lam[a * P1 + p]); labs[a] = rs; if (rs > amax) amax = rs; }
+        if (track) { rs += xabs(LamL[a * P1 + p]); labs[a] = rs; if (rs > amax) amax = rs; }
     }
     if (track) __syncwarp();
     // inactive rows: g_c = -Wh_ic + sum_l Wm_i,S_l Lambda_lc (c < p) and
@@ -1076,9 +1131,164 @@ __device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, ui
     return amax;
 }
 
+// mpLP (Q = 0) with |S| = k < n: x is not fixed by S, so LP2 keeps a
+// direction u in the null space of A_S (x = A_S^T Gamma(theta) + P u, P the
+// projector onto that null space) and the stationarity residual
+// (c + H theta) - A_S^T Psi(theta) = r0 + E theta as rows
+// |r0 + E theta| <= tol_feas, as the reference's LP2 keeps x and the
+// stationarity equalities (main.py:107-108).  Two phases: min sigma over
+// rows +-(r0 + E theta) - sigma <= tol_feas (sigma free); when sigma* <= 0
+// the row -sigma >= 0 is appended and max t solved from that basis.
+// Columns theta (p), u (n), t, sigma; rows: the m margin rows (G, reference
+// order, with A_i P in the u columns of the inactive rows), the ncp
+// parameter rows, 2n residual rows.  The set is never a region.  Same
+// operations as the oracle's lp2_short_mplp.
+__device__ void lp2_short_mplp(const DevBuffers &B, const Tol &tol, const InstDesc &I, uint64_t lo, uint64_t hi,
+                               int k, OptWs<double> &ws, OptResult &res)
+{
+    const int lane = lane_id();
+    const int m = I.m, n = I.n, p = I.p, ncp = I.ncp, P1 = p + 1, ld = I.ld2lp;
+    const int ncols = p + n + 2, ct = p + n, cs = p + n + 1;
+    const int nrows = m + ncp + 2 * n;
+    // Phi = Wm[S,S]^-1 A_S (x = A_S^T Gamma + P u, P = I - A_S^T Phi)
+    for (int idx = lane; idx < k * n; idx += 32) {
+        const int a = idx / n, j = idx - a * n;
+        ws.Phi[idx] = B.dpool[I.o_QiAT + (size_t)j * m + ws.S[a]];
+    }
+    __syncwarp();
+    chol_solve_inplace<double>(ws.R, k, ws.Phi, n, n);
+    const double *G = ws.G, *Phi = ws.Phi, *Psi = ws.Psi;
+    const double *At = B.dpool + I.o_QiAT, *Wm = B.dpool + I.o_Wm;
+    const double *Hm = B.dpool + I.o_Hm, *cv = B.dpool + I.o_cv;
+    const double *Ab = B.dpool + I.o_At, *bb = B.dpool + I.o_bt;
+    const int *S = ws.S;
+    double *T = ws.Tb;
+    uint8_t *bid = ws.ids, *nid = ws.ids + nrows + 1;
+    double t0 = pos_inf<double>();
+    for (int r = lane; r < m; r += 32) { const double h = G[r * P1 + p]; if (h < t0) t0 = h; }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) { const double o = __shfl_xor_sync(FULLMASK, t0, off); if (o < t0) t0 = o; }
+    for (int idx = lane; idx < (nrows + 2) * ld; idx += 32) T[idx] = 0.0;
+    __syncwarp();
+    for (int r = lane; r < m; r += 32) {
+        double *Tr = T + (size_t)r * ld;
+        for (int cc = 0; cc < p; cc++) Tr[cc] = G[r * P1 + cc];
+        Tr[ct] = 1.0;
+        double beta = xfma(-1.0, t0, G[r * P1 + p]);
+        if (!(beta > 0.0)) beta = 0.0;
+        Tr[ncols] = beta;
+    }
+    for (int i = lane; i < m; i += 32) {
+        if (mask_has(lo, hi, i)) continue;
+        double *Tr = T + (size_t)(k + i - mask_rank(lo, hi, i)) * ld;
+        for (int j = 0; j < n; j++) {
+            double acc = At[(size_t)j * m + i];
+            for (int l = 0; l < k; l++) acc = xfma(-Wm[(size_t)i * m + S[l]], Phi[l * n + j], acc);
+            Tr[p + j] = acc;
+        }
+    }
+    for (int ii = lane; ii < ncp; ii += 32) {
+        double *Tr = T + (size_t)(m + ii) * ld;
+        for (int cc = 0; cc < p; cc++) Tr[cc] = Ab[ii * p + cc];
+        Tr[ncols] = bb[ii];
+    }
+    const double eps = tol.tol_feas;
+    double rmax = 0.0;
+    for (int i = lane; i < n; i += 32) {
+        double *Tp = T + (size_t)(m + ncp + 2 * i) * ld, *Tn = Tp + ld;
+        for (int cc = 0; cc < p; cc++) {
+            double acc = Hm[i * p + cc];
+            for (int l = 0; l < k; l++) acc = xfma(-At[(size_t)i * m + S[l]], Psi[l * P1 + cc], acc);
+            Tp[cc] = acc;
+            Tn[cc] = -acc;
+        }
+        double acc = cv[i];
+        for (int l = 0; l < k; l++) acc = xfma(-At[(size_t)i * m + S[l]], Psi[l * P1 + p], acc);
+        Tp[cs] = -1.0;
+        Tn[cs] = -1.0;
+        Tp[ncols] = xadd(eps, -acc);
+        Tn[ncols] = xadd(eps, acc);
+        if (fabs(acc) > rmax) rmax = fabs(acc);
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) { const double o = __shfl_xor_sync(FULLMASK, rmax, off); if (o > rmax) rmax = o; }
+    const double s0 = xadd(rmax, -eps);
+    __syncwarp();
+    for (int r = m + ncp + lane; r < nrows; r += 32) {
+        double beta = xadd(T[(size_t)r * ld + ncols], s0);
+        if (!(beta > 0.0)) beta = 0.0;
+        T[(size_t)r * ld + ncols] = beta;
+    }
+    for (int r = lane; r < nrows; r += 32) bid[r] = (uint8_t)(ncols + r);
+    for (int cc = lane; cc < ncols; cc += 32) nid[cc] = (uint8_t)cc;
+    double *obj = T + (size_t)nrows * ld;
+    if (lane == 0) { obj[cs] = -1.0; obj[ncols] = s0; }
+    __syncwarp();
+    const double tpiv = tol.tol_piv, tdj = tol.tol_dj;
+    int piv1 = 0, piv2 = 0;
+    int st;
+    {
+        Lp<double> L{T, ld, nrows, ncols, ncols, bid, nid};
+        st = warp_simplex<double>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv1);
+    }
+    res.lp2_piv = piv1;
+    if (st != LP_OPTIMAL) { res.lp2_status = st; return; }
+    const double sig = obj[ncols];
+    if (sig > 0.0) { res.lp2_status = LP_INFEASIBLE; res.t = -pos_inf<double>(); return; }
+    // row nrows: s = -sigma >= 0 in the current basis (sigma basic in row rs,
+    // or nonbasic in column qs); row nrows + 1: the objective -t
+    int rs = -1, rt = -1, qs = -1, qt = -1;
+    for (int r0 = 0; r0 < nrows; r0 += 32) {
+        const int r = r0 + lane;
+        const unsigned bs = __ballot_sync(FULLMASK, r < nrows && bid[r] == cs);
+        const unsigned bt = __ballot_sync(FULLMASK, r < nrows && bid[r] == ct);
+        if (bs && rs < 0) rs = r0 + __ffs(bs) - 1;
+        if (bt && rt < 0) rt = r0 + __ffs(bt) - 1;
+    }
+    for (int c0 = 0; c0 < ncols; c0 += 32) {
+        const int cc = c0 + lane;
+        const unsigned bs = __ballot_sync(FULLMASK, cc < ncols && nid[cc] == cs);
+        const unsigned bt = __ballot_sync(FULLMASK, cc < ncols && nid[cc] == ct);
+        if (bs && qs < 0) qs = c0 + __ffs(bs) - 1;
+        if (bt && qt < 0) qt = c0 + __ffs(bt) - 1;
+    }
+    double *Ts = T + (size_t)nrows * ld, *ob = Ts + ld;
+    for (int cc = lane; cc <= ncols; cc += 32) {
+        double vs, vo;
+        if (rs >= 0) {
+            const double v = T[(size_t)rs * ld + cc];
+            vs = cc < ncols ? -v : xadd(-s0, -v);
+        } else {
+            vs = cc == qs ? 1.0 : (cc == ncols ? -s0 : 0.0);
+        }
+        if (rt >= 0) {
+            const double v = T[(size_t)rt * ld + cc];
+            vo = cc < ncols ? -v : xadd(-t0, -v);
+        } else {
+            vo = cc == qt ? 1.0 : (cc == ncols ? -t0 : 0.0);
+        }
+        Ts[cc] = vs;
+        ob[cc] = vo;
+    }
+    if (lane == 0) bid[nrows] = (uint8_t)(ncols + nrows);
+    __syncwarp();
+    {
+        Lp<double> L{T, ld, nrows + 1, ncols, ncols, bid, nid};
+        st = warp_simplex<double>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv2);
+    }
+    res.lp2_piv = piv1 + piv2;
+    res.lp2_status = st;
+    if (st == LP_OPTIMAL) {
+        res.t = -ob[ncols];
+        res.optimal = res.t > tol.tol_opt;
+    } else if (st == LP_UNBOUNDED) {
+        res.t = pos_inf<double>();
+    }
+}
+
 // Optimality and region verdict of one feasible set (the FP64 path; the FP32
-// screen of the mixed path is k_opt_screen).
-template <typename T>
+// screen of the mixed path is k_opt_screen).  LP: the instance is an mpLP.
+template <typename T, bool LP = false>
 __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const InstDesc &I, uint64_t lo, uint64_t hi,
                                      OptWs<T> &ws)
 {
@@ -1098,7 +1308,18 @@ __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const 
         res.licq = 0; res.lp2_status = LP_LICQ_FAIL;
         return res;
     }
-    region_rows<T>(D, I, lo, hi, k, ws);
+    if constexpr (LP) {
+        static_assert(sizeof(T) == 8, "mpLP instances are evaluated in FP64");
+        mplp_multipliers(B, I, k, ws);
+    }
+    region_rows<T, false, LP>(D, I, lo, hi, k, ws);
+    if constexpr (LP) {
+        if (k < I.n) {
+            // no unique law x(theta): LP2 keeps a null-space direction of A_S
+            lp2_short_mplp(B, tol, I, lo, hi, k, ws, res);
+            return res;
+        }
+    }
     const T *G = ws.G;
     // LP2: max t  s.t.  g theta + t <= h (constraint rows), At theta <= bt
     T t0 = pos_inf<T>();
@@ -1225,13 +1446,15 @@ __device__ void write_opt(const DevBuffers &B, const Node &nd, int level, const 
 }
 
 // Final FP64 verdicts of every feasible set of a level (the FP64 path;
-// instantiated for T = double only).
-template <typename T>
+// instantiated for T = double only).  LP = false takes the sets of mpQP
+// instances, LP = true those of mpLP instances (launched only when a batch
+// has one), so that the mpQP kernel carries no mpLP code.
+template <typename T, bool LP>
 __global__ void __launch_bounds__(128) k_optimality(DevBuffers B, Tol tol, SlotDims sd, int level)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
-    const size_t slot = opt_slot_bytes<T>(sd.maxK, sd.maxP1, sd.maxR2, sizeof(T) == 4 ? sd.maxLD2 : sd.maxLD2d);
+    const size_t slot = opt_slot_bytes<T>(sd);
     OptWs<T> ws(smem + wib * slot, sd);
     const int side = level & 1;
     Ctl *ctl = B.ctl;
@@ -1241,13 +1464,13 @@ __global__ void __launch_bounds__(128) k_optimality(DevBuffers B, Tol tol, SlotD
     lc.reset(-1);
     for (;;) {
         long long x;
-        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[3], 1ull);
+        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[LP ? 6 : 3], 1ull);
         x = __shfl_sync(FULLMASK, x, 0);
         if (x >= nn) break;
         const Node nd = B.node[side][x];
         if ((nd.flags & (NODE_VALID | NODE_FEASIBLE)) != (NODE_VALID | NODE_FEASIBLE)) continue;
         const InstDesc &I = B.inst[nd.inst];
-        if (level < I.k_min) continue;
+        if (level < I.k_min || (I.lp != 0) != LP) continue;
         if (nd.inst != lc.inst) {
             if (lc.inst >= 0 && lane == 0) {
                 atomicAdd((unsigned long long *)&B.ictl[lc.inst].optimal, (unsigned long long)lc.a);
@@ -1257,7 +1480,7 @@ __global__ void __launch_bounds__(128) k_optimality(DevBuffers B, Tol tol, SlotD
             }
             lc.reset(nd.inst);
         }
-        const OptResult res = eval_optimality<T>(B, tol, I, nd.lo, nd.hi, ws);
+        const OptResult res = eval_optimality<T, LP>(B, tol, I, nd.lo, nd.hi, ws);
         lc.c += res.lp2_piv;
         lc.d += res.cheb_piv;
         lc.a += res.optimal;
@@ -1273,23 +1496,25 @@ __global__ void __launch_bounds__(128) k_optimality(DevBuffers B, Tol tol, SlotD
     }
 }
 
+template <bool LP>
 __global__ void __launch_bounds__(128) k_optimality_fp64(DevBuffers B, Tol tol, SlotDims sd, int level)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
-    const size_t slot = opt_slot_bytes<double>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2d);
+    const size_t slot = opt_slot_bytes<double>(sd);
     OptWs<double> ws(smem + wib * slot, sd);
     const int side = level & 1;
     Ctl *ctl = B.ctl;
     const long long nq = ctl->n_q_opt < B.q_cap ? ctl->n_q_opt : B.q_cap;
     for (;;) {
         long long x;
-        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[4], 1ull);
+        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[LP ? 7 : 4], 1ull);
         x = __shfl_sync(FULLMASK, x, 0);
         if (x >= nq) break;
         const Node nd = B.node[side][B.q_opt[x]];
         const InstDesc &I = B.inst[nd.inst];
-        const OptResult res = eval_optimality<double>(B, tol, I, nd.lo, nd.hi, ws);
+        if ((I.lp != 0) != LP) continue;
+        const OptResult res = eval_optimality<double, LP>(B, tol, I, nd.lo, nd.hi, ws);
         if (lane == 0) {
             InstCtl *ic = &B.ictl[nd.inst];
             atomicAdd((unsigned long long *)&ic->fb_opt, 1ull);
@@ -1534,7 +1759,7 @@ __host__ __device__ inline size_t screen_warp_bytes(const SlotDims &sd, int rout
 // each carries only its own code.
 __host__ __device__ __forceinline__ bool dual_route(int mode, const InstDesc &I, const SlotDims &sd)
 {
-    return mode == 0 && I.box && I.p <= kDualMaxP && I.m + I.ncp <= kDualMaxRows && sd.maxLD2 >= kDualLd;
+    return mode == 0 && I.box && !I.lp && I.p <= kDualMaxP && I.m + I.ncp <= kDualMaxRows && sd.maxLD2 >= kDualLd;
 }
 
 template <int ROUTE>
@@ -1555,6 +1780,7 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
         ids = smem + o; o += align16((size_t)sd.maxR2 + sd.maxP1);
         ws.G = ROUTE == 1 ? (float *)(smem + o) : nullptr;
         ws.Tb = nullptr; ws.ids = nullptr;
+        ws.Psi = ws.Phi = nullptr;
     }
     const int side = level & 1;
     Ctl *ctl = B.ctl;
@@ -1587,7 +1813,9 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
         bool decided = false;
         int status = LP_SKIPPED, piv = 0;
         float t = 0.0f;
-        if (!kkt_factor<float>(D, I, nd.lo, nd.hi, tol.margin_licq32, ws, &k, &rho)) {
+        // mpLP instances (Q = 0) take the primal route and are not screened:
+        // every set goes to FP64 (dual_route excludes them)
+        if (!(ROUTE == 1 && I.lp) && !kkt_factor<float>(D, I, nd.lo, nd.hi, tol.margin_licq32, ws, &k, &rho)) {
             // LP2: max t  s.t.  g theta + t <= h (constraint rows), At theta <= bt
             // the dual screen (mode 0, a box, p <= 6, at most 96 rows; its layout
             // needs rows of kDualLd floats in the slot) or the primal tableau
@@ -1857,13 +2085,14 @@ __global__ void k_finalize(DevBuffers B, int level)
 // Output per set (stride doubles): lagrange rows [lagrange_A | lagrange_b]
 // (k x (p+1)), then parameter rows [parameter_A | parameter_b] (n x (p+1)),
 // then the normalised region rows [CR_As | CR_bs] (n_cr x (p+1)).
-// sizes = {k, n, p, n_cr}; k = -1 when the KKT factor fails (LICQ).
+// sizes = {k, n, p, n_cr}; k = -1 when the KKT factor fails (LICQ), k = -2
+// for an mpLP set with |S| < n (x(theta) is not unique; nothing written).
 __global__ void __launch_bounds__(128) k_region_laws(DevBuffers B, Tol tol, SlotDims sd, const uint64_t *masks,
                                                      long long n_sets, double *laws, int *sizes, long long stride)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
-    const size_t slot = opt_slot_bytes<double>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2d);
+    const size_t slot = opt_slot_bytes<double>(sd);
     OptWs<double> ws(smem + wib * slot, sd);
     const InstDesc &I = B.inst[0];
     const KktData<double> D = kkt_data<double>(B, I);
@@ -1879,11 +2108,22 @@ __global__ void __launch_bounds__(128) k_region_laws(DevBuffers B, Tol tol, Slot
             if (lane == 0) { sz[0] = -1; sz[1] = n; sz[2] = p; sz[3] = 0; }
             continue;
         }
-        region_rows<double>(D, I, lo, hi, k, ws);
+        if (I.lp && k < n) {   // mpLP with |S| < n: no unique law x(theta)
+            if (lane == 0) { sz[0] = -2; sz[1] = n; sz[2] = p; sz[3] = 0; }
+            __syncwarp();
+            continue;
+        }
+        if (I.lp) {
+            mplp_multipliers(B, I, k, ws);
+            region_rows<double, false, true>(D, I, lo, hi, k, ws);
+        } else {
+            region_rows<double>(D, I, lo, hi, k, ws);
+        }
         const double *Lam = ws.Lam;
+        const double *LamL = I.lp ? ws.Psi : Lam;
         const double *QiAT = B.dpool + I.o_QiAT, *QiH = B.dpool + I.o_QiH, *Qic = B.dpool + I.o_Qic;
         for (int a = lane; a < k; a += 32)
-            for (int cc = 0; cc < P1; cc++) out[a * P1 + cc] = -Lam[a * P1 + cc];
+            for (int cc = 0; cc < P1; cc++) out[a * P1 + cc] = -LamL[a * P1 + cc];
         double *par = out + (long long)m * P1;
         for (int r = lane; r < n; r += 32) {
             for (int cc = 0; cc < P1; cc++) {
@@ -1919,7 +2159,7 @@ __global__ void __launch_bounds__(128) k_region_laws(DevBuffers B, Tol tol, Slot
     }
 }
 
-size_t laws_smem_per_warp(const SlotDims &sd) { return opt_slot_bytes<double>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2d); }
+size_t laws_smem_per_warp(const SlotDims &sd) { return opt_slot_bytes<double>(sd); }
 
 cudaError_t launch_region_laws(const DevBuffers &B, const Tol &tol, const SlotDims &sd, const uint64_t *masks,
                                long long n_sets, double *laws, int *sizes, long long stride, int grid, size_t smem,
@@ -1943,8 +2183,7 @@ bool screen_dual_route(int mode, const InstDesc &I, const SlotDims &sd) { return
 
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd)
 {
-    return prec_bytes == 8 ? opt_slot_bytes<double>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2d)
-                           : opt_slot_bytes<float>(sd.maxK, sd.maxP1, sd.maxR2, sd.maxLD2);
+    return prec_bytes == 8 ? opt_slot_bytes<double>(sd) : opt_slot_bytes<float>(sd);
 }
 
 }  // namespace mq
@@ -1962,8 +2201,10 @@ const void *kernel_ptr(const char *name)
         {"feas64", (const void *)k_feasibility<double>},
         {"feas32", (const void *)k_feasibility<float>},
         {"lp1_fp64", (const void *)k_lp1_fp64},
-        {"opt64", (const void *)k_optimality<double>},
-        {"opt_fp64", (const void *)k_optimality_fp64},
+        {"opt64", (const void *)k_optimality<double, false>},
+        {"opt64_lp", (const void *)k_optimality<double, true>},
+        {"opt_fp64", (const void *)k_optimality_fp64<false>},
+        {"opt_fp64_lp", (const void *)k_optimality_fp64<true>},
         {"screen_dual", (const void *)k_opt_screen<0>},
         {"screen_primal", (const void *)k_opt_screen<1>},
         {"level0_64", (const void *)k_level0<double>},
@@ -2001,11 +2242,12 @@ cudaError_t launch_lp1_fp64(const DevBuffers &B, const Tol &tol, const SlotDims 
     return cudaGetLastError();
 }
 
-cudaError_t launch_optimality(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int prec,
+cudaError_t launch_optimality(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, bool lp,
                               int grid, size_t smem, cudaStream_t s)
 {
-    (void)prec;   // the FP32 screen of the mixed path is launch_opt_screen
-    k_optimality<double><<<grid, 128, smem, s>>>(B, tol, sd, level);
+    // the FP32 screen of the mixed path is launch_opt_screen
+    if (lp) k_optimality<double, true><<<grid, 128, smem, s>>>(B, tol, sd, level);
+    else k_optimality<double, false><<<grid, 128, smem, s>>>(B, tol, sd, level);
     return cudaGetLastError();
 }
 
@@ -2033,10 +2275,11 @@ cudaError_t launch_redundancy(const double *M, const double *d, int nrows, int n
     return cudaGetLastError();
 }
 
-cudaError_t launch_optimality_fp64(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int grid,
-                                   size_t smem, cudaStream_t s)
+cudaError_t launch_optimality_fp64(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, bool lp,
+                                   int grid, size_t smem, cudaStream_t s)
 {
-    k_optimality_fp64<<<grid, 128, smem, s>>>(B, tol, sd, level);
+    if (lp) k_optimality_fp64<true><<<grid, 128, smem, s>>>(B, tol, sd, level);
+    else k_optimality_fp64<false><<<grid, 128, smem, s>>>(B, tol, sd, level);
     return cudaGetLastError();
 }
 

@@ -56,20 +56,56 @@ std::mutex g_mu;
 inline int odd_up(int x) { return (x & 1) ? x : x + 1; }
 
 // FP64 KKT blocks of one instance (same operation order as the engine's
-// precompute) written straight into `pool`; offsets go into d.
-int precompute(const mpqp_problem &P, InstDesc &d, double *pool, size_t pool_cap)
+// precompute) written straight into `pool`; offsets go into d, the doubles
+// used into *used.
+int precompute(const mpqp_problem &P, InstDesc &d, double *pool, size_t pool_cap, size_t *used)
 {
     const int n = P.n, m = P.m, p = P.p, ncp = P.ncp;
     memset(&d, 0, sizeof(d));
     d.n = n; d.m = m; d.p = p; d.ncp = ncp;
     d.M1 = m + ncp; d.nv = n + p; d.ld1 = odd_up(d.nv + 1); d.ld2 = odd_up(p + 2);
     d.ld1d = d.ld1; d.ld2d = d.ld2;
+    d.lp = 1;
+    for (int i = 0; i < n * n && d.lp; i++) if (P.Q[i] != 0.0) d.lp = 0;
+    d.ld2lp = odd_up(p + n + 3);
     size_t o = 0;
     auto take = [&](size_t cnt) { const size_t at = o; o += (cnt + 3) & ~(size_t)3; return (long long)at; };
     d.o_Wm = take((size_t)m * m); d.o_Wh = take((size_t)m * p); d.o_wc = take(m);
     d.o_At = take((size_t)ncp * p); d.o_bt = take(ncp); d.o_QiAT = take((size_t)n * m);
     d.o_QiH = take((size_t)n * p); d.o_Qic = take(n);
+    if (d.lp) { d.o_WhL = take((size_t)m * p); d.o_wcL = take(m); d.o_Hm = take((size_t)n * p); d.o_cv = take(n); }
+    *used = o;
     if (o > pool_cap) return MPQP_ECAPACITY;
+    memcpy(pool + d.o_At, P.At, sizeof(double) * (size_t)ncp * p);
+    memcpy(pool + d.o_bt, P.bt, sizeof(double) * (size_t)ncp);
+    if (d.lp) {
+        // mpLP (Q = 0): Wm = A A^T, Wh = F, wc = b, QiAT = A^T, QiH = Qic = 0,
+        // WhL = A H, wcL = A c, Hm = H, cv = c
+        double *Wm = pool + d.o_Wm, *WhL = pool + d.o_WhL, *wcL = pool + d.o_wcL, *AT = pool + d.o_QiAT;
+        for (int r = 0; r < m; r++) {
+            for (int s = 0; s < m; s++) {
+                double acc = 0.0;
+                for (int i = 0; i < n; i++) acc = std::fma(P.A[(size_t)r * n + i], P.A[(size_t)s * n + i], acc);
+                Wm[(size_t)r * m + s] = acc;
+            }
+            for (int c = 0; c < p; c++) {
+                double acc = 0.0;
+                for (int i = 0; i < n; i++) acc = std::fma(P.A[(size_t)r * n + i], P.H[(size_t)i * p + c], acc);
+                WhL[(size_t)r * p + c] = acc;
+            }
+            double acc = 0.0;
+            for (int i = 0; i < n; i++) acc = std::fma(P.A[(size_t)r * n + i], P.c[i], acc);
+            wcL[r] = acc;
+            for (int i = 0; i < n; i++) AT[(size_t)i * m + r] = P.A[(size_t)r * n + i];
+        }
+        memcpy(pool + d.o_Wh, P.F, sizeof(double) * (size_t)m * p);
+        memcpy(pool + d.o_wc, P.b, sizeof(double) * (size_t)m);
+        memset(pool + d.o_QiH, 0, sizeof(double) * (size_t)n * p);
+        memset(pool + d.o_Qic, 0, sizeof(double) * (size_t)n);
+        memcpy(pool + d.o_Hm, P.H, sizeof(double) * (size_t)n * p);
+        memcpy(pool + d.o_cv, P.c, sizeof(double) * (size_t)n);
+        return MPQP_OK;
+    }
     double *L = g_work, *V = L + n * n, *U = V + (size_t)n * m, *u = U + (size_t)n * p;
     memset(g_work, 0, sizeof(g_work));
     for (int j = 0; j < n; j++) {
@@ -120,8 +156,6 @@ int precompute(const mpqp_problem &P, InstDesc &d, double *pool, size_t pool_cap
     for (int r = 0; r < m; r++) bwd(V + r, m, pool + d.o_QiAT + r, m);
     for (int c = 0; c < p; c++) bwd(U + c, p, pool + d.o_QiH + c, p);
     bwd(u, 1, pool + d.o_Qic, 1);
-    memcpy(pool + d.o_At, P.At, sizeof(double) * (size_t)ncp * p);
-    memcpy(pool + d.o_bt, P.bt, sizeof(double) * (size_t)ncp);
     return MPQP_OK;
 }
 
@@ -156,9 +190,9 @@ extern "C" int mpqp_region_laws_noalloc(const mpqp_problem *prob, long long n_se
     InstDesc d;
     double *pool = (double *)(g_stage + kDescBytes);
     const size_t pool_cap = (kScratchBytes - kDescBytes) / sizeof(double);
-    int rc = precompute(*prob, d, pool, pool_cap);
-    if (rc == MPQP_ENOTSPD) return fail(rc, "mpqp_region_laws_noalloc: Q is not positive definite");
-    const size_t pool_used = (size_t)(d.o_Qic + ((n + 3) & ~3));
+    size_t pool_used = 0;
+    int rc = precompute(*prob, d, pool, pool_cap, &pool_used);
+    if (rc == MPQP_ENOTSPD) return fail(rc, "mpqp_region_laws_noalloc: Q is neither positive definite nor zero");
     const size_t mask_off = kDescBytes + ((pool_used * sizeof(double) + 255) & ~(size_t)255);
     const size_t need = mask_off + (size_t)n_sets * 2 * sizeof(uint64_t);
     if (rc == MPQP_ECAPACITY || need > kScratchBytes)
@@ -184,7 +218,9 @@ extern "C" int mpqp_region_laws_noalloc(const mpqp_problem *prob, long long n_se
     sd.maxM1 = d.M1; sd.maxLD1 = d.ld1; sd.maxNv = d.nv;
     sd.maxK = kcap < 1 ? 1 : kcap;
     sd.maxP1 = p + 1; sd.maxR2 = m + ncp; sd.maxLD2 = d.ld2;
-    sd.maxLD1d = d.ld1d; sd.maxLD2d = d.ld2d;
+    sd.maxLD1d = d.ld1d; sd.maxLD2d = d.lp ? (d.ld2lp > d.ld2d ? d.ld2lp : d.ld2d) : d.ld2d;
+    sd.maxR2d = d.lp ? m + ncp + 2 * n + 1 : m + ncp;
+    sd.maxN = d.lp ? n : 0;
     const size_t smem = 4 * laws_smem_per_warp(sd);
     const void *fn = kernel_ptr("laws");
     int sms = 0, nb = 0;

@@ -101,6 +101,34 @@ def random_mpqp(n: int, m: int, p: int, seed: int, box: float = 1.0,
     return MPQP(Q, c, H, A, b, F, CRA, CRb, name=f"random(n={n},m={m},p={p},seed={seed})")
 
 
+def random_mplp(n: int, m: int, p: int, seed: int, box: float = 1.0, h_scale: float = 1.0) -> MPLP:
+    """Random multiparametric LP (Q = 0), bounded for every theta.
+
+    Draw order: c N(0,1); H (n x p) N(0,1) times ``h_scale`` (the cost
+    (c + H theta)^T x moves with theta; 0 gives a fixed cost); A0
+    ((m - 2n) x n) N(0,1) with unit-norm rows; b U[1,2] (m); F0
+    ((m - 2n) x p) N(0, 0.25), 0.25 read as the variance.  A = [A0; I; -I]
+    (the last 2n rows bound x), F = [F0; 0], theta box [-box, box]^p.
+    """
+    if m < 2 * n + 1:
+        raise ValueError("random_mplp needs m >= 2n + 1")
+    rng = np.random.default_rng(seed)
+    c = rng.standard_normal(n)
+    H = rng.standard_normal((n, p)) * h_scale
+    A0 = rng.standard_normal((m - 2 * n, n))
+    A0 /= np.linalg.norm(A0, axis=1, keepdims=True)
+    b = rng.uniform(1.0, 2.0, m)
+    F0 = rng.normal(0.0, 0.5, (m - 2 * n, p))
+    A = np.vstack([A0, np.eye(n), -np.eye(n)])
+    F = np.vstack([F0, np.zeros((2 * n, p))])
+    CRA, CRb = _box(p, box)
+    return MPQP(np.zeros((n, n)), c, H, np.ascontiguousarray(A), b, np.ascontiguousarray(F), CRA, CRb,
+                name=f"random_mplp(n={n},m={m},p={p},seed={seed},h_scale={h_scale})")
+
+
+MPLP = MPQP   # an mpLP is an MPQP whose Q is zero
+
+
 def random_n4_m10_p2() -> MPQP:
     return random_mpqp(4, 10, 2, seed=0)
 

@@ -338,7 +338,9 @@ def apply_row_status(prob, status):
 
 
 def region_laws(prob, sets):
-    """FP64 laws of the given active sets (device).  Returns a list of dicts."""
+    """FP64 laws of the given active sets (device).  Returns a list of dicts;
+    None for a set that fails the LICQ test and for an mpLP set with fewer
+    than n active constraints (its law x(theta) is not unique)."""
     lib = load()
     ps = _ProblemSet([prob], 0, 0, 0)
     masks = np.zeros((len(sets), 2), dtype=np.uint64)

@@ -25,12 +25,16 @@ typedef struct {
     int nv;      /* LP1 free variables: n + p                          */
     int ld1;     /* LP1 tableau row stride: nv + 1                     */
     int ld2;     /* LP2 / Chebyshev tableau row stride: p + 2          */
-    double *Wm;  /* m x m   A Q^-1 A^T                                 */
-    double *Wh;  /* m x p   A Q^-1 H + F                               */
-    double *wc;  /* m       b + A Q^-1 c                               */
-    double *QiAT;/* n x m   Q^-1 A^T                                   */
-    double *QiH; /* n x p   Q^-1 H                                     */
-    double *Qic; /* n       Q^-1 c                                     */
+    int lp;      /* 1: Q = 0 (mpLP); the blocks below change meaning    */
+    int ld2lp;   /* mpLP, |S| < n: LP2 row stride p + n + 3             */
+    double *Wm;  /* m x m   A Q^-1 A^T          (mpLP: A A^T)          */
+    double *Wh;  /* m x p   A Q^-1 H + F        (mpLP: F)              */
+    double *wc;  /* m       b + A Q^-1 c        (mpLP: b)              */
+    double *QiAT;/* n x m   Q^-1 A^T            (mpLP: A^T)            */
+    double *QiH; /* n x p   Q^-1 H              (mpLP: 0)              */
+    double *Qic; /* n       Q^-1 c              (mpLP: 0)              */
+    double *WhL; /* mpLP: m x p  A H                                   */
+    double *wcL; /* mpLP: m      A c                                   */
     double *root;/* (M1+1) x ld1, LP1 tableau of the empty set         */
     const orc_problem *pr;
 } orc_data;
@@ -51,6 +55,7 @@ void orc_default_tol(orc_tol *t)
 static void free_data(orc_data *d)
 {
     free(d->Wm); free(d->Wh); free(d->wc); free(d->QiAT); free(d->QiH); free(d->Qic); free(d->root);
+    free(d->WhL); free(d->wcL);
     memset(d, 0, sizeof(*d));
 }
 
@@ -85,6 +90,11 @@ static int prepare(const orc_problem *pr, orc_data *d)
     d->n = n; d->m = m; d->p = p; d->ncp = ncp;
     d->M1 = m + ncp; d->nv = n + p; d->ld1 = d->nv + 1; d->ld2 = p + 2;
     d->pr = pr;
+    d->lp = 1;
+    for (int i = 0; i < n * n && d->lp; i++) if (pr->Q[i] != 0.0) d->lp = 0;
+    d->ld2lp = p + n + 3;
+    /* mpLP, |S| < n: LP2 columns theta, u, t, sigma and rows m + ncp + 2n + 1 */
+    if (d->lp && (p + n + 2) + (m + ncp + 2 * n + 1) > 255) return -1;
     double *L = calloc((size_t)n * n, sizeof(double));
     double *V = calloc((size_t)n * m, sizeof(double));
     double *U = calloc((size_t)n * p, sizeof(double));
@@ -97,8 +107,32 @@ static int prepare(const orc_problem *pr, orc_data *d)
     d->Qic = calloc((size_t)n, sizeof(double));
     d->root = calloc((size_t)(d->M1 + 1) * d->ld1, sizeof(double));
     int rc = 0;
+    if (d->lp) {
+        /* mpLP (Q = 0): Wm = A A^T, Wh = F, wc = b, QiAT = A^T, QiH = Qic = 0,
+         * WhL = A H, wcL = A c; each entry sums over ascending i from 0 */
+        d->WhL = calloc((size_t)m * p, sizeof(double));
+        d->wcL = calloc((size_t)m, sizeof(double));
+        for (int r = 0; r < m; r++) {
+            for (int s = 0; s < m; s++) {
+                double acc = 0.0;
+                for (int i = 0; i < n; i++) acc = fma(pr->A[r * n + i], pr->A[s * n + i], acc);
+                d->Wm[r * m + s] = acc;
+            }
+            for (int c = 0; c < p; c++) {
+                d->Wh[r * p + c] = pr->F[r * p + c];
+                double acc = 0.0;
+                for (int i = 0; i < n; i++) acc = fma(pr->A[r * n + i], pr->H[i * p + c], acc);
+                d->WhL[r * p + c] = acc;
+            }
+            d->wc[r] = pr->b[r];
+            double acc = 0.0;
+            for (int i = 0; i < n; i++) acc = fma(pr->A[r * n + i], pr->c[i], acc);
+            d->wcL[r] = acc;
+            for (int i = 0; i < n; i++) d->QiAT[i * m + r] = pr->A[r * n + i];
+        }
+    }
     /* Cholesky Q = L L^T */
-    for (int j = 0; j < n && rc == 0; j++) {
+    for (int j = 0; j < n && rc == 0 && !d->lp; j++) {
         for (int i = j; i < n; i++) {
             double acc = pr->Q[i * n + j];
             for (int l = 0; l < j; l++) acc = fma(-L[i * n + l], L[j * n + l], acc);
@@ -110,7 +144,7 @@ static int prepare(const orc_problem *pr, orc_data *d)
             }
         }
     }
-    if (rc == 0) {
+    if (rc == 0 && !d->lp) {
         for (int r = 0; r < m; r++) fwd_sub(L, n, pr->A + (size_t)r * n, 1, V + r, m);
         for (int c = 0; c < p; c++) fwd_sub(L, n, pr->H + c, p, U + c, p);
         fwd_sub(L, n, pr->c, 1, u, 1);
@@ -132,6 +166,8 @@ static int prepare(const orc_problem *pr, orc_data *d)
         for (int r = 0; r < m; r++) bwd_sub(L, n, V + r, m, d->QiAT + r, m);
         for (int c = 0; c < p; c++) bwd_sub(L, n, U + c, p, d->QiH + c, p);
         bwd_sub(L, n, u, 1, d->Qic, 1);
+    }
+    if (rc == 0) {
         /* LP1 root tableau: rows [A -F; 0 At], rhs [b; bt], objective row 0 */
         const int ld = d->ld1;
         for (int i = 0; i < m; i++) {
@@ -283,25 +319,170 @@ typedef struct {
     double *Y;     /* k x (p+1) */
     double *Lam;   /* k x (p+1): Lambda = Wm[S,S]^-1 [Wh_S | wc_S] */
     double *G;     /* (m+ncp) x (p+1) region rows [g | h] in reference order */
-    double *T;     /* (m+ncp+1) x ld2 LP tableau */
+    double *T;     /* (m+ncp+1) x ld2 LP tableau (mpLP: (m+ncp+2n+2) x ld2lp) */
     uint8_t *bid, *nid;
+    double *Psi;   /* mpLP: k x (p+1), Wm[S,S]^-1 [WhL_S | wcL_S] (multiplier law) */
+    double *Phi;   /* mpLP: k x n,     Wm[S,S]^-1 A_S */
 } opt_ws;
 
 static void opt_ws_alloc(const orc_data *d, opt_ws *w)
 {
-    const int m = d->m, p = d->p, R = m + d->ncp;
+    const int m = d->m, p = d->p, n = d->n, R = m + d->ncp;
+    const size_t tq = (size_t)(R + 1) * d->ld2, tl = (size_t)(R + 2 * n + 2) * d->ld2lp;
     w->R = calloc((size_t)m * m, sizeof(double));
     w->Y = calloc((size_t)m * (p + 1), sizeof(double));
     w->Lam = calloc((size_t)m * (p + 1), sizeof(double));
     w->G = calloc((size_t)R * (p + 1), sizeof(double));
-    w->T = calloc((size_t)(R + 1) * d->ld2, sizeof(double));
-    w->bid = calloc((size_t)R, 1);
-    w->nid = calloc((size_t)p + 1, 1);
+    w->T = calloc(d->lp && tl > tq ? tl : tq, sizeof(double));
+    w->bid = calloc((size_t)R + 2 * n + 1, 1);
+    w->nid = calloc((size_t)p + n + 2, 1);
+    w->Psi = calloc((size_t)m * (p + 1), sizeof(double));
+    w->Phi = calloc((size_t)m * n, sizeof(double));
 }
 
 static void opt_ws_free(opt_ws *w)
 {
     free(w->R); free(w->Y); free(w->Lam); free(w->G); free(w->T); free(w->bid); free(w->nid);
+    free(w->Psi); free(w->Phi);
+}
+
+/* X = Wm[S,S]^-1 B in place (R the upper Cholesky factor, k x k): X holds
+ * B_S on entry (row stride ldx, ncols columns); per column a forward then a
+ * backward substitution, each accumulating in ascending l */
+static void chol_solve_inplace(const double *R, int k, double *X, int ldx, int ncols)
+{
+    for (int a = 0; a < k; a++)
+        for (int c = 0; c < ncols; c++) {
+            double acc = X[a * ldx + c];
+            for (int l = 0; l < a; l++) acc = fma(-R[l * k + a], X[l * ldx + c], acc);
+            X[a * ldx + c] = acc / R[a * k + a];
+        }
+    for (int a = k - 1; a >= 0; a--)
+        for (int c = 0; c < ncols; c++) {
+            double acc = X[a * ldx + c];
+            for (int l = a + 1; l < k; l++) acc = fma(-R[a * k + l], X[l * ldx + c], acc);
+            X[a * ldx + c] = acc / R[a * k + a];
+        }
+}
+
+/* mpLP (Q = 0) with |S| = k < n: x is not fixed by S, so LP2 keeps a
+ * direction u in the null space of A_S (x = A_S^T Gamma(theta) + P u, P the
+ * projector onto that null space) and the stationarity residual
+ * (c + H theta) - A_S^T Psi(theta) = r0 + E theta (zero when S can be
+ * optimal) as rows |r0 + E theta| <= tol_feas -- the reference's LP2 keeps x
+ * and the equalities of main.py:107-108 as they are.  Two phases: min sigma
+ * over rows +-(r0 + E theta) - sigma <= tol_feas (sigma free), then, when
+ * sigma* <= 0, the row -sigma >= 0 is appended and max t solved from that
+ * basis.  Columns theta (p), u (n), t, sigma; rows: the m margin rows (G,
+ * reference order, plus A_i P in the u columns of inactive rows), the ncp
+ * parameter rows, 2n residual rows. */
+static void lp2_short_mplp(const orc_data *d, const int *S, int k, const orc_tol *tol, opt_ws *w, orc_cand *rec)
+{
+    const int m = d->m, n = d->n, p = d->p, ncp = d->ncp, P1 = p + 1, ld = d->ld2lp;
+    const int ncols = p + n + 2, ct = p + n, cs = p + n + 1;
+    const int nrows = m + ncp + 2 * n;
+    const double *G = w->G, *Phi = w->Phi, *Psi = w->Psi, *A = d->QiAT;
+    double *T = w->T;
+    double t0 = INFINITY;
+    for (int r = 0; r < m; r++) if (G[r * P1 + p] < t0) t0 = G[r * P1 + p];
+    memset(T, 0, sizeof(double) * (size_t)(nrows + 2) * ld);
+    int si = 0, row = k;
+    for (int r = 0; r < k; r++) {
+        double *Tr = T + (size_t)r * ld;
+        for (int c = 0; c < p; c++) Tr[c] = G[r * P1 + c];
+        Tr[ct] = 1.0;
+        double beta = fma(-1.0, t0, G[r * P1 + p]);
+        if (!(beta > 0.0)) beta = 0.0;
+        Tr[ncols] = beta;
+    }
+    for (int i = 0; i < m; i++) {
+        if (si < k && S[si] == i) { si++; continue; }
+        double *Tr = T + (size_t)row * ld;
+        for (int c = 0; c < p; c++) Tr[c] = G[row * P1 + c];
+        for (int j = 0; j < n; j++) {
+            double acc = A[j * m + i];
+            for (int l = 0; l < k; l++) acc = fma(-d->Wm[i * m + S[l]], Phi[l * n + j], acc);
+            Tr[p + j] = acc;
+        }
+        Tr[ct] = 1.0;
+        double beta = fma(-1.0, t0, G[row * P1 + p]);
+        if (!(beta > 0.0)) beta = 0.0;
+        Tr[ncols] = beta;
+        row++;
+    }
+    for (int i = 0; i < ncp; i++) {
+        double *Tr = T + (size_t)(m + i) * ld;
+        for (int c = 0; c < p; c++) Tr[c] = d->pr->At[i * p + c];
+        Tr[ncols] = d->pr->bt[i];
+    }
+    const double eps = tol->tol_feas;
+    double rmax = 0.0;
+    for (int i = 0; i < n; i++) {
+        double *Tp = T + (size_t)(m + ncp + 2 * i) * ld, *Tn = Tp + ld;
+        for (int c = 0; c < p; c++) {
+            double acc = d->pr->H[i * p + c];
+            for (int l = 0; l < k; l++) acc = fma(-A[i * m + S[l]], Psi[l * P1 + c], acc);
+            Tp[c] = acc;
+            Tn[c] = -acc;
+        }
+        double acc = d->pr->c[i];
+        for (int l = 0; l < k; l++) acc = fma(-A[i * m + S[l]], Psi[l * P1 + p], acc);
+        Tp[cs] = -1.0; Tn[cs] = -1.0;
+        Tp[ncols] = eps - acc;   /* rhs before the sigma shift */
+        Tn[ncols] = eps + acc;
+        if (fabs(acc) > rmax) rmax = fabs(acc);
+    }
+    const double s0 = rmax - eps;
+    for (int r = m + ncp; r < nrows; r++) {
+        double beta = T[(size_t)r * ld + ncols] + s0;
+        if (!(beta > 0.0)) beta = 0.0;
+        T[(size_t)r * ld + ncols] = beta;
+    }
+    for (int r = 0; r < nrows; r++) w->bid[r] = (uint8_t)(ncols + r);
+    for (int c = 0; c < ncols; c++) w->nid[c] = (uint8_t)c;
+    /* phase 1: min sigma = s0 + sigma' */
+    double *obj = T + (size_t)nrows * ld;
+    obj[cs] = -1.0;
+    obj[ncols] = s0;
+    int piv1 = 0, piv2 = 0;
+    int st = tucker_solve(T, ld, nrows, ncols, w->bid, w->nid, ncols, tol, &piv1);
+    rec->lp2_pivots = piv1;
+    if (st != ORC_OPTIMAL) { rec->lp2_status = st; return; }
+    const double sig = obj[ncols];
+    if (sig > 0.0) { rec->lp2_status = ORC_INFEASIBLE; rec->t = -INFINITY; return; }
+    /* row nrows: s = -sigma >= 0 in the current basis (sigma basic in row rs,
+     * or nonbasic in column qs); row nrows + 1: objective -t */
+    int rs = -1, qs = -1, rt = -1, qt = -1;
+    for (int r = 0; r < nrows; r++) { if (w->bid[r] == cs) rs = r; if (w->bid[r] == ct) rt = r; }
+    for (int c = 0; c < ncols; c++) { if (w->nid[c] == cs) qs = c; if (w->nid[c] == ct) qt = c; }
+    double *Ts = T + (size_t)nrows * ld, *ob = Ts + ld;
+    for (int c = 0; c <= ncols; c++) { Ts[c] = 0.0; ob[c] = 0.0; }
+    if (rs >= 0) {
+        const double *Tr = T + (size_t)rs * ld;
+        for (int c = 0; c < ncols; c++) Ts[c] = -Tr[c];
+        Ts[ncols] = -s0 - Tr[ncols];
+    } else {
+        Ts[qs] = 1.0;
+        Ts[ncols] = -s0;
+    }
+    w->bid[nrows] = (uint8_t)(ncols + nrows);
+    if (rt >= 0) {
+        const double *Tr = T + (size_t)rt * ld;
+        for (int c = 0; c < ncols; c++) ob[c] = -Tr[c];
+        ob[ncols] = -t0 - Tr[ncols];
+    } else {
+        ob[qt] = 1.0;
+        ob[ncols] = -t0;
+    }
+    st = tucker_solve(T, ld, nrows + 1, ncols, w->bid, w->nid, ncols, tol, &piv2);
+    rec->lp2_pivots = piv1 + piv2;
+    rec->lp2_status = st;
+    if (st == ORC_OPTIMAL) {
+        rec->t = -ob[ncols];
+        rec->optimal = rec->t > tol->tol_opt;
+    } else if (st == ORC_UNBOUNDED) {
+        rec->t = INFINITY;
+    }
 }
 
 /* Tableau for max t (LP2) or max r (Chebyshev) over rows g theta + a_r * v <= h,
@@ -372,12 +553,21 @@ static void optimality(const orc_data *d, const int *S, int k, const orc_tol *to
             Lam[a * P1 + c] = acc / R[a * k + a];
         }
     }
+    /* mpLP: Lam is Gamma = Wm[S,S]^-1 [F_S | b_S] (x = A_S^T Gamma(theta));
+     * the multipliers are lambda(theta) = -Psi(theta), Psi = Wm[S,S]^-1 [A_S H | A_S c] */
+    const double *LamL = Lam;
+    if (d->lp) {
+        for (int a = 0; a < k; a++)
+            for (int c = 0; c < P1; c++) w->Psi[a * P1 + c] = (c < p) ? d->WhL[S[a] * p + c] : d->wcL[S[a]];
+        chol_solve_inplace(R, k, w->Psi, P1, P1);
+        LamL = w->Psi;
+    }
     /* region rows, reference order: lambda rows (S order), inactive rows
      * (ascending), parameter box rows */
     int row = 0;
     for (int a = 0; a < k; a++, row++) {
-        for (int c = 0; c < p; c++) G[row * P1 + c] = Lam[a * P1 + c];
-        G[row * P1 + p] = -Lam[a * P1 + p];
+        for (int c = 0; c < p; c++) G[row * P1 + c] = LamL[a * P1 + c];
+        G[row * P1 + p] = -LamL[a * P1 + p];
     }
     int si = 0;
     for (int i = 0; i < m; i++) {
@@ -397,6 +587,14 @@ static void optimality(const orc_data *d, const int *S, int k, const orc_tol *to
         G[row * P1 + p] = d->pr->bt[i];
     }
     const int nrows = m + ncp;
+    if (d->lp && k < n) {
+        /* no unique law x(theta): LP2 with a null-space direction; never a region */
+        for (int a = 0; a < k; a++)
+            for (int j = 0; j < n; j++) w->Phi[a * n + j] = d->QiAT[j * m + S[a]];
+        chol_solve_inplace(R, k, w->Phi, n, n);
+        lp2_short_mplp(d, S, k, tol, w, rec);
+        return;
+    }
     /* LP2: max t s.t. g theta + t <= h (constraint rows), At theta <= bt */
     double coef[256];
     double t0 = INFINITY;
@@ -455,8 +653,8 @@ static void optimality(const orc_data *d, const int *S, int k, const orc_tol *to
     if (laws && rec->region) {
         double *lA = laws, *lb = laws + k * p, *pA = lb + k, *pb = pA + n * p;
         for (int a = 0; a < k; a++) {
-            for (int c = 0; c < p; c++) lA[a * p + c] = -Lam[a * P1 + c];
-            lb[a] = -Lam[a * P1 + p];
+            for (int c = 0; c < p; c++) lA[a * p + c] = -LamL[a * P1 + c];
+            lb[a] = -LamL[a * P1 + p];
         }
         for (int r = 0; r < n; r++) {
             for (int c = 0; c < p; c++) {

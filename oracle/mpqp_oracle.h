@@ -18,6 +18,12 @@
  *     eliminating x and lambda through the KKT factor;
  *   - critical region rows, normalisation and the Chebyshev-ball LP with the
  *     1e-8 radius test (utils.py:18-97).
+ * Q = 0 (an mpLP, README.md:5) runs the same LP1 and the same LP2 verdict
+ * (main.py:107 with the Q block zero): the KKT factor is that of A_S A_S^T,
+ * x(theta) = A_S^T (A_S A_S^T)^-1 (b_S + F_S theta) and lambda(theta) =
+ * -(A_S A_S^T)^-1 A_S (c + H theta); a set with |S| < n keeps a null-space
+ * direction of A_S and the stationarity residual in its LP2 (lp2_short_mplp)
+ * and is never a region (no unique law x(theta)).
  * Parity of the verdict definitions with the reference's own LP matrices is
  * checked independently (HiGHS on the matrices main.py builds) in the tests.
  */
@@ -32,7 +38,7 @@ extern "C" {
 
 typedef struct {
     int n, m, p, ncp;
-    const double *Q;   /* n x n, row-major, symmetric positive definite */
+    const double *Q;   /* n x n, row-major, symmetric positive definite, or all zero (mpLP) */
     const double *c;   /* n */
     const double *H;   /* n x p */
     const double *A;   /* m x n */
@@ -55,7 +61,8 @@ typedef struct {
 } orc_tol;
 
 /* LP status codes (shared with the device code) */
-enum { ORC_OPTIMAL = 0, ORC_UNBOUNDED = 1, ORC_ITER_LIMIT = 2, ORC_SKIPPED = 3, ORC_LICQ_FAIL = 4 };
+enum { ORC_OPTIMAL = 0, ORC_UNBOUNDED = 1, ORC_ITER_LIMIT = 2, ORC_SKIPPED = 3, ORC_LICQ_FAIL = 4,
+       ORC_INFEASIBLE = 5 };
 #define ORC_ENOMEM (-5)   /* host memory exhausted */
 
 typedef struct {

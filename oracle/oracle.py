@@ -19,7 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "mpqp_oracle.c")
 LIB = os.path.join(HERE, "libmpqp_oracle.so")
 
-OPTIMAL, UNBOUNDED, ITER_LIMIT, SKIPPED, LICQ_FAIL = range(5)
+OPTIMAL, UNBOUNDED, ITER_LIMIT, SKIPPED, LICQ_FAIL, INFEASIBLE = range(6)
 
 
 def build(force: bool = False) -> str:

@@ -54,7 +54,8 @@ def test_gpu_results_prefix_matches_reference_layout():
 
 
 @pytest.mark.parametrize("make", [P.random_n4_m10_p2, P.random_n10_m43_p4, P.illcond_n16_m62_p8, lambda: P.mpc_mpqp(3),
-                                  lambda: P.batch_member(5)])
+                                  lambda: P.batch_member(5), lambda: P.random_mplp(4, 13, 3, seed=5),
+                                  lambda: P.random_mplp(6, 20, 3, seed=3, h_scale=0.0)])
 def test_unpack_lp_recovers_the_problem(lib, make):
     prog = host.MPQPProb.from_mpqp(make())
     prog.process_constraints(scale_method=1)
@@ -81,4 +82,11 @@ def test_unpack_lp_rejects_other_layouts(lib):
     bad = dict(d, A0=np.asfortranarray(d["A0"] + 1.0))
     with pytest.raises(solver.MpqpError) as e:
         solver.unpack_lp(bad)
+    assert e.value.code == solver.ELAYOUT
+    # a stationarity row whose multiplier block is not A^T (main.py:106)
+    A2 = np.array(d["A2"], order="F", copy=True)
+    r0 = d["num_c"] + 1 + (d["M1"] - d["num_c"])
+    A2[r0, d["num_x"] + d["num_t"]] += 0.5
+    with pytest.raises(solver.MpqpError) as e:
+        solver.unpack_lp(dict(d, A2=A2))
     assert e.value.code == solver.ELAYOUT
