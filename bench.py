@@ -252,6 +252,50 @@ def cpu_baseline(steps: int = 1, warmup: int = 0) -> dict:
             "seconds_per_step": n / statistics.median(vals)}
 
 
+def mplp_measure(prec, stream, dev, steps: int = 3) -> dict:
+    """The mpLP row (Q = 0): 32 random mpLPs of mixed sizes (``mplp_batch``),
+    every instance enumerated to |S| = n, device-resident plan, CUDA events
+    around `steps` runs; the plain FP64 path beside it (same regions) and the
+    C oracle on the host on the first 8 instances."""
+    import torch
+    from mpqpcudasolver_gb300 import problems as P
+    from mpqpcudasolver_gb300 import solver
+    from oracle import oracle as O
+    probs = [P.scale_problem(p) for p in P.mplp_batch()]
+
+    def timed(precision):
+        plan = solver.Plan(probs, precision=precision, mem_fraction=0.85)
+        for _ in range(2):
+            plan.run(stream.cuda_stream)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            plan.run(stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        res = plan.results()
+        plan.close()
+        assert res.status == 0, res.status
+        return res, e0.elapsed_time(e1) / steps
+
+    res, ms = timed(prec)
+    r64, ms64 = timed(solver.FP64)
+    threads = os.cpu_count() or 1
+    sample = probs[:8]
+    t0 = time.perf_counter()
+    n_cpu = sum(O.enumerate_sets(pr, k_max=pr.n, nthreads=threads, keep_records=False).n_cand for pr in sample)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": "32 random mpLPs (Q = 0; n~U{4..8}, m~U{2n+6..2n+16}, p~U{2..4}, parametric cost), "
+                        "all instances to |S| = n",
+            "candidates_per_step": res.candidates, "ms_per_step": ms, "value": res.candidates / (ms / 1e3),
+            "unit": UNIT, "optimal": res.total("optimal"), "regions": res.total("regions"),
+            "fp64_path": {"ms_per_step": ms64, "value": r64.candidates / (ms64 / 1e3),
+                          "regions_identical": same_regions(res, r64)},
+            "cpu_baseline": {"value": n_cpu / cpu_s, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"C oracle, the first 8 instances to |S| = n ({n_cpu} candidates)"}}
+
+
 def run_reference(args):
     world, rank, local, dist = dist_setup(args.gpus)
     if rank != 0:
@@ -373,6 +417,7 @@ def run_ours(args):
                         "per candidate (levels >= 1): 8 B record + 48 B parent node + parent LP1 tableau "
                         "(M1+1)*ld1*s + basis ids; per feasible child 80 B; per stored child its tableau and ids")
     cb = cpu_baseline(steps=1)
+    mplp = None if args.skip_mplp else mplp_measure(prec, stream, dev)
     clocks = clk.summary()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -392,6 +437,7 @@ def run_ours(args):
         "kernels_ms_per_step": {k: round(v[0], 3) for k, v in sorted(kt.items(), key=lambda kv: -kv[1][0])},
         "dominant_kernel": dominant,
         "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "mplp": mplp,
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "mpqp_solve_batch (C ABI): host arrays in, plan + upload + run + download + free"},
         "clocks": clocks,
@@ -410,6 +456,7 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-mplp", action="store_true", help="leave out the mpLP (Q = 0) measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

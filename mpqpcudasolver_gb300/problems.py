@@ -279,6 +279,24 @@ def scale_problem(prob: MPQP) -> MPQP:
     return out
 
 
+def mplp_member(seed: int) -> MPQP:
+    """One instance of the mpLP batch; sizes drawn first from the same stream
+    (n ~ U{4..8}, m ~ U{2n+6..2n+16}, p ~ U{2..4}), then ``random_mplp``
+    with a parametric cost (h_scale 1) on that stream."""
+    rng = np.random.default_rng(10_000 + seed)
+    n = int(rng.integers(4, 9))
+    m = int(rng.integers(2 * n + 6, 2 * n + 17))
+    p = int(rng.integers(2, 5))
+    prob = random_mplp(n, m, p, seed=10_000 + seed)
+    prob.name = f"mplp_member(seed={seed},n={n},m={m},p={p})"
+    return prob
+
+
+def mplp_batch(n_instances: int = 32) -> list[MPQP]:
+    """32 random mpLPs (Q = 0) of mixed sizes, enumerated to |S| = n."""
+    return [mplp_member(s) for s in range(n_instances)]
+
+
 def pop_like_set(n_problems: int = 24, seed: int = 0, n_max: int = 5, m_max: int = 16) -> list[MPQP]:
     """A seeded stand-in for a set of test problems of mixed sizes (the
     reference's driver loops over a public test set, which is not copied
@@ -306,4 +324,5 @@ WORKLOADS = {
     "illcond-n16-m62-p8": lambda: [illcond_n16_m62_p8()],
     "mpc-batch": mpc_batch,
     "pop-like": pop_like_set,
+    "mplp-batch": mplp_batch,
 }

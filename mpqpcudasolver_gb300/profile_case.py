@@ -5,7 +5,7 @@
 CASE: m62-k3 | m62-k4 | m62-k5 (the n=12, m=62, p=6 instance up to |S| = k)
 | m62-batch (the bench batch) | n10m43p4-k4 | illcond-k3 | mpc-batch (64 MPC
 instances, |S| <= 3) | pop-like (64 problems of mixed sizes, n <= 8, m <= 30,
-every |S| <= n).
+every |S| <= n) | mplp-batch (32 mpLPs, Q = 0, every |S| <= n).
 Prints one JSON line with the candidates, the device time of the last run
 and the per-kernel times of a timed run.
 """
@@ -31,6 +31,9 @@ def workload(case: str):
         return [P.scale_problem(P.illcond_n16_m62_p8())], 3, 0
     if case == "pop-like":
         probs = [P.scale_problem(p) for p in P.pop_like_set(64, seed=0, n_max=8, m_max=30)]
+        return probs, [p.n for p in probs], 0
+    if case == "mplp-batch":
+        probs = [P.scale_problem(p) for p in P.mplp_batch()]
         return probs, [p.n for p in probs], 0
     if case == "mpc-batch":
         return [P.scale_problem(p) for p in P.mpc_batch(64)], 3, 0
