@@ -826,8 +826,9 @@ extern "C" int mpqp_plan_results(mpqp_plan *P, mpqp_batch_result **out)
     R->n_inst = P->n_inst;
     R->device_ms = ms;
     R->overflow = ctl.overflow;
-    R->status = ctl.overflow ? MPQP_ECAPACITY : MPQP_OK;
-    if (ctl.overflow) set_err("device buffer overflow (bits " + std::to_string(ctl.overflow) + ")");
+    R->status = ctl.overflow ? ((ctl.overflow & OV_WAIT) ? MPQP_ECUDA : MPQP_ECAPACITY) : MPQP_OK;
+    if (ctl.overflow & OV_WAIT) set_err("a bulk copy did not complete within its bounded wait");
+    else if (ctl.overflow) set_err("device buffer overflow (bits " + std::to_string(ctl.overflow) + ")");
     R->inst = (mpqp_inst_stats *)calloc(P->n_inst, sizeof(mpqp_inst_stats));
     int nlev = 0;
     for (int i = 0; i < P->n_inst; i++) {

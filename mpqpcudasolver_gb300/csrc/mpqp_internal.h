@@ -151,7 +151,9 @@ struct Ctl {
     long long hcap[2];          // slots of the hash in use per side (a power of 2 <= hash_cap)
 };
 
-enum Overflow : int { OV_CAND = 1, OV_NODE = 2, OV_TAB = 4, OV_IDS = 8, OV_OPT = 16, OV_REC = 32, OV_QUEUE = 64, OV_HASH = 128 };
+// OV_WAIT: a bounded wait for a bulk copy ran out (the launch's results are void)
+enum Overflow : int { OV_CAND = 1, OV_NODE = 2, OV_TAB = 4, OV_IDS = 8, OV_OPT = 16, OV_REC = 32, OV_QUEUE = 64, OV_HASH = 128,
+                      OV_WAIT = 256 };
 
 // Largest per-warp shared-memory footprint over the instances of a batch
 struct SlotDims {

@@ -426,12 +426,69 @@ __device__ __forceinline__ int warp_simplex_f32(const Lp<float> &L, float tol_pi
 // ---------------------------------------------------------------------
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-// LP1 slot: tableau (maxM1+1) x maxLD1 + ids (maxM1 + maxNv)
+// LP1 slot: tableau (maxM1+1) x maxLD1 + ids (maxM1 + maxNv) + the warp's
+// mbarrier (16 bytes, last)
 template <typename T>
 __host__ __device__ inline size_t lp1_slot_bytes(int maxM1, int maxLD1, int maxNv)
 {
-    return align16((((size_t)(maxM1 + 1) * maxLD1 + 3) & ~(size_t)3) * sizeof(T)) + align16((size_t)maxM1 + maxNv);
+    return align16((((size_t)(maxM1 + 1) * maxLD1 + 3) & ~(size_t)3) * sizeof(T)) + align16((size_t)maxM1 + maxNv) + 16;
 }
+
+// ---------------------------------------------------------------------
+// bulk (TMA) copies between global and shared memory
+// ---------------------------------------------------------------------
+// Addresses 16-byte aligned and sizes multiples of 16 bytes (tableaus are
+// multiples of 4 elements at offsets that are multiples of 4 elements; basis
+// ids are padded to 16 bytes).  Loads complete on an mbarrier of the warp's
+// slot; stores go in bulk groups that the issuing lane waits for before the
+// slot is written again.
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// orders this thread's generic shared-memory accesses before later bulk copies
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect(uint64_t *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// Wait for the phase of parity `parity` to complete, at most kWaitTries
+// tries (each suspends for a bounded, implementation-defined time); false
+// when the limit ran out.
+constexpr int kWaitTries = 1 << 20;
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
+{
+    for (int it = 0; it < kWaitTries; it++) {
+        unsigned ok;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void bulk_store(void *dst, const void *src, unsigned bytes)
+{
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// the bulk stores issued by this thread have read their shared-memory source
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// ... and have completed
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 // optimality slot: R (kmax^2), Y and Lambda (kmax x P1), G (R2 x P1),
 // tableau (rows+1) x ld2, ids (rows + P1, + n + 1 with mpLP instances), S
@@ -577,10 +634,13 @@ __device__ __forceinline__ void warp_copy_v(T *dst, const T *src, int n)
 // Append a feasible (or, exhaustive, any) candidate as a node of `side`;
 // stores its tableau when it can have children.  Returns the node index or -1.
 // src_ld: row stride of `tab` (0: the plan's stride, copied as is).
+// bulk: tab and ids are a shared-memory slot of the plan's layout (src_ld 0,
+// TT = TS); lane 0 copies them with bulk stores (bulk_wait_read before the
+// slot is written again, bulk_wait_all before the kernel ends).
 template <typename TT, typename TS>
 __device__ long long store_node(const DevBuffers &B, int side, int level, const InstDesc &I, int inst,
                                 uint64_t lo, uint64_t hi, bool feasible, const TS *tab, const uint8_t *ids,
-                                long long rec, long long hcap, int extra_flags, int src_ld = 0)
+                                long long rec, long long hcap, int extra_flags, int src_ld = 0, bool bulk = false)
 {
     const int lane = lane_id();
     Ctl *ctl = B.ctl;
@@ -615,7 +675,15 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
     if (need_tab) {
         if (lane == 0) atomicAdd((unsigned long long *)&B.ictl[inst].stored, 1ull);
         TT *dst = (TT *)B.tab[side] + toff;
-        if (src_ld == 0) {
+        if (bulk) {
+            fence_proxy_async_smem();
+            __syncwarp();
+            if (lane == 0) {
+                bulk_store(dst, tab, (unsigned)(I.tab_elems * sizeof(TT)));
+                bulk_store(B.ids[side] + ioff, ids, (unsigned)I.ids_bytes);
+                bulk_commit();
+            }
+        } else if (src_ld == 0) {
             warp_copy_v<TT>(dst, (const TT *)tab, I.tab_elems);
         } else {
             // re-stride (and convert) row by row; padding columns become 0
@@ -625,8 +693,10 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
                 dst[e] = (i <= I.M1 && j < ncol) ? (TT)tab[(size_t)i * src_ld + j] : TT(0);
             }
         }
-        uint8_t *di = B.ids[side] + ioff;
-        for (int e = lane; e < I.M1 + I.nv; e += 32) di[e] = ids[e];
+        if (!bulk) {
+            uint8_t *di = B.ids[side] + ioff;
+            for (int e = lane; e < I.M1 + I.nv; e += 32) di[e] = ids[e];
+        }
     }
     if (lane == 0) {
         Node nd;
@@ -659,11 +729,15 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
     unsigned char *base = smem + wib * slot;
     T *tab = (T *)base;
     uint8_t *ids = base + align16((((size_t)(sd.maxM1 + 1) * mld + 3) & ~(size_t)3) * sizeof(T));
+    uint64_t *bar = (uint64_t *)(base + slot - 16);
     const int side = level & 1, pside = side ^ 1;
     Ctl *ctl = B.ctl;
     const long long ncand = ctl->n_cand;
     const long long hcap = hash_cap_for(B, ncand);   // slots of this level's hash
     const bool mixed = sizeof(T) == 4;
+    if (lane == 0) mbar_init(bar);
+    __syncwarp();
+    unsigned parity = 0;
     const T tpiv = mixed ? (T)tol.tol_piv32 : (T)tol.tol_piv;
     const T tdj = mixed ? (T)tol.tol_dj32 : (T)tol.tol_dj;
     LocalInstCounters lc;
@@ -693,11 +767,24 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
             lc.reset(inst);
         }
         const int M1 = I.M1, nv = I.nv, ld = I.ld1;
-        // stage the parent tableau and basis (16-byte vector loads)
-        warp_copy_v<T>(tab, (const T *)B.tab[pside] + par.tab_off, I.tab_elems);
-        const uint8_t *sid = B.ids[pside] + par.ids_off;
-        for (int e = lane; e < M1 + nv; e += 32) ids[e] = sid[e];
+        // stage the parent tableau and basis: one bulk copy each, completing
+        // on the warp's mbarrier (this warp's earlier accesses to the slot,
+        // and the bulk store of the previous child, come first)
+        fence_proxy_async_smem();
         __syncwarp();
+        if (lane == 0) {
+            bulk_wait_read();
+            const unsigned tb = (unsigned)(I.tab_elems * sizeof(T)), ib = (unsigned)I.ids_bytes;
+            mbar_expect(bar, tb + ib);
+            bulk_load(tab, (const T *)B.tab[pside] + par.tab_off, tb, bar);
+            bulk_load(ids, B.ids[pside] + par.ids_off, ib, bar);
+        }
+        if (!__all_sync(FULLMASK, mbar_wait(bar, parity))) {
+            if (lane == 0) atomicOr(&ctl->overflow, OV_WAIT);
+            (void)mbar_wait(bar, parity);   // the copies in flight, once more bounded
+            break;
+        }
+        parity ^= 1u;
         uint8_t *bid = ids, *nid = ids + M1;
         T *obj = tab + (size_t)M1 * ld;
         // objective += w_j
@@ -791,8 +878,10 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         }
         if (feasible) { lc.a++; lc.c += (long long)mask_digest(lo, hi); }
         if (feasible || B.exhaustive)
-            store_node<T, T>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap, par.flags & NODE_FP64CHAIN);
+            store_node<T, T>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap, par.flags & NODE_FP64CHAIN,
+                             0, true);
     }
+    if (lane == 0) bulk_wait_all();
     if (lc.inst >= 0 && lane == 0) {
         atomicAdd((unsigned long long *)&B.ictl[lc.inst].feasible, (unsigned long long)lc.a);
         atomicAdd((unsigned long long *)&B.ictl[lc.inst].lp1_piv, (unsigned long long)lc.b);
