@@ -23,6 +23,7 @@
 
 namespace mq {
 size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd);
+size_t feas_smem_per_warp(int prec_bytes, const SlotDims &sd);
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd);
 size_t screen_smem_per_warp(const SlotDims &sd, int route);
 bool screen_dual_route(int mode, const InstDesc &I, const SlotDims &sd);
@@ -693,7 +694,7 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
     CK(cudaMemset(B.hash[1], 0xff, sizeof(HashSlot) * hash_cap));
     CK(cudaMemset(B.ctl, 0, sizeof(Ctl)));
     // kernel geometry
-    P->smem_feas = 4 * lp1_smem_per_warp(P->prec == PREC_MIXED ? 4 : 8, sd);
+    P->smem_feas = 4 * feas_smem_per_warp(P->prec == PREC_MIXED ? 4 : 8, sd);
     P->smem_lp1fb = 4 * lp1_smem_per_warp(8, sd);
     // mixed precision: the grouped FP32 screen, one warp per block
     P->smem_opt = P->prec == PREC_MIXED ? screen_smem_per_warp(sd, 0) : 4 * opt_smem_per_warp(8, sd);

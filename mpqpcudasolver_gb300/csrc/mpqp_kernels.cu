@@ -426,13 +426,32 @@ __device__ __forceinline__ int warp_simplex_f32(const Lp<float> &L, float tol_pi
 // ---------------------------------------------------------------------
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-// LP1 slot: tableau (maxM1+1) x maxLD1 + ids (maxM1 + maxNv) + the warp's
-// mbarrier (16 bytes, last)
+// LP1 buffer: tableau (maxM1+1) x maxLD1 + ids (maxM1 + maxNv)
+template <typename T>
+__host__ __device__ inline size_t lp1_buf_bytes(int maxM1, int maxLD1, int maxNv)
+{
+    return align16((((size_t)(maxM1 + 1) * maxLD1 + 3) & ~(size_t)3) * sizeof(T)) + align16((size_t)maxM1 + maxNv);
+}
+
+// LP1 slot of k_lp1_fp64: one buffer + 16 bytes
 template <typename T>
 __host__ __device__ inline size_t lp1_slot_bytes(int maxM1, int maxLD1, int maxNv)
 {
-    return align16((((size_t)(maxM1 + 1) * maxLD1 + 3) & ~(size_t)3) * sizeof(T)) + align16((size_t)maxM1 + maxNv) + 16;
+    return lp1_buf_bytes<T>(maxM1, maxLD1, maxNv) + 16;
 }
+
+// slot of k_feasibility: one buffer and the warp's mbarrier (16 bytes, last)
+template <typename T>
+__host__ __device__ inline size_t feas_slot_bytes(int maxM1, int maxLD1, int maxNv)
+{
+    return lp1_buf_bytes<T>(maxM1, maxLD1, maxNv) + 16;
+}
+
+// candidates a warp claims at a time: consecutive candidates share parents
+// (children of one parent are consecutive in the candidate list), so the
+// first child loads its parent from DRAM and the others find it in L2, and
+// the next candidate's parent is known one candidate ahead (L2 prefetch)
+constexpr int kFeasChunk = 32;
 
 // ---------------------------------------------------------------------
 // bulk (TMA) copies between global and shared memory
@@ -477,6 +496,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
         if (ok) return true;
     }
     return false;
+}
+
+// a hint: bring [src, src + bytes) into L2 (no completion to wait for)
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src, unsigned bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
 
 __device__ __forceinline__ void bulk_store(void *dst, const void *src, unsigned bytes)
@@ -724,8 +749,9 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
-    const int mld = sizeof(T) == 4 ? sd.maxLD1 : sd.maxLD1d;
-    const size_t slot = lp1_slot_bytes<T>(sd.maxM1, mld, sd.maxNv);
+    constexpr bool mixed = sizeof(T) == 4;
+    const int mld = mixed ? sd.maxLD1 : sd.maxLD1d;
+    const size_t slot = feas_slot_bytes<T>(sd.maxM1, mld, sd.maxNv);
     unsigned char *base = smem + wib * slot;
     T *tab = (T *)base;
     uint8_t *ids = base + align16((((size_t)(sd.maxM1 + 1) * mld + 3) & ~(size_t)3) * sizeof(T));
@@ -733,21 +759,39 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
     const int side = level & 1, pside = side ^ 1;
     Ctl *ctl = B.ctl;
     const long long ncand = ctl->n_cand;
+    const long long wend = ncand < B.cand_cap ? ncand : B.cand_cap;
     const long long hcap = hash_cap_for(B, ncand);   // slots of this level's hash
-    const bool mixed = sizeof(T) == 4;
     if (lane == 0) mbar_init(bar);
     __syncwarp();
     unsigned parity = 0;
+    bool abort = false;
     const T tpiv = mixed ? (T)tol.tol_piv32 : (T)tol.tol_piv;
     const T tdj = mixed ? (T)tol.tol_dj32 : (T)tol.tol_dj;
     LocalInstCounters lc;
     lc.reset(-1);
     for (;;) {
-        long long w;
-        if (lane == 0) w = (long long)atomicAdd(&ctl->ctr[0], 1ull);
-        w = __shfl_sync(FULLMASK, w, 0);
-        if (w >= ncand || w >= B.cand_cap) break;
-        const Cand c = B.cand[w];
+        long long w0;
+        if (lane == 0) w0 = (long long)atomicAdd(&ctl->ctr[0], (unsigned long long)kFeasChunk);
+        w0 = __shfl_sync(FULLMASK, w0, 0);
+        if (w0 >= wend || abort) break;
+        const int cnt = wend - w0 < kFeasChunk ? (int)(wend - w0) : kFeasChunk;
+        const Cand mine = lane < cnt ? B.cand[w0 + lane] : Cand{-1, 0};
+        // lane t holds candidate t's parent tableau offset (for the prefetch)
+        const long long my_toff = lane < cnt ? B.node[pside][mine.parent].tab_off : -1;
+        const int my_inst = lane < cnt ? B.node[pside][mine.parent].inst : 0;
+    for (int t = 0; t < cnt; t++) {
+        const long long w = w0 + t;
+        Cand c;
+        c.parent = __shfl_sync(FULLMASK, mine.parent, t);
+        c.j = __shfl_sync(FULLMASK, mine.j, t);
+        {
+            // the next candidate's parent into L2 while this one is solved
+            const int np = __shfl_sync(FULLMASK, mine.parent, (t + 1) & 31);
+            const long long ntoff = __shfl_sync(FULLMASK, my_toff, (t + 1) & 31);
+            const int ninst = __shfl_sync(FULLMASK, my_inst, (t + 1) & 31);
+            if (lane == 0 && t + 1 < cnt && np != c.parent && ntoff >= 0)
+                bulk_prefetch_l2((const T *)B.tab[pside] + ntoff, (unsigned)(B.inst[ninst].tab_elems * sizeof(T)));
+        }
         const Node par = B.node[pside][c.parent];
         const int inst = par.inst;
         const InstDesc &I = B.inst[inst];
@@ -782,6 +826,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         if (!__all_sync(FULLMASK, mbar_wait(bar, parity))) {
             if (lane == 0) atomicOr(&ctl->overflow, OV_WAIT);
             (void)mbar_wait(bar, parity);   // the copies in flight, once more bounded
+            abort = true;
             break;
         }
         parity ^= 1u;
@@ -880,6 +925,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         if (feasible || B.exhaustive)
             store_node<T, T>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap, par.flags & NODE_FP64CHAIN,
                              0, true);
+    }
     }
     if (lane == 0) bulk_wait_all();
     if (lc.inst >= 0 && lane == 0) {
@@ -2261,6 +2307,12 @@ cudaError_t launch_region_laws(const DevBuffers &B, const Tol &tol, const SlotDi
 // ---------------------------------------------------------------------
 // explicit instantiations / host-visible launch wrappers
 // ---------------------------------------------------------------------
+size_t feas_smem_per_warp(int prec_bytes, const SlotDims &sd)
+{
+    return prec_bytes == 8 ? feas_slot_bytes<double>(sd.maxM1, sd.maxLD1d, sd.maxNv)
+                           : feas_slot_bytes<float>(sd.maxM1, sd.maxLD1, sd.maxNv);
+}
+
 size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd)
 {
     return prec_bytes == 8 ? lp1_slot_bytes<double>(sd.maxM1, sd.maxLD1d, sd.maxNv)
