@@ -554,15 +554,27 @@ __global__ void k_enumerate(DevBuffers B, int level)
     int cur_inst = -1;
     long long loc_cand = 0, loc_pruned = 0;
     for (;;) {
-        long long pi;
-        if (lane == 0) pi = (long long)atomicAdd(&ctl->ctr[1], 1ull);
-        pi = __shfl_sync(FULLMASK, pi, 0);
-        if (pi >= npar) break;
+        // parents are claimed 32 at a time (one atomic per chunk: levels
+        // past an instance's last level hold many parents that are skipped)
+        long long p0;
+        if (lane == 0) p0 = (long long)atomicAdd(&ctl->ctr[1], 32ull);
+        p0 = __shfl_sync(FULLMASK, p0, 0);
+        if (p0 >= npar) break;
+        const int cnt = npar - p0 < 32 ? (int)(npar - p0) : 32;
+        // lane t: whether parent p0 + t is expanded at this level
+        bool expand = false;
+        if (lane < cnt) {
+            const Node pn = B.node[pside][p0 + lane];
+            expand = (pn.flags & NODE_VALID) && (B.exhaustive || (pn.flags & NODE_FEASIBLE)) &&
+                     !B.ictl[pn.inst].stopped && level <= B.inst[pn.inst].k_max;
+        }
+        unsigned todo = __ballot_sync(FULLMASK, expand);
+    while (todo) {
+        const int t = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const long long pi = p0 + t;
         const Node par = B.node[pside][pi];
-        if (!(par.flags & NODE_VALID)) continue;
-        if (!B.exhaustive && !(par.flags & NODE_FEASIBLE)) continue;
         const InstDesc &I = B.inst[par.inst];
-        if (B.ictl[par.inst].stopped || level > I.k_max) continue;
         if (par.inst != cur_inst) {
             if (cur_inst >= 0 && lane == 0) {
                 atomicAdd((unsigned long long *)&B.ictl[cur_inst].lvl_cand, (unsigned long long)loc_cand);
@@ -619,6 +631,7 @@ __global__ void k_enumerate(DevBuffers B, int level)
                 }
             }
         }
+    }
     }
     if (cur_inst >= 0 && lane == 0) {
         atomicAdd((unsigned long long *)&B.ictl[cur_inst].lvl_cand, (unsigned long long)loc_cand);
