@@ -1823,7 +1823,9 @@ __device__ int lp2_dual_screen(const float *T, int m, int R2, int p, const float
         unsigned key = 0xffffffffu, kid = 0xffffffffu;
         int kq = -1;
         float dbest = 0.0f;
-#pragma unroll
+        // not unrolled: the kernel is bound by instruction fetch (the code of
+        // the three row slots would be three copies of this body)
+#pragma unroll 1
         for (int s = 0; s < NR; s++) {
             const int r = lane + 32 * s;
             if (r < R2 && !((basic >> s) & 1u)) {
