@@ -1970,14 +1970,54 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
             // the dual screen (mode 0, a box, p <= 6, at most 96 rows; its layout
             // needs rows of kDualLd floats in the slot) or the primal tableau
             constexpr bool dual = ROUTE == 0;
+            float bmax = 0.0f;
+            for (int ii = lane; ii < ncp; ii += 32) { const float v = fabsf(D.bt[ii]); if (v > bmax) bmax = v; }
+            bmax = warp_max(bmax);
+            bool done = false;
+            if constexpr (dual) {
+                // First the LP over the multiplier rows and the box alone: it
+                // drops the inactive rows, so its optimum bounds t* from above
+                // and a verified "not optimal" from it is final.  It settles
+                // most non-optimal sets (about nine in ten at |S| = 5 of the
+                // m = 62 instance) without the m - k inactive rows.
+                if (k > 0) {
+                    float amaxA = 0.0f;
+                    for (int a = lane; a < k; a += 32) {
+                        float *tr = Tb + (size_t)a * kDualLd;
+                        const float *lam = ws.Lam + a * P1;
+                        float rs = 0.0f;
+                        for (int cc = 0; cc < p; cc++) { tr[cc] = lam[cc]; rs += fabsf(lam[cc]); }
+                        for (int cc = p; cc < kDualMaxP; cc++) tr[cc] = 0.0f;
+                        tr[6] = 1.0f;
+                        tr[7] = -lam[p];
+                        rs += fabsf(lam[p]);
+                        amaxA = fmaxf(amaxA, rs);
+                    }
+                    for (int ii = lane; ii < ncp; ii += 32) {
+                        float *tr = Tb + (size_t)(k + ii) * kDualLd;
+                        for (int cc = 0; cc < kDualMaxP; cc++) tr[cc] = cc < p ? D.At[ii * p + cc] : 0.0f;
+                        tr[6] = 0.0f;
+                        tr[7] = D.bt[ii];
+                    }
+                    amaxA = warp_max(amaxA);
+                    const float scaleA = __fdividef(amaxA, rho) * (1.0f + (float)p * bmax);
+                    __syncwarp();
+                    float boundA;
+                    int pivA = 0;
+                    done = lp2_dual_screen(Tb, k, k + ncp, p, B.fpool + I.f_blo, B.fpool + I.f_bhi,
+                                           tol.margin_t32 * scaleA, tol.tol_piv32, tol.tol_dj32, tol.max_pivots,
+                                           tol.degen_switch, &pivA, &boundA);
+                    piv = pivA;
+                    if (done) { decided = true; status = LP_BOUND; t = boundA; }
+                    __syncwarp();
+                }
+            }
+            if (!done) {
             float t0, g0;
             // dual: rows straight into the dual layout; primal: rows into G,
             // kept unpivoted for the bound that verifies the verdict
             const float amax = dual ? region_rows<float, true>(D, I, nd.lo, nd.hi, k, ws, Tb, kDualLd, 7, &t0, &g0)
                                     : region_rows<float, true>(D, I, nd.lo, nd.hi, k, ws, nullptr, 0, 0, &t0, &g0);
-            float bmax = 0.0f;
-            for (int ii = lane; ii < ncp; ii += 32) { const float v = fabsf(D.bt[ii]); if (v > bmax) bmax = v; }
-            bmax = warp_max(bmax);
             // error scale of the FP32 rows: row magnitude / smallest Cholesky
             // pivot ratio, times the reach of theta inside the box (rho >
             // margin_licq, so the quotient is tame)
@@ -1992,8 +2032,10 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
                 }
                 __syncwarp();
                 float bound;
+                int pivB = 0;
                 decided = lp2_dual_screen(Tb, m, R2, p, B.fpool + I.f_blo, B.fpool + I.f_bhi, tol.margin_t32 * scale,
-                                          tol.tol_piv32, tol.tol_dj32, tol.max_pivots, tol.degen_switch, &piv, &bound);
+                                          tol.tol_piv32, tol.tol_dj32, tol.max_pivots, tol.degen_switch, &pivB, &bound);
+                piv += pivB;
                 status = LP_BOUND;
                 t = bound;
             } else {
@@ -2053,6 +2095,7 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
                     decided = bound < -tol.margin_t32 * scale;
                     t = bound;
                 }
+            }
             }
         }
         lc.c += piv;
