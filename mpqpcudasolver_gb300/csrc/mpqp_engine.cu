@@ -272,6 +272,7 @@ struct mpqp_plan {
     int grid_opt_lp = 0, grid_optfb_lp = 0;   // FP64 optimality kernels of the mpLP instances
     bool pooled = false;        // allocations came from the device pool
     int grid_opt2 = 0;          // grid of the primal route (grid_opt: the dual route)
+    int grid_opt3 = 0;          // grid of the dual route's second stage
     size_t smem_opt2 = 0;       // shared memory per block of the primal route
     int grid_enum = 0, grid_feas = 0, grid_lp1fb = 0, grid_opt = 0, grid_optfb = 0;
     size_t smem_feas = 0, smem_lp1fb = 0, smem_opt = 0, smem_optfb = 0;
@@ -466,8 +467,11 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
                   launch_optimality(B, P->tol, P->sd, level, true, P->grid_opt_lp, P->smem_opt, s));
             return MPQP_OK;
         }
-        if (P->screen_dual)
+        if (P->screen_dual) {
             L("k_opt_screen<dual>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 0, P->grid_opt, P->smem_opt, s));
+            L("k_opt_screen<dual,rows>",
+              launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 2, P->grid_opt3, P->smem_opt, s));
+        }
         if (P->screen_primal)
             L("k_opt_screen<primal>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 1, P->grid_opt2, P->smem_opt2, s));
         return MPQP_OK;
@@ -713,6 +717,7 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
                   ? grid_for(kernel_ptr("screen_dual"), P->smem_opt, &P->grid_opt, 32)
                   : grid_for(kernel_ptr("opt64"), P->smem_opt, &P->grid_opt)) ||
         (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_primal"), P->smem_opt2, &P->grid_opt2, 32) : 0) ||
+        (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_dual_rows"), P->smem_opt, &P->grid_opt3, 32) : 0) ||
         (rc = grid_for(kernel_ptr("opt_fp64"), P->smem_optfb, &P->grid_optfb)) ||
         (rc = P->has_lp && P->prec != PREC_MIXED ? grid_for(kernel_ptr("opt64_lp"), P->smem_opt, &P->grid_opt_lp) : 0) ||
         (rc = P->has_lp ? grid_for(kernel_ptr("opt_fp64_lp"), P->smem_optfb, &P->grid_optfb_lp) : 0)) {

@@ -143,6 +143,7 @@ struct Ctl {
     long long n_rec;            // records written so far
     long long rec_base;         // record index of the current level's first candidate
     long long n_q_lp1, n_q_opt; // FP64 fallback queue lengths
+    long long n_q_scr;          // sets the first stage of the dual screen left to its second
     unsigned long long ctr[8];  // work counters (reset every level)
     int overflow;               // bit mask of overflowed buffers
     int level;

@@ -1912,9 +1912,15 @@ __host__ __device__ __forceinline__ bool dual_route(int mode, const InstDesc &I,
     return mode == 0 && I.box && !I.lp && I.p <= kDualMaxP && I.m + I.ncp <= kDualMaxRows && sd.maxLD2 >= kDualLd;
 }
 
-template <int ROUTE>
+// STAGE (dual route only): 0 screens every set of the level with the
+// multiplier rows and the box and queues the sets that this does not settle;
+// 1 takes that queue through the full rows.  Two kernels, so that each warp's
+// instruction stream stays small (the kernel is bound by instruction fetch)
+// and the rarely needed full-row code does not share the cache with the rest.
+template <int ROUTE, int STAGE = 0>
 __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, SlotDims sd, int level, int mode)
 {
+    static_assert(ROUTE == 0 || STAGE == 0, "only the dual route has two stages");
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = lane_id();
     OptWs<float> ws;
@@ -1934,14 +1940,18 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
     }
     const int side = level & 1;
     Ctl *ctl = B.ctl;
-    const long long nn = ctl->n_node[side] < B.node_cap ? ctl->n_node[side] : B.node_cap;
+    const long long nn = STAGE == 0 ? (ctl->n_node[side] < B.node_cap ? ctl->n_node[side] : B.node_cap)
+                                    : (ctl->n_q_scr < B.q_cap ? ctl->n_q_scr : B.q_cap);
     LocalInstCounters lc;
     lc.reset(-1);
     for (;;) {
         long long x;
-        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[ROUTE == 0 ? 3 : 5], 1ull);
+        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[STAGE == 1 ? 6 : (ROUTE == 0 ? 3 : 5)], 1ull);
         x = __shfl_sync(FULLMASK, x, 0);
         if (x >= nn) break;
+        // stage 1 reads the queue of stage 0 (kept in q_lp1: the LP1 queue is
+        // consumed before the screen runs)
+        if (STAGE == 1) x = B.q_lp1[x];
         const Node nd = B.node[side][x];
         if ((nd.flags & (NODE_VALID | NODE_FEASIBLE)) != (NODE_VALID | NODE_FEASIBLE)) continue;
         const InstDesc &I = B.inst[nd.inst];
@@ -1974,7 +1984,7 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
             for (int ii = lane; ii < ncp; ii += 32) { const float v = fabsf(D.bt[ii]); if (v > bmax) bmax = v; }
             bmax = warp_max(bmax);
             bool done = false;
-            if constexpr (dual) {
+            if constexpr (dual && STAGE == 0) {
                 // First the LP over the multiplier rows and the box alone: it
                 // drops the inactive rows, so its optimum bounds t* from above
                 // and a verified "not optimal" from it is final.  It settles
@@ -2010,6 +2020,16 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
                     piv = pivA;
                     if (done) { decided = true; status = LP_BOUND; t = boundA; }
                     __syncwarp();
+                }
+                if (!done) {
+                    // to stage 1
+                    if (lane == 0) {
+                        const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_scr, 1ull);
+                        if (qi < B.q_cap) B.q_lp1[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
+                    }
+                    lc.c += piv;
+                    __syncwarp();
+                    continue;
                 }
             }
             if (!done) {
@@ -2268,6 +2288,7 @@ __global__ void k_finalize(DevBuffers B, int level)
         for (int c = 0; c < 8; c++) ctl->ctr[c] = 0;
         ctl->n_q_lp1 = 0;
         ctl->n_q_opt = 0;
+        ctl->n_q_scr = 0;
         ctl->level = level;
     }
 }
@@ -2405,6 +2426,7 @@ const void *kernel_ptr(const char *name)
         {"opt_fp64", (const void *)k_optimality_fp64<false>},
         {"opt_fp64_lp", (const void *)k_optimality_fp64<true>},
         {"screen_dual", (const void *)k_opt_screen<0>},
+        {"screen_dual_rows", (const void *)k_opt_screen<0, 1>},
         {"screen_primal", (const void *)k_opt_screen<1>},
         {"level0_64", (const void *)k_level0<double>},
         {"level0_32", (const void *)k_level0<float>},
@@ -2453,7 +2475,9 @@ cudaError_t launch_optimality(const DevBuffers &B, const Tol &tol, const SlotDim
 cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode, int route,
                               int grid, size_t smem, cudaStream_t s)
 {
+    // route 0: the dual route's first stage, 2: its second stage, 1: the primal route
     if (route == 0) k_opt_screen<0><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
+    else if (route == 2) k_opt_screen<0, 1><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
     else k_opt_screen<1><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
     return cudaGetLastError();
 }
