@@ -1116,7 +1116,10 @@ __device__ void mplp_multipliers(const DevBuffers &B, const InstDesc &I, int k, 
 }
 
 // Cholesky of Wm[S,S] (row-oriented; each entry accumulates in ascending l),
-// then Y = R^-T [Wh_S | wc_S] and Lambda = R^-1 Y (lane per column).
+// then Y = R^-T [Wh_S | wc_S] and Lambda = R^-1 Y (lane per column).  FP64
+// divides by the pivots (the oracle's operations); the FP32 screen keeps the
+// correctly rounded reciprocal of each pivot on the diagonal and multiplies
+// (one rounding more per entry, well inside the screen's margin).
 // Returns 0 on success, 1 when a pivot fails the threshold thr (relative to
 // the diagonal).  Fills ws.S with the sorted active set.
 template <typename T>
@@ -1140,8 +1143,13 @@ __device__ int kkt_factor(const KktData<T> &D, const InstDesc &I, uint64_t lo, u
             T acc = d0;
             for (int l = 0; l < a; l++) acc = xfma(-R[l * k + a], R[l * k + a], acc);
             if (!(acc > thr * d0)) fail = 1;
+            else if constexpr (sizeof(T) == 4) R[a * k + a] = __frcp_rn(__fsqrt_rn(acc));   // FP32: 1 / pivot
             else R[a * k + a] = xsqrt(acc);
-            if (rho_out && !fail) { const T rr = acc / d0; if (rr < rho) rho = rr; }
+            if (rho_out && !fail) {
+                T rr;
+                if constexpr (sizeof(T) == 4) rr = __fdividef(acc, d0); else rr = acc / d0;
+                if (rr < rho) rho = rr;
+            }
         }
         fail = __shfl_sync(FULLMASK, fail, 0);
         if (fail) return 1;
@@ -1149,7 +1157,8 @@ __device__ int kkt_factor(const KktData<T> &D, const InstDesc &I, uint64_t lo, u
         for (int b = a + 1 + lane; b < k; b += 32) {
             T acc = D.Wm[(size_t)S[a] * m + S[b]];
             for (int l = 0; l < a; l++) acc = xfma(-R[l * k + a], R[l * k + b], acc);
-            R[a * k + b] = xdiv(acc, R[a * k + a]);
+            if constexpr (sizeof(T) == 4) R[a * k + b] = acc * R[a * k + a];
+            else R[a * k + b] = xdiv(acc, R[a * k + a]);
         }
         __syncwarp();
     }
@@ -1158,12 +1167,14 @@ __device__ int kkt_factor(const KktData<T> &D, const InstDesc &I, uint64_t lo, u
         for (int a = 0; a < k; a++) {
             T acc = (cc < p) ? D.Wh[(size_t)S[a] * p + cc] : D.wc[S[a]];
             for (int l = 0; l < a; l++) acc = xfma(-R[l * k + a], Y[l * P1 + cc], acc);
-            Y[a * P1 + cc] = xdiv(acc, R[a * k + a]);
+            if constexpr (sizeof(T) == 4) Y[a * P1 + cc] = acc * R[a * k + a];
+            else Y[a * P1 + cc] = xdiv(acc, R[a * k + a]);
         }
         for (int a = k - 1; a >= 0; a--) {
             T acc = Y[a * P1 + cc];
             for (int l = a + 1; l < k; l++) acc = xfma(-R[a * k + l], Lam[l * P1 + cc], acc);
-            Lam[a * P1 + cc] = xdiv(acc, R[a * k + a]);
+            if constexpr (sizeof(T) == 4) Lam[a * P1 + cc] = acc * R[a * k + a];
+            else Lam[a * P1 + cc] = xdiv(acc, R[a * k + a]);
         }
     }
     __syncwarp();
