@@ -281,9 +281,12 @@ __device__ int warp_simplex(const Lp<T> &L, T tol_piv, T tol_dj, int max_piv, in
 constexpr int kFastRows = 96;
 constexpr int kFastChunks = 6;
 
+// fix_lo/fix_hi (optional): variables with id fix_base + i, i in the mask,
+// stay at zero while nonbasic (never priced in)
 template <int NCH>
 __device__ int simplex_fast32(float *tab, int ld, int nrows, int ncols, uint8_t *bid, uint8_t *nid, float tol_piv,
-                              float tol_dj, int max_piv, int degen_switch, int *piv_out)
+                              float tol_dj, int max_piv, int degen_switch, int *piv_out, uint64_t fix_lo = 0,
+                              uint64_t fix_hi = 0, int fix_base = 0)
 {
     constexpr int NR = kFastRows / 32;
     const int lane = lane_id();
@@ -308,7 +311,9 @@ __device__ int simplex_fast32(float *tab, int ld, int nrows, int ncols, uint8_t 
         int kidx = -1;
         if (lane < ncols) {
             const float sc = nidl < nfree ? fabsf(ob) : ob;
-            if (sc > tol_dj) { key = bland ? 0u : ~key_of(sc); kid = (unsigned)nidl; kidx = lane; }
+            const int fi = nidl - fix_base;
+            const bool fixed = fi >= 0 && fi < 128 && mask_has(fix_lo, fix_hi, fi);
+            if (sc > tol_dj && !fixed) { key = bland ? 0u : ~key_of(sc); kid = (unsigned)nidl; kidx = lane; }
         }
         const int q = warp_argmin(key, kid, kidx);
         if (q < 0) { status = LP_OPTIMAL; break; }
@@ -403,18 +408,19 @@ __device__ int simplex_fast32(float *tab, int ld, int nrows, int ncols, uint8_t 
 // most MAXCH chunks), else the generic loop (the same pivots either way)
 template <int MAXCH>
 __device__ __forceinline__ int warp_simplex_f32(const Lp<float> &L, float tol_piv, float tol_dj, int max_piv,
-                                                int degen_switch, int *piv_out)
+                                                int degen_switch, int *piv_out, uint64_t fix_lo = 0,
+                                                uint64_t fix_hi = 0, int fix_base = 0)
 {
     static_assert(MAXCH >= 1 && MAXCH <= kFastChunks, "chunk count");
     const int nch = (L.ncols + 4) >> 2;
     if (L.nrows <= kFastRows && L.nfree == L.ncols && (L.ld & 3) == 0 && nch <= MAXCH) {
         switch (nch) {
-        case 1: return simplex_fast32<1>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out);
-        case 2: return simplex_fast32<2>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out);
-        case 3: if constexpr (MAXCH >= 3) return simplex_fast32<3>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out);
-        case 4: if constexpr (MAXCH >= 4) return simplex_fast32<4>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out);
-        case 5: if constexpr (MAXCH >= 5) return simplex_fast32<5>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out);
-        case 6: if constexpr (MAXCH >= 6) return simplex_fast32<6>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out);
+        case 1: return simplex_fast32<1>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base);
+        case 2: return simplex_fast32<2>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base);
+        case 3: if constexpr (MAXCH >= 3) return simplex_fast32<3>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base);
+        case 4: if constexpr (MAXCH >= 4) return simplex_fast32<4>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base);
+        case 5: if constexpr (MAXCH >= 5) return simplex_fast32<5>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base);
+        case 6: if constexpr (MAXCH >= 6) return simplex_fast32<6>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base);
         default: break;
         }
     }
@@ -860,7 +866,11 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         Lp<T> L{tab, ld, M1, nv, nv, bid, nid};
         int piv = 0;
         int st;
-        if constexpr (sizeof(T) == 4) st = warp_simplex_f32<kFastChunks>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv);
+        // FP32: the slacks of the parent's set stay at zero while nonbasic
+        // (the parent is feasible: on that face the objective is w_j alone, so
+        // the LP is min w_j there, the same verdict without detours through w_S)
+        if constexpr (sizeof(T) == 4) st = warp_simplex_f32<kFastChunks>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv,
+                                                                          par.lo, par.hi, nv);
         else st = warp_simplex<T>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv);
         const T z = obj[nv];
         uint64_t lo = par.lo, hi = par.hi;
