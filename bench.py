@@ -395,8 +395,8 @@ def run_ours(args):
     peaks = measured_peaks()
     peak_src = peaks["source"] + " (MEASURED_PEAKS.json hbm_gbs)"
 
-    def roofline(kname, step_bytes, units, traffic_file, per_unit_text):
-        ms, nl = kt.get(kname, (0.0, 0))
+    def roofline(kname, step_bytes, units, traffic_file, per_unit_text, timed=None):
+        ms, nl = timed if timed else kt.get(kname, (0.0, 0))
         nl = max(nl, 1)
         achieved = step_bytes / (ms / 1e3) / 1e9 if ms > 0 else None
         return {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
@@ -407,11 +407,21 @@ def run_ours(args):
                 "per_unit": per_unit_text}
 
     n_eval = res.total("feasible")
-    opt_name = next((k for k in kt if k.startswith("k_opt_screen")), f"k_optimality<{tname}>")
+    # the optimality screen: both stages of the dual route (and the primal
+    # route) as one logical kernel
+    screen = [k for k in kt if k.startswith("k_opt_screen")]
+    if screen:
+        opt_name = "+".join(screen)
+        opt_timed = (sum(kt[k][0] for k in screen), max(kt[k][1] for k in screen))
+    else:
+        opt_name, opt_timed = f"k_optimality<{tname}>", None
     roof = roofline(opt_name, opt_algorithmic_bytes(probs, res, elem), n_eval,
                     "opt_traffic.json",
                     "per evaluated (feasible) set: 8*m*(n+p+1) KKT gather + 8*R*(p+2) region tableau + 16 B "
-                    "mask/verdict, plus 2*(R+1)*(p+2)*s per LP2/Chebyshev pivot (s = 4 B FP32)")
+                    "mask/verdict, plus 2*(R+1)*(p+2)*s per LP2/Chebyshev pivot (s = 4 B FP32); the model "
+                    "counts the full region tableau of every set, which the screen's first stage builds only "
+                    "for the multiplier rows and the box (the full rows for about 4 % of the sets), so this "
+                    "fraction overstates the bytes moved", opt_timed)
     roof_lp1 = roofline(f"k_feasibility<{tname}>", lp1_hbm_bytes(probs, kmax, res, elem),
                         res.candidates - len(probs), "lp1_traffic.json",
                         "per candidate (levels >= 1): 8 B record + 48 B parent node + parent LP1 tableau "
@@ -431,8 +441,10 @@ def run_ours(args):
         "fp64_fallbacks": {"lp1": res.total("fallback_lp1"), "optimality": res.total("fallback_opt")},
         "fp64_path": fp64,
         "speedup_vs_fp64": (value / world / fp64["value"]) if fp64 else None,
-        "roofline": roof,
-        "roofline_lp1": roof_lp1,
+        # the dominant kernel's roofline; the other large kernel beside it
+        "roofline": roof_lp1 if (dominant or "").startswith("k_feasibility") else roof,
+        "roofline_screen" if (dominant or "").startswith("k_feasibility") else "roofline_lp1":
+            roof if (dominant or "").startswith("k_feasibility") else roof_lp1,
         "model_bytes_touched_per_s": model_bytes_touched(probs, res, elem) / (ms_step / 1e3),
         "kernels_ms_per_step": {k: round(v[0], 3) for k, v in sorted(kt.items(), key=lambda kv: -kv[1][0])},
         "dominant_kernel": dominant,
