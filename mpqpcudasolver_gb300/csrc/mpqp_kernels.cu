@@ -684,7 +684,8 @@ __device__ __forceinline__ void warp_copy_v(T *dst, const T *src, int n)
 template <typename TT, typename TS>
 __device__ long long store_node(const DevBuffers &B, int side, int level, const InstDesc &I, int inst,
                                 uint64_t lo, uint64_t hi, bool feasible, const TS *tab, const uint8_t *ids,
-                                long long rec, long long hcap, int extra_flags, int src_ld = 0, bool bulk = false)
+                                long long rec, long long hcap, int extra_flags, int src_ld = 0, bool bulk = false,
+                                long long pre_idx = -1)
 {
     const int lane = lane_id();
     Ctl *ctl = B.ctl;
@@ -693,7 +694,9 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
     if (lane == 0) {
         // one arena per kind, side 0 filled upward from 0, side 1 downward
         // from the top; the other side holds the parents and is fixed here
-        idx = (long long)atomicAdd((unsigned long long *)&ctl->n_node[side], 1ull);
+        // pre_idx >= 0: the caller's slot (a candidate's node lives at the
+        // candidate's index)
+        idx = pre_idx >= 0 ? pre_idx : (long long)atomicAdd((unsigned long long *)&ctl->n_node[side], 1ull);
         if (idx >= B.node_cap) { atomicOr(&ctl->overflow, OV_NODE); idx = -1; }
         if (need_tab && idx >= 0) {
             const long long told = (long long)atomicAdd((unsigned long long *)&ctl->tab_used[side], (unsigned long long)I.tab_elems);
@@ -795,6 +798,15 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         if (w0 >= wend || abort) break;
         const int cnt = wend - w0 < kFeasChunk ? (int)(wend - w0) : kFeasChunk;
         const Cand mine = lane < cnt ? B.cand[w0 + lane] : Cand{-1, 0};
+        // candidate w's node goes to slot w (also when the FP64 re-solve
+        // stores it); a candidate that stores none leaves an invalid record
+        const long long nbase = w0;
+        if (lane == 0) atomicMax((unsigned long long *)&ctl->n_node[side], (unsigned long long)(w0 + cnt));
+        if (lane < cnt && nbase + lane < B.node_cap) {
+            Node gap;
+            gap.lo = 0; gap.hi = 0; gap.inst = 0; gap.flags = 0; gap.tab_off = -1; gap.ids_off = -1; gap.rec = -1;
+            B.node[side][nbase + lane] = gap;
+        }
         // lane t holds candidate t's parent tableau offset (for the prefetch)
         const long long my_toff = lane < cnt ? B.node[pside][mine.parent].tab_off : -1;
         const int my_inst = lane < cnt ? B.node[pside][mine.parent].inst : 0;
@@ -947,7 +959,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         if (feasible) { lc.a++; lc.c += (long long)mask_digest(lo, hi); }
         if (feasible || B.exhaustive)
             store_node<T, T>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap, par.flags & NODE_FP64CHAIN,
-                             0, true);
+                             0, true, nbase + t);
     }
     }
     if (lane == 0) bulk_wait_all();
@@ -1020,7 +1032,7 @@ __global__ void __launch_bounds__(128) k_lp1_fp64(DevBuffers B, Tol tol, SlotDim
         }
         if (feasible || B.exhaustive)
             store_node<float, double>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap, NODE_FP64CHAIN,
-                                      I.ld1d);
+                                      I.ld1d, false, w);
     }
 }
 
