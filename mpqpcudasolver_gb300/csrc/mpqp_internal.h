@@ -90,6 +90,10 @@ struct Node {                   // a feasible (or, when exhaustive, any) active 
 // from, needed the FP64 re-solve (mixed precision); FP32 "infeasible"
 // verdicts below such a node are re-solved in FP64 too.
 enum NodeFlags : int { NODE_FEASIBLE = 1, NODE_VALID = 2, NODE_FP64CHAIN = 4 };
+// bits 8..16 of the flags: 1 + the live rows of the stored FP32 LP1 tableau
+// (rows of basic free variables dropped, the objective row right after them);
+// 0: all M1 rows
+constexpr int kNodeRowsShift = 8;
 
 struct Cand { int parent; int j; };
 

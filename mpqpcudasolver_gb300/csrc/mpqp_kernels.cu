@@ -52,6 +52,14 @@ __device__ __forceinline__ bool mask_has(uint64_t lo, uint64_t hi, int j)
 
 __device__ __forceinline__ int mask_pop(uint64_t lo, uint64_t hi) { return __popcll(lo) + __popcll(hi); }
 
+// live rows of a stored LP1 tableau (node flags bits 8..16 hold rows + 1;
+// 0: all M1 rows)
+__device__ __forceinline__ int node_rows(int flags, int M1)
+{
+    const int r = (flags >> kNodeRowsShift) & 0x1ff;
+    return r > 0 ? r - 1 : M1;
+}
+
 // number of mask bits below position i
 __device__ __forceinline__ int mask_rank(uint64_t lo, uint64_t hi, int i)
 {
@@ -282,13 +290,18 @@ constexpr int kFastRows = 96;
 constexpr int kFastChunks = 6;
 
 // fix_lo/fix_hi (optional): variables with id fix_base + i, i in the mask,
-// stay at zero while nonbasic (never priced in)
-template <int NCH>
+// stay at zero while nonbasic (never priced in).  NRS: row slots per lane
+// (nrows <= 32 * NRS).  compact: a free variable that enters the basis never
+// leaves it again, and its row is read by no later decision (pricing uses
+// the objective row, the ratio test and the pivot only slack rows), so the
+// row is dropped -- the last row moves into its place and nrows shrinks;
+// *nrows_out receives the final count (the objective row stays where it was).
+template <int NCH, int NRS>
 __device__ int simplex_fast32(float *tab, int ld, int nrows, int ncols, uint8_t *bid, uint8_t *nid, float tol_piv,
-                              float tol_dj, int max_piv, int degen_switch, int *piv_out, uint64_t fix_lo = 0,
-                              uint64_t fix_hi = 0, int fix_base = 0)
+                              float tol_dj, int max_piv, int degen_switch, int *piv_out, uint64_t fix_lo,
+                              uint64_t fix_hi, int fix_base, bool compact, int *nrows_out)
 {
-    constexpr int NR = kFastRows / 32;
+    constexpr int NR = NRS;
     const int lane = lane_id();
     const int nfree = ncols;
     int rowoff[NR], bidr[NR];
@@ -390,6 +403,26 @@ __device__ int simplex_fast32(float *tab, int ld, int nrows, int ncols, uint8_t 
         }
         if (lane == q) nidl = lid;
         __syncwarp();
+        if (compact && eid < nfree) {
+            // row r now belongs to a free variable: the last row takes its place
+            const int last = nrows - 1;
+            if (r != last) {
+                const float v = lane <= ncols ? tab[last * ld + lane] : 0.0f;
+                int lb = 0;
+#pragma unroll
+                for (int s = 0; s < NR; s++) if (s == (last >> 5)) lb = bidr[s];
+                lb = __shfl_sync(FULLMASK, lb, last & 31);
+                if (lane <= ncols) Rp[lane] = v;
+                if (lane == owner) {
+#pragma unroll
+                    for (int s = 0; s < NR; s++) if (s == oslot) bidr[s] = lb;
+                }
+            }
+            nrows = last;
+#pragma unroll
+            for (int s = 0; s < NR; s++) valid[s] = lane + 32 * s < nrows;
+            __syncwarp();
+        }
         piv++;
         degen = (rr == 0.0f) ? degen + 1 : 0;
         bland = degen >= degen_switch;
@@ -401,29 +434,49 @@ __device__ int simplex_fast32(float *tab, int ld, int nrows, int ncols, uint8_t 
     for (int s = 0; s < NR; s++) if (valid[s]) bid[lane + 32 * s] = (uint8_t)bidr[s];
     __syncwarp();
     *piv_out = piv;
+    if (nrows_out) *nrows_out = nrows;
     return status;
 }
 
 // warp_simplex for an FP32 tableau: simplex_fast32 when it fits (rows of at
 // most MAXCH chunks), else the generic loop (the same pivots either way)
+template <int NCH>
+__device__ __forceinline__ int simplex_fast32_rows(const Lp<float> &L, float tol_piv, float tol_dj, int max_piv,
+                                                   int degen_switch, int *piv_out, uint64_t fix_lo, uint64_t fix_hi,
+                                                   int fix_base, bool compact, int *nrows_out)
+{
+    if (L.nrows <= 32)
+        return simplex_fast32<NCH, 1>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv,
+                                      degen_switch, piv_out, fix_lo, fix_hi, fix_base, compact, nrows_out);
+    if (L.nrows <= 64)
+        return simplex_fast32<NCH, 2>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv,
+                                      degen_switch, piv_out, fix_lo, fix_hi, fix_base, compact, nrows_out);
+    return simplex_fast32<NCH, 3>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv,
+                                  degen_switch, piv_out, fix_lo, fix_hi, fix_base, compact, nrows_out);
+}
+
+// compact / nrows_out: see simplex_fast32 (the generic loop never compacts;
+// *nrows_out is then L.nrows)
 template <int MAXCH>
 __device__ __forceinline__ int warp_simplex_f32(const Lp<float> &L, float tol_piv, float tol_dj, int max_piv,
                                                 int degen_switch, int *piv_out, uint64_t fix_lo = 0,
-                                                uint64_t fix_hi = 0, int fix_base = 0)
+                                                uint64_t fix_hi = 0, int fix_base = 0, bool compact = false,
+                                                int *nrows_out = nullptr)
 {
     static_assert(MAXCH >= 1 && MAXCH <= kFastChunks, "chunk count");
     const int nch = (L.ncols + 4) >> 2;
     if (L.nrows <= kFastRows && L.nfree == L.ncols && (L.ld & 3) == 0 && nch <= MAXCH) {
         switch (nch) {
-        case 1: return simplex_fast32<1>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base);
-        case 2: return simplex_fast32<2>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base);
-        case 3: if constexpr (MAXCH >= 3) return simplex_fast32<3>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base);
-        case 4: if constexpr (MAXCH >= 4) return simplex_fast32<4>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base);
-        case 5: if constexpr (MAXCH >= 5) return simplex_fast32<5>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base);
-        case 6: if constexpr (MAXCH >= 6) return simplex_fast32<6>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base);
+        case 1: return simplex_fast32_rows<1>(L, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base, compact, nrows_out);
+        case 2: return simplex_fast32_rows<2>(L, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base, compact, nrows_out);
+        case 3: if constexpr (MAXCH >= 3) return simplex_fast32_rows<3>(L, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base, compact, nrows_out);
+        case 4: if constexpr (MAXCH >= 4) return simplex_fast32_rows<4>(L, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base, compact, nrows_out);
+        case 5: if constexpr (MAXCH >= 5) return simplex_fast32_rows<5>(L, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base, compact, nrows_out);
+        case 6: if constexpr (MAXCH >= 6) return simplex_fast32_rows<6>(L, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base, compact, nrows_out);
         default: break;
         }
     }
+    if (nrows_out) *nrows_out = L.nrows;
     return warp_simplex<float>(L, tol_piv, tol_dj, max_piv, degen_switch, piv_out);
 }
 
@@ -685,7 +738,7 @@ template <typename TT, typename TS>
 __device__ long long store_node(const DevBuffers &B, int side, int level, const InstDesc &I, int inst,
                                 uint64_t lo, uint64_t hi, bool feasible, const TS *tab, const uint8_t *ids,
                                 long long rec, long long hcap, int extra_flags, int src_ld = 0, bool bulk = false,
-                                long long pre_idx = -1)
+                                long long pre_idx = -1, int rows_store = -1)
 {
     const int lane = lane_id();
     Ctl *ctl = B.ctl;
@@ -726,7 +779,9 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
             fence_proxy_async_smem();
             __syncwarp();
             if (lane == 0) {
-                bulk_store(dst, tab, (unsigned)(I.tab_elems * sizeof(TT)));
+                // rows_store >= 0: the live rows and the objective row after them
+                bulk_store(dst, tab, rows_store >= 0 ? (unsigned)((rows_store + 1) * I.ld1 * sizeof(TT))
+                                                     : (unsigned)(I.tab_elems * sizeof(TT)));
                 bulk_store(B.ids[side] + ioff, ids, (unsigned)I.ids_bytes);
                 bulk_commit();
             }
@@ -747,7 +802,9 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
     }
     if (lane == 0) {
         Node nd;
-        nd.lo = lo; nd.hi = hi; nd.inst = inst; nd.flags = NODE_VALID | (feasible ? NODE_FEASIBLE : 0) | extra_flags;
+        nd.lo = lo; nd.hi = hi; nd.inst = inst;
+        nd.flags = NODE_VALID | (feasible ? NODE_FEASIBLE : 0) | extra_flags |
+                   (rows_store >= 0 ? (rows_store + 1) << kNodeRowsShift : 0);
         nd.tab_off = toff; nd.ids_off = ioff; nd.rec = rec;
         B.node[side][idx] = nd;
         // the hash serves the subset test of the next level only
@@ -842,6 +899,9 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
             lc.reset(inst);
         }
         const int M1 = I.M1, nv = I.nv, ld = I.ld1;
+        // the parent's live rows (FP32 tableaus drop the rows of basic free
+        // variables; the objective row follows the live rows)
+        const int prows = node_rows(par.flags, M1);
         // stage the parent tableau and basis: one bulk copy each, completing
         // on the warp's mbarrier (this warp's earlier accesses to the slot,
         // and the bulk store of the previous child, come first)
@@ -849,7 +909,8 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         __syncwarp();
         if (lane == 0) {
             bulk_wait_read();
-            const unsigned tb = (unsigned)(I.tab_elems * sizeof(T)), ib = (unsigned)I.ids_bytes;
+            const unsigned tb = mixed ? (unsigned)((prows + 1) * ld * sizeof(T)) : (unsigned)(I.tab_elems * sizeof(T));
+            const unsigned ib = (unsigned)I.ids_bytes;
             mbar_expect(bar, tb + ib);
             bulk_load(tab, (const T *)B.tab[pside] + par.tab_off, tb, bar);
             bulk_load(ids, B.ids[pside] + par.ids_off, ib, bar);
@@ -862,11 +923,11 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         }
         parity ^= 1u;
         uint8_t *bid = ids, *nid = ids + M1;
-        T *obj = tab + (size_t)M1 * ld;
+        T *obj = tab + (size_t)prows * ld;
         // objective += w_j
         const int wid = nv + c.j;
         int rho = -1;
-        for (int i = lane; i < M1; i += 32) if (bid[i] == wid) rho = i;
+        for (int i = lane; i < prows; i += 32) if (bid[i] == wid) rho = i;
         rho = __reduce_max_sync(FULLMASK, rho);
         if (rho >= 0) {
             const T *row = tab + (size_t)rho * ld;
@@ -875,14 +936,16 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
             for (int cc = lane; cc < nv; cc += 32) if (nid[cc] == wid) obj[cc] = obj[cc] - T(1);
         }
         __syncwarp();
-        Lp<T> L{tab, ld, M1, nv, nv, bid, nid};
+        Lp<T> L{tab, ld, prows, nv, nv, bid, nid};
         int piv = 0;
         int st;
+        int rows = prows;   // live rows after the simplex
         // FP32: the slacks of the parent's set stay at zero while nonbasic
         // (the parent is feasible: on that face the objective is w_j alone, so
-        // the LP is min w_j there, the same verdict without detours through w_S)
+        // the LP is min w_j there, the same verdict without detours through w_S),
+        // and rows of free variables that enter the basis are dropped
         if constexpr (sizeof(T) == 4) st = warp_simplex_f32<kFastChunks>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv,
-                                                                          par.lo, par.hi, nv);
+                                                                          par.lo, par.hi, nv, true, &rows);
         else st = warp_simplex<T>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv);
         const T z = obj[nv];
         uint64_t lo = par.lo, hi = par.hi;
@@ -899,7 +962,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
                 // (~ |B^-1 N|), by which the FP32 errors of the basic values grow
                 bool s_basic = false;
                 T minb = pos_inf<T>(), gmax = T(1);
-                for (int i = lane; i < M1; i += 32) {
+                for (int i = lane; i < rows; i += 32) {
                     const T *Ti = tab + (size_t)i * ld;
                     int j = 0;
                     if constexpr (sizeof(T) == 4) {
@@ -957,9 +1020,15 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
             continue;
         }
         if (feasible) { lc.a++; lc.c += (long long)mask_digest(lo, hi); }
-        if (feasible || B.exhaustive)
+        if (feasible || B.exhaustive) {
+            if (mixed && rows != prows && level < I.k_max) {
+                // the objective row follows the live rows in the stored tableau
+                for (int cc = lane; cc < ld; cc += 32) tab[(size_t)rows * ld + cc] = obj[cc];
+                __syncwarp();
+            }
             store_node<T, T>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap, par.flags & NODE_FP64CHAIN,
-                             0, true, nbase + t);
+                             0, true, nbase + t, mixed ? rows : -1);
+        }
     }
     }
     if (lane == 0) bulk_wait_all();
