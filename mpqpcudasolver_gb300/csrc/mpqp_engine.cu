@@ -26,6 +26,7 @@ size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd);
 size_t feas_smem_per_warp(int prec_bytes, const SlotDims &sd);
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd);
 size_t screen_smem_per_warp(const SlotDims &sd, int route);
+size_t screen_tiles_smem(const SlotDims &sd);
 bool screen_dual_route(int mode, const InstDesc &I, const SlotDims &sd);
 size_t laws_smem_per_warp(const SlotDims &sd);
 const void *kernel_ptr(const char *name);
@@ -273,6 +274,8 @@ struct mpqp_plan {
     bool pooled = false;        // allocations came from the device pool
     int grid_opt2 = 0;          // grid of the primal route (grid_opt: the dual route)
     int grid_opt3 = 0;          // grid of the dual route's second stage
+    int grid_tiles = 0;         // the dual route's first stage (two sets per warp)
+    size_t smem_tiles = 0;
     size_t smem_opt2 = 0;       // shared memory per block of the primal route
     int grid_enum = 0, grid_feas = 0, grid_lp1fb = 0, grid_opt = 0, grid_optfb = 0;
     size_t smem_feas = 0, smem_lp1fb = 0, smem_opt = 0, smem_optfb = 0;
@@ -468,7 +471,7 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
             return MPQP_OK;
         }
         if (P->screen_dual) {
-            L("k_opt_screen<dual>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 0, P->grid_opt, P->smem_opt, s));
+            L("k_opt_screen<dual>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 0, P->grid_tiles, P->smem_tiles, s));
             L("k_opt_screen<dual,rows>",
               launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 2, P->grid_opt3, P->smem_opt, s));
         }
@@ -703,6 +706,7 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
     // mixed precision: the grouped FP32 screen, one warp per block
     P->smem_opt = P->prec == PREC_MIXED ? screen_smem_per_warp(sd, 0) : 4 * opt_smem_per_warp(8, sd);
     P->smem_opt2 = screen_smem_per_warp(sd, 1);
+    P->smem_tiles = screen_tiles_smem(sd);
     for (const InstDesc &d : P->desc) {
         if (d.lp) P->has_lp = true; else P->has_qp = true;
         if (P->prec != PREC_MIXED) continue;
@@ -718,6 +722,7 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
                   : grid_for(kernel_ptr("opt64"), P->smem_opt, &P->grid_opt)) ||
         (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_primal"), P->smem_opt2, &P->grid_opt2, 32) : 0) ||
         (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_dual_rows"), P->smem_opt, &P->grid_opt3, 32) : 0) ||
+        (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_dual_tiles"), P->smem_tiles, &P->grid_tiles, 32) : 0) ||
         (rc = grid_for(kernel_ptr("opt_fp64"), P->smem_optfb, &P->grid_optfb)) ||
         (rc = P->has_lp && P->prec != PREC_MIXED ? grid_for(kernel_ptr("opt64_lp"), P->smem_opt, &P->grid_opt_lp) : 0) ||
         (rc = P->has_lp ? grid_for(kernel_ptr("opt_fp64_lp"), P->smem_optfb, &P->grid_optfb_lp) : 0)) {

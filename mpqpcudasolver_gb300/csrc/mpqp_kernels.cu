@@ -17,6 +17,8 @@
 // multiply-add, sums in ascending index order, IEEE division and square root,
 // compiled with -fmad=false.  This is the operation order of the CPU oracle,
 // so FP64 LP values and verdicts are bit-identical to it.
+#include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -1809,7 +1811,7 @@ __device__ __forceinline__ float warp_sum(float v)
 constexpr int kDualMaxP = 6;      // p <= 6
 constexpr int kDualMaxRows = 96;
 constexpr int kDualLd = 12;       // row stride of the dual layout (conflict-free 128-bit loads)
-enum : int { LP_BOUND = 5 };      // record status: "not optimal" proven by a dual bound (t = the bound)
+enum : int { LP_BOUND = 6 };      // record status: "not optimal" proven by a dual bound (t = the bound)
 
 // Dual bound of LP2 for an instance whose parameter set is a box
 // lo <= theta <= hi (constraint rows m..m+2p-1: theta_c <= hi_c scaled, then
@@ -2012,6 +2014,372 @@ __host__ __device__ inline size_t screen_warp_bytes(const SlotDims &sd, int rout
 __host__ __device__ __forceinline__ bool dual_route(int mode, const InstDesc &I, const SlotDims &sd)
 {
     return mode == 0 && I.box && !I.lp && I.p <= kDualMaxP && I.m + I.ncp <= kDualMaxRows && sd.maxLD2 >= kDualLd;
+}
+
+// ---------------------------------------------------------------------
+// Screen stage 0 on half-warps
+// ---------------------------------------------------------------------
+// Stage 0 of the dual route works on small LPs -- the k multiplier rows and
+// the 2p box rows (k + 2p <= 44), a basis of p + 1 <= 7 -- so a full warp
+// left half of its lanes idle.  Here each 16-thread tile of a warp screens its
+// own set: the same operations as kkt_factor<float> and lp2_dual_screen, with
+// tile-wide shuffles and reductions.
+namespace cgx = cooperative_groups;
+constexpr int kTileW = 16;
+constexpr int kTileRows = 48;                  // k + 2p rows, three slots of 16
+using ScreenTile = cgx::thread_block_tile<kTileW, cgx::thread_block>;
+
+__device__ __forceinline__ int tile_argmin(const ScreenTile &t, unsigned key, unsigned id, int idx)
+{
+    const unsigned kmin = cgx::reduce(t, key, cgx::less<unsigned>());
+    if (kmin == 0xffffffffu) return -1;
+    const bool m = key == kmin;
+    const unsigned idm = cgx::reduce(t, m ? id : 0xffffffffu, cgx::less<unsigned>());
+    const unsigned win = t.ballot(m && id == idm);
+    return t.shfl(idx, __ffs(win) - 1);
+}
+
+__device__ __forceinline__ float tile_max(const ScreenTile &t, float v)
+{
+#pragma unroll
+    for (int off = kTileW / 2; off; off >>= 1) v = fmaxf(v, t.shfl_xor(v, off));
+    return v;
+}
+
+__device__ __forceinline__ float tile_sum(const ScreenTile &t, float v)
+{
+#pragma unroll
+    for (int off = kTileW / 2; off; off >>= 1) v += t.shfl_xor(v, off);
+    return v;
+}
+
+// Stage-0 slot of one tile: R (maxK^2), Y and Lambda (maxK x P1), S, the
+// dual-layout rows (k + 2p <= maxK + 2 kDualMaxP rows of kDualLd floats)
+__host__ __device__ inline int tile_rows(const SlotDims &sd)
+{
+    return sd.maxK + 2 * kDualMaxP < kTileRows ? sd.maxK + 2 * kDualMaxP : kTileRows;
+}
+__host__ __device__ inline size_t tile_slot_bytes(const SlotDims &sd)
+{
+    return align16((size_t)sd.maxK * sd.maxK * 4) + 2 * align16((size_t)sd.maxK * sd.maxP1 * 4) +
+           align16((size_t)sd.maxK * sizeof(int)) + align16((size_t)tile_rows(sd) * kDualLd * 4);
+}
+
+// kkt_factor<float> with the lanes of a tile (the same operations in the same
+// order; R keeps the reciprocal pivot on its diagonal).  Returns 0, or 1 when
+// a pivot ratio fails thr.
+__device__ int kkt_factor_tile(const ScreenTile &t, const KktData<float> &D, const InstDesc &I, uint64_t lo,
+                               uint64_t hi, float thr, float *R, float *Y, float *Lam, int *S, int *k_out,
+                               float *rho_out)
+{
+    const int tl = t.thread_rank();
+    const int m = I.m, p = I.p, P1 = p + 1;
+    const int k = mask_pop(lo, hi);
+    *k_out = k;
+    for (int i = tl; i < m; i += kTileW)
+        if (mask_has(lo, hi, i)) S[mask_rank(lo, hi, i)] = i;
+    t.sync();
+    float rho = 1.0f;
+    for (int a = 0; a < k; a++) {
+        int fail = 0;
+        if (tl == 0) {
+            const float d0 = D.Wm[(size_t)S[a] * m + S[a]];
+            float acc = d0;
+            for (int l = 0; l < a; l++) acc = __fmaf_rn(-R[l * k + a], R[l * k + a], acc);
+            if (!(acc > thr * d0)) fail = 1;
+            else {
+                R[a * k + a] = __frcp_rn(__fsqrt_rn(acc));
+                const float rr = __fdividef(acc, d0);
+                if (rr < rho) rho = rr;
+            }
+        }
+        fail = t.shfl(fail, 0);
+        if (fail) return 1;
+        t.sync();
+        for (int b = a + 1 + tl; b < k; b += kTileW) {
+            float acc = D.Wm[(size_t)S[a] * m + S[b]];
+            for (int l = 0; l < a; l++) acc = __fmaf_rn(-R[l * k + a], R[l * k + b], acc);
+            R[a * k + b] = acc * R[a * k + a];
+        }
+        t.sync();
+    }
+    for (int cc = tl; cc < P1; cc += kTileW) {
+        for (int a = 0; a < k; a++) {
+            float acc = (cc < p) ? D.Wh[(size_t)S[a] * p + cc] : D.wc[S[a]];
+            for (int l = 0; l < a; l++) acc = __fmaf_rn(-R[l * k + a], Y[l * P1 + cc], acc);
+            Y[a * P1 + cc] = acc * R[a * k + a];
+        }
+        for (int a = k - 1; a >= 0; a--) {
+            float acc = Y[a * P1 + cc];
+            for (int l = a + 1; l < k; l++) acc = __fmaf_rn(-R[a * k + l], Lam[l * P1 + cc], acc);
+            Lam[a * P1 + cc] = acc * R[a * k + a];
+        }
+    }
+    t.sync();
+    *rho_out = t.shfl(rho, 0);
+    return 0;
+}
+
+// lp2_dual_screen with the lanes of a tile: rows r = lane + 16 s (three
+// slots), basis rows in lanes 0..p.  Same pricing, ratio test, pivot and
+// verified bound.
+__device__ int lp2_dual_screen_tile(const ScreenTile &t, const float *T, int m, int R2, int p, const float *blo,
+                                    const float *bhi, float thr, float tol_piv, float tol_dj, int max_it,
+                                    int degen_switch, int *it_out, float *bound_out)
+{
+    constexpr int NR = kTileRows / kTileW;
+    constexpr int MP = kDualMaxP;
+    constexpr int LD = kDualLd;
+    const int lane = t.thread_rank();
+    const int P1 = p + 1;
+    auto row8 = [&](int r, float *a) {
+        const float4 v0 = reinterpret_cast<const float4 *>(T + r * LD)[0];
+        const float4 v1 = reinterpret_cast<const float4 *>(T + r * LD)[1];
+        a[0] = v0.x; a[1] = v0.y; a[2] = v0.z; a[3] = v0.w; a[4] = v1.x; a[5] = v1.y; a[6] = v1.z; a[7] = v1.w;
+    };
+    float lo[MP], hi[MP];
+#pragma unroll
+    for (int c = 0; c < MP; c++) { lo[c] = c < p ? blo[c] : 0.0f; hi[c] = c < p ? bhi[c] : 0.0f; }
+    unsigned bkey = 0xffffffffu;
+    int bi = -1;
+    for (int r = lane; r < m; r += kTileW) {
+        float a[8];
+        row8(r, a);
+        float b = a[7];
+#pragma unroll
+        for (int c = 0; c < MP; c++) b -= a[c] > 0.0f ? a[c] * lo[c] : a[c] * hi[c];
+        const unsigned k = key_signed(b);
+        if (bi < 0 || k < bkey) { bkey = k; bi = r; }
+    }
+    const int istar = tile_argmin(t, bkey, (unsigned)bi, bi);
+    float gi[8];
+    row8(istar, gi);
+    float binv[MP], pi[MP], binvp = 0.0f, y = 0.0f;
+    float pip = gi[7];
+    int bidx = -1;
+#pragma unroll
+    for (int c = 0; c < MP; c++) {
+        binv[c] = 0.0f;
+        pi[c] = 0.0f;
+        if (c < p) {
+            const bool upper = !(gi[c] > 0.0f);
+            const int row = m + (upper ? c : p + c);
+            const float sc = T[row * LD + c];
+            pi[c] = upper ? hi[c] : lo[c];
+            const float yc = __fdividef(-gi[c], sc);
+            pip = __fmaf_rn(yc, T[row * LD + 7], pip);
+            if (lane == 1 + c) { bidx = row; y = yc; binv[c] = __fdividef(1.0f, sc); binvp = yc; }
+        }
+    }
+    if (lane == 0) { bidx = istar; y = 1.0f; binvp = 1.0f; }
+    unsigned basic = 0;
+#pragma unroll 1
+    for (int s = 0; s < NR; s++) {
+        const int r = lane + kTileW * s;
+        bool b = r == istar;
+        if (r >= m && r < m + p) b = !(T[istar * LD + (r - m)] > 0.0f);
+        else if (r >= m + p && r < m + 2 * p) b = T[istar * LD + (r - m - p)] > 0.0f;
+        if (b) basic |= 1u << s;
+    }
+    float reach = 0.0f;
+#pragma unroll
+    for (int c = 0; c < MP; c++) if (lane == c) reach = fmaxf(fabsf(lo[c]), fabsf(hi[c]));
+    const int vcol = lane < p ? lane : (lane == p ? 6 : 7);
+    auto verify = [&]() -> float {
+        float acc = 0.0f;
+#pragma unroll
+        for (int i = 0; i <= MP; i++) {
+            if (i < P1) {
+                const float yi = t.shfl(fmaxf(y, 0.0f), i);
+                const int ri = t.shfl(bidx, i);
+                if (lane <= P1) acc = __fmaf_rn(yi, T[ri * LD + vcol], acc);
+            }
+        }
+        const float cy = t.shfl(acc, p);
+        const float num = tile_sum(t, lane < p ? fabsf(acc) * reach : (lane == P1 ? acc : 0.0f));
+        return cy > 0.0f ? __fdividef(num, cy) : pos_inf<float>();
+    };
+    int it = 0, degen = 0, proven = 0;
+    bool bland = false;
+    float bound = pos_inf<float>();
+    for (;;) {
+        if (pip < -thr) {
+            bound = verify();
+            if (bound < -thr) { proven = 1; break; }
+        }
+        if (it >= max_it) break;
+        unsigned key = 0xffffffffu, kid = 0xffffffffu;
+        int kq = -1;
+        float dbest = 0.0f;
+#pragma unroll 1
+        for (int s = 0; s < NR; s++) {
+            const int r = lane + kTileW * s;
+            if (r < R2 && !((basic >> s) & 1u)) {
+                float a[8];
+                row8(r, a);
+                float d = __fmaf_rn(-pip, a[6], a[7]);
+#pragma unroll
+                for (int c = 0; c < MP; c++) d = __fmaf_rn(-pi[c], a[c], d);
+                if (d < -tol_dj) {
+                    const unsigned k = bland ? 0u : ~key_of(-d);
+                    if (kq < 0 || k < key || (k == key && (unsigned)r < kid)) { key = k; kid = r; kq = r; dbest = d; }
+                }
+            }
+        }
+        const int q = tile_argmin(t, key, kid, kq);
+        if (q < 0) {
+            bound = verify();
+            proven = bound < -thr;
+            break;
+        }
+        const float dq = t.shfl(dbest, q & (kTileW - 1));
+        float aq[8];
+        row8(q, aq);
+        float u = binvp * aq[6];
+#pragma unroll
+        for (int c = 0; c < MP; c++) u = __fmaf_rn(binv[c], aq[c], u);
+        unsigned rk = 0xffffffffu, rid = 0xffffffffu;
+        int rl = -1;
+        if (lane < P1 && u > tol_piv) { rk = key_of(__fdividef(fmaxf(y, 0.0f), u)); rid = (unsigned)bidx; rl = lane; }
+        const int l = tile_argmin(t, rk, rid, rl);
+        if (l < 0) break;
+        const float ul = t.shfl(u, l);
+        const float yl = t.shfl(fmaxf(y, 0.0f), l);
+        const int oldb = t.shfl(bidx, l);
+        const float inv = __fdividef(1.0f, ul);
+        const float theta = yl * inv;
+        const float f = u * inv, fp = dq * inv;
+        const bool own = lane == l, other = lane < P1 && lane != l;
+#pragma unroll
+        for (int c = 0; c < MP; c++) {
+            const float rj = t.shfl(binv[c], l);
+            binv[c] = own ? rj * inv : (other ? __fmaf_rn(-f, rj, binv[c]) : binv[c]);
+            pi[c] = __fmaf_rn(fp, rj, pi[c]);
+        }
+        {
+            const float rj = t.shfl(binvp, l);
+            binvp = own ? rj * inv : (other ? __fmaf_rn(-f, rj, binvp) : binvp);
+            pip = __fmaf_rn(fp, rj, pip);
+        }
+        if (own) { y = theta; bidx = q; }
+        else if (other) y = __fmaf_rn(-theta, u, y);
+        if (lane == (q & (kTileW - 1))) basic |= 1u << (q >> 4);
+        if (lane == (oldb & (kTileW - 1))) basic &= ~(1u << (oldb >> 4));
+        it++;
+        degen = (theta == 0.0f) ? degen + 1 : 0;
+        bland = degen >= degen_switch;
+    }
+    *it_out = it;
+    *bound_out = bound;
+    return proven;
+}
+
+// Stage 0 of the dual route, one set per tile (two per warp): KKT factor,
+// the multiplier rows and the box, dual bound; the sets it cannot settle go
+// to stage 1 (k_opt_screen<0, 1>), a failed KKT margin to the FP64 queue.
+__global__ void __launch_bounds__(32, 32) k_opt_screen_tiles(DevBuffers B, Tol tol, SlotDims sd, int level, int mode)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const ScreenTile t = cgx::tiled_partition<kTileW>(cgx::this_thread_block());
+    const int lane = t.thread_rank();
+    float *R, *Y, *Lam, *Tb;
+    int *S;
+    {
+        unsigned char *base = smem + (threadIdx.x / kTileW) * tile_slot_bytes(sd);
+        size_t o = 0;
+        R = (float *)(base + o); o += align16((size_t)sd.maxK * sd.maxK * 4);
+        Y = (float *)(base + o); o += align16((size_t)sd.maxK * sd.maxP1 * 4);
+        Lam = (float *)(base + o); o += align16((size_t)sd.maxK * sd.maxP1 * 4);
+        S = (int *)(base + o); o += align16((size_t)sd.maxK * sizeof(int));
+        Tb = (float *)(base + o);
+    }
+    const int side = level & 1;
+    Ctl *ctl = B.ctl;
+    const long long nn = ctl->n_node[side] < B.node_cap ? ctl->n_node[side] : B.node_cap;
+    LocalInstCounters lc;
+    lc.reset(-1);
+    auto flush = [&]() {
+        if (lc.inst >= 0 && lane == 0) {
+            atomicAdd((unsigned long long *)&B.ictl[lc.inst].lp2_piv, (unsigned long long)lc.c);
+        }
+    };
+    for (;;) {
+        long long x;
+        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[3], 1ull);
+        x = t.shfl(x, 0);
+        if (x >= nn) break;
+        const Node nd = B.node[side][x];
+        if ((nd.flags & (NODE_VALID | NODE_FEASIBLE)) != (NODE_VALID | NODE_FEASIBLE)) continue;
+        const InstDesc &I = B.inst[nd.inst];
+        if (level < I.k_min) continue;
+        if (!dual_route(mode, I, sd)) continue;
+        if (nd.inst != lc.inst) { flush(); lc.reset(nd.inst); }
+        const KktData<float> D = kkt_data<float>(B, I);
+        const int p = I.p, ncp = I.ncp, P1 = p + 1;
+        int k = 0, piv = 0;
+        float rho = 1.0f, bound = 0.0f;
+        bool proven = false, to_rows = false;
+        if (!kkt_factor_tile(t, D, I, nd.lo, nd.hi, tol.margin_licq32, R, Y, Lam, S, &k, &rho)) {
+            to_rows = true;
+            if (k > 0 && k + ncp <= tile_rows(sd)) {
+                float bmax = 0.0f;
+                for (int ii = lane; ii < ncp; ii += kTileW) bmax = fmaxf(bmax, fabsf(D.bt[ii]));
+                bmax = tile_max(t, bmax);
+                float amaxA = 0.0f;
+                for (int a = lane; a < k; a += kTileW) {
+                    float *tr = Tb + (size_t)a * kDualLd;
+                    const float *lam = Lam + a * P1;
+                    float rs = 0.0f;
+                    for (int cc = 0; cc < p; cc++) { tr[cc] = lam[cc]; rs += fabsf(lam[cc]); }
+                    for (int cc = p; cc < kDualMaxP; cc++) tr[cc] = 0.0f;
+                    tr[6] = 1.0f;
+                    tr[7] = -lam[p];
+                    rs += fabsf(lam[p]);
+                    amaxA = fmaxf(amaxA, rs);
+                }
+                for (int ii = lane; ii < ncp; ii += kTileW) {
+                    float *tr = Tb + (size_t)(k + ii) * kDualLd;
+                    for (int cc = 0; cc < kDualMaxP; cc++) tr[cc] = cc < p ? D.At[ii * p + cc] : 0.0f;
+                    tr[6] = 0.0f;
+                    tr[7] = D.bt[ii];
+                }
+                amaxA = tile_max(t, amaxA);
+                const float scaleA = __fdividef(amaxA, rho) * (1.0f + (float)p * bmax);
+                t.sync();
+                proven = lp2_dual_screen_tile(t, Tb, k, k + ncp, p, B.fpool + I.f_blo, B.fpool + I.f_bhi,
+                                              tol.margin_t32 * scaleA, tol.tol_piv32, tol.tol_dj32, tol.max_pivots,
+                                              tol.degen_switch, &piv, &bound);
+                to_rows = !proven;
+                t.sync();
+            }
+        }
+        lc.c += piv;
+        if (!proven) {
+            // stage 1 takes the sets with a KKT factor; a failed KKT margin goes to FP64
+            if (lane == 0) {
+                if (to_rows) {
+                    const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_scr, 1ull);
+                    if (qi < B.q_cap) B.q_lp1[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
+                } else {
+                    const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_opt, 1ull);
+                    if (qi < B.q_cap) B.q_opt[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
+                }
+            }
+            t.sync();
+            continue;
+        }
+        // a final "not optimal" only leaves a diagnostic record
+        if (lane == 0 && nd.rec >= 0 && B.rec) {
+            OptResult res;
+            res.licq = 1; res.lp2_status = LP_BOUND; res.lp2_piv = piv;
+            res.cheb_status = LP_SKIPPED; res.cheb_piv = 0; res.optimal = 0; res.region = 0;
+            res.t = (double)bound; res.r = __longlong_as_double(0x7ff8000000000000LL);
+            res.decided = true;
+            write_opt(B, nd, level, res, false);
+        }
+        t.sync();
+    }
+    flush();
 }
 
 // STAGE (dual route only): 0 screens every set of the level with the
@@ -2501,6 +2869,7 @@ size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd)
 }
 
 size_t screen_smem_per_warp(const SlotDims &sd, int route) { return screen_warp_bytes(sd, route); }
+size_t screen_tiles_smem(const SlotDims &sd) { return 2 * tile_slot_bytes(sd); }
 bool screen_dual_route(int mode, const InstDesc &I, const SlotDims &sd) { return dual_route(mode, I, sd); }
 
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd)
@@ -2529,6 +2898,7 @@ const void *kernel_ptr(const char *name)
         {"opt_fp64_lp", (const void *)k_optimality_fp64<true>},
         {"screen_dual", (const void *)k_opt_screen<0>},
         {"screen_dual_rows", (const void *)k_opt_screen<0, 1>},
+        {"screen_dual_tiles", (const void *)k_opt_screen_tiles},
         {"screen_primal", (const void *)k_opt_screen<1>},
         {"level0_64", (const void *)k_level0<double>},
         {"level0_32", (const void *)k_level0<float>},
@@ -2578,7 +2948,7 @@ cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDim
                               int grid, size_t smem, cudaStream_t s)
 {
     // route 0: the dual route's first stage, 2: its second stage, 1: the primal route
-    if (route == 0) k_opt_screen<0><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
+    if (route == 0) k_opt_screen_tiles<<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
     else if (route == 2) k_opt_screen<0, 1><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
     else k_opt_screen<1><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
     return cudaGetLastError();
