@@ -274,7 +274,7 @@ struct mpqp_plan {
     bool pooled = false;        // allocations came from the device pool
     int grid_opt2 = 0;          // grid of the primal route (grid_opt: the dual route)
     int grid_opt3 = 0;          // grid of the dual route's second stage
-    int grid_tiles = 0;         // the dual route's first stage (two sets per warp)
+    int grid_tiles = 0;         // the dual route's first stage (one set per 8-thread tile)
     size_t smem_tiles = 0;
     size_t smem_opt2 = 0;       // shared memory per block of the primal route
     int grid_enum = 0, grid_feas = 0, grid_lp1fb = 0, grid_opt = 0, grid_optfb = 0;

@@ -2021,12 +2021,14 @@ __host__ __device__ __forceinline__ bool dual_route(int mode, const InstDesc &I,
 // ---------------------------------------------------------------------
 // Stage 0 of the dual route works on small LPs -- the k multiplier rows and
 // the 2p box rows (k + 2p <= 44), a basis of p + 1 <= 7 -- so a full warp
-// left half of its lanes idle.  Here each 16-thread tile of a warp screens its
-// own set: the same operations as kkt_factor<float> and lp2_dual_screen, with
-// tile-wide shuffles and reductions.
+// left half of its lanes idle.  Here each 8-thread tile of a warp screens its
+// own set (four per warp; 16-thread tiles were slower: 124 against 111 ms on
+// the m = 62 batch): the same operations as kkt_factor<float> and
+// lp2_dual_screen, with tile-wide shuffles and reductions.
 namespace cgx = cooperative_groups;
-constexpr int kTileW = 16;
-constexpr int kTileRows = 48;                  // k + 2p rows, three slots of 16
+constexpr int kTileShift = 3;
+constexpr int kTileW = 1 << kTileShift;
+constexpr int kTileRows = 48;                  // k + 2p rows, 48 / kTileW slots
 using ScreenTile = cgx::thread_block_tile<kTileW, cgx::thread_block>;
 
 __device__ __forceinline__ int tile_argmin(const ScreenTile &t, unsigned key, unsigned id, int idx)
@@ -2263,8 +2265,8 @@ __device__ int lp2_dual_screen_tile(const ScreenTile &t, const float *T, int m, 
         }
         if (own) { y = theta; bidx = q; }
         else if (other) y = __fmaf_rn(-theta, u, y);
-        if (lane == (q & (kTileW - 1))) basic |= 1u << (q >> 4);
-        if (lane == (oldb & (kTileW - 1))) basic &= ~(1u << (oldb >> 4));
+        if (lane == (q & (kTileW - 1))) basic |= 1u << (q >> kTileShift);
+        if (lane == (oldb & (kTileW - 1))) basic &= ~(1u << (oldb >> kTileShift));
         it++;
         degen = (theta == 0.0f) ? degen + 1 : 0;
         bland = degen >= degen_switch;
@@ -2274,7 +2276,7 @@ __device__ int lp2_dual_screen_tile(const ScreenTile &t, const float *T, int m, 
     return proven;
 }
 
-// Stage 0 of the dual route, one set per tile (two per warp): KKT factor,
+// Stage 0 of the dual route, one set per tile (32 / kTileW per warp): KKT factor,
 // the multiplier rows and the box, dual bound; the sets it cannot settle go
 // to stage 1 (k_opt_screen<0, 1>), a failed KKT margin to the FP64 queue.
 __global__ void __launch_bounds__(32, 32) k_opt_screen_tiles(DevBuffers B, Tol tol, SlotDims sd, int level, int mode)
@@ -2869,7 +2871,7 @@ size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd)
 }
 
 size_t screen_smem_per_warp(const SlotDims &sd, int route) { return screen_warp_bytes(sd, route); }
-size_t screen_tiles_smem(const SlotDims &sd) { return 2 * tile_slot_bytes(sd); }
+size_t screen_tiles_smem(const SlotDims &sd) { return (32 / kTileW) * tile_slot_bytes(sd); }   // a 32-thread block
 bool screen_dual_route(int mode, const InstDesc &I, const SlotDims &sd) { return dual_route(mode, I, sd); }
 
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd)
