@@ -718,7 +718,7 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
         (rc = grid_for(kernel_ptr(P->prec == PREC_MIXED ? "feas32" : "feas64"), P->smem_feas, &P->grid_feas)) ||
         (rc = grid_for(kernel_ptr("lp1_fp64"), P->smem_lp1fb, &P->grid_lp1fb)) ||
         (rc = P->prec == PREC_MIXED
-                  ? grid_for(kernel_ptr("screen_dual"), P->smem_opt, &P->grid_opt, 32)
+                  ? grid_for(kernel_ptr("screen_dual_rows"), P->smem_opt, &P->grid_opt, 32)
                   : grid_for(kernel_ptr("opt64"), P->smem_opt, &P->grid_opt)) ||
         (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_primal"), P->smem_opt2, &P->grid_opt2, 32) : 0) ||
         (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_dual_rows"), P->smem_opt, &P->grid_opt3, 32) : 0) ||

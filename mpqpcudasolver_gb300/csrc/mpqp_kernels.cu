@@ -2384,15 +2384,15 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen_tiles(DevBuffers B, Tol t
     flush();
 }
 
-// STAGE (dual route only): 0 screens every set of the level with the
-// multiplier rows and the box and queues the sets that this does not settle;
-// 1 takes that queue through the full rows.  Two kernels, so that each warp's
-// instruction stream stays small (the kernel is bound by instruction fetch)
-// and the rarely needed full-row code does not share the cache with the rest.
+// ROUTE 1: the primal route, every set of the level.  ROUTE 0 with STAGE 1:
+// the dual route's second stage -- the sets its first stage
+// (k_opt_screen_tiles) could not settle from the multiplier rows and the
+// box, through all region rows.  Separate kernels, so that each instruction
+// stream stays small (the one-kernel screen was bound by instruction fetch).
 template <int ROUTE, int STAGE = 0>
 __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, SlotDims sd, int level, int mode)
 {
-    static_assert(ROUTE == 0 || STAGE == 0, "only the dual route has two stages");
+    static_assert((ROUTE == 0) == (STAGE == 1), "the dual route's first stage is k_opt_screen_tiles");
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = lane_id();
     OptWs<float> ws;
@@ -2455,56 +2455,7 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
             float bmax = 0.0f;
             for (int ii = lane; ii < ncp; ii += 32) { const float v = fabsf(D.bt[ii]); if (v > bmax) bmax = v; }
             bmax = warp_max(bmax);
-            bool done = false;
-            if constexpr (dual && STAGE == 0) {
-                // First the LP over the multiplier rows and the box alone: it
-                // drops the inactive rows, so its optimum bounds t* from above
-                // and a verified "not optimal" from it is final.  It settles
-                // most non-optimal sets (about nine in ten at |S| = 5 of the
-                // m = 62 instance) without the m - k inactive rows.
-                if (k > 0) {
-                    float amaxA = 0.0f;
-                    for (int a = lane; a < k; a += 32) {
-                        float *tr = Tb + (size_t)a * kDualLd;
-                        const float *lam = ws.Lam + a * P1;
-                        float rs = 0.0f;
-                        for (int cc = 0; cc < p; cc++) { tr[cc] = lam[cc]; rs += fabsf(lam[cc]); }
-                        for (int cc = p; cc < kDualMaxP; cc++) tr[cc] = 0.0f;
-                        tr[6] = 1.0f;
-                        tr[7] = -lam[p];
-                        rs += fabsf(lam[p]);
-                        amaxA = fmaxf(amaxA, rs);
-                    }
-                    for (int ii = lane; ii < ncp; ii += 32) {
-                        float *tr = Tb + (size_t)(k + ii) * kDualLd;
-                        for (int cc = 0; cc < kDualMaxP; cc++) tr[cc] = cc < p ? D.At[ii * p + cc] : 0.0f;
-                        tr[6] = 0.0f;
-                        tr[7] = D.bt[ii];
-                    }
-                    amaxA = warp_max(amaxA);
-                    const float scaleA = __fdividef(amaxA, rho) * (1.0f + (float)p * bmax);
-                    __syncwarp();
-                    float boundA;
-                    int pivA = 0;
-                    done = lp2_dual_screen(Tb, k, k + ncp, p, B.fpool + I.f_blo, B.fpool + I.f_bhi,
-                                           tol.margin_t32 * scaleA, tol.tol_piv32, tol.tol_dj32, tol.max_pivots,
-                                           tol.degen_switch, &pivA, &boundA);
-                    piv = pivA;
-                    if (done) { decided = true; status = LP_BOUND; t = boundA; }
-                    __syncwarp();
-                }
-                if (!done) {
-                    // to stage 1
-                    if (lane == 0) {
-                        const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_scr, 1ull);
-                        if (qi < B.q_cap) B.q_lp1[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
-                    }
-                    lc.c += piv;
-                    __syncwarp();
-                    continue;
-                }
-            }
-            if (!done) {
+            {
             float t0, g0;
             // dual: rows straight into the dual layout; primal: rows into G,
             // kept unpivoted for the bound that verifies the verdict
@@ -2898,7 +2849,6 @@ const void *kernel_ptr(const char *name)
         {"opt64_lp", (const void *)k_optimality<double, true>},
         {"opt_fp64", (const void *)k_optimality_fp64<false>},
         {"opt_fp64_lp", (const void *)k_optimality_fp64<true>},
-        {"screen_dual", (const void *)k_opt_screen<0>},
         {"screen_dual_rows", (const void *)k_opt_screen<0, 1>},
         {"screen_dual_tiles", (const void *)k_opt_screen_tiles},
         {"screen_primal", (const void *)k_opt_screen<1>},
