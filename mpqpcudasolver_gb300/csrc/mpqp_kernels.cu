@@ -487,6 +487,11 @@ __device__ __forceinline__ int warp_simplex_f32(const Lp<float> &L, float tol_pi
 // ---------------------------------------------------------------------
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
+// column of the dual-screen row layout (stride 12: g 0..5, c 6, h 7) that
+// holds each row's error scale: the sum of the magnitudes of the terms the
+// FP32 row was computed from (0 for the exact box rows)
+constexpr int kRowScaleCol = 8;
+
 // LP1 buffer: tableau (maxM1+1) x maxLD1 + ids (maxM1 + maxNv)
 template <typename T>
 __host__ __device__ inline size_t lp1_buf_bytes(int maxM1, int maxLD1, int maxNv)
@@ -1314,7 +1319,10 @@ __device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, ui
         const T h = -LamL[a * P1 + p];
         G[a * ldg + hc] = h;
         if (want_t0 && h < tmin) tmin = h;
-        if (track) { rs += xabs(LamL[a * P1 + p]); labs[a] = rs; if (rs > amax) amax = rs; }
+        if (track) {
+            rs += xabs(LamL[a * P1 + p]); labs[a] = rs; if (rs > amax) amax = rs;
+            if (out) G[a * ldg + kRowScaleCol] = rs;
+        }
     }
     if (track) __syncwarp();
     // inactive rows: g_c = -Wh_ic + sum_l Wm_i,S_l Lambda_lc (c < p) and
@@ -1357,6 +1365,7 @@ __device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, ui
             }
         }
         if (track && rs > amax) amax = rs;
+        if (track && out) G[pos * ldg + kRowScaleCol] = rs;
     }
     for (int ii = lane; ii < ncp; ii += 32) {
         for (int cc = 0; cc < p; cc++) {
@@ -1365,6 +1374,7 @@ __device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, ui
             if (want_t0 && xabs(v) > gmax) gmax = xabs(v);
         }
         G[(m + ii) * ldg + hc] = D.bt[ii];
+        if (track && out) G[(m + ii) * ldg + kRowScaleCol] = T(0);   // the box rows are exact
     }
     if (want_t0) {
 #pragma unroll
@@ -1832,8 +1842,12 @@ enum : int { LP_BOUND = 6 };      // record status: "not optimal" proven by a du
 // Row layout (stride kDualLd): columns 0..5 g_r (zero beyond p), 6 c_r, 7 h_r.
 // Returns 1 when "not optimal" is proven; *it_out iterations, *bound_out the
 // last verified bound (+inf when none was computed).
+// thr: the threshold from the largest row error scale (when to try the
+// bound); ethr: threshold per unit of error scale -- a bound is final when it
+// is below -ethr * sum_r y_r e_r / (c.y), e_r the error scale of row r
+// (column kRowScaleCol), which is at most thr
 __device__ int lp2_dual_screen(const float *T, int m, int R2, int p, const float *blo, const float *bhi, float thr,
-                               float tol_piv, float tol_dj, int max_it, int degen_switch, int *it_out,
+                               float ethr, float tol_piv, float tol_dj, int max_it, int degen_switch, int *it_out,
                                float *bound_out)
 {
     constexpr int NR = kDualMaxRows / 32;
@@ -1899,18 +1913,21 @@ __device__ int lp2_dual_screen(const float *T, int m, int R2, int p, const float
     for (int c = 0; c < MP; c++) if (lane == c) reach = fmaxf(fabsf(lo[c]), fabsf(hi[c]));
     // verified bound from max(y, 0): lane c < p sums (G^T y)_c, lane p c.y, lane p+1 h.y
     const int vcol = lane < p ? lane : (lane == p ? 6 : 7);
+    float thr_row = thr;   // the per-row threshold of the last verified y
     auto verify = [&]() -> float {
-        float acc = 0.0f;
+        float acc = 0.0f, ey = 0.0f;
 #pragma unroll
         for (int i = 0; i <= MP; i++) {
             if (i < P1) {
                 const float yi = __shfl_sync(FULLMASK, fmaxf(y, 0.0f), i);
                 const int ri = __shfl_sync(FULLMASK, bidx, i);
                 if (lane <= P1) acc = __fmaf_rn(yi, T[ri * LD + vcol], acc);
+                ey = __fmaf_rn(yi, T[ri * LD + kRowScaleCol], ey);
             }
         }
         const float cy = __shfl_sync(FULLMASK, acc, p);
         const float num = warp_sum(lane < p ? fabsf(acc) * reach : (lane == P1 ? acc : 0.0f));
+        thr_row = cy > 0.0f ? fminf(thr, ethr * __fdividef(ey, cy)) : thr;
         return cy > 0.0f ? __fdividef(num, cy) : pos_inf<float>();
     };
 
@@ -1920,7 +1937,7 @@ __device__ int lp2_dual_screen(const float *T, int m, int R2, int p, const float
     for (;;) {
         if (pip < -thr) {
             bound = verify();
-            if (bound < -thr) { proven = 1; break; }
+            if (bound < -thr_row) { proven = 1; break; }
         }
         if (it >= max_it) break;
         // pricing: most negative reduced cost d_r = h_r - pi.a_r (Bland: smallest r)
@@ -1947,7 +1964,7 @@ __device__ int lp2_dual_screen(const float *T, int m, int R2, int p, const float
         const int q = warp_argmin(key, kid, kq);
         if (q < 0) {                       // dual optimum: pip is the LP2 optimum t*
             bound = verify();
-            proven = bound < -thr;
+            proven = bound < -thr_row;
             break;
         }
         const float dq = __shfl_sync(FULLMASK, dbest, q & 31);
@@ -2126,7 +2143,7 @@ __device__ int kkt_factor_tile(const ScreenTile &t, const KktData<float> &D, con
 // slots), basis rows in lanes 0..p.  Same pricing, ratio test, pivot and
 // verified bound.
 __device__ int lp2_dual_screen_tile(const ScreenTile &t, const float *T, int m, int R2, int p, const float *blo,
-                                    const float *bhi, float thr, float tol_piv, float tol_dj, int max_it,
+                                    const float *bhi, float thr, float ethr, float tol_piv, float tol_dj, int max_it,
                                     int degen_switch, int *it_out, float *bound_out)
 {
     constexpr int NR = kTileRows / kTileW;
@@ -2187,18 +2204,21 @@ __device__ int lp2_dual_screen_tile(const ScreenTile &t, const float *T, int m, 
 #pragma unroll
     for (int c = 0; c < MP; c++) if (lane == c) reach = fmaxf(fabsf(lo[c]), fabsf(hi[c]));
     const int vcol = lane < p ? lane : (lane == p ? 6 : 7);
+    float thr_row = thr;   // the per-row threshold of the last verified y
     auto verify = [&]() -> float {
-        float acc = 0.0f;
+        float acc = 0.0f, ey = 0.0f;
 #pragma unroll
         for (int i = 0; i <= MP; i++) {
             if (i < P1) {
                 const float yi = t.shfl(fmaxf(y, 0.0f), i);
                 const int ri = t.shfl(bidx, i);
                 if (lane <= P1) acc = __fmaf_rn(yi, T[ri * LD + vcol], acc);
+                ey = __fmaf_rn(yi, T[ri * LD + kRowScaleCol], ey);
             }
         }
         const float cy = t.shfl(acc, p);
         const float num = tile_sum(t, lane < p ? fabsf(acc) * reach : (lane == P1 ? acc : 0.0f));
+        thr_row = cy > 0.0f ? fminf(thr, ethr * __fdividef(ey, cy)) : thr;
         return cy > 0.0f ? __fdividef(num, cy) : pos_inf<float>();
     };
     int it = 0, degen = 0, proven = 0;
@@ -2207,7 +2227,7 @@ __device__ int lp2_dual_screen_tile(const ScreenTile &t, const float *T, int m, 
     for (;;) {
         if (pip < -thr) {
             bound = verify();
-            if (bound < -thr) { proven = 1; break; }
+            if (bound < -thr_row) { proven = 1; break; }
         }
         if (it >= max_it) break;
         unsigned key = 0xffffffffu, kid = 0xffffffffu;
@@ -2231,7 +2251,7 @@ __device__ int lp2_dual_screen_tile(const ScreenTile &t, const float *T, int m, 
         const int q = tile_argmin(t, key, kid, kq);
         if (q < 0) {
             bound = verify();
-            proven = bound < -thr;
+            proven = bound < -thr_row;
             break;
         }
         const float dq = t.shfl(dbest, q & (kTileW - 1));
@@ -2337,6 +2357,7 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen_tiles(DevBuffers B, Tol t
                     tr[6] = 1.0f;
                     tr[7] = -lam[p];
                     rs += fabsf(lam[p]);
+                    tr[kRowScaleCol] = rs;
                     amaxA = fmaxf(amaxA, rs);
                 }
                 for (int ii = lane; ii < ncp; ii += kTileW) {
@@ -2344,13 +2365,16 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen_tiles(DevBuffers B, Tol t
                     for (int cc = 0; cc < kDualMaxP; cc++) tr[cc] = cc < p ? D.At[ii * p + cc] : 0.0f;
                     tr[6] = 0.0f;
                     tr[7] = D.bt[ii];
+                    tr[kRowScaleCol] = 0.0f;
                 }
                 amaxA = tile_max(t, amaxA);
-                const float scaleA = __fdividef(amaxA, rho) * (1.0f + (float)p * bmax);
+                // error scale per unit of row magnitude: 1 / smallest pivot ratio
+                // times the reach of theta inside the box
+                const float escale = __fdividef(1.0f + (float)p * bmax, rho);
                 t.sync();
                 proven = lp2_dual_screen_tile(t, Tb, k, k + ncp, p, B.fpool + I.f_blo, B.fpool + I.f_bhi,
-                                              tol.margin_t32 * scaleA, tol.tol_piv32, tol.tol_dj32, tol.max_pivots,
-                                              tol.degen_switch, &piv, &bound);
+                                              tol.margin_t32 * escale * amaxA, tol.margin_t32 * escale, tol.tol_piv32,
+                                              tol.tol_dj32, tol.max_pivots, tol.degen_switch, &piv, &bound);
                 to_rows = !proven;
                 t.sync();
             }
@@ -2477,7 +2501,8 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
                 float bound;
                 int pivB = 0;
                 decided = lp2_dual_screen(Tb, m, R2, p, B.fpool + I.f_blo, B.fpool + I.f_bhi, tol.margin_t32 * scale,
-                                          tol.tol_piv32, tol.tol_dj32, tol.max_pivots, tol.degen_switch, &pivB, &bound);
+                                          tol.margin_t32 * __fdividef(1.0f + (float)p * bmax, rho), tol.tol_piv32,
+                                          tol.tol_dj32, tol.max_pivots, tol.degen_switch, &pivB, &bound);
                 piv += pivB;
                 status = LP_BOUND;
                 t = bound;
