@@ -104,6 +104,19 @@ __device__ __forceinline__ long long hash_cap_for(const DevBuffers &B, long long
     return c < B.hash_cap ? c : B.hash_cap;
 }
 
+// probing from slot s (the key's home slot, or later after a collision)
+__device__ int hash_find_from(const HashSlot *tab, long long cap, int tag, int inst, uint64_t lo, uint64_t hi,
+                              uint64_t s)
+{
+    for (long long probe = 0; probe < cap; probe++) {
+        const HashSlot *h = tab + s;
+        if (h->tag != tag) return -1;
+        if (h->lo == lo && h->hi == hi && h->inst == inst) return h->val;
+        s = (s + 1) & (uint64_t)(cap - 1);
+    }
+    return -1;
+}
+
 __device__ int hash_find(const HashSlot *tab, long long cap, int tag, int inst, uint64_t lo, uint64_t hi)
 {
     uint64_t s = hash_key(inst, lo, hi) & (uint64_t)(cap - 1);
@@ -657,14 +670,40 @@ __global__ void k_enumerate(DevBuffers B, int level)
             if (ok && !B.exhaustive) {
                 uint64_t lo = par.lo, hi = par.hi;
                 if (j < 64) lo |= 1ull << j; else hi |= 1ull << (j - 64);
+                // the subsets child minus a, a in the parent, four at a time: the
+                // home slots of all four are read before any is checked, so the
+                // random accesses overlap; a collision probes on from there
                 uint64_t rlo = par.lo, rhi = par.hi;
+                const HashSlot *tab = B.hash[pside];
                 while (ok && (rlo | rhi)) {
-                    int a;
-                    if (rlo) { a = __ffsll((long long)rlo) - 1; rlo &= rlo - 1; }
-                    else { a = 64 + __ffsll((long long)rhi) - 1; rhi &= rhi - 1; }
-                    uint64_t slo = lo, shi = hi;
-                    if (a < 64) slo &= ~(1ull << a); else shi &= ~(1ull << (a - 64));
-                    if (hash_find(B.hash[pside], hcap, tag_prev, par.inst, slo, shi) < 0) ok = false;
+                    constexpr int G = 4;
+                    uint64_t slo[G], shi[G], sidx[G];
+                    int n = 0;
+#pragma unroll
+                    for (int g = 0; g < G; g++) {
+                        slo[g] = 0; shi[g] = 0; sidx[g] = 0;
+                        if (rlo | rhi) {
+                            int a;
+                            if (rlo) { a = __ffsll((long long)rlo) - 1; rlo &= rlo - 1; }
+                            else { a = 64 + __ffsll((long long)rhi) - 1; rhi &= rhi - 1; }
+                            slo[g] = lo; shi[g] = hi;
+                            if (a < 64) slo[g] &= ~(1ull << a); else shi[g] &= ~(1ull << (a - 64));
+                            sidx[g] = hash_key(par.inst, slo[g], shi[g]) & (uint64_t)(hcap - 1);
+                            n = g + 1;
+                        }
+                    }
+                    HashSlot hs[G];
+#pragma unroll
+                    for (int g = 0; g < G; g++) if (g < n) hs[g] = tab[sidx[g]];
+#pragma unroll
+                    for (int g = 0; g < G; g++) {
+                        if (g < n && ok) {
+                            if (hs[g].tag != tag_prev) ok = false;
+                            else if (!(hs[g].lo == slo[g] && hs[g].hi == shi[g] && hs[g].inst == par.inst))
+                                ok = hash_find_from(tab, hcap, tag_prev, par.inst, slo[g], shi[g],
+                                                    (sidx[g] + 1) & (uint64_t)(hcap - 1)) >= 0;
+                        }
+                    }
                 }
             }
             const unsigned okm = __ballot_sync(FULLMASK, ok);
