@@ -609,11 +609,15 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
     {
         std::vector<double> lvl(kMaxK + 2, 0.0), lvl_tab(kMaxK + 2, 0.0);
         for (int i = 0; i < n_inst; i++) {
+            // an instance with a budget writes at most that many candidates
+            // (and nodes) at any level: a level is enumerated only while it fits
+            const double cap_i = P->desc[i].budget > 0 ? (double)P->desc[i].budget : 1e300;
             double cmk = 1.0;
             for (int k = 0; k <= P->desc[i].k_max; k++) {
                 if (k > 0) cmk = cmk * (double)(P->desc[i].m - k + 1) / (double)k;
-                lvl[k] += cmk;
-                if (k < P->desc[i].k_max) lvl_tab[k] += cmk * (double)P->desc[i].tab_elems * (double)es;
+                const double nk = std::min(cmk, cap_i);
+                lvl[k] += nk;
+                if (k < P->desc[i].k_max) lvl_tab[k] += nk * (double)P->desc[i].tab_elems * (double)es;
             }
         }
         for (int k = 0; k <= kMaxK; k++) {
@@ -812,13 +816,65 @@ extern "C" int mpqp_plan_kernel_times(mpqp_plan *P, int max_kernels, char *names
     return n;
 }
 
-static bool set_less(uint64_t alo, uint64_t ahi, uint64_t blo, uint64_t bhi)
+static uint64_t bit_reverse64(uint64_t x)
 {
-    // lexicographic order of the sorted element lists of two equal-size sets
-    uint64_t dlo = alo ^ blo, dhi = ahi ^ bhi;
-    if (dlo) return (alo & (dlo & (~dlo + 1))) != 0;
-    if (dhi) return (ahi & (dhi & (~dhi + 1))) != 0;
-    return false;
+    x = ((x >> 1) & 0x5555555555555555ULL) | ((x & 0x5555555555555555ULL) << 1);
+    x = ((x >> 2) & 0x3333333333333333ULL) | ((x & 0x3333333333333333ULL) << 2);
+    x = ((x >> 4) & 0x0F0F0F0F0F0F0F0FULL) | ((x & 0x0F0F0F0F0F0F0F0FULL) << 4);
+    x = ((x >> 8) & 0x00FF00FF00FF00FFULL) | ((x & 0x00FF00FF00FF00FFULL) << 8);
+    x = ((x >> 16) & 0x0000FFFF0000FFFFULL) | ((x & 0x0000FFFF0000FFFFULL) << 16);
+    return (x >> 32) | (x << 32);
+}
+
+// indices of the optimal-set records in (inst, level, set) order
+static std::vector<uint32_t> sorted_opt_order(const std::vector<OptRec> &ov)
+{
+    const size_t n = ov.size();
+    std::vector<uint32_t> order(n), tmp(n);
+    for (size_t i = 0; i < n; i++) order[i] = (uint32_t)i;
+    if (n < 2) return order;
+    // the three 64-bit sort keys of every record, by record index
+    std::vector<uint64_t> khi(n), klo(n), kgrp(n);
+    uint64_t or_hi = 0, or_lo = 0, or_grp = 0;
+    for (size_t i = 0; i < n; i++) {
+        khi[i] = bit_reverse64(ov[i].hi);
+        klo[i] = bit_reverse64(ov[i].lo);
+        kgrp[i] = ((uint64_t)(uint32_t)ov[i].inst << 32) | (uint32_t)ov[i].level;
+        or_hi |= khi[i]; or_lo |= klo[i]; or_grp |= kgrp[i];
+    }
+    constexpr int kBits = 11, kBins = 1 << kBits;
+    std::vector<uint32_t> hist((size_t)6 * kBins);
+    // one stable LSD phase on one key (ascending order of ~key when flip):
+    // all digit histograms in one pass, then a scatter pass per digit that
+    // varies; digits above the highest set bit of any key are skipped
+    auto phase = [&](const std::vector<uint64_t> &key, uint64_t any, bool flip) {
+        if (!any) return;
+        const int nd = (64 - __builtin_clzll(any) + kBits - 1) / kBits;
+        const uint64_t fl = flip ? ~0ULL : 0ULL;
+        std::fill(hist.begin(), hist.begin() + (size_t)nd * kBins, 0u);
+        for (size_t i = 0; i < n; i++) {
+            const uint64_t k = key[order[i]] ^ fl;
+            for (int d = 0; d < nd; d++) hist[(size_t)d * kBins + ((k >> (d * kBits)) & (kBins - 1))]++;
+        }
+        for (int d = 0; d < nd; d++) {
+            uint32_t *h = &hist[(size_t)d * kBins];
+            const int sh = d * kBits;
+            if (h[((key[order[0]] ^ fl) >> sh) & (kBins - 1)] == n) continue;   // all keys share this digit
+            uint32_t sum = 0;
+            for (int b = 0; b < kBins; b++) { const uint32_t c = h[b]; h[b] = sum; sum += c; }
+            for (size_t i = 0; i < n; i++) {
+                const uint32_t r = order[i];
+                tmp[h[((key[r] ^ fl) >> sh) & (kBins - 1)]++] = r;
+            }
+            order.swap(tmp);
+        }
+    };
+    // least significant first: high mask word, low mask word, (inst, level);
+    // a zero word is skipped whole (every mask of an m <= 64 problem)
+    phase(khi, or_hi, true);
+    phase(klo, or_lo, true);
+    phase(kgrp, or_grp, false);
+    return order;
 }
 
 extern "C" int mpqp_plan_results(mpqp_plan *P, mpqp_batch_result **out)
@@ -857,17 +913,20 @@ extern "C" int mpqp_plan_results(mpqp_plan *P, mpqp_batch_result **out)
     long long nopt = std::min(ctl.n_opt, P->B.opt_cap);
     std::vector<OptRec> ov(nopt);
     if (nopt) CK(cudaMemcpy(ov.data(), P->B.opt, sizeof(OptRec) * nopt, cudaMemcpyDeviceToHost));
-    std::sort(ov.begin(), ov.end(), [](const OptRec &a, const OptRec &b) {
-        if (a.inst != b.inst) return a.inst < b.inst;
-        if (a.level != b.level) return a.level < b.level;
-        return set_less(a.lo, a.hi, b.lo, b.hi);
-    });
+    // order (inst, level, set), sets of one size in the lexicographic order of
+    // their sorted element lists: for equal-size sets that is the ascending
+    // order of the bit-reversed, complemented masks.  An LSD radix sort on
+    // those integer keys (high mask word, low mask word, then instance and
+    // level) moves indices, not records, and skips every digit that all sets
+    // share.
+    std::vector<uint32_t> order = sorted_opt_order(ov);
     R->n_opt = nopt;
     R->opt = (mpqp_opt_set *)calloc(nopt ? nopt : 1, sizeof(mpqp_opt_set));
     for (long long i = 0; i < nopt; i++) {
+        const OptRec &v = ov[order[i]];
         mpqp_opt_set &o = R->opt[i];
-        o.mask_lo = ov[i].lo; o.mask_hi = ov[i].hi; o.inst = ov[i].inst; o.level = ov[i].level;
-        o.t = ov[i].t; o.r = ov[i].r; o.region = ov[i].region; o.fp64 = ov[i].fp64; o.rec = ov[i].rec;
+        o.mask_lo = v.lo; o.mask_hi = v.hi; o.inst = v.inst; o.level = v.level;
+        o.t = v.t; o.r = v.r; o.region = v.region; o.fp64 = v.fp64; o.rec = v.rec;
     }
     R->h2d_bytes = P->h2d_bytes;
     R->d2h_bytes = (long long)(sizeof(Ctl) + sizeof(InstCtl) * P->n_inst + sizeof(OptRec) * nopt);
