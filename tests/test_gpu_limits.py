@@ -8,6 +8,9 @@
 * m = 129 and an empty instance list are rejected with MPQP_EINVAL.
 * k_min > 0: lower levels are enumerated for pruning but not evaluated; the
   evaluated sets match the oracle's.
+* The optimal sets come back ordered by instance, then size, then the sorted
+  element lists (also for masks that use the high word), and equal the
+  oracle's.
 """
 import numpy as np
 import pytest
@@ -59,3 +62,18 @@ def test_k_min_evaluates_only_upper_levels(gpu_lib, precision):
     assert res.candidates == ref.n_cand and res.total("feasible") == ref.n_feasible
     assert res.total("optimal") == ref.n_optimal and res.total("regions") == ref.n_region
     assert all(int(o["level"]) >= 2 for o in res.opt)
+
+
+def test_optimal_sets_in_instance_level_lexicographic_order(gpu_lib):
+    probs = [P.scale_problem(P.random_mpqp(3, 128, 2, seed=7)), P.scale_problem(P.random_n4_m10_p2()),
+             P.scale_problem(P.random_mpqp(5, 70, 3, seed=3))]
+    res = solver.solve(probs, precision=solver.MIXED, k_max=3, cand_cap=1 << 20, arena_bytes=1 << 28)
+    assert res.status == 0 and len(res.opt) > 0
+    keys = [(int(o["inst"]), int(o["level"]), tuple(solver.mask_to_set(o["mask_lo"], o["mask_hi"]))) for o in res.opt]
+    assert all(len(k[2]) == k[1] for k in keys)
+    assert all(a < b for a, b in zip(keys, keys[1:]))
+    assert any(max(k[2]) >= 64 for k in keys if k[2])                      # high-word masks are ordered too
+    for i, prob in enumerate(probs):
+        ref = O.enumerate_sets(prob, k_max=3, nthreads=8)
+        want = sorted((c["level"], tuple(O.mask_to_set(c["mask_lo"], c["mask_hi"]))) for c in ref.cand if c["optimal"])
+        assert [(k[1], k[2]) for k in keys if k[0] == i] == want, i
