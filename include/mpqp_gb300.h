@@ -171,7 +171,10 @@ typedef struct {
     double device_ms;             /* events around the device work          */
     mpqp_inst_stats *inst;        /* n_inst                                 */
     long long n_opt;
-    mpqp_opt_set *opt;            /* n_opt, sorted (inst, level, mask)      */
+    mpqp_opt_set *opt;            /* n_opt, ordered by instance, then |S|,
+                                     then the ascending element lists of S
+                                     (lexicographic); the same order on
+                                     every run                               */
     long long n_rec;
     void *rec;                    /* n_rec records (104 bytes each) or NULL */
     long long h2d_bytes;          /* problem data uploaded by the plan      */
