@@ -89,7 +89,10 @@ struct Node {                   // a feasible (or, when exhaustive, any) active 
 // NODE_FP64CHAIN: this set, or one of the sets its LP1 warm start descends
 // from, needed the FP64 re-solve (mixed precision); FP32 "infeasible"
 // verdicts below such a node are re-solved in FP64 too.
-enum NodeFlags : int { NODE_FEASIBLE = 1, NODE_VALID = 2, NODE_FP64CHAIN = 4 };
+// NODE_CERT: the stored FP32 tableau is the one whose basic solution
+// certified this set feasible (every slack of the set nonbasic, every basic
+// slack clear of the growth-scaled margin).
+enum NodeFlags : int { NODE_FEASIBLE = 1, NODE_VALID = 2, NODE_FP64CHAIN = 4, NODE_CERT = 8 };
 // bits 8..16 of the flags: 1 + the live rows of the stored FP32 LP1 tableau
 // (rows of basic free variables dropped, the objective row right after them);
 // 0: all M1 rows

@@ -913,6 +913,28 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         // lane t holds candidate t's parent tableau offset (for the prefetch)
         const long long my_toff = lane < cnt ? B.node[pside][mine.parent].tab_off : -1;
         const int my_inst = lane < cnt ? B.node[pside][mine.parent].inst : 0;
+        // Candidates of their instance's last level (nothing is stored there)
+        // decided without an LP: every nonbasic slack is zero at a certified
+        // vertex of the parent's face, so a child whose new slack is nonbasic
+        // in the parent's certified tableau -- or, below, in the final
+        // tableau of a sibling certified feasible -- is feasible with that
+        // vertex's certificate.  (The zero-pivot LP of such a child ends at
+        // the same vertex.)  Not with records or exhaustive enumeration.
+        const bool at_vertex = mixed && !B.rec && !B.exhaustive;
+        unsigned done = 0;
+        if (at_vertex) {
+            bool q = false;
+            if (lane < cnt) {
+                const Node &pn = B.node[pside][mine.parent];
+                const InstDesc &Il = B.inst[pn.inst];
+                if ((pn.flags & NODE_CERT) && level == Il.k_max) {
+                    const uint8_t *pnid = B.ids[pside] + pn.ids_off + Il.M1;
+                    const int want = Il.nv + mine.j;
+                    for (int cc = 0; cc < Il.nv; cc++) q |= (int)pnid[cc] == want;
+                }
+            }
+            done = __ballot_sync(FULLMASK, q);
+        }
     for (int t = 0; t < cnt; t++) {
         const long long w = w0 + t;
         Cand c;
@@ -943,6 +965,25 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
                 atomicAdd(&B.ictl[lc.inst].feas_digest, (unsigned long long)lc.c);
             }
             lc.reset(inst);
+        }
+        if ((done >> t) & 1u) {
+            // the last level stores no tableau and inserts nothing into the hash
+            uint64_t lo = par.lo, hi = par.hi;
+            if (c.j < 64) lo |= 1ull << c.j; else hi |= 1ull << (c.j - 64);
+            lc.a++;
+            lc.c += (long long)mask_digest(lo, hi);
+            if (lane == 0) {
+                if (nbase + t < B.node_cap) {
+                    Node nd;
+                    nd.lo = lo; nd.hi = hi; nd.inst = inst;
+                    nd.flags = NODE_VALID | NODE_FEASIBLE | (par.flags & NODE_FP64CHAIN);
+                    nd.tab_off = -1; nd.ids_off = -1; nd.rec = -1;
+                    B.node[side][nbase + t] = nd;
+                } else {
+                    atomicOr(&ctl->overflow, OV_NODE);
+                }
+            }
+            continue;
         }
         const int M1 = I.M1, nv = I.nv, ld = I.ld1;
         // the parent's live rows (FP32 tableaus drop the rows of basic free
@@ -1072,8 +1113,27 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
                 for (int cc = lane; cc < ld; cc += 32) tab[(size_t)rows * ld + cc] = obj[cc];
                 __syncwarp();
             }
-            store_node<T, T>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap, par.flags & NODE_FP64CHAIN,
-                             0, true, nbase + t, mixed ? rows : -1);
+            store_node<T, T>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap,
+                             (par.flags & NODE_FP64CHAIN) | (mixed && feasible ? NODE_CERT : 0), 0, true, nbase + t,
+                             mixed ? rows : -1);
+        }
+        if (at_vertex && feasible && level == I.k_max) {
+            // later siblings whose new slack is nonbasic at this vertex
+            unsigned nb0 = 0, nb1 = 0, nb2 = 0, nb3 = 0;
+            for (int cc = lane; cc < nv; cc += 32) {
+                const int id = (int)nid[cc] - nv;
+                if (id >= 0 && id < I.m) {
+                    const unsigned bit = 1u << (id & 31);
+                    const int wd = id >> 5;
+                    nb0 |= wd == 0 ? bit : 0u; nb1 |= wd == 1 ? bit : 0u;
+                    nb2 |= wd == 2 ? bit : 0u; nb3 |= wd == 3 ? bit : 0u;
+                }
+            }
+            nb0 = __reduce_or_sync(FULLMASK, nb0); nb1 = __reduce_or_sync(FULLMASK, nb1);
+            nb2 = __reduce_or_sync(FULLMASK, nb2); nb3 = __reduce_or_sync(FULLMASK, nb3);
+            const int mj = mine.j;
+            const unsigned wsel = mj < 32 ? nb0 : mj < 64 ? nb1 : mj < 96 ? nb2 : nb3;
+            done |= __ballot_sync(FULLMASK, lane > t && lane < cnt && mine.parent == c.parent && ((wsel >> (mj & 31)) & 1u));
         }
     }
     }
