@@ -16,6 +16,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/mpqp_gb300.h"
@@ -826,29 +827,34 @@ static uint64_t bit_reverse64(uint64_t x)
     return (x >> 32) | (x << 32);
 }
 
-// indices of the optimal-set records in (inst, level, set) order
-static std::vector<uint32_t> sorted_opt_order(const std::vector<OptRec> &ov)
+// Sort keys of the optimal-set records, by record index: the order is
+// (grp, ~lo, ~hi) ascending, grp = (inst, level), lo / hi the bit-reversed
+// mask words (the complements order the sorted element lists of equal-size
+// sets lexicographically).
+struct OptKeys {
+    std::vector<uint64_t> hi, lo, grp;
+    uint64_t or_hi = 0, or_lo = 0, or_grp = 0;   // which bits occur at all
+};
+
+static bool opt_key_less(const OptKeys &K, uint32_t a, uint32_t b)
 {
-    const size_t n = ov.size();
+    if (K.grp[a] != K.grp[b]) return K.grp[a] < K.grp[b];
+    if (K.lo[a] != K.lo[b]) return K.lo[a] > K.lo[b];
+    return K.hi[a] > K.hi[b];
+}
+
+// Stable LSD radix sort of the record indices [b, e) into out[0, e - b): per
+// key all digit histograms in one pass, then a scatter pass per digit that
+// varies; digits above the highest bit any key has are skipped.
+static void radix_order_range(const OptKeys &K, size_t b, size_t e, uint32_t *out)
+{
+    const size_t n = e - b;
     std::vector<uint32_t> order(n), tmp(n);
-    for (size_t i = 0; i < n; i++) order[i] = (uint32_t)i;
-    if (n < 2) return order;
-    // the three 64-bit sort keys of every record, by record index
-    std::vector<uint64_t> khi(n), klo(n), kgrp(n);
-    uint64_t or_hi = 0, or_lo = 0, or_grp = 0;
-    for (size_t i = 0; i < n; i++) {
-        khi[i] = bit_reverse64(ov[i].hi);
-        klo[i] = bit_reverse64(ov[i].lo);
-        kgrp[i] = ((uint64_t)(uint32_t)ov[i].inst << 32) | (uint32_t)ov[i].level;
-        or_hi |= khi[i]; or_lo |= klo[i]; or_grp |= kgrp[i];
-    }
+    for (size_t i = 0; i < n; i++) order[i] = (uint32_t)(b + i);
     constexpr int kBits = 11, kBins = 1 << kBits;
     std::vector<uint32_t> hist((size_t)6 * kBins);
-    // one stable LSD phase on one key (ascending order of ~key when flip):
-    // all digit histograms in one pass, then a scatter pass per digit that
-    // varies; digits above the highest set bit of any key are skipped
     auto phase = [&](const std::vector<uint64_t> &key, uint64_t any, bool flip) {
-        if (!any) return;
+        if (!any || n < 2) return;
         const int nd = (64 - __builtin_clzll(any) + kBits - 1) / kBits;
         const uint64_t fl = flip ? ~0ULL : 0ULL;
         std::fill(hist.begin(), hist.begin() + (size_t)nd * kBins, 0u);
@@ -861,7 +867,7 @@ static std::vector<uint32_t> sorted_opt_order(const std::vector<OptRec> &ov)
             const int sh = d * kBits;
             if (h[((key[order[0]] ^ fl) >> sh) & (kBins - 1)] == n) continue;   // all keys share this digit
             uint32_t sum = 0;
-            for (int b = 0; b < kBins; b++) { const uint32_t c = h[b]; h[b] = sum; sum += c; }
+            for (int q = 0; q < kBins; q++) { const uint32_t c = h[q]; h[q] = sum; sum += c; }
             for (size_t i = 0; i < n; i++) {
                 const uint32_t r = order[i];
                 tmp[h[((key[r] ^ fl) >> sh) & (kBins - 1)]++] = r;
@@ -871,9 +877,63 @@ static std::vector<uint32_t> sorted_opt_order(const std::vector<OptRec> &ov)
     };
     // least significant first: high mask word, low mask word, (inst, level);
     // a zero word is skipped whole (every mask of an m <= 64 problem)
-    phase(khi, or_hi, true);
-    phase(klo, or_lo, true);
-    phase(kgrp, or_grp, false);
+    phase(K.hi, K.or_hi, true);
+    phase(K.lo, K.or_lo, true);
+    phase(K.grp, K.or_grp, false);
+    std::copy(order.begin(), order.end(), out);
+}
+
+// f(0) .. f(T-1) on up to T threads (the calling thread included); when a
+// thread cannot be started, the calling thread runs the rest
+template <typename F>
+static void run_parallel(unsigned T, F f)
+{
+    std::vector<std::thread> th;
+    try {
+        for (unsigned t = 1; t < T; t++) th.emplace_back(f, t);
+    } catch (...) {
+    }
+    f(0u);
+    for (unsigned t = (unsigned)th.size() + 1; t < T; t++) f(t);
+    for (std::thread &x : th) x.join();
+}
+
+// indices of the optimal-set records in (inst, level, set) order
+static std::vector<uint32_t> sorted_opt_order(const std::vector<OptRec> &ov)
+{
+    const size_t n = ov.size();
+    OptKeys K;
+    K.hi.resize(n); K.lo.resize(n); K.grp.resize(n);
+    for (size_t i = 0; i < n; i++) {
+        K.hi[i] = bit_reverse64(ov[i].hi);
+        K.lo[i] = bit_reverse64(ov[i].lo);
+        K.grp[i] = ((uint64_t)(uint32_t)ov[i].inst << 32) | (uint32_t)ov[i].level;
+        K.or_hi |= K.hi[i]; K.or_lo |= K.lo[i]; K.or_grp |= K.grp[i];
+    }
+    std::vector<uint32_t> order(n);
+    // large result sets: T contiguous chunks sorted concurrently, then merged
+    // pairwise; a merge takes the earlier chunk first on ties, so the result
+    // is the same stable order as one sort
+    unsigned T = std::thread::hardware_concurrency();
+    T = n >= ((size_t)1 << 16) ? std::min(std::max(T, 1u), 8u) : 1u;
+    if (T == 1) {
+        radix_order_range(K, 0, n, order.data());
+        return order;
+    }
+    std::vector<size_t> cut(T + 1);
+    for (unsigned t = 0; t <= T; t++) cut[t] = n * t / T;
+    run_parallel(T, [&](unsigned t) { radix_order_range(K, cut[t], cut[t + 1], order.data() + cut[t]); });
+    std::vector<uint32_t> tmp(n);
+    const auto less = [&K](uint32_t a, uint32_t b) { return opt_key_less(K, a, b); };
+    for (unsigned width = 1; width < T; width *= 2) {
+        const unsigned pairs = (T + 2 * width - 1) / (2 * width);
+        run_parallel(pairs, [&](unsigned q) {
+            const unsigned t = q * 2 * width;
+            const size_t a = cut[t], m = cut[std::min(t + width, T)], e = cut[std::min(t + 2 * width, T)];
+            std::merge(order.begin() + a, order.begin() + m, order.begin() + m, order.begin() + e, tmp.begin() + a, less);
+        });
+        order.swap(tmp);
+    }
     return order;
 }
 
