@@ -100,7 +100,7 @@ enum {
     MPQP_ELAYOUT = -4,     /* LP matrices do not have the reference layout */
     MPQP_ECUDA = -5,       /* CUDA runtime error                           */
     MPQP_ECAPACITY = -6,   /* a device buffer overflowed                   */
-    MPQP_ENOMEM = -7       /* device allocation failed                     */
+    MPQP_ENOMEM = -7       /* device (or host) allocation failed           */
 };
 
 enum { MPQP_FP64 = 0, MPQP_MIXED = 1 };

@@ -14,6 +14,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
+#include <new>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -884,18 +886,25 @@ static void radix_order_range(const OptKeys &K, size_t b, size_t e, uint32_t *ou
 }
 
 // f(0) .. f(T-1) on up to T threads (the calling thread included); when a
-// thread cannot be started, the calling thread runs the rest
+// thread cannot be started, the calling thread runs the rest.  An exception
+// of any f(t) is rethrown in the calling thread once all have finished.
 template <typename F>
 static void run_parallel(unsigned T, F f)
 {
+    std::vector<std::exception_ptr> err(T);
+    auto guarded = [&](unsigned t) {
+        try { f(t); } catch (...) { err[t] = std::current_exception(); }
+    };
     std::vector<std::thread> th;
     try {
-        for (unsigned t = 1; t < T; t++) th.emplace_back(f, t);
+        for (unsigned t = 1; t < T; t++) th.emplace_back(guarded, t);
     } catch (...) {
     }
-    f(0u);
-    for (unsigned t = (unsigned)th.size() + 1; t < T; t++) f(t);
+    guarded(0u);
+    for (unsigned t = (unsigned)th.size() + 1; t < T; t++) guarded(t);
     for (std::thread &x : th) x.join();
+    for (const std::exception_ptr &e : err)
+        if (e) std::rethrow_exception(e);
 }
 
 // indices of the optimal-set records in (inst, level, set) order
@@ -937,10 +946,11 @@ static std::vector<uint32_t> sorted_opt_order(const std::vector<OptRec> &ov)
     return order;
 }
 
-extern "C" int mpqp_plan_results(mpqp_plan *P, mpqp_batch_result **out)
+// The body of mpqp_plan_results: R is built here; *complete is set only when
+// the whole result is in R (the caller frees a partial one).  Host
+// allocation failures throw std::bad_alloc.
+static int plan_results_impl(mpqp_plan *P, mpqp_batch_result *&R, bool *complete)
 {
-    *out = nullptr;
-    if (!P || !P->ran) { set_err("plan has not run"); return MPQP_EINVAL; }
     CK(cudaEventSynchronize(P->ev1));
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, P->ev0, P->ev1));
@@ -949,7 +959,8 @@ extern "C" int mpqp_plan_results(mpqp_plan *P, mpqp_batch_result **out)
     CK(cudaMemcpy(&ctl, P->B.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
     std::vector<InstCtl> ic(P->n_inst);
     CK(cudaMemcpy(ic.data(), P->B.ictl, sizeof(InstCtl) * P->n_inst, cudaMemcpyDeviceToHost));
-    mpqp_batch_result *R = (mpqp_batch_result *)calloc(1, sizeof(mpqp_batch_result));
+    R = (mpqp_batch_result *)calloc(1, sizeof(mpqp_batch_result));
+    if (!R) throw std::bad_alloc();
     R->n_inst = P->n_inst;
     R->device_ms = ms;
     R->overflow = ctl.overflow;
@@ -957,6 +968,7 @@ extern "C" int mpqp_plan_results(mpqp_plan *P, mpqp_batch_result **out)
     if (ctl.overflow & OV_WAIT) set_err("a bulk copy did not complete within its bounded wait");
     else if (ctl.overflow) set_err("device buffer overflow (bits " + std::to_string(ctl.overflow) + ")");
     R->inst = (mpqp_inst_stats *)calloc(P->n_inst, sizeof(mpqp_inst_stats));
+    if (!R->inst) throw std::bad_alloc();
     int nlev = 0;
     for (int i = 0; i < P->n_inst; i++) {
         mpqp_inst_stats &s = R->inst[i];
@@ -982,6 +994,7 @@ extern "C" int mpqp_plan_results(mpqp_plan *P, mpqp_batch_result **out)
     std::vector<uint32_t> order = sorted_opt_order(ov);
     R->n_opt = nopt;
     R->opt = (mpqp_opt_set *)calloc(nopt ? nopt : 1, sizeof(mpqp_opt_set));
+    if (!R->opt) throw std::bad_alloc();
     for (long long i = 0; i < nopt; i++) {
         const OptRec &v = ov[order[i]];
         mpqp_opt_set &o = R->opt[i];
@@ -995,10 +1008,35 @@ extern "C" int mpqp_plan_results(mpqp_plan *P, mpqp_batch_result **out)
         R->d2h_bytes += (long long)sizeof(CandRec) * nrec;
         R->n_rec = nrec;
         R->rec = malloc(sizeof(CandRec) * (nrec ? nrec : 1));
+        if (!R->rec) throw std::bad_alloc();
         if (nrec) CK(cudaMemcpy(R->rec, P->B.rec, sizeof(CandRec) * nrec, cudaMemcpyDeviceToHost));
     }
-    *out = R;
+    *complete = true;
     return R->status;
+}
+
+extern "C" int mpqp_plan_results(mpqp_plan *P, mpqp_batch_result **out)
+{
+    *out = nullptr;
+    if (!P || !P->ran) { set_err("plan has not run"); return MPQP_EINVAL; }
+    mpqp_batch_result *R = nullptr;
+    bool complete = false;
+    int rc;
+    try {
+        rc = plan_results_impl(P, R, &complete);
+    } catch (const std::bad_alloc &) {
+        set_err("host memory allocation failed while reading the results back");
+        rc = MPQP_ENOMEM;
+    } catch (...) {
+        set_err("host error while reading the results back");
+        rc = MPQP_ENOMEM;
+    }
+    if (!complete) {
+        mpqp_batch_free(R);
+        return rc;
+    }
+    *out = R;
+    return rc;
 }
 
 extern "C" void mpqp_plan_destroy(mpqp_plan *P)
