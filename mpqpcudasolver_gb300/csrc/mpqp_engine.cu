@@ -296,6 +296,17 @@ struct mpqp_plan {
     long long h2d_bytes = 0;
 };
 
+// An exported entry point lets no C++ exception through (a failed host
+// allocation inside becomes MPQP_ENOMEM).
+static int host_failure(const char *where)
+{
+    try {
+        set_err(std::string(where) + ": host memory allocation failed");
+    } catch (...) {
+    }
+    return MPQP_ENOMEM;
+}
+
 extern "C" void mpqp_default_options(mpqp_options *o)
 {
     memset(o, 0, sizeof(*o));
@@ -519,7 +530,7 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
     return MPQP_OK;
 }
 
-extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpqp_options *opt_in, mpqp_plan **out)
+static int mpqp_plan_create_impl(int n_inst, const mpqp_problem *probs, const mpqp_options *opt_in, mpqp_plan **out)
 {
     std::lock_guard<std::mutex> lk(g_mu);
     *out = nullptr;
@@ -762,6 +773,15 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
     return MPQP_OK;
 }
 
+extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpqp_options *opt_in, mpqp_plan **out)
+{
+    try {
+        return mpqp_plan_create_impl(n_inst, probs, opt_in, out);
+    } catch (...) {
+        return host_failure("mpqp_plan_create");
+    }
+}
+
 extern "C" int mpqp_plan_run(mpqp_plan *P, void *stream)
 {
     if (!P) return MPQP_EINVAL;
@@ -780,7 +800,7 @@ extern "C" int mpqp_plan_run(mpqp_plan *P, void *stream)
 
 extern "C" int mpqp_plan_launches(const mpqp_plan *P) { return P ? P->n_launches : 0; }
 
-extern "C" int mpqp_plan_run_timed(mpqp_plan *P, void *stream)
+static int mpqp_plan_run_timed_impl(mpqp_plan *P, void *stream)
 {
     if (!P) return MPQP_EINVAL;
     cudaStream_t s = (cudaStream_t)stream;
@@ -793,7 +813,16 @@ extern "C" int mpqp_plan_run_timed(mpqp_plan *P, void *stream)
     return MPQP_OK;
 }
 
-extern "C" int mpqp_plan_kernel_times(mpqp_plan *P, int max_kernels, char *names, double *ms, int *count)
+extern "C" int mpqp_plan_run_timed(mpqp_plan *P, void *stream)
+{
+    try {
+        return mpqp_plan_run_timed_impl(P, stream);
+    } catch (...) {
+        return host_failure("mpqp_plan_run_timed");
+    }
+}
+
+static int mpqp_plan_kernel_times_impl(mpqp_plan *P, int max_kernels, char *names, double *ms, int *count)
 {
     if (!P || !P->timed) { set_err("no timed run"); return MPQP_EINVAL; }
     CK(cudaEventSynchronize(P->ev1));
@@ -817,6 +846,15 @@ extern "C" int mpqp_plan_kernel_times(mpqp_plan *P, int max_kernels, char *names
         count[i] = c[i];
     }
     return n;
+}
+
+extern "C" int mpqp_plan_kernel_times(mpqp_plan *P, int max_kernels, char *names, double *ms, int *count)
+{
+    try {
+        return mpqp_plan_kernel_times_impl(P, max_kernels, names, ms, count);
+    } catch (...) {
+        return host_failure("mpqp_plan_kernel_times");
+    }
 }
 
 static uint64_t bit_reverse64(uint64_t x)
@@ -1077,8 +1115,8 @@ extern "C" long long mpqp_region_laws_stride(const mpqp_problem *pr)
     return (long long)pr->m * P1 + (long long)pr->n * P1 + (long long)(pr->m + pr->ncp) * P1;
 }
 
-extern "C" int mpqp_region_laws(const mpqp_problem *prob, long long n_sets, const uint64_t *masks, double *laws,
-                                int *sizes)
+static int mpqp_region_laws_impl(const mpqp_problem *prob, long long n_sets, const uint64_t *masks, double *laws,
+                                 int *sizes)
 {
     if (!prob || n_sets < 0 || (n_sets && (!masks || !laws || !sizes))) { set_err("bad arguments"); return MPQP_EINVAL; }
     if (n_sets == 0) return MPQP_OK;
@@ -1120,6 +1158,16 @@ extern "C" int mpqp_region_laws(const mpqp_problem *prob, long long n_sets, cons
     }
     mpqp_plan_destroy(P);
     return rc;
+}
+
+extern "C" int mpqp_region_laws(const mpqp_problem *prob, long long n_sets, const uint64_t *masks, double *laws,
+                                int *sizes)
+{
+    try {
+        return mpqp_region_laws_impl(prob, n_sets, masks, laws, sizes);
+    } catch (...) {
+        return host_failure("mpqp_region_laws");
+    }
 }
 
 // ---------------------------------------------------------------------
@@ -1214,10 +1262,10 @@ static int unpack_lp(const double *AxT, int n_c, int n_x, int n_t, const double 
     return MPQP_OK;
 }
 
-extern "C" int mpqp_unpack_lp(const double *AxT, int n_c, int n_x, int n_t, const double *A1, const double *xb1,
-                              int M1, int N1, const double *A2, const double *xb2, int M2, int N2, int n_eqs,
-                              double *Q, double *c, double *H, double *A, double *b, double *F, double *At,
-                              double *bt, int *n_cp)
+static int mpqp_unpack_lp_impl(const double *AxT, int n_c, int n_x, int n_t, const double *A1, const double *xb1,
+                               int M1, int N1, const double *A2, const double *xb2, int M2, int N2, int n_eqs,
+                               double *Q, double *c, double *H, double *A, double *b, double *F, double *At,
+                               double *bt, int *n_cp)
 {
     std::vector<double> q, cc, h, a, bb, f, at, btv;
     int ncp = 0;
@@ -1230,10 +1278,23 @@ extern "C" int mpqp_unpack_lp(const double *AxT, int n_c, int n_x, int n_t, cons
     return MPQP_OK;
 }
 
-extern "C" GPUResults *mpqp(const double *AxT, int n_c, int n_x, int n_t, int k_min, int k_max, int extra_batches,
-                            const double *A1, const double *xb1, const int *b1, int M1, int N1, const double *A2,
-                            const double *xb2, const int *b2, const int *non_b2, int M2, int N2, int n_eqs,
-                            int reserved_memory)
+extern "C" int mpqp_unpack_lp(const double *AxT, int n_c, int n_x, int n_t, const double *A1, const double *xb1,
+                              int M1, int N1, const double *A2, const double *xb2, int M2, int N2, int n_eqs,
+                              double *Q, double *c, double *H, double *A, double *b, double *F, double *At,
+                              double *bt, int *n_cp)
+{
+    try {
+        return mpqp_unpack_lp_impl(AxT, n_c, n_x, n_t, A1, xb1, M1, N1, A2, xb2, M2, N2, n_eqs, Q, c, H, A, b, F,
+                                   At, bt, n_cp);
+    } catch (...) {
+        return host_failure("mpqp_unpack_lp");
+    }
+}
+
+static GPUResults *mpqp_impl(const double *AxT, int n_c, int n_x, int n_t, int k_min, int k_max, int extra_batches,
+                             const double *A1, const double *xb1, const int *b1, int M1, int N1, const double *A2,
+                             const double *xb2, const int *b2, const int *non_b2, int M2, int N2, int n_eqs,
+                             int reserved_memory)
 {
     (void)b1; (void)b2; (void)non_b2; (void)extra_batches;
     {
@@ -1310,6 +1371,24 @@ extern "C" GPUResults *mpqp(const double *AxT, int n_c, int n_x, int n_t, int k_
     std::lock_guard<std::mutex> lk(g_mu);
     g_last = G;
     return G;
+}
+
+extern "C" GPUResults *mpqp(const double *AxT, int n_c, int n_x, int n_t, int k_min, int k_max, int extra_batches,
+                            const double *A1, const double *xb1, const int *b1, int M1, int N1, const double *A2,
+                            const double *xb2, const int *b2, const int *non_b2, int M2, int N2, int n_eqs,
+                            int reserved_memory)
+{
+    try {
+        return mpqp_impl(AxT, n_c, n_x, n_t, k_min, k_max, extra_batches, A1, xb1, b1, M1, N1, A2, xb2, b2, non_b2,
+                         M2, N2, n_eqs, reserved_memory);
+    } catch (...) {
+        host_failure("mpqp");
+        try {
+            return g_last = error_result(MPQP_ENOMEM);
+        } catch (...) {
+            return nullptr;
+        }
+    }
 }
 
 extern "C" void warm_up(void)

@@ -48,7 +48,7 @@ struct DevMem {
 
 }  // namespace
 
-extern "C" int mpqp_reduce_constraints(const mpqp_problem *prob, int *row_status)
+static int mpqp_reduce_constraints_impl(const mpqp_problem *prob, int *row_status)
 {
     if (!prob || !row_status) return fail(MPQP_EINVAL, "mpqp_reduce_constraints: null argument");
     const mpqp_problem &P = *prob;
@@ -157,4 +157,18 @@ extern "C" int mpqp_reduce_constraints(const mpqp_problem *prob, int *row_status
     for (int c = 0; c < n_check; c++)
         if (out[c]) row_status[check_pos[c]] = MPQP_ROW_REDUNDANT;
     return MPQP_OK;
+}
+
+extern "C" int mpqp_reduce_constraints(const mpqp_problem *prob, int *row_status)
+{
+    try {
+        return mpqp_reduce_constraints_impl(prob, row_status);
+    } catch (...) {
+        // no C++ exception leaves an exported entry point
+        try {
+            return fail(MPQP_ENOMEM, "mpqp_reduce_constraints: host memory allocation failed");
+        } catch (...) {
+            return MPQP_ENOMEM;
+        }
+    }
 }
