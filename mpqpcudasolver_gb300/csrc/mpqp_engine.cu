@@ -782,7 +782,7 @@ extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpq
     }
 }
 
-extern "C" int mpqp_plan_run(mpqp_plan *P, void *stream)
+static int mpqp_plan_run_impl(mpqp_plan *P, void *stream)
 {
     if (!P) return MPQP_EINVAL;
     cudaStream_t s = (cudaStream_t)stream;
@@ -796,6 +796,15 @@ extern "C" int mpqp_plan_run(mpqp_plan *P, void *stream)
     CK(cudaEventRecord(P->ev1, s));
     P->ran = true;
     return MPQP_OK;
+}
+
+extern "C" int mpqp_plan_run(mpqp_plan *P, void *stream)
+{
+    try {
+        return mpqp_plan_run_impl(P, stream);
+    } catch (...) {
+        return host_failure("mpqp_plan_run");
+    }
 }
 
 extern "C" int mpqp_plan_launches(const mpqp_plan *P) { return P ? P->n_launches : 0; }
