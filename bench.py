@@ -127,7 +127,11 @@ def lp1_hbm_bytes(probs, kmax, res, elem: int) -> float:
     Per checked candidate (levels >= 1): candidate record 8 B, parent node
     48 B, parent LP1 tableau (M1+1)*ld1*s and basis ids M1+nv (read).  Per
     feasible child: node 48 B and hash slot 32 B (write); per child kept as a
-    parent of the next level: its tableau and ids (write).
+    parent of the next level: its tableau and ids (write).  The model keeps
+    the tableau read for the last-level candidates decided at a certified
+    vertex without one (about 14 % of a last level) and the hash slot of
+    last-level sets (never inserted), so it overstates the bytes by up to
+    about a tenth.
     """
     total = 0.0
     for i, pr in enumerate(probs):
