@@ -2,7 +2,6 @@
 the reference's main.py calls mpqp_cuda.so (main.py:25-50,60,144), and the
 host mirror of main.py's loop, against the oracle and the reference's own
 regions (golden fixtures)."""
-import ctypes
 import os
 
 import numpy as np
