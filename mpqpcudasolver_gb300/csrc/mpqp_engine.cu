@@ -456,7 +456,7 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
     int nl = 0;
     if (timed) P->kname.clear();
     auto chk = [&](const char *name, cudaError_t e) -> int {
-        if (e != cudaSuccess) { set_err(std::string("launch: ") + cudaGetErrorString(e)); return MPQP_ECUDA; }
+        if (e != cudaSuccess) { set_err(std::string("launch of ") + name + ": " + cudaGetErrorString(e)); return MPQP_ECUDA; }
         return MPQP_OK;
     };
     auto pre = [&](const char *name) -> int {
