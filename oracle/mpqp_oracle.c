@@ -1007,6 +1007,108 @@ void orc_free_result(orc_result *res)
     res->cand = NULL;
 }
 
+/* Dual certificate of LP1 infeasibility from a final basis.  LP1 of a set T
+ * is  min c.w  s.t.  G u + w = beta, w >= 0, u free  (c = 1 on T, 0 elsewhere),
+ * whose dual is  max beta.y  s.t.  G^T y = 0, y <= c; every such y gives
+ * z*(T) >= beta.y.  The final basis fixes y_i = c_i on the rows whose slack is
+ * basic; with every free variable basic, the duals of the nv nonbasic slacks
+ * solve the square system  G_N^T y_N = -G_B^T c_B  (Gaussian elimination with
+ * partial pivoting).  Returns 1 with *bound = beta.y when that y meets
+ * y <= c + sign_tol, else 0.  (Not part of the reference's algorithm: the
+ * checker for a certificate built from FP32 bases.) */
+static int lp1_basis_bound(const orc_data *d, const lp1_state *s, const int *T, int k, double sign_tol,
+                           double *bound)
+{
+    const int nv = d->nv, M1 = d->M1, ld = d->ld1;
+    for (int c = 0; c < nv; c++) if (s->nid[c] < nv) return 0;     /* a free variable nonbasic */
+    double *cost = calloc((size_t)M1, sizeof(double));
+    double *y = calloc((size_t)M1, sizeof(double));
+    double *M = malloc(sizeof(double) * (size_t)nv * (nv + 1));     /* [G_N^T | rhs] */
+    for (int a = 0; a < k; a++) cost[T[a]] = 1.0;
+    for (int r = 0; r < M1; r++) {
+        const int i = s->bid[r] - nv;
+        if (i >= 0) y[i] = cost[i];
+    }
+    for (int v = 0; v < nv; v++) {
+        double rhs = 0.0;
+        for (int r = 0; r < M1; r++) {
+            const int i = s->bid[r] - nv;
+            if (i >= 0 && cost[i] != 0.0) rhs -= d->root[(size_t)i * ld + v] * cost[i];
+        }
+        for (int c = 0; c < nv; c++) M[(size_t)v * (nv + 1) + c] = d->root[(size_t)(s->nid[c] - nv) * ld + v];
+        M[(size_t)v * (nv + 1) + nv] = rhs;
+    }
+    int ok = 1;
+    for (int col = 0; col < nv && ok; col++) {
+        int piv = col;
+        double best = fabs(M[(size_t)col * (nv + 1) + col]), scale = 0.0;
+        for (int r = col; r < nv; r++) {
+            const double a = fabs(M[(size_t)r * (nv + 1) + col]);
+            if (a > best) { best = a; piv = r; }
+            if (a > scale) scale = a;
+        }
+        if (!(best > 1e-13 * (scale > 1.0 ? scale : 1.0))) { ok = 0; break; }
+        if (piv != col)
+            for (int c = 0; c <= nv; c++) {
+                const double t = M[(size_t)col * (nv + 1) + c];
+                M[(size_t)col * (nv + 1) + c] = M[(size_t)piv * (nv + 1) + c];
+                M[(size_t)piv * (nv + 1) + c] = t;
+            }
+        for (int r = col + 1; r < nv; r++) {
+            const double f = M[(size_t)r * (nv + 1) + col] / M[(size_t)col * (nv + 1) + col];
+            for (int c = col; c <= nv; c++) M[(size_t)r * (nv + 1) + c] -= f * M[(size_t)col * (nv + 1) + c];
+        }
+    }
+    if (ok) {
+        for (int r = nv - 1; r >= 0; r--) {
+            double acc = M[(size_t)r * (nv + 1) + nv];
+            for (int c = r + 1; c < nv; c++) acc -= M[(size_t)r * (nv + 1) + c] * y[s->nid[c] - nv];
+            y[s->nid[r] - nv] = acc / M[(size_t)r * (nv + 1) + r];
+        }
+        double b = 0.0;
+        for (int i = 0; i < M1 && ok; i++) {
+            if (y[i] > cost[i] + sign_tol) ok = 0;
+            b += d->root[(size_t)i * ld + nv] * y[i];
+        }
+        *bound = b;
+    }
+    free(cost); free(y); free(M);
+    return ok;
+}
+
+int orc_lp1_dual_bound(const orc_problem *pr, const orc_tol *tol, const int *S, int k, double sign_tol,
+                       double *bound, double *z_out, int *k_used)
+{
+    orc_data d;
+    int rc = prepare(pr, &d);
+    if (rc) return rc;
+    for (int a = 1; a < k; a++) if (S[a] <= S[a - 1]) { free_data(&d); return -4; }
+    if (k > 0 && (S[0] < 0 || S[k - 1] >= d.m)) { free_data(&d); return -4; }
+    const size_t tsz = (size_t)(d.M1 + 1) * d.ld1;
+    lp1_state a = { malloc(tsz * 8), malloc(d.M1), malloc(d.nv) };
+    lp1_state b = { malloc(tsz * 8), malloc(d.M1), malloc(d.nv) };
+    lp1_init_root(&d, &a);
+    /* the warm-start chain of the prefixes, up to the first infeasible one
+       (whose bound also bounds every superset) */
+    int used = 0, status = ORC_OPTIMAL;
+    double z = 0.0;
+    for (int i = 0; i < k; i++) {
+        int pv;
+        lp1_child(&d, &a, S[i], &b, tol, &status, &pv, &z);
+        lp1_state t = a; a = b; b = t;
+        used = i + 1;
+        if (!(status == ORC_OPTIMAL && z <= tol->tol_feas)) break;
+    }
+    int got = 0;
+    *bound = 0.0;
+    if (status == ORC_OPTIMAL) got = lp1_basis_bound(&d, &a, S, used, sign_tol, bound);
+    *z_out = z;
+    *k_used = used;
+    free(a.T); free(a.bid); free(a.nid); free(b.T); free(b.bid); free(b.nid);
+    free_data(&d);
+    return got;
+}
+
 int orc_check_set(const orc_problem *pr, const orc_tol *tol, const int *S, int k,
                   orc_cand *rec, double *laws, double *cr_rows, int *n_cr_rows)
 {

@@ -114,6 +114,14 @@ int orc_check_set(const orc_problem *pr, const orc_tol *tol, const int *S, int k
                   orc_cand *rec, double *laws, double *cr_rows, int *n_cr_rows);
 
 /* Precomputed KKT data, exposed for tests: Wm (m x m), Wh (m x p), wc (m). */
+/* Dual certificate of LP1 infeasibility: replays S's warm-start chain up to its
+ * first infeasible prefix (k_used elements) and builds the dual y of that
+ * final basis (y_i = 1 on the prefix's basic slacks, the nonbasic slacks' duals
+ * from G_N^T y_N = -G_B^T c_B).  Returns 1 with *bound = beta.y <= z* when
+ * y <= c + sign_tol holds, 0 when the basis gives no such y, < 0 on bad input.
+ * *z_out: the LP1 value of that prefix. */
+int orc_lp1_dual_bound(const orc_problem *pr, const orc_tol *tol, const int *S, int k, double sign_tol,
+                       double *bound, double *z_out, int *k_used);
 int orc_kkt_data(const orc_problem *pr, double *Wm, double *Wh, double *wc);
 
 #ifdef __cplusplus

@@ -95,6 +95,11 @@ def lib():
         _lib.orc_kkt_data.argtypes = [ctypes.POINTER(OrcProblem)] + [ctypes.POINTER(ctypes.c_double)] * 3
         _lib.orc_kkt_data.restype = ctypes.c_int
         _lib.orc_default_tol.argtypes = [ctypes.POINTER(OrcTol)]
+        _lib.orc_lp1_dual_bound.argtypes = [ctypes.POINTER(OrcProblem), ctypes.POINTER(OrcTol),
+                                            ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_double,
+                                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                            ctypes.POINTER(ctypes.c_int)]
+        _lib.orc_lp1_dual_bound.restype = ctypes.c_int
     return _lib
 
 
@@ -191,6 +196,26 @@ def check_set(prob, S, tol: OrcTol | None = None, want_laws: bool = False):
         out = dict(lagrange_A=lA.copy(), lagrange_b=lb.copy(), parameter_A=pA.copy(),
                    parameter_b=pb.copy(), CR_As=rows[:, :p].copy(), CR_bs=rows[:, p].copy())
     return d, out
+
+
+def lp1_dual_bound(prob, S, sign_tol: float = 1e-9, tol: OrcTol | None = None):
+    """Dual certificate of LP1 infeasibility for a sorted active set.
+
+    Replays the set's warm-start chain up to its first infeasible prefix and
+    builds the dual y of that final basis.  Returns (certified, bound, z,
+    k_used): certified when y <= c + sign_tol, then bound = beta.y <= z*, the
+    LP1 value z of the k_used-element prefix.
+    """
+    pp = _Prob(prob)
+    S = np.ascontiguousarray(sorted(int(s) for s in S), dtype=np.intc)
+    tol = tol or default_tol()
+    bound, z, used = ctypes.c_double(0.0), ctypes.c_double(0.0), ctypes.c_int(0)
+    rc = lib().orc_lp1_dual_bound(ctypes.byref(pp.s), ctypes.byref(tol),
+                                  S.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(S), sign_tol,
+                                  ctypes.byref(bound), ctypes.byref(z), ctypes.byref(used))
+    if rc < 0:
+        raise RuntimeError(f"oracle lp1_dual_bound failed: {rc}")
+    return rc == 1, bound.value, z.value, used.value
 
 
 def kkt_data(prob):
