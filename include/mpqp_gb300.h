@@ -67,7 +67,9 @@ typedef struct GPUResults {
  * extra_batches, reserved_memory  accepted for compatibility; reserved_memory
  *          (MiB) is left free on the device.
  * The problem data are read back from A1/xb1/A2/xb2; the LP layouts are
- * validated and a malformed input returns a result with status != 0. */
+ * validated and a malformed input returns a result with status != 0.  Every
+ * failure is such a result; NULL only when the host cannot allocate even
+ * that. */
 GPUResults *mpqp(const double *AxT, int n_c, int n_x, int n_t, int k_min, int k_max, int extra_batches,
                  const double *A1, const double *xb1, const int *b1, int M1, int N1,
                  const double *A2, const double *xb2, const int *b2, const int *non_b2, int M2, int N2,

@@ -1204,6 +1204,7 @@ extern "C" void mpqp_free(GPUResults *res)
 static GPUResults *error_result(int status)
 {
     GPUResults *r = (GPUResults *)calloc(1, sizeof(GPUResults));
+    if (!r) return nullptr;   // out of host memory: the caller gets NULL
     r->status = status;
     r->active_sets = (int *)calloc(1, sizeof(int));
     r->t_star = (double *)calloc(1, sizeof(double));
