@@ -1340,6 +1340,7 @@ static GPUResults *mpqp_impl(const double *AxT, int n_c, int n_x, int n_t, int k
         return g_last = error_result(rc ? rc : MPQP_ECUDA);
     }
     GPUResults *G = (GPUResults *)calloc(1, sizeof(GPUResults));
+    if (!G) { mpqp_batch_free(R); throw std::bad_alloc(); }
     const long long nf = R->n_opt;
     const int kmin = k_min < 0 ? 0 : k_min;
     long long nsel = 0;
@@ -1358,6 +1359,11 @@ static GPUResults *mpqp_impl(const double *AxT, int n_c, int n_x, int n_t, int k
     G->t_star = (double *)malloc(sizeof(double) * (nsel ? nsel : 1));
     G->radius = (double *)malloc(sizeof(double) * (nsel ? nsel : 1));
     G->is_region = (int *)malloc(sizeof(int) * (nsel ? nsel : 1));
+    if (!G->active_sets || !G->t_star || !G->radius || !G->is_region) {
+        free_gpu_results(G);
+        mpqp_batch_free(R);
+        throw std::bad_alloc();   // the exported wrapper returns an MPQP_ENOMEM result
+    }
     long long w = 0;
     int nreg = 0;
     for (long long i = 0; i < nf; i++) {
