@@ -1,6 +1,7 @@
 """The C-ABI library on the CPU: it builds, loads, exports every symbol the
-public header declares, and rebuilds the problem from the reference's LP
-matrices exactly (host-only entry point; nothing here launches a kernel)."""
+public header declares, rebuilds the problem from the reference's LP
+matrices exactly (host-only entry point), and rejects bad arguments before
+any device work; nothing here launches a kernel."""
 import ctypes
 import os
 import re
@@ -90,3 +91,36 @@ def test_unpack_lp_rejects_other_layouts(lib):
     with pytest.raises(solver.MpqpError) as e:
         solver.unpack_lp(dict(d, A2=A2))
     assert e.value.code == solver.ELAYOUT
+
+
+def test_entry_points_reject_bad_arguments_before_any_device_work(lib):
+    """Null plans, empty instance lists and bad options come back as MPQP_EINVAL
+    with a message (no CUDA call is reached); the free functions take NULL."""
+    out = ctypes.POINTER(solver.BatchResult)()
+    assert lib.mpqp_plan_results(None, ctypes.byref(out)) == solver.EINVAL and not out
+    assert "not run" in solver.last_error()
+    assert lib.mpqp_plan_run(None, None) == solver.EINVAL
+    assert lib.mpqp_plan_run_timed(None, None) == solver.EINVAL
+    names = ctypes.create_string_buffer(64)
+    ms, cnt = (ctypes.c_double * 1)(), (ctypes.c_int * 1)()
+    assert lib.mpqp_plan_kernel_times(None, 1, names, ms, cnt) == solver.EINVAL
+    assert lib.mpqp_plan_launches(None) == 0
+    lib.mpqp_plan_destroy(None)
+    lib.mpqp_batch_free(None)
+    lib.mpqp_free(None)
+    h = ctypes.c_void_p()
+    assert lib.mpqp_plan_create(0, None, None, ctypes.byref(h)) == solver.EINVAL and not h.value
+    assert "no instances" in solver.last_error()
+    assert lib.mpqp_solve_batch(0, None, None, ctypes.byref(out)) == solver.EINVAL and not out
+    ps = solver._ProblemSet([P.scale_problem(P.random_n4_m10_p2())])
+    opts = solver.Options()
+    lib.mpqp_default_options(ctypes.byref(opts))
+    assert opts.precision == solver.FP64 and opts.use_graph == 1
+    opts.lp2_screen = 7
+    assert lib.mpqp_plan_create(1, ps.arr, ctypes.byref(opts), ctypes.byref(h)) == solver.EINVAL and not h.value
+    assert "lp2_screen" in solver.last_error()
+    assert lib.mpqp_region_laws(None, 1, None, None, None) == solver.EINVAL
+    assert lib.mpqp_region_laws(ps.arr, -1, None, None, None) == solver.EINVAL
+    assert lib.mpqp_region_laws(ps.arr, 0, None, None, None) == solver.OK      # nothing to do
+    assert lib.mpqp_reduce_constraints(None, None) == solver.EINVAL
+    assert lib.mpqp_version().decode().startswith("mpqp_gb300")
