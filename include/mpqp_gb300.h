@@ -135,6 +135,9 @@ typedef struct {
     /* tolerances (0 selects the default) */
     double tol_feas, tol_opt, tol_licq, r_min, tol_piv, tol_dj;
     int max_pivots, degen_switch;
+    /* margin_z: an FP32 LP1 optimum that is not certified feasible goes to the
+     * FP64 dual certificate when its z exceeds margin_z, else straight to the
+     * FP64 re-solve (routing only: no verdict rests on it) */
     double tol_piv32, tol_dj32, margin_z, margin_beta, margin_t, margin_licq;
     double tol_zero_row;     /* region row zero when max|g| <= tol * max(1,|h|) */
     int lp2_screen;          /* MPQP_MIXED, FP32 optimality screen: 0 the dual
@@ -163,6 +166,11 @@ typedef struct {
      * equal sets, up to hash collisions) */
     unsigned long long feasible_digest, optimal_digest, region_digest;
     int last_level, truncated;
+    /* mixed precision: FP32 LP1 optima proven infeasible by the FP64 dual
+     * certificate of their final basis, those it could not prove (re-solved
+     * in FP64; fallback_lp1 counts every re-solve), and of those the ones
+     * with a free variable nonbasic in the final basis */
+    long long lp1_certified, lp1_cert_missed, lp1_cert_freevar;
 } mpqp_inst_stats;
 
 typedef struct {
@@ -178,7 +186,7 @@ typedef struct {
                                      (lexicographic); the same order on
                                      every run                               */
     long long n_rec;
-    void *rec;                    /* n_rec records (104 bytes each) or NULL */
+    void *rec;                    /* n_rec records (112 bytes each) or NULL */
     long long h2d_bytes;          /* problem data uploaded by the plan      */
     long long d2h_bytes;          /* result bytes copied back               */
 } mpqp_batch_result;

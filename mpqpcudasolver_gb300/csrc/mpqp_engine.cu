@@ -38,6 +38,9 @@ cudaError_t launch_feasibility(const DevBuffers &B, const Tol &tol, const SlotDi
                                int grid, size_t smem, cudaStream_t s);
 cudaError_t launch_lp1_fp64(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int grid,
                             size_t smem, cudaStream_t s);
+cudaError_t launch_lp1_cert(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int grid,
+                            size_t smem, cudaStream_t s);
+size_t cert_smem_per_warp(const SlotDims &sd);
 cudaError_t launch_optimality(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, bool lp,
                               int grid, size_t smem, cudaStream_t s);
 cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode, int route,
@@ -280,8 +283,8 @@ struct mpqp_plan {
     int grid_tiles = 0;         // the dual route's first stage (one set per 8-thread tile)
     size_t smem_tiles = 0;
     size_t smem_opt2 = 0;       // shared memory per block of the primal route
-    int grid_enum = 0, grid_feas = 0, grid_lp1fb = 0, grid_opt = 0, grid_optfb = 0;
-    size_t smem_feas = 0, smem_lp1fb = 0, smem_opt = 0, smem_optfb = 0;
+    int grid_enum = 0, grid_feas = 0, grid_lp1fb = 0, grid_opt = 0, grid_optfb = 0, grid_cert = 0;
+    size_t smem_feas = 0, smem_lp1fb = 0, smem_opt = 0, smem_optfb = 0, smem_cert = 0;
     int n_launches = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -323,7 +326,7 @@ extern "C" void mpqp_default_options(mpqp_options *o)
     o->degen_switch = 8;
     o->tol_piv32 = 1e-6;
     o->tol_dj32 = 1e-6;
-    o->margin_z = 1e-3;
+    o->margin_z = 1e-6;      // routing only: FP32 z above it -> FP64 dual certificate
     o->margin_beta = 3e-5;   // x max(1, max |T_ij|) of the final FP32 LP1 tableau
     o->margin_t = 1e-5;   // x (row magnitude / pivot ratio) x (1 + p |theta|max)
     o->margin_licq = 1e-3;
@@ -512,7 +515,10 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
     for (int k = 1; k <= P->kmax; k++) {
         L("k_enumerate", launch_enumerate(B, k, P->grid_enum, s));
         L(feas, launch_feasibility(B, P->tol, P->sd, k, P->prec, P->grid_feas, P->smem_feas, s));
-        if (mixed) L("k_lp1_fp64", launch_lp1_fp64(B, P->tol, P->sd, k, P->grid_lp1fb, P->smem_lp1fb, s));
+        if (mixed) {
+            L("k_lp1_cert", launch_lp1_cert(B, P->tol, P->sd, k, P->grid_cert, P->smem_cert, s));
+            L("k_lp1_fp64", launch_lp1_fp64(B, P->tol, P->sd, k, P->grid_lp1fb, P->smem_lp1fb, s));
+        }
         { const int _o = launch_opt(k); if (_o) return _o; }
         { const int _o = launch_optfb(k); if (_o) return _o; }
         L("k_finalize", launch_finalize(B, k, s));
@@ -656,7 +662,8 @@ static int mpqp_plan_create_impl(int n_inst, const mpqp_problem *probs, const mp
     long long arena_bytes = o.arena_bytes;
     if (arena_bytes <= 0) {
         const double used = (double)cand_cap * 12 + (double)node_cap * (2 * sizeof(Node) + 4) +
-                            (double)hash_cap * 2 * sizeof(HashSlot);
+                            (double)hash_cap * 2 * sizeof(HashSlot) +
+                            (P->prec == PREC_MIXED ? (double)cand_cap / 8 * 48 : 0.0);   // certificate queue
         arena_bytes = (long long)std::max(usable - used, (double)(64 << 20));
         if (all_budget) {
             // parents of the deepest checked level hold at most the budget
@@ -684,6 +691,10 @@ static int mpqp_plan_create_impl(int n_inst, const mpqp_problem *probs, const mp
     B.hash_cap = hash_cap;
     B.cand_cap = cand_cap;
     B.q_cap = cand_cap;
+    // certificate queue (mixed precision): FP32 LP1 optima that are not
+    // certified feasible; beyond its capacity they go to the FP64 re-solve
+    B.cert_stride = (int)((4 + std::min(sd.maxNv, 32) + 15) & ~15);
+    B.cert_cap = P->prec == PREC_MIXED ? std::max(cand_cap / 8, (long long)4096) : 0;
     B.opt_cap = opt_cap;
     B.rec_cap = rec_cap;
     B.exhaustive = o.exhaustive ? 1 : 0;
@@ -705,6 +716,7 @@ static int mpqp_plan_create_impl(int n_inst, const mpqp_problem *probs, const mp
     AL(B.cand, sizeof(Cand) * cand_cap);
     AL(B.q_lp1, sizeof(int) * cand_cap);
     AL(B.q_opt, sizeof(int) * cand_cap);
+    AL(B.cert_q, (size_t)B.cert_stride * B.cert_cap);
     AL(B.opt, sizeof(OptRec) * opt_cap);
     if (rec_cap) AL(B.rec, sizeof(CandRec) * rec_cap);
     AL(B.ictl, sizeof(InstCtl) * n_inst);
@@ -721,6 +733,7 @@ static int mpqp_plan_create_impl(int n_inst, const mpqp_problem *probs, const mp
     // kernel geometry
     P->smem_feas = 4 * feas_smem_per_warp(P->prec == PREC_MIXED ? 4 : 8, sd);
     P->smem_lp1fb = 4 * lp1_smem_per_warp(8, sd);
+    P->smem_cert = 4 * cert_smem_per_warp(sd);
     // mixed precision: the grouped FP32 screen, one warp per block
     P->smem_opt = P->prec == PREC_MIXED ? screen_smem_per_warp(sd, 0) : 4 * opt_smem_per_warp(8, sd);
     P->smem_opt2 = screen_smem_per_warp(sd, 1);
@@ -735,6 +748,7 @@ static int mpqp_plan_create_impl(int n_inst, const mpqp_problem *probs, const mp
     if ((rc = grid_for(kernel_ptr("enumerate"), 0, &P->grid_enum)) ||
         (rc = grid_for(kernel_ptr(P->prec == PREC_MIXED ? "feas32" : "feas64"), P->smem_feas, &P->grid_feas)) ||
         (rc = grid_for(kernel_ptr("lp1_fp64"), P->smem_lp1fb, &P->grid_lp1fb)) ||
+        (rc = grid_for(kernel_ptr("lp1_cert"), P->smem_cert, &P->grid_cert)) ||
         (rc = P->prec == PREC_MIXED
                   ? grid_for(kernel_ptr("screen_dual_rows"), P->smem_opt, &P->grid_opt, 32)
                   : grid_for(kernel_ptr("opt64"), P->smem_opt, &P->grid_opt)) ||
@@ -1023,6 +1037,7 @@ static int plan_results_impl(mpqp_plan *P, mpqp_batch_result *&R, bool *complete
         s.optimal = ic[i].optimal; s.regions = ic[i].region; s.lp1_pivots = ic[i].lp1_piv;
         s.lp2_pivots = ic[i].lp2_piv; s.cheb_pivots = ic[i].cheb_piv; s.fallback_lp1 = ic[i].fb_lp1;
         s.fallback_opt = ic[i].fb_opt; s.stored = ic[i].stored;
+        s.lp1_certified = ic[i].cert_lp1; s.lp1_cert_missed = ic[i].cert_miss; s.lp1_cert_freevar = ic[i].cert_free;
         s.feasible_digest = ic[i].feas_digest; s.optimal_digest = ic[i].opt_digest;
         s.region_digest = ic[i].reg_digest;
         s.last_level = ic[i].last_level; s.truncated = ic[i].truncated;

@@ -12,6 +12,8 @@
 //   mask hash x2               tagged open-addressing table of feasible masks
 //   candidate list             (parent node, added constraint) pairs, 8 B
 //   fallback queues            candidates / nodes re-solved in FP64
+//   certificate queue          FP32 LP1 optima to certify infeasible in FP64
+//                              (candidate index + final nonbasic ids)
 //   optimal-set list           one OptRec per optimal active set
 //   records (optional)         one CandRec per checked candidate (parity)
 #pragma once
@@ -44,7 +46,7 @@ struct Tol {
     // candidate to the FP64 re-solve
     float tol_piv32;
     float tol_dj32;
-    double margin_z;    // FP32 LP1 z above this -> infeasible without FP64
+    double margin_z;    // FP32 LP1 z above this -> the FP64 dual certificate, else the FP64 re-solve (routing only)
     double margin_beta; // FP32 basic slacks above margin_beta * max(1, tableau growth) certify feasibility
     double margin_t;    // FP32 LP2 t below -margin_t * error scale -> not optimal without FP64
     double margin_licq; // FP32 Cholesky pivot ratio below this -> FP64
@@ -86,13 +88,10 @@ struct Node {                   // a feasible (or, when exhaustive, any) active 
     long long rec;              // record index (or -1)
 };
 
-// NODE_FP64CHAIN: this set, or one of the sets its LP1 warm start descends
-// from, needed the FP64 re-solve (mixed precision); FP32 "infeasible"
-// verdicts below such a node are re-solved in FP64 too.
 // NODE_CERT: the stored FP32 tableau is the one whose basic solution
 // certified this set feasible (every slack of the set nonbasic, every basic
 // slack clear of the growth-scaled margin).
-enum NodeFlags : int { NODE_FEASIBLE = 1, NODE_VALID = 2, NODE_FP64CHAIN = 4, NODE_CERT = 8 };
+enum NodeFlags : int { NODE_FEASIBLE = 1, NODE_VALID = 2, NODE_CERT = 8 };
 // bits 8..16 of the flags: 1 + the live rows of the stored FP32 LP1 tableau
 // (rows of basic free variables dropped, the objective row right after them);
 // 0: all M1 rows
@@ -117,9 +116,11 @@ struct CandRec {                // identical field layout to the oracle's record
     int32_t feasible, licq, optimal, region;
     int32_t lp2_status, lp2_pivots, cheb_status, cheb_pivots;
     double t, r;
-    int32_t inst, fp64;         // instance; bit0 LP1 / bit1 LP2 decided in FP64
+    int32_t inst, fp64;         // instance; bit0 LP1 / bit1 LP2 decided in FP64, bit2 LP1
+                                // infeasible by the FP64 dual certificate of the final FP32 basis
     float lp1_growth;           // FP32 LP1: max |T_ij| of the final tableau (mixed precision)
     float lp1_minbeta;          // FP32 LP1: smallest basic slack value
+    double lp1_bound;           // FP64 dual certificate: the lower bound on z* it proved (NaN: none)
 };
 
 struct HashSlot { uint64_t lo, hi; int inst; int tag; int val; int pad; };
@@ -132,6 +133,9 @@ struct InstCtl {
     long long feasible, optimal, region;
     long long lp1_piv, lp2_piv, cheb_piv;
     long long fb_lp1, fb_opt;   // FP64 fallbacks (mixed precision)
+    long long cert_lp1;         // FP32 LP1 optima certified infeasible by the FP64 dual bound
+    long long cert_miss;        // ... that the certificate could not prove (sent to the FP64 re-solve)
+    long long cert_free;        // ... of those, the misses with a free variable nonbasic (no square system)
     long long stored;           // LP1 tableaus written for the next level
     // order-independent digests (sum mod 2^64 of a 64-bit hash of each mask)
     unsigned long long feas_digest, opt_digest, reg_digest;
@@ -140,6 +144,8 @@ struct InstCtl {
     int last_level;
     int pad;
 };
+
+constexpr int kCtlCounters = 12;
 
 struct Ctl {
     long long n_cand;           // candidates at the current level
@@ -151,7 +157,8 @@ struct Ctl {
     long long rec_base;         // record index of the current level's first candidate
     long long n_q_lp1, n_q_opt; // FP64 fallback queue lengths
     long long n_q_scr;          // sets the first stage of the dual screen left to its second
-    unsigned long long ctr[8];  // work counters (reset every level)
+    long long n_q_cert;         // FP32 LP1 optima waiting for the FP64 dual certificate
+    unsigned long long ctr[kCtlCounters];  // work counters (reset every level)
     int overflow;               // bit mask of overflowed buffers
     int level;
     int epoch;                  // run counter; hash tags are (epoch << 8) | level
@@ -190,6 +197,10 @@ struct DevBuffers {
     int *q_lp1;                 // candidate indices for the FP64 LP1 re-solve
     int *q_opt;                 // node indices for the FP64 optimality re-solve
     long long q_cap;
+    uint8_t *cert_q;            // certificate queue: entries of cert_stride bytes, an int candidate
+                                // index then the nv nonbasic ids of its final FP32 basis
+    long long cert_cap;         // entries (a full queue sends candidates to the FP64 re-solve)
+    int cert_stride;
     OptRec *opt;
     long long opt_cap;
     CandRec *rec;               // may be null

@@ -862,6 +862,26 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
     return idx;
 }
 
+// An FP32 LP1 candidate without a final verdict, by one lane: with nid (the
+// nonbasic ids of its final basis) to the FP64 dual certificate's queue, else
+// -- or when that queue is full -- to the FP64 re-solve.  Not inlined: the
+// LP1 kernel's registers stay with its simplex.
+__device__ __noinline__ void queue_undecided_lp1(const DevBuffers &B, int w, const uint8_t *nid, int nv)
+{
+    Ctl *ctl = B.ctl;
+    if (nid) {
+        const long long ci = (long long)atomicAdd((unsigned long long *)&ctl->n_q_cert, 1ull);
+        if (ci < B.cert_cap) {
+            uint8_t *e = B.cert_q + ci * B.cert_stride;
+            *reinterpret_cast<int *>(e) = w;
+            for (int c = 0; c < nv; c++) e[4 + c] = nid[c];
+            return;
+        }
+    }
+    const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_lp1, 1ull);
+    if (qi < B.q_cap) B.q_lp1[qi] = w; else atomicOr(&ctl->overflow, OV_QUEUE);
+}
+
 // ---------------------------------------------------------------------
 // K2: LP1 feasibility, warm-started from the parent
 // ---------------------------------------------------------------------
@@ -976,7 +996,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
                 if (nbase + t < B.node_cap) {
                     Node nd;
                     nd.lo = lo; nd.hi = hi; nd.inst = inst;
-                    nd.flags = NODE_VALID | NODE_FEASIBLE | (par.flags & NODE_FP64CHAIN);
+                    nd.flags = NODE_VALID | NODE_FEASIBLE;
                     nd.tab_off = -1; nd.ids_off = -1; nd.rec = -1;
                     B.node[side][nbase + t] = nd;
                 } else {
@@ -1037,7 +1057,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         const T z = obj[nv];
         uint64_t lo = par.lo, hi = par.hi;
         if (c.j < 64) lo |= 1ull << c.j; else hi |= 1ull << (c.j - 64);
-        bool feasible = false, decided = true;
+        bool feasible = false, decided = true, to_cert = false;
         float lp1_growth = 0.0f, lp1_minbeta = 0.0f;
         if (!mixed) {
             feasible = (st == LP_OPTIMAL) && ((double)z <= tol.tol_feas);
@@ -1075,17 +1095,15 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
                 }
                 lp1_growth = (float)gmax;
                 lp1_minbeta = (float)minb;
-                // infeasible: z clearly positive -- except in a chain that has
-                // already needed FP64 (nearly degenerate, badly conditioned
-                // bases, where the FP32 simplex can stop at a wrong optimum)
-                if (z > (T)tol.margin_z32) {
-                    if (par.flags & NODE_FP64CHAIN) decided = false;
-                    else feasible = false;
-                }
                 // feasible: every slack of S nonbasic (all rows of S tight at
                 // the basic solution) and every basic slack clearly positive
-                else if (!s_basic && minb > (T)tol.margin_beta32 * gmax) feasible = true;
-                else decided = false;
+                if (!s_basic && minb > (T)tol.margin_beta32 * gmax) feasible = true;
+                // infeasible only by the FP64 dual certificate of this final
+                // basis (k_lp1_cert); z32 near zero goes to the FP64 re-solve
+                else {
+                    decided = false;
+                    to_cert = z > (T)tol.margin_z32 && nv <= 32 && !B.exhaustive;
+                }
             }
         }
         lc.b += piv;
@@ -1098,12 +1116,11 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
             R.t = __longlong_as_double(0x7ff8000000000000LL); R.r = R.t;
             R.inst = inst; R.fp64 = decided ? (mixed ? 0 : 1) : 0;
             R.lp1_growth = lp1_growth; R.lp1_minbeta = lp1_minbeta;
+            R.lp1_bound = __longlong_as_double(0x7ff8000000000000LL);
         }
         if (!decided) {
-            if (lane == 0) {
-                const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_lp1, 1ull);
-                if (qi < B.q_cap) B.q_lp1[qi] = (int)w; else atomicOr(&ctl->overflow, OV_QUEUE);
-            }
+            if (lane == 0) queue_undecided_lp1(B, (int)w, to_cert ? nid : nullptr, nv);
+            __syncwarp();
             continue;
         }
         if (feasible) { lc.a++; lc.c += (long long)mask_digest(lo, hi); }
@@ -1114,8 +1131,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
                 __syncwarp();
             }
             store_node<T, T>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap,
-                             (par.flags & NODE_FP64CHAIN) | (mixed && feasible ? NODE_CERT : 0), 0, true, nbase + t,
-                             mixed ? rows : -1);
+                             mixed && feasible ? NODE_CERT : 0, 0, true, nbase + t, mixed ? rows : -1);
         }
         if (at_vertex && feasible && level == I.k_max) {
             // later siblings whose new slack is nonbasic at this vertex
@@ -1206,8 +1222,161 @@ __global__ void __launch_bounds__(128) k_lp1_fp64(DevBuffers B, Tol tol, SlotDim
             }
         }
         if (feasible || B.exhaustive)
-            store_node<float, double>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap, NODE_FP64CHAIN,
-                                      I.ld1d, false, w);
+            store_node<float, double>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap, 0, I.ld1d, false,
+                                      w);
+    }
+}
+
+// ---------------------------------------------------------------------
+// K2c: FP64 dual certificate of FP32 LP1 optima (mixed precision)
+// ---------------------------------------------------------------------
+// LP1 of S' = S u {j}:  min c.w  s.t.  G u + w = beta, w >= 0, u free, with
+// c_i = 1 on S' and 0 elsewhere (G = [A -F; 0 At], beta = [b; bt]: the FP64
+// root tableau).  Its dual is  max beta.y  s.t.  G^T y = 0, y <= c, and by
+// weak duality every such y gives z* >= beta.y.  The candidate's final FP32
+// basis fixes y_i = c_i on its basic slacks; when every free variable is
+// basic, the duals of the nv nonbasic slacks solve the square system
+// G_N^T y_N = -G_B^T c_B, here by FP64 Gaussian elimination with partial
+// pivoting.  The FP32 LP kept the parent's nonbasic slacks at zero, so their
+// duals may exceed c_i = 1: y / s, s = max(1, max_{i in S'} y_i), is a
+// feasible dual point as soon as y_i <= tol_dj (the FP64 simplex's own
+// optimality tolerance) on the nonbasic slacks outside S'.  The set is
+// infeasible when beta.y / s > tol_feas -- whatever path the FP32 simplex
+// took, since only the final basis enters; every other candidate goes on to
+// the FP64 re-solve.  One warp per queued candidate, lane r owns row r of
+// G_N^T in shared memory (row stride odd in doubles); instances with nv > 32
+// never reach this kernel.
+__host__ __device__ inline size_t cert_slot_bytes(int maxNv)
+{
+    const int nvm = maxNv < 32 ? maxNv : 32;
+    return align16((size_t)nvm * (nvm | 1) * sizeof(double));
+}
+
+__device__ __forceinline__ double warp_max_d(double v)
+{
+#pragma unroll
+    for (int off = 16; off; off >>= 1) v = fmax(v, __shfl_xor_sync(FULLMASK, v, off));
+    return v;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v)
+{
+#pragma unroll
+    for (int off = 16; off; off >>= 1) v = __dadd_rn(v, __shfl_xor_sync(FULLMASK, v, off));
+    return v;
+}
+
+__global__ void __launch_bounds__(128) k_lp1_cert(DevBuffers B, Tol tol, SlotDims sd, int level)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const int nvm = sd.maxNv < 32 ? sd.maxNv : 32, ldm = nvm | 1;
+    double *M = (double *)(smem + wib * cert_slot_bytes(sd.maxNv));
+    double *Mr = M + (size_t)(lane < nvm ? lane : 0) * ldm;   // this lane's row
+    const int pside = (level & 1) ^ 1;
+    Ctl *ctl = B.ctl;
+    const long long nq = ctl->n_q_cert < B.cert_cap ? ctl->n_q_cert : B.cert_cap;
+    for (;;) {
+        long long x;
+        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[8], 1ull);
+        x = __shfl_sync(FULLMASK, x, 0);
+        if (x >= nq) break;
+        const uint8_t *e = B.cert_q + x * B.cert_stride;
+        const int w = *reinterpret_cast<const int *>(e);
+        const Cand c = B.cand[w];
+        const Node par = B.node[pside][c.parent];
+        const int inst = par.inst;
+        const InstDesc &I = B.inst[inst];
+        const int nv = I.nv, ld = I.ld1d;
+        uint64_t lo = par.lo, hi = par.hi;
+        if (c.j < 64) lo |= 1ull << c.j; else hi |= 1ull << (c.j - 64);
+        const double *G = B.dpool + I.o_root;
+        // lane cc < nv: the slack nonbasic in column cc (negative: a free variable)
+        const int nb = lane < nv ? (int)e[4 + lane] - nv : 0;
+        const bool all_slack = __all_sync(FULLMASK, nb >= 0) && nv <= nvm;
+        bool ok = all_slack;
+        double bound = 0.0;
+        if (ok) {
+            // lane v: row v of G_N^T and rhs_v = -sum_{i in S' basic} G[i][v]
+            for (int cc = 0; cc < nv; cc++) {
+                const int i = __shfl_sync(FULLMASK, nb, cc);
+                if (lane < nv) Mr[cc] = G[(size_t)i * ld + lane];
+            }
+            double rhs = 0.0, by = 0.0;   // by: beta.y over the basic slacks of S' (y = 1)
+            uint64_t rl = lo, rh = hi;
+            while (rl | rh) {
+                int i;
+                if (rl) { i = __ffsll((long long)rl) - 1; rl &= rl - 1; }
+                else { i = 64 + __ffsll((long long)rh) - 1; rh &= rh - 1; }
+                if (__any_sync(FULLMASK, lane < nv && nb == i)) continue;   // nonbasic: its y is unknown
+                if (lane < nv) rhs = __dsub_rn(rhs, G[(size_t)i * ld + lane]);
+                by = __dadd_rn(by, G[(size_t)i * ld + nv]);
+            }
+            __syncwarp();
+            double amax = 0.0;
+            if (lane < nv) for (int cc = 0; cc < nv; cc++) amax = fmax(amax, fabs(Mr[cc]));
+            const double thr = 1e-13 * fmax(warp_max_d(amax), 1.0);
+            // elimination: the pivot of column col is the unused row with the
+            // largest |entry| (smallest lane on ties)
+            bool used = lane >= nv;
+            int mycol = -1;
+            for (int col = 0; col < nv; col++) {
+                const double a = used ? -1.0 : fabs(Mr[col]);
+                const double amx = warp_max_d(a);
+                if (!(amx > thr)) { ok = false; break; }
+                const int pr = __ffs(__ballot_sync(FULLMASK, !used && a == amx)) - 1;
+                const double *P = M + (size_t)pr * ldm;
+                const double prhs = __shfl_sync(FULLMASK, rhs, pr);
+                if (lane == pr) {
+                    used = true;
+                    mycol = col;
+                } else if (!used) {
+                    const double f = xdiv(Mr[col], P[col]);
+                    for (int cc = col + 1; cc < nv; cc++) Mr[cc] = xfma(-f, P[cc], Mr[cc]);
+                    rhs = xfma(-f, prhs, rhs);
+                }
+                __syncwarp();
+            }
+            // back substitution, last column first; lane cc keeps y of column cc
+            double y = 0.0;
+            for (int col = nv - 1; col >= 0 && ok; col--) {
+                const int pr = __ffs(__ballot_sync(FULLMASK, mycol == col)) - 1;
+                double yc = lane == pr ? xdiv(rhs, Mr[col]) : 0.0;
+                yc = __shfl_sync(FULLMASK, yc, pr);
+                if (lane == col) y = yc;
+                if (mycol >= 0 && mycol < col) rhs = xfma(-Mr[col], yc, rhs);
+            }
+            if (ok) {
+                // dual feasibility after scaling, and beta.y / s
+                double smax = 1.0, byn = 0.0;
+                bool bad = false;
+                if (lane < nv) {
+                    const bool inS = nb < I.m && mask_has(lo, hi, nb);
+                    if (inS) smax = fmax(smax, y);
+                    else bad = !(y <= tol.tol_dj);
+                    byn = xmul(G[(size_t)nb * ld + nv], y);
+                }
+                bad = __any_sync(FULLMASK, bad);
+                smax = warp_max_d(smax);
+                byn = warp_sum_d(byn);
+                bound = xdiv(xadd(by, byn), smax);
+                ok = !bad && bound > tol.tol_feas;
+            }
+        }
+        if (lane == 0) {
+            InstCtl *ic = &B.ictl[inst];
+            const long long rec = (B.rec && ctl->rec_base + w < B.rec_cap) ? ctl->rec_base + w : -1;
+            if (ok) {
+                atomicAdd((unsigned long long *)&ic->cert_lp1, 1ull);
+                if (rec >= 0) { B.rec[rec].fp64 |= 4; B.rec[rec].lp1_bound = bound; }
+            } else {
+                atomicAdd((unsigned long long *)&ic->cert_miss, 1ull);
+                if (!all_slack) atomicAdd((unsigned long long *)&ic->cert_free, 1ull);
+                const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_lp1, 1ull);
+                if (qi < B.q_cap) B.q_lp1[qi] = w; else atomicOr(&ctl->overflow, OV_QUEUE);
+            }
+        }
+        __syncwarp();   // the slot is rewritten for the next entry
     }
 }
 
@@ -2768,7 +2937,7 @@ __global__ void k_level0(DevBuffers B)
             R.lp2_status = LP_SKIPPED; R.lp2_pivots = 0; R.cheb_status = LP_SKIPPED; R.cheb_pivots = 0;
             R.t = __longlong_as_double(0x7ff8000000000000LL); R.r = R.t;
             R.inst = inst; R.fp64 = 1;
-            R.lp1_growth = 0.0f; R.lp1_minbeta = 0.0f;
+            R.lp1_growth = 0.0f; R.lp1_minbeta = 0.0f; R.lp1_bound = R.t;
         }
         InstCtl *ic = &B.ictl[inst];
         ic->lvl_cand = 1;
@@ -2832,8 +3001,9 @@ __global__ void k_finalize(DevBuffers B, int level)
             ctl->tab_used[pside] = 0;
             ctl->ids_used[pside] = 0;
         }
-        for (int c = 0; c < 8; c++) ctl->ctr[c] = 0;
+        for (int c = 0; c < kCtlCounters; c++) ctl->ctr[c] = 0;
         ctl->n_q_lp1 = 0;
+        ctl->n_q_cert = 0;
         ctl->n_q_opt = 0;
         ctl->n_q_scr = 0;
         ctl->level = level;
@@ -2939,6 +3109,8 @@ size_t feas_smem_per_warp(int prec_bytes, const SlotDims &sd)
                            : feas_slot_bytes<float>(sd.maxM1, sd.maxLD1, sd.maxNv);
 }
 
+size_t cert_smem_per_warp(const SlotDims &sd) { return cert_slot_bytes(sd.maxNv); }
+
 size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd)
 {
     return prec_bytes == 8 ? lp1_slot_bytes<double>(sd.maxM1, sd.maxLD1d, sd.maxNv)
@@ -2969,6 +3141,7 @@ const void *kernel_ptr(const char *name)
         {"feas64", (const void *)k_feasibility<double>},
         {"feas32", (const void *)k_feasibility<float>},
         {"lp1_fp64", (const void *)k_lp1_fp64},
+        {"lp1_cert", (const void *)k_lp1_cert},
         {"opt64", (const void *)k_optimality<double, false>},
         {"opt64_lp", (const void *)k_optimality<double, true>},
         {"opt_fp64", (const void *)k_optimality_fp64<false>},
@@ -3008,6 +3181,13 @@ cudaError_t launch_lp1_fp64(const DevBuffers &B, const Tol &tol, const SlotDims 
                             size_t smem, cudaStream_t s)
 {
     k_lp1_fp64<<<grid, 128, smem, s>>>(B, tol, sd, level);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lp1_cert(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int grid,
+                            size_t smem, cudaStream_t s)
+{
+    k_lp1_cert<<<grid, 128, smem, s>>>(B, tol, sd, level);
     return cudaGetLastError();
 }
 

@@ -54,7 +54,8 @@ class InstStats(ctypes.Structure):
                                                     "lp1_pivots", "lp2_pivots", "cheb_pivots", "fallback_lp1",
                                                     "fallback_opt", "stored")] + \
         [(nm, ctypes.c_ulonglong) for nm in ("feasible_digest", "optimal_digest", "region_digest")] + \
-        [("last_level", ctypes.c_int), ("truncated", ctypes.c_int)]
+        [("last_level", ctypes.c_int), ("truncated", ctypes.c_int)] + \
+        [(nm, ctypes.c_longlong) for nm in ("lp1_certified", "lp1_cert_missed", "lp1_cert_freevar")]
 
 
 class BatchResult(ctypes.Structure):
@@ -81,7 +82,7 @@ REC_DTYPE = np.dtype([("mask_lo", "<u8"), ("mask_hi", "<u8"), ("level", "<i4"), 
                       ("feasible", "<i4"), ("licq", "<i4"), ("optimal", "<i4"), ("region", "<i4"),
                       ("lp2_status", "<i4"), ("lp2_pivots", "<i4"), ("cheb_status", "<i4"),
                       ("cheb_pivots", "<i4"), ("t", "<f8"), ("r", "<f8"), ("inst", "<i4"), ("fp64", "<i4"),
-                      ("lp1_growth", "<f4"), ("lp1_minbeta", "<f4")])
+                      ("lp1_growth", "<f4"), ("lp1_minbeta", "<f4"), ("lp1_bound", "<f8")])
 
 EXPORTS = ("mpqp", "warm_up", "mpqp_free", "mpqp_unpack_lp", "mpqp_default_options", "mpqp_solve_batch", "mpqp_batch_free",
            "mpqp_plan_create", "mpqp_plan_run", "mpqp_plan_results", "mpqp_plan_launches", "mpqp_plan_destroy",
@@ -212,7 +213,8 @@ class Result:
 
 _INST_DTYPE = np.dtype([(f[0], "<i8") for f in InstStats._fields_[:11]] +
                        [("feasible_digest", "<u8"), ("optimal_digest", "<u8"), ("region_digest", "<u8"),
-                        ("last_level", "<i4"), ("truncated", "<i4")])
+                        ("last_level", "<i4"), ("truncated", "<i4"), ("lp1_certified", "<i8"),
+                        ("lp1_cert_missed", "<i8"), ("lp1_cert_freevar", "<i8")])
 _OPT_DTYPE = np.dtype([("mask_lo", "<u8"), ("mask_hi", "<u8"), ("inst", "<i4"), ("level", "<i4"), ("t", "<f8"),
                        ("r", "<f8"), ("region", "<i4"), ("fp64", "<i4"), ("rec", "<i8")])
 assert _INST_DTYPE.itemsize == ctypes.sizeof(InstStats)

@@ -5,6 +5,8 @@
 * Mixed precision (FP32 pivots + FP64 certificates): the feasible, optimal
   and region sets are identical to the FP64 path's.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -34,13 +36,7 @@ def _same(a, b):
     return np.array_equal(a, b) or np.array_equal(np.nan_to_num(a, nan=12345.0), np.nan_to_num(b, nan=12345.0))
 
 
-@pytest.mark.parametrize("case", list(CASES))
-def test_fp64_bit_exact_vs_oracle(gpu_lib, case):
-    make, kmax, exh = CASES[case]
-    prob = P.scale_problem(make())
-    ref = O.enumerate_sets(prob, k_max=kmax, exhaustive=exh, nthreads=4)
-    res = solver.solve([prob], precision=solver.FP64, k_max=kmax, exhaustive=int(exh), record=1,
-                       rec_cap=ref.n_cand + 16, cand_cap=max(4096, ref.n_cand), arena_bytes=1 << 28)
+def _fp64_records_equal_oracle(res, ref):
     assert res.status == 0 and res.overflow == 0
     assert res.candidates == ref.n_cand
     g = _sorted(res.rec)
@@ -57,6 +53,78 @@ def test_fp64_bit_exact_vs_oracle(gpu_lib, case):
     assert res.total("optimal") == ref.n_optimal == len(res.opt)
     assert res.total("regions") == ref.n_region
     assert res.total("pruned") == ref.n_pruned
+    return g, o
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_fp64_bit_exact_vs_oracle(gpu_lib, case):
+    make, kmax, exh = CASES[case]
+    prob = P.scale_problem(make())
+    ref = O.enumerate_sets(prob, k_max=kmax, exhaustive=exh, nthreads=4)
+    res = solver.solve([prob], precision=solver.FP64, k_max=kmax, exhaustive=int(exh), record=1,
+                       rec_cap=ref.n_cand + 16, cand_cap=max(4096, ref.n_cand), arena_bytes=1 << 28)
+    _fp64_records_equal_oracle(res, ref)
+
+
+DEEP = {
+    "m62-k5": (lambda: P.random_n12_m62_p6(), 5),      # 6.6M candidates
+    "mpc-k4": (lambda: P.mpc_mpqp(0), 4),
+    "illcond-k4": (lambda: P.illcond_n16_m62_p8(), 4),
+}
+
+
+@pytest.mark.parametrize("case", list(DEEP))
+def test_deep_levels_vs_oracle(gpu_lib, case):
+    """Record-level parity at the deep levels: the FP64 kernels bit-identical
+    to the oracle on every checked candidate, and the mixed path's feasible,
+    optimal and region verdicts -- with the FP64 t* and r* of every optimal
+    set -- equal to the oracle's."""
+    make, kmax = DEEP[case]
+    prob = P.scale_problem(make())
+    ref = O.enumerate_sets(prob, k_max=kmax, nthreads=os.cpu_count() or 4)
+    kw = dict(k_max=kmax, record=1, rec_cap=ref.n_cand + 16, cand_cap=ref.n_cand + 1024, mem_fraction=0.5)
+    r64 = solver.solve([prob], precision=solver.FP64, **kw)
+    _, o = _fp64_records_equal_oracle(r64, ref)
+    del r64
+    r32 = solver.solve([prob], precision=solver.MIXED, **kw)
+    assert r32.status == 0 and r32.overflow == 0
+    g = _sorted(r32.rec)
+    assert np.array_equal(g["mask_lo"], o["mask_lo"]) and np.array_equal(g["mask_hi"], o["mask_hi"])
+    for f in ("feasible", "optimal", "region"):
+        assert np.array_equal(g[f], o[f]), (f, int(np.sum(g[f] != o[f])))
+    opt = o["optimal"] == 1
+    assert _same(g["t"][opt], o["t"][opt]) and _same(g["r"][opt], o["r"][opt])
+    print(case, "candidates", ref.n_cand, "feasible", ref.n_feasible, "optimal", ref.n_optimal,
+          "certified infeasible", r32.total("lp1_certified"), "FP64 re-solves", r32.total("fallback_lp1"))
+
+
+def test_level6_sample_vs_oracle(gpu_lib):
+    """The bench's depth (|S| <= 6 on the m = 62 instance, 54.3M candidates)
+    in mixed precision, sampled against the oracle (each set's warm-start
+    chain replayed in FP64): a seeded sample of the level-6 optimal sets keeps
+    the oracle's verdicts and bit-identical t* and r*; a seeded sample of
+    random 6-sets is optimal for the oracle exactly when the device lists it."""
+    prob = P.scale_problem(P.random_n12_m62_p6())
+    r32 = solver.solve([prob], precision=solver.MIXED, k_max=6, mem_fraction=0.8)
+    assert r32.status == 0
+    opt6 = r32.opt[r32.opt["level"] == 6]
+    assert len(opt6) > 1000
+    listed = {(int(a), int(b)) for a, b in zip(r32.opt["mask_lo"], r32.opt["mask_hi"])}
+    rng = np.random.default_rng(6)
+    for row in opt6[rng.permutation(len(opt6))[:1500]]:
+        S = O.mask_to_set(row["mask_lo"], row["mask_hi"])
+        d, _ = O.check_set(prob, S)
+        assert d["feasible"] == 1 and d["optimal"] == 1, S
+        assert d["t"] == row["t"] and d["r"] == row["r"] and d["region"] == row["region"], S
+    hits = 0
+    for _ in range(3000):
+        S = sorted(rng.choice(prob.m, 6, replace=False).tolist())
+        d, _ = O.check_set(prob, S)
+        lo = sum(1 << j for j in S if j < 64)
+        hi = sum(1 << (j - 64) for j in S if j >= 64)
+        assert bool(d["optimal"]) == ((lo, hi) in listed), S
+        hits += d["optimal"]
+    print("level 6: optimal sets", len(opt6), "random sets found optimal", hits)
 
 
 @pytest.mark.parametrize("case", list(CASES))
@@ -141,6 +209,14 @@ def test_mixed_equals_fp64_on_the_full_bench_batch(gpu_lib):
               "truncated", "last_level"):
         assert np.array_equal(r32.inst[f], r64.inst[f]), f
     assert r32.candidates == 60802277
+    # LP1 infeasible verdicts of the mixed path: the FP64 dual certificate
+    # (no re-solve) or the FP64 re-solve; never more than the infeasible sets
+    infeasible = r32.inst["candidates"] - r32.inst["feasible"]
+    assert np.all(r32.inst["lp1_certified"] <= infeasible)
+    assert r32.total("lp1_certified") > 0
+    print("bench batch: infeasible", int(infeasible.sum()), "certified", r32.total("lp1_certified"),
+          "cert missed", r32.total("lp1_cert_missed"), "free-variable misses", r32.total("lp1_cert_freevar"),
+          "FP64 LP1 re-solves", r32.total("fallback_lp1"))
 
 
 def test_mixed_equals_fp64_on_mixed_size_problems_to_full_depth(gpu_lib):
