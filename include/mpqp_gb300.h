@@ -33,9 +33,13 @@ extern "C" {
  *   n_final_lps      candidate active sets found optimal (LP2); their sets
  *                    are in active_sets, row-major n_final_lps x n_x,
  *                    ascending indices, unused entries -1 (utils.py:105-116)
- *   time_feas        seconds in enumeration + feasibility kernels
- *   time_opti        seconds in optimality kernels
+ *   time_feas        seconds in the enumeration and LP1 kernels (events
+ *                    around each launch)
+ *   time_opti        seconds in the optimality kernels
  *   time_GPU         seconds of device time for the whole call
+ * mpqp() runs in mixed precision (FP32 pivots, every verdict certified or
+ * re-solved in FP64; the same sets as the FP64 path); the environment
+ * variable MPQP_PRECISION=fp64 selects the plain FP64 kernels.
  * The structure and its arrays stay valid until mpqp_free() or the next
  * mpqp() call, whichever comes first. */
 typedef struct GPUResults {
@@ -232,6 +236,14 @@ int mpqp_release_cached_memory(void);
 long long mpqp_region_laws_stride(const mpqp_problem *prob);
 int mpqp_region_laws(const mpqp_problem *prob, long long n_sets, const uint64_t *masks /* 2 per set */,
                      double *laws, int *sizes);
+
+/* Replaces compute_critical_region (utils.py:23-97) for a list of active
+ * sets: mpqp_region_laws plus each set's Chebyshev radius (radius: n_sets
+ * doubles; NaN when the set fails the LICQ test or has no unique law).  A
+ * set is a critical region when radius >= 1e-8 (utils.py:86), so a caller
+ * needs no enumeration to filter the sets it holds. */
+int mpqp_critical_regions(const mpqp_problem *prob, long long n_sets, const uint64_t *masks, double *laws,
+                          int *sizes, double *radius);
 
 /* Region laws without any device allocation.  No counterpart in the
  * reference: its region laws are computed on the host (utils.py:23-97).

@@ -53,6 +53,9 @@ cudaError_t launch_finalize(const DevBuffers &B, int level, cudaStream_t s);
 cudaError_t launch_region_laws(const DevBuffers &B, const Tol &tol, const SlotDims &sd, const uint64_t *masks,
                                long long n_sets, double *laws, int *sizes, long long stride, int grid,
                                size_t smem, cudaStream_t s);
+cudaError_t launch_region_laws_r(const DevBuffers &B, const Tol &tol, const SlotDims &sd, const uint64_t *masks,
+                                 long long n_sets, double *laws, int *sizes, long long stride, double *radius,
+                                 int grid, size_t smem, cudaStream_t s);
 }  // namespace mq
 
 using namespace mq;
@@ -880,6 +883,23 @@ extern "C" int mpqp_plan_kernel_times(mpqp_plan *P, int max_kernels, char *names
     }
 }
 
+// Device time of the last timed run split into the LP1 phase (reset, level
+// 0, enumeration, LP1 and its FP64 certificate / re-solve, level
+// bookkeeping) and the optimality phase (screens and FP64 optimality), the
+// split main.py:18-20 reads as time_feas / time_opti.
+static int phase_times(mpqp_plan *P, double *feas_ms, double *opti_ms)
+{
+    *feas_ms = *opti_ms = 0.0;
+    if (!P || !P->timed) { set_err("no timed run"); return MPQP_EINVAL; }
+    CK(cudaEventSynchronize(P->ev1));
+    for (size_t i = 0; i < P->kname.size(); i++) {
+        float e = 0;
+        CK(cudaEventElapsedTime(&e, P->kev[i], P->kev[i + 1]));
+        if (!strncmp(P->kname[i], "k_opt", 5)) *opti_ms += e; else *feas_ms += e;
+    }
+    return MPQP_OK;
+}
+
 static uint64_t bit_reverse64(uint64_t x)
 {
     x = ((x >> 1) & 0x5555555555555555ULL) | ((x & 0x5555555555555555ULL) << 1);
@@ -1140,7 +1160,7 @@ extern "C" long long mpqp_region_laws_stride(const mpqp_problem *pr)
 }
 
 static int mpqp_region_laws_impl(const mpqp_problem *prob, long long n_sets, const uint64_t *masks, double *laws,
-                                 int *sizes)
+                                 int *sizes, double *radius)
 {
     if (!prob || n_sets < 0 || (n_sets && (!masks || !laws || !sizes))) { set_err("bad arguments"); return MPQP_EINVAL; }
     if (n_sets == 0) return MPQP_OK;
@@ -1166,7 +1186,7 @@ static int mpqp_region_laws_impl(const mpqp_problem *prob, long long n_sets, con
     SlotDims sd = P->sd;
     sd.maxK = std::max(1, kcap);
     const long long stride = mpqp_region_laws_stride(prob);
-    uint64_t *dm = nullptr; double *dl = nullptr; int *ds = nullptr;
+    uint64_t *dm = nullptr; double *dl = nullptr, *dr = nullptr; int *ds = nullptr;
     size_t smem = 4 * laws_smem_per_warp(sd);
     int grid = 0;
     rc = grid_for(kernel_ptr("laws"), smem, &grid);
@@ -1174,11 +1194,14 @@ static int mpqp_region_laws_impl(const mpqp_problem *prob, long long n_sets, con
         CK(cudaMalloc(&dm, sizeof(uint64_t) * 2 * n_sets));
         CK(cudaMalloc(&dl, sizeof(double) * stride * n_sets));
         CK(cudaMalloc(&ds, sizeof(int) * 4 * n_sets));
+        if (radius) CK(cudaMalloc(&dr, sizeof(double) * n_sets));
         CK(cudaMemcpy(dm, masks, sizeof(uint64_t) * 2 * n_sets, cudaMemcpyHostToDevice));
-        CK(launch_region_laws(P->B, P->tol, sd, dm, n_sets, dl, ds, stride, grid, smem, nullptr));
+        CK(launch_region_laws_r(P->B, P->tol, sd, dm, n_sets, dl, ds, stride, dr, grid, smem, nullptr));
         CK(cudaMemcpy(laws, dl, sizeof(double) * stride * n_sets, cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(sizes, ds, sizeof(int) * 4 * n_sets, cudaMemcpyDeviceToHost));
+        if (radius) CK(cudaMemcpy(radius, dr, sizeof(double) * n_sets, cudaMemcpyDeviceToHost));
         cudaFree(dm); cudaFree(dl); cudaFree(ds);
+        if (dr) cudaFree(dr);
     }
     mpqp_plan_destroy(P);
     return rc;
@@ -1188,9 +1211,20 @@ extern "C" int mpqp_region_laws(const mpqp_problem *prob, long long n_sets, cons
                                 int *sizes)
 {
     try {
-        return mpqp_region_laws_impl(prob, n_sets, masks, laws, sizes);
+        return mpqp_region_laws_impl(prob, n_sets, masks, laws, sizes, nullptr);
     } catch (...) {
         return host_failure("mpqp_region_laws");
+    }
+}
+
+extern "C" int mpqp_critical_regions(const mpqp_problem *prob, long long n_sets, const uint64_t *masks, double *laws,
+                                     int *sizes, double *radius)
+{
+    try {
+        if (!radius && n_sets > 0) { set_err("radius is NULL"); return MPQP_EINVAL; }
+        return mpqp_region_laws_impl(prob, n_sets, masks, laws, sizes, radius);
+    } catch (...) {
+        return host_failure("mpqp_critical_regions");
     }
 }
 
@@ -1338,8 +1372,14 @@ static GPUResults *mpqp_impl(const double *AxT, int n_c, int n_x, int n_t, int k
     pr.At = At.data(); pr.bt = bt.data();
     mpqp_options o;
     mpqp_default_options(&o);
+    // mixed precision (FP32 pivots, FP64 certificates and re-solves; verdicts
+    // identical to the FP64 path) unless MPQP_PRECISION=fp64
+    o.precision = MPQP_MIXED;
     const char *env = getenv("MPQP_PRECISION");
-    if (env && (!strcmp(env, "mixed") || !strcmp(env, "1"))) o.precision = MPQP_MIXED;
+    if (env && (!strcmp(env, "fp64") || !strcmp(env, "0"))) o.precision = MPQP_FP64;
+    // one run: launched without a graph, with an event before every launch,
+    // so that the device time splits into its LP1 and optimality phases
+    o.use_graph = 0;
     if (reserved_memory > 0) {
         size_t fb = 0, tb = 0;
         if (cudaMemGetInfo(&fb, &tb) == cudaSuccess) {
@@ -1349,7 +1389,15 @@ static GPUResults *mpqp_impl(const double *AxT, int n_c, int n_x, int n_t, int k
         }
     }
     mpqp_batch_result *R = nullptr;
-    rc = mpqp_solve_batch(1, &pr, &o, &R);
+    double feas_ms = 0.0, opti_ms = 0.0;
+    {
+        mpqp_plan *P = nullptr;
+        rc = mpqp_plan_create(1, &pr, &o, &P);
+        if (!rc) rc = mpqp_plan_run_timed(P, nullptr);
+        if (!rc) rc = mpqp_plan_results(P, &R);
+        if (!rc) rc = phase_times(P, &feas_ms, &opti_ms);
+        mpqp_plan_destroy(P);
+    }
     if (rc || !R) {
         mpqp_batch_free(R);
         return g_last = error_result(rc ? rc : MPQP_ECUDA);
@@ -1365,8 +1413,8 @@ static GPUResults *mpqp_impl(const double *AxT, int n_c, int n_x, int n_t, int k
     G->n_feasible_lps = (int)R->inst[0].feasible;
     G->n_final_lps = (int)nsel;
     G->time_GPU = R->device_ms * 1e-3;
-    G->time_feas = G->time_GPU;
-    G->time_opti = 0.0;
+    G->time_feas = feas_ms * 1e-3;
+    G->time_opti = opti_ms * 1e-3;
     G->status = R->status;
     G->n_candidates = R->inst[0].candidates;
     G->n_pruned = R->inst[0].pruned;

@@ -1816,6 +1816,79 @@ __device__ void lp2_short_mplp(const DevBuffers &B, const Tol &tol, const InstDe
     }
 }
 
+// Chebyshev ball of the region rows in ws.G (utils.py:39-86): the box rows
+// and the rows with a nonzero theta part, each normalised, then max r over
+// the ball; res.cheb_status / cheb_piv / r / region.  Uses ws.Tb and ws.ids.
+template <typename T>
+__device__ void chebyshev_ball(const Tol &tol, const InstDesc &I, OptWs<T> &ws, OptResult &res)
+{
+    const int lane = lane_id();
+    const int m = I.m, p = I.p, ncp = I.ncp, P1 = p + 1, R2 = m + ncp;
+    const int ld2 = sizeof(T) == 4 ? I.ld2 : I.ld2d;
+    const T tpiv = (T)tol.tol_piv;
+    const T tdj = (T)tol.tol_dj;
+    const T *G = ws.G;
+    T *Tb = ws.Tb;
+    uint8_t *bid = ws.ids, *nid = ws.ids + R2;
+    // Chebyshev ball: keep box rows and rows with a nonzero theta part
+    int nc = 0;
+    for (int r0 = 0; r0 < R2; r0 += 32) {
+        const int r = r0 + lane;
+        bool keep = false;
+        if (r < R2) {
+            if (r >= m) keep = true;
+            else keep = nonzero_row<T>(G + (size_t)r * P1, p, tol.tol_zero_row);
+        }
+        const unsigned km = __ballot_sync(FULLMASK, keep);
+        if (keep) {
+            const int np = nc + __popc(km & ((1u << lane) - 1u));
+            const T *g = G + (size_t)r * P1;
+            T acc = T(0);
+            for (int cc = 0; cc < p; cc++) acc = xfma(g[cc], g[cc], acc);
+            const T inv = xdiv(T(1), xsqrt(acc));
+            T *tr = Tb + (size_t)np * ld2;
+            T nn = T(0);
+            for (int cc = 0; cc < p; cc++) { const T v = xmul(g[cc], inv); tr[cc] = v; nn = xfma(v, v, nn); }
+            tr[p] = xsqrt(nn);
+            tr[p + 1] = xmul(g[p], inv);
+            bid[np] = (uint8_t)(P1 + np);
+        }
+        nc += __popc(km);
+    }
+    __syncwarp();
+    T r0v = pos_inf<T>();
+    for (int r = lane; r < nc; r += 32) {
+        const T v = xdiv(Tb[(size_t)r * ld2 + p + 1], Tb[(size_t)r * ld2 + p]);
+        if (v < r0v) r0v = v;
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) { const T o = __shfl_xor_sync(FULLMASK, r0v, off); if (o < r0v) r0v = o; }
+    for (int r = lane; r < nc; r += 32) {
+        T *tr = Tb + (size_t)r * ld2;
+        T beta = xfma(-tr[p], r0v, tr[p + 1]);
+        if (!(beta > T(0))) beta = T(0);
+        tr[p + 1] = beta;
+    }
+    for (int cc = lane; cc <= P1; cc += 32) {
+        T *ob = Tb + (size_t)nc * ld2;
+        ob[cc] = (cc == p) ? T(1) : (cc == P1 ? -r0v : T(0));
+        if (cc < P1) nid[cc] = (uint8_t)cc;
+    }
+    __syncwarp();
+    {
+        Lp<T> L{Tb, ld2, nc, P1, P1, bid, nid};
+        int piv = 0;
+        res.cheb_status = warp_simplex<T>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv);
+        res.cheb_piv = piv;
+    }
+    if (res.cheb_status == LP_OPTIMAL) {
+        res.r = (double)(-Tb[(size_t)nc * ld2 + P1]);
+        res.region = res.r >= tol.r_min;
+    } else if (res.cheb_status == LP_UNBOUNDED) {
+        res.r = pos_inf<double>();
+    }
+}
+
 // Optimality and region verdict of one feasible set (the FP64 path; the FP32
 // screen of the mixed path is k_opt_screen).  LP: the instance is an mpLP.
 template <typename T, bool LP = false>
@@ -1889,63 +1962,7 @@ __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const 
         if (res.lp2_status == LP_UNBOUNDED) res.t = pos_inf<double>();
     }
     if (!res.optimal) return res;
-    // Chebyshev ball: keep box rows and rows with a nonzero theta part
-    int nc = 0;
-    for (int r0 = 0; r0 < R2; r0 += 32) {
-        const int r = r0 + lane;
-        bool keep = false;
-        if (r < R2) {
-            if (r >= m) keep = true;
-            else keep = nonzero_row<T>(G + (size_t)r * P1, p, tol.tol_zero_row);
-        }
-        const unsigned km = __ballot_sync(FULLMASK, keep);
-        if (keep) {
-            const int np = nc + __popc(km & ((1u << lane) - 1u));
-            const T *g = G + (size_t)r * P1;
-            T acc = T(0);
-            for (int cc = 0; cc < p; cc++) acc = xfma(g[cc], g[cc], acc);
-            const T inv = xdiv(T(1), xsqrt(acc));
-            T *tr = Tb + (size_t)np * ld2;
-            T nn = T(0);
-            for (int cc = 0; cc < p; cc++) { const T v = xmul(g[cc], inv); tr[cc] = v; nn = xfma(v, v, nn); }
-            tr[p] = xsqrt(nn);
-            tr[p + 1] = xmul(g[p], inv);
-            bid[np] = (uint8_t)(P1 + np);
-        }
-        nc += __popc(km);
-    }
-    __syncwarp();
-    T r0v = pos_inf<T>();
-    for (int r = lane; r < nc; r += 32) {
-        const T v = xdiv(Tb[(size_t)r * ld2 + p + 1], Tb[(size_t)r * ld2 + p]);
-        if (v < r0v) r0v = v;
-    }
-#pragma unroll
-    for (int off = 16; off; off >>= 1) { const T o = __shfl_xor_sync(FULLMASK, r0v, off); if (o < r0v) r0v = o; }
-    for (int r = lane; r < nc; r += 32) {
-        T *tr = Tb + (size_t)r * ld2;
-        T beta = xfma(-tr[p], r0v, tr[p + 1]);
-        if (!(beta > T(0))) beta = T(0);
-        tr[p + 1] = beta;
-    }
-    for (int cc = lane; cc <= P1; cc += 32) {
-        T *ob = Tb + (size_t)nc * ld2;
-        ob[cc] = (cc == p) ? T(1) : (cc == P1 ? -r0v : T(0));
-        if (cc < P1) nid[cc] = (uint8_t)cc;
-    }
-    __syncwarp();
-    {
-        Lp<T> L{Tb, ld2, nc, P1, P1, bid, nid};
-        int piv = 0;
-        res.cheb_status = warp_simplex<T>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv);
-        res.cheb_piv = piv;
-    }
-    if (res.cheb_status == LP_OPTIMAL) {
-        res.r = (double)(-Tb[(size_t)nc * ld2 + P1]);
-        res.region = res.r >= tol.r_min;
-    } else if (res.cheb_status == LP_UNBOUNDED) {
-        res.r = pos_inf<double>();
-    }
+    chebyshev_ball<T>(tol, I, ws, res);
     return res;
 }
 
@@ -3019,7 +3036,8 @@ __global__ void k_finalize(DevBuffers B, int level)
 // sizes = {k, n, p, n_cr}; k = -1 when the KKT factor fails (LICQ), k = -2
 // for an mpLP set with |S| < n (x(theta) is not unique; nothing written).
 __global__ void __launch_bounds__(128) k_region_laws(DevBuffers B, Tol tol, SlotDims sd, const uint64_t *masks,
-                                                     long long n_sets, double *laws, int *sizes, long long stride)
+                                                     long long n_sets, double *laws, int *sizes, long long stride,
+                                                     double *radius)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
@@ -3035,6 +3053,7 @@ __global__ void __launch_bounds__(128) k_region_laws(DevBuffers B, Tol tol, Slot
         double *out = laws + x * stride;
         int *sz = sizes + 4 * x;
         int k = 0;
+        if (radius && lane == 0) radius[x] = __longlong_as_double(0x7ff8000000000000LL);
         if (kkt_factor<double>(D, I, lo, hi, tol.tol_licq, ws, &k)) {
             if (lane == 0) { sz[0] = -1; sz[1] = n; sz[2] = p; sz[3] = 0; }
             continue;
@@ -3087,6 +3106,14 @@ __global__ void __launch_bounds__(128) k_region_laws(DevBuffers B, Tol tol, Slot
         }
         if (lane == 0) { sz[0] = k; sz[1] = n; sz[2] = p; sz[3] = nc; }
         __syncwarp();
+        if (radius) {
+            // the Chebyshev radius of the same rows (region when >= r_min)
+            OptResult res;
+            res.r = __longlong_as_double(0x7ff8000000000000LL); res.region = 0;
+            chebyshev_ball<double>(tol, I, ws, res);
+            if (lane == 0) radius[x] = res.r;
+            __syncwarp();
+        }
     }
 }
 
@@ -3096,7 +3123,16 @@ cudaError_t launch_region_laws(const DevBuffers &B, const Tol &tol, const SlotDi
                                long long n_sets, double *laws, int *sizes, long long stride, int grid, size_t smem,
                                cudaStream_t s)
 {
-    k_region_laws<<<grid, 128, smem, s>>>(B, tol, sd, masks, n_sets, laws, sizes, stride);
+    k_region_laws<<<grid, 128, smem, s>>>(B, tol, sd, masks, n_sets, laws, sizes, stride, nullptr);
+    return cudaGetLastError();
+}
+
+// the same with each set's Chebyshev radius (radius: n_sets doubles)
+cudaError_t launch_region_laws_r(const DevBuffers &B, const Tol &tol, const SlotDims &sd, const uint64_t *masks,
+                                 long long n_sets, double *laws, int *sizes, long long stride, double *radius,
+                                 int grid, size_t smem, cudaStream_t s)
+{
+    k_region_laws<<<grid, 128, smem, s>>>(B, tol, sd, masks, n_sets, laws, sizes, stride, radius);
     return cudaGetLastError();
 }
 

@@ -149,32 +149,33 @@ def decode_active_sets(all_active_sets, n_sets: int, num_x: int) -> list[list[in
     return out
 
 
-def active_sets_to_regions(prog: MPQPProb, all_active_sets) -> list[dict]:
+def active_sets_to_regions(prog: MPQPProb, all_active_sets, is_region=None) -> list[dict]:
     """``utils.py:128-144``: one region dict per active set whose Chebyshev
     radius is at least 1e-8.  Laws and normalised region rows come from the
-    device in FP64; the radius test is the one the device already ran."""
+    device in FP64.  ``is_region`` (optional, e.g. ``GPUResults.is_region``):
+    the radius test ``mpqp()`` already ran for these sets; without it the
+    device computes each set's radius with its laws (``mpqp_critical_regions``).
+    Neither way enumerates any set."""
     sets = decode_active_sets(all_active_sets, prog.n_active_sets, prog.num_x)
     if not sets:
         return []
     prob = prog.to_mpqp()
-    laws = solver.region_laws(prob, sets)
-    res = solver.solve([prob], k_max=max(len(s) for s in sets), precision=solver.FP64)
-    region_masks = {(int(o["mask_lo"]), int(o["mask_hi"])) for o in res.opt if o["region"]}
-    out = []
-    for S, law in zip(sets, laws):
-        lo = sum(1 << j for j in S if j < 64)
-        hi = sum(1 << (j - 64) for j in S if j >= 64)
-        if law is not None and (lo, hi) in region_masks:
-            out.append(law)
-    return out
+    if is_region is not None:
+        laws = solver.region_laws(prob, sets)
+        keep = [bool(is_region[i]) for i in range(len(sets))]
+    else:
+        laws = solver.region_laws(prob, sets, with_radius=True)
+        keep = [law is not None and law["r"] >= 1e-8 for law in laws]
+    return [law for law, k in zip(laws, keep) if law is not None and k]
 
 
-def calculate_mpqp_with_CUDA(problems, precision: str = "fp64", reduce: bool = False, reserved_memory: int = 0):
+def calculate_mpqp_with_CUDA(problems, precision: str = "mixed", reduce: bool = False, reserved_memory: int = 0):
     """``main.py:11-173`` over a list of ``MPQP`` problems, one call each.
 
     Returns rows (index, n_regions, total_time, time_GPU) like the reference,
-    plus the raw results.  ``precision`` selects the plain FP64 kernels or the
-    FP32 kernels with FP64 certificates (environment variable MPQP_PRECISION);
+    plus the raw results.  ``precision`` selects the FP32 kernels with FP64
+    certificates ("mixed", the default of ``mpqp()``) or the plain FP64
+    kernels ("fp64"; environment variable MPQP_PRECISION);
     ``reduce`` runs the device row reduction first (the ppopt steps of
     ``utils.py:165-190``); ``reserved_memory`` (MiB) is the argument of
     ``main.py:144``: device memory left free when the call sizes its buffers.

@@ -87,7 +87,8 @@ REC_DTYPE = np.dtype([("mask_lo", "<u8"), ("mask_hi", "<u8"), ("level", "<i4"), 
 EXPORTS = ("mpqp", "warm_up", "mpqp_free", "mpqp_unpack_lp", "mpqp_default_options", "mpqp_solve_batch", "mpqp_batch_free",
            "mpqp_plan_create", "mpqp_plan_run", "mpqp_plan_results", "mpqp_plan_launches", "mpqp_plan_destroy",
            "mpqp_plan_run_timed", "mpqp_plan_kernel_times",
-           "mpqp_region_laws_stride", "mpqp_region_laws", "mpqp_reduce_constraints", "mpqp_release_cached_memory",
+           "mpqp_region_laws_stride", "mpqp_region_laws", "mpqp_critical_regions", "mpqp_reduce_constraints",
+           "mpqp_release_cached_memory", "mpqp_region_laws_noalloc",
            "mpqp_version",
            "mpqp_last_error")
 
@@ -144,6 +145,9 @@ def load(build_if_missing: bool = False):
     lib.mpqp_region_laws.argtypes = [P(Problem), ctypes.c_longlong, P(ctypes.c_uint64), P(ctypes.c_double),
                                      P(ctypes.c_int)]
     lib.mpqp_region_laws.restype = ctypes.c_int
+    lib.mpqp_critical_regions.argtypes = [P(Problem), ctypes.c_longlong, P(ctypes.c_uint64), P(ctypes.c_double),
+                                          P(ctypes.c_int), P(ctypes.c_double)]
+    lib.mpqp_critical_regions.restype = ctypes.c_int
     lib.mpqp_reduce_constraints.argtypes = [P(Problem), P(ctypes.c_int)]
     lib.mpqp_reduce_constraints.restype = ctypes.c_int
     lib.mpqp_release_cached_memory.restype = ctypes.c_int
@@ -339,10 +343,12 @@ def apply_row_status(prob, status):
     return out
 
 
-def region_laws(prob, sets):
+def region_laws(prob, sets, with_radius: bool = False):
     """FP64 laws of the given active sets (device).  Returns a list of dicts;
     None for a set that fails the LICQ test and for an mpLP set with fewer
-    than n active constraints (its law x(theta) is not unique)."""
+    than n active constraints (its law x(theta) is not unique).  with_radius:
+    each dict also holds the set's Chebyshev radius ``r`` (``mpqp_critical_regions``;
+    a critical region when r >= 1e-8, utils.py:86)."""
     lib = load()
     ps = _ProblemSet([prob], 0, 0, 0)
     masks = np.zeros((len(sets), 2), dtype=np.uint64)
@@ -352,9 +358,13 @@ def region_laws(prob, sets):
     stride = lib.mpqp_region_laws_stride(ps.arr)
     laws = np.zeros((max(len(sets), 1), stride))
     sizes = np.zeros((max(len(sets), 1), 4), dtype=np.intc)
-    _check(lib.mpqp_region_laws(ps.arr, len(sets), masks.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
-                                laws.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
-                                sizes.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+    radius = np.full(max(len(sets), 1), np.nan)
+    args = (ps.arr, len(sets), masks.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+            laws.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), sizes.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    if with_radius:
+        _check(lib.mpqp_critical_regions(*args, radius.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    else:
+        _check(lib.mpqp_region_laws(*args))
     out = []
     m, n, p = prob.m, prob.n, prob.p
     P1 = p + 1
@@ -366,9 +376,12 @@ def region_laws(prob, sets):
         lag = laws[i, :k * P1].reshape(k, P1)
         par = laws[i, m * P1:m * P1 + n * P1].reshape(n, P1)
         cr = laws[i, (m + n) * P1:(m + n) * P1 + ncr * P1].reshape(ncr, P1)
-        out.append(dict(lagrange_A=lag[:, :p].copy(), lagrange_b=lag[:, p].copy(), parameter_A=par[:, :p].copy(),
-                        parameter_b=par[:, p].copy(), CR_As=cr[:, :p].copy(), CR_bs=cr[:, p].copy(),
-                        active_set=list(sets[i])))
+        d = dict(lagrange_A=lag[:, :p].copy(), lagrange_b=lag[:, p].copy(), parameter_A=par[:, :p].copy(),
+                 parameter_b=par[:, p].copy(), CR_As=cr[:, :p].copy(), CR_bs=cr[:, p].copy(),
+                 active_set=list(sets[i]))
+        if with_radius:
+            d["r"] = float(radius[i])
+        out.append(d)
     return out
 
 

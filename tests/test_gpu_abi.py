@@ -29,9 +29,14 @@ def ref():
 
 
 @pytest.mark.parametrize("label", list(GEN))
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["default", "fp64", "mixed"])
 def test_mpqp_drop_in_matches_oracle_and_reference(gpu_lib, ref, label, precision, monkeypatch):
-    monkeypatch.setenv("MPQP_PRECISION", precision)
+    """No environment variable: mpqp() runs in mixed precision, the same sets
+    as the FP64 kernels and the oracle."""
+    if precision == "default":
+        monkeypatch.delenv("MPQP_PRECISION", raising=False)
+    else:
+        monkeypatch.setenv("MPQP_PRECISION", precision)
     lib = host.load_mpqp_cuda()
     lib.warm_up()
     prog = host.MPQPProb.from_mpqp(GEN[label]())
@@ -47,6 +52,9 @@ def test_mpqp_drop_in_matches_oracle_and_reference(gpu_lib, ref, label, precisio
     assert g.n_feasible_lps == e.n_feasible and g.n_candidates == e.n_cand
     assert g.n_regions == e.n_region == int(ref[f"{label}/n_regions"][0])
     assert g.time_GPU > 0 and g.n_batches >= 1
+    # the device time split like main.py:18-20 reads it
+    assert g.time_feas > 0 and g.time_opti > 0
+    assert g.time_feas + g.time_opti <= g.time_GPU * 1.001 + 1e-6
     lib.mpqp_free(r)
 
 
@@ -78,6 +86,38 @@ def test_calculate_mpqp_with_cuda_region_counts_match_reference(gpu_lib, ref):
     rows, raw = host.calculate_mpqp_with_CUDA(probs)
     for i, label in enumerate(GEN):
         assert int(rows[i, 1]) == int(ref[f"{label}/n_regions"][0]), label
+
+
+@pytest.mark.parametrize("label", list(GEN))
+def test_regions_pass_enumerates_nothing(gpu_lib, ref, label, monkeypatch):
+    """main.py:144-157: mpqp() returns the optimal sets, then the regions pass
+    forms each region (utils.py:128-144).  Both ways of the pass -- with the
+    radius test mpqp() already ran (GPUResults.is_region) and with the radii
+    computed beside the laws -- keep the reference's regions and launch no
+    enumeration (solver.solve is not called)."""
+    lib = host.load_mpqp_cuda()
+    prog = host.MPQPProb.from_mpqp(GEN[label]())
+    prog.process_constraints(scale_method=1)
+    d = host.build_lp_data(prog)
+    r = host.call_mpqp(lib, d)
+    g = r.contents
+    assert g.status == 0
+    prog.num_x = d["num_x"]
+    prog.n_active_sets = g.n_final_lps
+
+    def no_enumeration(*a, **k):
+        raise AssertionError("the regions pass enumerated")
+    monkeypatch.setattr(solver, "solve", no_enumeration)
+    a = host.active_sets_to_regions(prog, g.active_sets, g.is_region)
+    b = host.active_sets_to_regions(prog, g.active_sets)
+    want = int(ref[f"{label}/n_regions"][0])
+    assert len(a) == len(b) == g.n_regions == want
+    for x, y in zip(a, b):
+        assert x["active_set"] == y["active_set"]
+        assert np.array_equal(x["parameter_A"], y["parameter_A"])
+    radii = sorted(y["r"] for y in b)
+    assert all(rr >= 1e-8 for rr in radii)
+    lib.mpqp_free(r)
 
 
 @pytest.mark.parametrize("label", list(GEN))
