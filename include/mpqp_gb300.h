@@ -59,6 +59,8 @@ typedef struct GPUResults {
     double *t_star;          /* n_final_lps: LP2 optimum (max margin)       */
     double *radius;          /* n_final_lps: Chebyshev radius               */
     int *is_region;          /* n_final_lps: 1 when radius >= 1e-8          */
+    double *law_error;       /* n_final_lps: stated relative error of the
+                                set's affine laws (see mpqp_opt_set.err)   */
 } GPUResults;
 
 /* Replaces mpqp_cuda.so:mpqp (called at main.py:144, argtypes main.py:28-50).
@@ -158,6 +160,14 @@ typedef struct {
     double r;                    /* Chebyshev radius                         */
     int region, fp64;
     long long rec;
+    /* The error stated for this result: the size of one FP64 iterative-
+     * refinement step of the KKT solve (residual of Wm[S,S] Lambda =
+     * [Wh_S | wc_S] solved with the same factor) relative to the largest
+     * entry of Lambda -- an estimate of the relative forward error of the
+     * multiplier law lambda(theta) and of the primal law x(theta), which is
+     * linear in it.  The laws themselves are the unrefined FP64 values (the
+     * oracle's operations); t and r are FP64 LP optima. */
+    double err;
 } mpqp_opt_set;
 
 /* Per-instance counters */
@@ -243,7 +253,7 @@ int mpqp_region_laws(const mpqp_problem *prob, long long n_sets, const uint64_t 
  * set is a critical region when radius >= 1e-8 (utils.py:86), so a caller
  * needs no enumeration to filter the sets it holds. */
 int mpqp_critical_regions(const mpqp_problem *prob, long long n_sets, const uint64_t *masks, double *laws,
-                          int *sizes, double *radius);
+                          int *sizes, double *radius, double *err /* n_sets, may be NULL: the stated law error */);
 
 /* Region laws without any device allocation.  No counterpart in the
  * reference: its region laws are computed on the host (utils.py:23-97).

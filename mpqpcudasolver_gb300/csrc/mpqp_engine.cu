@@ -55,7 +55,7 @@ cudaError_t launch_region_laws(const DevBuffers &B, const Tol &tol, const SlotDi
                                size_t smem, cudaStream_t s);
 cudaError_t launch_region_laws_r(const DevBuffers &B, const Tol &tol, const SlotDims &sd, const uint64_t *masks,
                                  long long n_sets, double *laws, int *sizes, long long stride, double *radius,
-                                 int grid, size_t smem, cudaStream_t s);
+                                 double *err, int grid, size_t smem, cudaStream_t s);
 }  // namespace mq
 
 using namespace mq;
@@ -1081,7 +1081,7 @@ static int plan_results_impl(mpqp_plan *P, mpqp_batch_result *&R, bool *complete
         const OptRec &v = ov[order[i]];
         mpqp_opt_set &o = R->opt[i];
         o.mask_lo = v.lo; o.mask_hi = v.hi; o.inst = v.inst; o.level = v.level;
-        o.t = v.t; o.r = v.r; o.region = v.region; o.fp64 = v.fp64; o.rec = v.rec;
+        o.t = v.t; o.r = v.r; o.region = v.region; o.fp64 = v.fp64; o.rec = v.rec; o.err = v.err;
     }
     R->h2d_bytes = P->h2d_bytes;
     R->d2h_bytes = (long long)(sizeof(Ctl) + sizeof(InstCtl) * P->n_inst + sizeof(OptRec) * nopt);
@@ -1160,7 +1160,7 @@ extern "C" long long mpqp_region_laws_stride(const mpqp_problem *pr)
 }
 
 static int mpqp_region_laws_impl(const mpqp_problem *prob, long long n_sets, const uint64_t *masks, double *laws,
-                                 int *sizes, double *radius)
+                                 int *sizes, double *radius, double *err)
 {
     if (!prob || n_sets < 0 || (n_sets && (!masks || !laws || !sizes))) { set_err("bad arguments"); return MPQP_EINVAL; }
     if (n_sets == 0) return MPQP_OK;
@@ -1186,7 +1186,7 @@ static int mpqp_region_laws_impl(const mpqp_problem *prob, long long n_sets, con
     SlotDims sd = P->sd;
     sd.maxK = std::max(1, kcap);
     const long long stride = mpqp_region_laws_stride(prob);
-    uint64_t *dm = nullptr; double *dl = nullptr, *dr = nullptr; int *ds = nullptr;
+    uint64_t *dm = nullptr; double *dl = nullptr, *dr = nullptr, *de = nullptr; int *ds = nullptr;
     size_t smem = 4 * laws_smem_per_warp(sd);
     int grid = 0;
     rc = grid_for(kernel_ptr("laws"), smem, &grid);
@@ -1195,13 +1195,16 @@ static int mpqp_region_laws_impl(const mpqp_problem *prob, long long n_sets, con
         CK(cudaMalloc(&dl, sizeof(double) * stride * n_sets));
         CK(cudaMalloc(&ds, sizeof(int) * 4 * n_sets));
         if (radius) CK(cudaMalloc(&dr, sizeof(double) * n_sets));
+        if (err) CK(cudaMalloc(&de, sizeof(double) * n_sets));
         CK(cudaMemcpy(dm, masks, sizeof(uint64_t) * 2 * n_sets, cudaMemcpyHostToDevice));
-        CK(launch_region_laws_r(P->B, P->tol, sd, dm, n_sets, dl, ds, stride, dr, grid, smem, nullptr));
+        CK(launch_region_laws_r(P->B, P->tol, sd, dm, n_sets, dl, ds, stride, dr, de, grid, smem, nullptr));
         CK(cudaMemcpy(laws, dl, sizeof(double) * stride * n_sets, cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(sizes, ds, sizeof(int) * 4 * n_sets, cudaMemcpyDeviceToHost));
         if (radius) CK(cudaMemcpy(radius, dr, sizeof(double) * n_sets, cudaMemcpyDeviceToHost));
+        if (err) CK(cudaMemcpy(err, de, sizeof(double) * n_sets, cudaMemcpyDeviceToHost));
         cudaFree(dm); cudaFree(dl); cudaFree(ds);
         if (dr) cudaFree(dr);
+        if (de) cudaFree(de);
     }
     mpqp_plan_destroy(P);
     return rc;
@@ -1211,18 +1214,18 @@ extern "C" int mpqp_region_laws(const mpqp_problem *prob, long long n_sets, cons
                                 int *sizes)
 {
     try {
-        return mpqp_region_laws_impl(prob, n_sets, masks, laws, sizes, nullptr);
+        return mpqp_region_laws_impl(prob, n_sets, masks, laws, sizes, nullptr, nullptr);
     } catch (...) {
         return host_failure("mpqp_region_laws");
     }
 }
 
 extern "C" int mpqp_critical_regions(const mpqp_problem *prob, long long n_sets, const uint64_t *masks, double *laws,
-                                     int *sizes, double *radius)
+                                     int *sizes, double *radius, double *err)
 {
     try {
         if (!radius && n_sets > 0) { set_err("radius is NULL"); return MPQP_EINVAL; }
-        return mpqp_region_laws_impl(prob, n_sets, masks, laws, sizes, radius);
+        return mpqp_region_laws_impl(prob, n_sets, masks, laws, sizes, radius, err);
     } catch (...) {
         return host_failure("mpqp_critical_regions");
     }
@@ -1240,6 +1243,7 @@ static void free_gpu_results(GPUResults *r)
     free(r->t_star);
     free(r->radius);
     free(r->is_region);
+    free(r->law_error);
     free(r);
 }
 
@@ -1259,6 +1263,7 @@ static GPUResults *error_result(int status)
     r->t_star = (double *)calloc(1, sizeof(double));
     r->radius = (double *)calloc(1, sizeof(double));
     r->is_region = (int *)calloc(1, sizeof(int));
+    r->law_error = (double *)calloc(1, sizeof(double));
     return r;
 }
 
@@ -1422,7 +1427,8 @@ static GPUResults *mpqp_impl(const double *AxT, int n_c, int n_x, int n_t, int k
     G->t_star = (double *)malloc(sizeof(double) * (nsel ? nsel : 1));
     G->radius = (double *)malloc(sizeof(double) * (nsel ? nsel : 1));
     G->is_region = (int *)malloc(sizeof(int) * (nsel ? nsel : 1));
-    if (!G->active_sets || !G->t_star || !G->radius || !G->is_region) {
+    G->law_error = (double *)malloc(sizeof(double) * (nsel ? nsel : 1));
+    if (!G->active_sets || !G->t_star || !G->radius || !G->is_region || !G->law_error) {
         free_gpu_results(G);
         mpqp_batch_free(R);
         throw std::bad_alloc();   // the exported wrapper returns an MPQP_ENOMEM result
@@ -1442,6 +1448,7 @@ static GPUResults *mpqp_impl(const double *AxT, int n_c, int n_x, int n_t, int k
         G->t_star[w] = o2.t;
         G->radius[w] = o2.r;
         G->is_region[w] = o2.region;
+        G->law_error[w] = o2.err;
         nreg += o2.region;
         w++;
     }

@@ -106,6 +106,7 @@ struct OptRec {
     int region;
     int fp64;                   // verdict decided by the FP64 kernels
     long long rec;
+    double err;                 // estimated relative error of the set's law (FP64 refinement step)
 };
 
 struct CandRec {                // identical field layout to the oracle's record

@@ -1236,20 +1236,31 @@ __global__ void __launch_bounds__(128) k_lp1_fp64(DevBuffers B, Tol tol, SlotDim
 // weak duality every such y gives z* >= beta.y.  The candidate's final FP32
 // basis fixes y_i = c_i on its basic slacks; when every free variable is
 // basic, the duals of the nv nonbasic slacks solve the square system
-// G_N^T y_N = -G_B^T c_B, here by FP64 Gaussian elimination with partial
-// pivoting.  The FP32 LP kept the parent's nonbasic slacks at zero, so their
-// duals may exceed c_i = 1: y / s, s = max(1, max_{i in S'} y_i), is a
-// feasible dual point as soon as y_i <= tol_dj (the FP64 simplex's own
-// optimality tolerance) on the nonbasic slacks outside S'.  The set is
-// infeasible when beta.y / s > tol_feas -- whatever path the FP32 simplex
-// took, since only the final basis enters; every other candidate goes on to
-// the FP64 re-solve.  One warp per queued candidate, lane r owns row r of
-// G_N^T in shared memory (row stride odd in doubles); instances with nv > 32
-// never reach this kernel.
+// M y_N = rhs,  M = G_N^T,  rhs = -G_B^T c_B.  The FP32 LP kept the parent's
+// nonbasic slacks at zero, so their duals may exceed c_i = 1: y / s,
+// s = max(1, max_{i in S'} y_i), is a feasible dual point as soon as
+// y_i <= tol_dj (the FP64 simplex's own optimality tolerance) on the
+// nonbasic slacks outside S'.  The set is infeasible when beta.y / s >
+// tol_feas -- whatever path the FP32 simplex took, since only the final
+// basis enters; every other candidate goes on to the FP64 re-solve.
+//
+// The system is solved by mixed-precision iterative refinement: an FP32 LU
+// with partial pivoting, then corrections from FP64 residuals rhs - M y
+// (three FP32 solves in all); y is accepted when the last FP64 residual is
+// at FP64 rounding level (<= kCertResid * (|M| |y| + |rhs|)).  y, the sign
+// tests and beta.y are FP64; only the correction solves run in FP32, so the
+// FP64 pipe (a small fraction of the FP32 rate on this GPU) does the O(nv^2)
+// residuals, not the O(nv^3) factorisation.  One warp per queued candidate,
+// lane r owns row r of M (FP64 copy and FP32 LU in shared memory, row
+// stride odd); instances with nv > 32 never reach this kernel.
+constexpr int kCertSolves = 3;
+constexpr double kCertResid = 1e-13;
+
 __host__ __device__ inline size_t cert_slot_bytes(int maxNv)
 {
-    const int nvm = maxNv < 32 ? maxNv : 32;
-    return align16((size_t)nvm * (nvm | 1) * sizeof(double));
+    const int nvm = maxNv < 32 ? maxNv : 32, ldm = nvm | 1;
+    return align16((size_t)nvm * ldm * sizeof(double)) + align16((size_t)nvm * ldm * sizeof(float)) +
+           align16((size_t)nvm * sizeof(double));
 }
 
 __device__ __forceinline__ double warp_max_d(double v)
@@ -1266,13 +1277,25 @@ __device__ __forceinline__ double warp_sum_d(double v)
     return v;
 }
 
+__device__ __forceinline__ float warp_max_f(float v)
+{
+#pragma unroll
+    for (int off = 16; off; off >>= 1) v = fmaxf(v, __shfl_xor_sync(FULLMASK, v, off));
+    return v;
+}
+
 __global__ void __launch_bounds__(128) k_lp1_cert(DevBuffers B, Tol tol, SlotDims sd, int level)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
     const int nvm = sd.maxNv < 32 ? sd.maxNv : 32, ldm = nvm | 1;
-    double *M = (double *)(smem + wib * cert_slot_bytes(sd.maxNv));
-    double *Mr = M + (size_t)(lane < nvm ? lane : 0) * ldm;   // this lane's row
+    unsigned char *base = smem + wib * cert_slot_bytes(sd.maxNv);
+    double *Md = (double *)base;                                                     // M, FP64
+    float *Mf = (float *)(base + align16((size_t)nvm * ldm * sizeof(double)));      // its FP32 LU
+    double *yv = (double *)((unsigned char *)Mf + align16((size_t)nvm * ldm * sizeof(float)));
+    const int row = lane < nvm ? lane : 0;
+    double *Mdr = Md + (size_t)row * ldm;   // this lane's row
+    float *Mfr = Mf + (size_t)row * ldm;
     const int pside = (level & 1) ^ 1;
     Ctl *ctl = B.ctl;
     const long long nq = ctl->n_q_cert < B.cert_cap ? ctl->n_q_cert : B.cert_cap;
@@ -1287,22 +1310,24 @@ __global__ void __launch_bounds__(128) k_lp1_cert(DevBuffers B, Tol tol, SlotDim
         const Node par = B.node[pside][c.parent];
         const int inst = par.inst;
         const InstDesc &I = B.inst[inst];
-        const int nv = I.nv, ld = I.ld1d;
+        const int nv = I.nv, ld = I.ld1d, ldf = I.ld1;
         uint64_t lo = par.lo, hi = par.hi;
         if (c.j < 64) lo |= 1ull << c.j; else hi |= 1ull << (c.j - 64);
         const double *G = B.dpool + I.o_root;
+        const float *Gf = B.fpool + I.f_root;
         // lane cc < nv: the slack nonbasic in column cc (negative: a free variable)
         const int nb = lane < nv ? (int)e[4 + lane] - nv : 0;
         const bool all_slack = __all_sync(FULLMASK, nb >= 0) && nv <= nvm;
         bool ok = all_slack;
         double bound = 0.0;
         if (ok) {
-            // lane v: row v of G_N^T and rhs_v = -sum_{i in S' basic} G[i][v]
+            // lane v: row v of M (M[v][cc] = G[nb_cc][v]) and rhs_v = -sum over
+            // the basic slacks i of S' of G[i][v]; by = their beta_i (y_i = 1)
             for (int cc = 0; cc < nv; cc++) {
                 const int i = __shfl_sync(FULLMASK, nb, cc);
-                if (lane < nv) Mr[cc] = G[(size_t)i * ld + lane];
+                if (lane < nv) { Mdr[cc] = G[(size_t)i * ld + lane]; Mfr[cc] = Gf[(size_t)i * ldf + lane]; }
             }
-            double rhs = 0.0, by = 0.0;   // by: beta.y over the basic slacks of S' (y = 1)
+            double rhs = 0.0, by = 0.0;
             uint64_t rl = lo, rh = hi;
             while (rl | rh) {
                 int i;
@@ -1313,40 +1338,68 @@ __global__ void __launch_bounds__(128) k_lp1_cert(DevBuffers B, Tol tol, SlotDim
                 by = __dadd_rn(by, G[(size_t)i * ld + nv]);
             }
             __syncwarp();
-            double amax = 0.0;
-            if (lane < nv) for (int cc = 0; cc < nv; cc++) amax = fmax(amax, fabs(Mr[cc]));
-            const double thr = 1e-13 * fmax(warp_max_d(amax), 1.0);
-            // elimination: the pivot of column col is the unused row with the
-            // largest |entry| (smallest lane on ties)
+            // FP32 LU with partial pivoting: the pivot of column col is the
+            // unused row with the largest |entry| (smallest lane on ties); the
+            // multipliers stay in the eliminated positions
+            float amax = 0.0f;
+            if (lane < nv) for (int cc = 0; cc < nv; cc++) amax = fmaxf(amax, fabsf(Mfr[cc]));
+            amax = warp_max_f(amax);
+            const float thr = 1e-6f * fmaxf(amax, 1.0f);
             bool used = lane >= nv;
-            int mycol = -1;
+            int mycol = -1, mypl = 0;   // mypl (lane col): the row that pivoted column col
+            float ipiv = 0.0f;
             for (int col = 0; col < nv; col++) {
-                const double a = used ? -1.0 : fabs(Mr[col]);
-                const double amx = warp_max_d(a);
+                const float a = used ? -1.0f : fabsf(Mfr[col]);
+                const float amx = warp_max_f(a);
                 if (!(amx > thr)) { ok = false; break; }
                 const int pr = __ffs(__ballot_sync(FULLMASK, !used && a == amx)) - 1;
-                const double *P = M + (size_t)pr * ldm;
-                const double prhs = __shfl_sync(FULLMASK, rhs, pr);
+                const float *P = Mf + (size_t)pr * ldm;
+                if (lane == col) mypl = pr;
                 if (lane == pr) {
                     used = true;
                     mycol = col;
+                    ipiv = __frcp_rn(P[col]);
                 } else if (!used) {
-                    const double f = xdiv(Mr[col], P[col]);
-                    for (int cc = col + 1; cc < nv; cc++) Mr[cc] = xfma(-f, P[cc], Mr[cc]);
-                    rhs = xfma(-f, prhs, rhs);
+                    const float f = __fdiv_rn(Mfr[col], P[col]);
+                    Mfr[col] = f;
+                    for (int cc = col + 1; cc < nv; cc++) Mfr[cc] = __fmaf_rn(-f, P[cc], Mfr[cc]);
                 }
                 __syncwarp();
             }
-            // back substitution, last column first; lane cc keeps y of column cc
-            double y = 0.0;
-            for (int col = nv - 1; col >= 0 && ok; col--) {
-                const int pr = __ffs(__ballot_sync(FULLMASK, mycol == col)) - 1;
-                double yc = lane == pr ? xdiv(rhs, Mr[col]) : 0.0;
-                yc = __shfl_sync(FULLMASK, yc, pr);
-                if (lane == col) y = yc;
-                if (mycol >= 0 && mycol < col) rhs = xfma(-Mr[col], yc, rhs);
-            }
             if (ok) {
+                double y = 0.0, rr = rhs;
+                const double rhsmax = warp_max_d(fabs(rhs));
+                double mmax = 0.0;
+                if (lane < nv) { for (int cc = 0; cc < nv; cc++) mmax = fmax(mmax, fabs(Mdr[cc])); }
+                mmax = warp_max_d(mmax);
+                for (int it = 0; it < kCertSolves; it++) {
+                    // the correction d of M d = rr in FP32, scaled by a power of two
+                    const float rm = warp_max_f(fabsf((float)rr));
+                    if (!(rm > 0.0f)) break;
+                    const int ex = ilogbf(rm);   // |ex| <= 149: 2^-ex and 2^ex are normal doubles
+                    float b = (float)(rr * __longlong_as_double((long long)(1023 - ex) << 52));
+                    for (int col = 0; col < nv; col++) {            // L (unit lower)
+                        const float bp = __shfl_sync(FULLMASK, b, __shfl_sync(FULLMASK, mypl, col));
+                        if (mycol > col) b = __fmaf_rn(-Mfr[col], bp, b);
+                    }
+                    float d = 0.0f;
+                    for (int col = nv - 1; col >= 0; col--) {       // U
+                        const int pr = __shfl_sync(FULLMASK, mypl, col);
+                        const float dc = __shfl_sync(FULLMASK, b * ipiv, pr);
+                        if (lane == col) d = dc;
+                        if (mycol >= 0 && mycol < col) b = __fmaf_rn(-Mfr[col], dc, b);
+                    }
+                    y = fma((double)d, __longlong_as_double((long long)(1023 + ex) << 52), y);
+                    // FP64 residual rr = rhs - M y
+                    if (lane < nv) yv[lane] = y;
+                    __syncwarp();
+                    rr = rhs;
+                    if (lane < nv) for (int cc = 0; cc < nv; cc++) rr = fma(-Mdr[cc], yv[cc], rr);
+                    __syncwarp();
+                }
+                const double ymax = warp_max_d(lane < nv ? fabs(y) : 0.0);
+                const double rres = warp_max_d(lane < nv ? fabs(rr) : 0.0);
+                ok = rres <= kCertResid * (mmax * ymax + rhsmax) && ymax == ymax;
                 // dual feasibility after scaling, and beta.y / s
                 double smax = 1.0, byn = 0.0;
                 bool bad = false;
@@ -1354,13 +1407,13 @@ __global__ void __launch_bounds__(128) k_lp1_cert(DevBuffers B, Tol tol, SlotDim
                     const bool inS = nb < I.m && mask_has(lo, hi, nb);
                     if (inS) smax = fmax(smax, y);
                     else bad = !(y <= tol.tol_dj);
-                    byn = xmul(G[(size_t)nb * ld + nv], y);
+                    byn = G[(size_t)nb * ld + nv] * y;
                 }
                 bad = __any_sync(FULLMASK, bad);
                 smax = warp_max_d(smax);
                 byn = warp_sum_d(byn);
-                bound = xdiv(xadd(by, byn), smax);
-                ok = !bad && bound > tol.tol_feas;
+                bound = __dadd_rn(by, byn) / smax;
+                ok = ok && !bad && bound > tol.tol_feas;
             }
         }
         if (lane == 0) {
@@ -1414,6 +1467,7 @@ __device__ __forceinline__ bool nonzero_row(const T *g, int p, double tz)
 struct OptResult {
     int licq, lp2_status, lp2_piv, cheb_status, cheb_piv, optimal, region;
     double t, r;
+    double err;         // estimated relative error of the law (law_error), NaN when not computed
     bool decided;
 };
 
@@ -1479,6 +1533,41 @@ __device__ void mplp_multipliers(const DevBuffers &B, const InstDesc &I, int k, 
     }
     __syncwarp();
     chol_solve_inplace<double>(ws.R, k, ws.Psi, P1, P1);
+}
+
+// Stated error of a set's law: one step of iterative refinement in FP64.
+// The residual [Wh_S | wc_S] - Wm[S,S] Lambda (and, for an mpLP instance,
+// [WhL_S | wcL_S] - Wm[S,S] Psi) is solved with the same Cholesky factor;
+// the largest correction relative to the largest law entry estimates the
+// relative forward error of the multiplier law, and with it of the primal
+// law (linear in Lambda).  Not applied: the law stays the oracle's values.
+// Uses ws.Y (free once Lambda is known).  Warp-uniform result.
+__device__ double law_error(const DevBuffers &B, const InstDesc &I, int k, OptWs<double> &ws)
+{
+    const int lane = lane_id();
+    const int m = I.m, p = I.p, P1 = p + 1;
+    const int *S = ws.S;
+    const double *Wm = B.dpool + I.o_Wm;
+    double *X = ws.Y;
+    double num = 0.0, den = 0.0;
+    for (int pass = 0; pass < (I.lp ? 2 : 1); pass++) {
+        const double *L = pass ? ws.Psi : ws.Lam;
+        const double *Wh = B.dpool + (pass ? I.o_WhL : I.o_Wh), *wc = B.dpool + (pass ? I.o_wcL : I.o_wc);
+        for (int idx = lane; idx < k * P1; idx += 32) {
+            const int a = idx / P1, cc = idx - a * P1;
+            double acc = cc < p ? Wh[(size_t)S[a] * p + cc] : wc[S[a]];
+            for (int b = 0; b < k; b++) acc = xfma(-Wm[(size_t)S[a] * m + S[b]], L[b * P1 + cc], acc);
+            X[idx] = acc;
+            den = fmax(den, fabs(L[idx]));
+        }
+        __syncwarp();
+        chol_solve_inplace<double>(ws.R, k, X, P1, P1);
+        for (int idx = lane; idx < k * P1; idx += 32) num = fmax(num, fabs(X[idx]));
+        __syncwarp();
+    }
+    num = warp_max_d(num);
+    den = warp_max_d(den);
+    return den > 0.0 ? num / den : (num > 0.0 ? pos_inf<double>() : 0.0);
 }
 
 // Cholesky of Wm[S,S] (row-oriented; each entry accumulates in ascending l),
@@ -1902,7 +1991,7 @@ __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const 
     OptResult res;
     res.licq = 1; res.lp2_status = LP_SKIPPED; res.lp2_piv = 0; res.cheb_status = LP_SKIPPED; res.cheb_piv = 0;
     res.optimal = 0; res.region = 0;
-    res.t = __longlong_as_double(0x7ff8000000000000LL); res.r = res.t;
+    res.t = __longlong_as_double(0x7ff8000000000000LL); res.r = res.t; res.err = res.t;
     res.decided = true;
     const T tpiv = (T)tol.tol_piv;
     const T tdj = (T)tol.tol_dj;
@@ -1963,6 +2052,7 @@ __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const 
     }
     if (!res.optimal) return res;
     chebyshev_ball<T>(tol, I, ws, res);
+    if constexpr (sizeof(T) == 8) res.err = law_error(B, I, k, ws);
     return res;
 }
 
@@ -1976,7 +2066,7 @@ __device__ void write_opt(const DevBuffers &B, const Node &nd, int level, const 
         if (oi < B.opt_cap) {
             OptRec o;
             o.lo = nd.lo; o.hi = nd.hi; o.inst = nd.inst; o.level = level; o.t = res.t; o.r = res.r;
-            o.region = res.region; o.fp64 = fp64; o.rec = nd.rec;
+            o.region = res.region; o.fp64 = fp64; o.rec = nd.rec; o.err = res.err;
             B.opt[oi] = o;
         } else {
             atomicOr(&ctl->overflow, OV_OPT);
@@ -3037,7 +3127,7 @@ __global__ void k_finalize(DevBuffers B, int level)
 // for an mpLP set with |S| < n (x(theta) is not unique; nothing written).
 __global__ void __launch_bounds__(128) k_region_laws(DevBuffers B, Tol tol, SlotDims sd, const uint64_t *masks,
                                                      long long n_sets, double *laws, int *sizes, long long stride,
-                                                     double *radius)
+                                                     double *radius, double *err)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
@@ -3054,6 +3144,7 @@ __global__ void __launch_bounds__(128) k_region_laws(DevBuffers B, Tol tol, Slot
         int *sz = sizes + 4 * x;
         int k = 0;
         if (radius && lane == 0) radius[x] = __longlong_as_double(0x7ff8000000000000LL);
+        if (err && lane == 0) err[x] = __longlong_as_double(0x7ff8000000000000LL);
         if (kkt_factor<double>(D, I, lo, hi, tol.tol_licq, ws, &k)) {
             if (lane == 0) { sz[0] = -1; sz[1] = n; sz[2] = p; sz[3] = 0; }
             continue;
@@ -3114,6 +3205,11 @@ __global__ void __launch_bounds__(128) k_region_laws(DevBuffers B, Tol tol, Slot
             if (lane == 0) radius[x] = res.r;
             __syncwarp();
         }
+        if (err) {
+            const double e = law_error(B, I, k, ws);
+            if (lane == 0) err[x] = e;
+            __syncwarp();
+        }
     }
 }
 
@@ -3123,16 +3219,17 @@ cudaError_t launch_region_laws(const DevBuffers &B, const Tol &tol, const SlotDi
                                long long n_sets, double *laws, int *sizes, long long stride, int grid, size_t smem,
                                cudaStream_t s)
 {
-    k_region_laws<<<grid, 128, smem, s>>>(B, tol, sd, masks, n_sets, laws, sizes, stride, nullptr);
+    k_region_laws<<<grid, 128, smem, s>>>(B, tol, sd, masks, n_sets, laws, sizes, stride, nullptr, nullptr);
     return cudaGetLastError();
 }
 
-// the same with each set's Chebyshev radius (radius: n_sets doubles)
+// the same with each set's Chebyshev radius and law error (n_sets doubles
+// each, either may be null)
 cudaError_t launch_region_laws_r(const DevBuffers &B, const Tol &tol, const SlotDims &sd, const uint64_t *masks,
                                  long long n_sets, double *laws, int *sizes, long long stride, double *radius,
-                                 int grid, size_t smem, cudaStream_t s)
+                                 double *err, int grid, size_t smem, cudaStream_t s)
 {
-    k_region_laws<<<grid, 128, smem, s>>>(B, tol, sd, masks, n_sets, laws, sizes, stride, radius);
+    k_region_laws<<<grid, 128, smem, s>>>(B, tol, sd, masks, n_sets, laws, sizes, stride, radius, err);
     return cudaGetLastError();
 }
 

@@ -46,7 +46,7 @@ class Options(ctypes.Structure):
 class OptSet(ctypes.Structure):
     _fields_ = [("mask_lo", ctypes.c_uint64), ("mask_hi", ctypes.c_uint64), ("inst", ctypes.c_int),
                 ("level", ctypes.c_int), ("t", ctypes.c_double), ("r", ctypes.c_double), ("region", ctypes.c_int),
-                ("fp64", ctypes.c_int), ("rec", ctypes.c_longlong)]
+                ("fp64", ctypes.c_int), ("rec", ctypes.c_longlong), ("err", ctypes.c_double)]
 
 
 class InstStats(ctypes.Structure):
@@ -73,7 +73,8 @@ class GPUResults(ctypes.Structure):
                 ('time_GPU', ctypes.c_double), ('active_sets', ctypes.POINTER(ctypes.c_int)),
                 ('status', ctypes.c_int), ('n_regions', ctypes.c_int), ('n_candidates', ctypes.c_longlong),
                 ('n_pruned', ctypes.c_longlong), ('t_star', ctypes.POINTER(ctypes.c_double)),
-                ('radius', ctypes.POINTER(ctypes.c_double)), ('is_region', ctypes.POINTER(ctypes.c_int))]
+                ('radius', ctypes.POINTER(ctypes.c_double)), ('is_region', ctypes.POINTER(ctypes.c_int)),
+                ('law_error', ctypes.POINTER(ctypes.c_double))]
 
 
 # record layout written by the device (identical prefix to the oracle's)
@@ -146,7 +147,7 @@ def load(build_if_missing: bool = False):
                                      P(ctypes.c_int)]
     lib.mpqp_region_laws.restype = ctypes.c_int
     lib.mpqp_critical_regions.argtypes = [P(Problem), ctypes.c_longlong, P(ctypes.c_uint64), P(ctypes.c_double),
-                                          P(ctypes.c_int), P(ctypes.c_double)]
+                                          P(ctypes.c_int), P(ctypes.c_double), P(ctypes.c_double)]
     lib.mpqp_critical_regions.restype = ctypes.c_int
     lib.mpqp_reduce_constraints.argtypes = [P(Problem), P(ctypes.c_int)]
     lib.mpqp_reduce_constraints.restype = ctypes.c_int
@@ -220,7 +221,7 @@ _INST_DTYPE = np.dtype([(f[0], "<i8") for f in InstStats._fields_[:11]] +
                         ("last_level", "<i4"), ("truncated", "<i4"), ("lp1_certified", "<i8"),
                         ("lp1_cert_missed", "<i8"), ("lp1_cert_freevar", "<i8")])
 _OPT_DTYPE = np.dtype([("mask_lo", "<u8"), ("mask_hi", "<u8"), ("inst", "<i4"), ("level", "<i4"), ("t", "<f8"),
-                       ("r", "<f8"), ("region", "<i4"), ("fp64", "<i4"), ("rec", "<i8")])
+                       ("r", "<f8"), ("region", "<i4"), ("fp64", "<i4"), ("rec", "<i8"), ("err", "<f8")])
 assert _INST_DTYPE.itemsize == ctypes.sizeof(InstStats)
 assert _OPT_DTYPE.itemsize == ctypes.sizeof(OptSet)
 
@@ -348,7 +349,8 @@ def region_laws(prob, sets, with_radius: bool = False):
     None for a set that fails the LICQ test and for an mpLP set with fewer
     than n active constraints (its law x(theta) is not unique).  with_radius:
     each dict also holds the set's Chebyshev radius ``r`` (``mpqp_critical_regions``;
-    a critical region when r >= 1e-8, utils.py:86)."""
+    a critical region when r >= 1e-8, utils.py:86) and the stated relative
+    error ``err`` of its laws (one FP64 iterative-refinement step)."""
     lib = load()
     ps = _ProblemSet([prob], 0, 0, 0)
     masks = np.zeros((len(sets), 2), dtype=np.uint64)
@@ -359,10 +361,12 @@ def region_laws(prob, sets, with_radius: bool = False):
     laws = np.zeros((max(len(sets), 1), stride))
     sizes = np.zeros((max(len(sets), 1), 4), dtype=np.intc)
     radius = np.full(max(len(sets), 1), np.nan)
+    err = np.full(max(len(sets), 1), np.nan)
     args = (ps.arr, len(sets), masks.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
             laws.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), sizes.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
     if with_radius:
-        _check(lib.mpqp_critical_regions(*args, radius.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        _check(lib.mpqp_critical_regions(*args, radius.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                         err.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
     else:
         _check(lib.mpqp_region_laws(*args))
     out = []
@@ -381,6 +385,7 @@ def region_laws(prob, sets, with_radius: bool = False):
                  active_set=list(sets[i]))
         if with_radius:
             d["r"] = float(radius[i])
+            d["err"] = float(err[i])
         out.append(d)
     return out
 

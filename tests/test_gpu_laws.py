@@ -67,3 +67,51 @@ def test_region_laws_reject_bad_sets(gpu_lib):
         solver.region_laws(prob, [[0, 1, 2, 3, 4]])        # |S| > n
     with pytest.raises(solver.MpqpError):
         solver.region_laws(prob, [[prob.m]])               # index out of range
+
+
+ERR_CASES = {
+    "m62-k3": (lambda: P.random_n12_m62_p6(), 3),
+    "illcond-k3": (lambda: P.illcond_n16_m62_p8(), 3),
+    "mpc-k3": (lambda: P.mpc_mpqp(0), 3),
+    "mplp-n5": (lambda: P.random_mplp(5, 16, 3, seed=2), 5),
+}
+
+
+@pytest.mark.parametrize("case", list(ERR_CASES))
+def test_every_result_states_its_error(gpu_lib, case):
+    """Each optimal set carries the stated relative error of its laws (one
+    FP64 iterative-refinement step of its KKT solve, mpqp_opt_set.err), in
+    both precisions and identical between them; mpqp_critical_regions states
+    the same error beside the laws.  The stated error is a sound estimate:
+    the laws' actual deviation from an independent numpy restatement of
+    utils.py:25-36 stays within max(1e3 x err, 1e-12), and every region here
+    states an error below the 1e-8 target."""
+    make, kmax = ERR_CASES[case]
+    prob = P.scale_problem(make())
+    kw = dict(k_max=kmax, cand_cap=1 << 20, arena_bytes=1 << 28)
+    r64 = solver.solve([prob], precision=solver.FP64, **kw)
+    r32 = solver.solve([prob], precision=solver.MIXED, **kw)
+    assert r64.status == 0 and r32.status == 0
+    key = lambda r: {(int(o["mask_lo"]), int(o["mask_hi"])): float(o["err"]) for o in r.opt}
+    e64, e32 = key(r64), key(r32)
+    assert e64.keys() == e32.keys() and e64
+    for k in e64:
+        assert e64[k] == e32[k] or (np.isnan(e64[k]) and np.isnan(e32[k])), k
+    # every optimal set states a finite error, except an mpLP set with
+    # |S| < n (no unique law: never a region)
+    errs = np.array(list(e64.values()))
+    short = np.array([len(solver.mask_to_set(*k)) < prob.n for k in e64]) if not prob.Q.any() else 0
+    assert np.all(np.isfinite(errs) | short) and np.all(errs[np.isfinite(errs)] >= 0)
+    errs = errs[np.isfinite(errs)]
+    regions = [o for o in r64.opt if o["region"]]
+    assert regions and max(float(o["err"]) for o in regions) < 1e-8
+    sets = [solver.mask_to_set(o["mask_lo"], o["mask_hi"]) for o in regions[:100]]
+    laws = solver.region_laws(prob, sets, with_radius=True)
+    for o, S, law in zip(regions[:100], sets, laws):
+        assert law is not None and law["err"] == float(o["err"]) and law["r"] == float(o["r"]), S
+        if prob.Q.any():
+            reg, _ = R.region_for(prob, S, zero_tol=1e-12)
+            dev = _rel(law["lagrange_A"], reg["lagrange_A"])
+            assert dev <= max(1e3 * law["err"], 1e-12), (S, dev, law["err"])
+    print(case, "optimal sets", len(errs), "max stated error", float(errs.max()),
+          "median", float(np.median(errs)))
