@@ -267,8 +267,12 @@ int mpqp_critical_regions(const mpqp_problem *prob, long long n_sets, const uint
  * Scratch: a fixed MPQP_NOALLOC_SCRATCH_BYTES (1 MiB) device array holds the
  * instance's FP64 KKT blocks plus 16 bytes per set; larger calls return
  * MPQP_ECAPACITY.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress), so make it before any stream capture.
- * All calls share the array: calls whose work overlaps on the GPU race. */
+ * address (cudaGetSymbolAddress).  Calls may not be captured into a CUDA
+ * graph (the data are staged through one host buffer that every call
+ * rewrites): a call on a stream that is being captured returns MPQP_EINVAL.
+ * All calls share the array: calls whose work overlaps on the GPU race.
+ * Inputs are checked as mpqp_region_laws checks them (same codes), plus
+ * n <= 32. */
 #define MPQP_NOALLOC_SCRATCH_BYTES (1 << 20)
 int mpqp_region_laws_noalloc(const mpqp_problem *prob, long long n_sets, const uint64_t *masks, double *laws,
                              int *sizes, void *stream);
@@ -299,6 +303,7 @@ int mpqp_region_laws_noalloc(const mpqp_problem *prob, long long n_sets, const u
 int mpqp_reduce_constraints(const mpqp_problem *prob, int *row_status);
 
 const char *mpqp_version(void);
+/* The text of the last error of the calling thread. */
 const char *mpqp_last_error(void);
 
 #ifdef __cplusplus

@@ -60,7 +60,8 @@ cudaError_t launch_region_laws_r(const DevBuffers &B, const Tol &tol, const Slot
 
 using namespace mq;
 
-static std::string g_err;
+// the last error text of each calling thread (mpqp_last_error)
+static thread_local std::string g_err;
 static std::mutex g_mu;
 
 static void set_err(const std::string &s) { g_err = s; }

@@ -1368,10 +1368,9 @@ __global__ void __launch_bounds__(128) k_lp1_cert(DevBuffers B, Tol tol, SlotDim
             }
             if (ok) {
                 double y = 0.0, rr = rhs;
-                const double rhsmax = warp_max_d(fabs(rhs));
-                double mmax = 0.0;
-                if (lane < nv) { for (int cc = 0; cc < nv; cc++) mmax = fmax(mmax, fabs(Mdr[cc])); }
-                mmax = warp_max_d(mmax);
+                // max norms for the residual test, in FP32 (thresholds only;
+                // amax is max |M| of the FP32 copy)
+                const float rhsmax = warp_max_f(fabsf((float)rhs));
                 for (int it = 0; it < kCertSolves; it++) {
                     // the correction d of M d = rr in FP32, scaled by a power of two
                     const float rm = warp_max_f(fabsf((float)rr));
@@ -1397,9 +1396,9 @@ __global__ void __launch_bounds__(128) k_lp1_cert(DevBuffers B, Tol tol, SlotDim
                     if (lane < nv) for (int cc = 0; cc < nv; cc++) rr = fma(-Mdr[cc], yv[cc], rr);
                     __syncwarp();
                 }
-                const double ymax = warp_max_d(lane < nv ? fabs(y) : 0.0);
-                const double rres = warp_max_d(lane < nv ? fabs(rr) : 0.0);
-                ok = rres <= kCertResid * (mmax * ymax + rhsmax) && ymax == ymax;
+                const float ymax = warp_max_f(lane < nv ? fabsf((float)y) : 0.0f);
+                const float rres = warp_max_f(lane < nv ? fabsf((float)rr) : 0.0f);
+                ok = rres <= (float)kCertResid * (amax * ymax + rhsmax) && ymax == ymax && ymax <= 1e30f;
                 // dual feasibility after scaling, and beta.y / s
                 double smax = 1.0, byn = 0.0;
                 bool bad = false;

@@ -14,11 +14,18 @@
 // every GPU loading the library keeps until the process exits.  In host code
 // that name is only a stand-in for the symbol, not a device address, so the
 // first call on each device (with that device current) resolves the address
-// with cudaGetSymbolAddress and keeps it; make that first call before any
-// stream capture.  Every call reuses the same array: a call writes all the
-// scratch it later reads (nothing has to start at zero), and two calls whose
-// work overlaps on the GPU -- calls on different streams, or from different
-// threads -- race on it.  Calls on one stream are ordered.
+// with cudaGetSymbolAddress and keeps it.  A call may not be captured into a
+// CUDA graph: it stages its data through one host buffer that the next call
+// rewrites, so a replay would upload whatever that buffer then holds; a call
+// on a stream that is being captured is refused (MPQP_EINVAL).  Every call
+// reuses the same array: a call writes all the scratch it later reads
+// (nothing has to start at zero), and two calls whose work overlaps on the
+// GPU -- calls on different streams, or from different threads -- race on
+// it.  Calls on one stream are ordered.
+//
+// Inputs are checked like the allocating entry point (mpqp_region_laws)
+// checks them, so both accept and reject the same problems, with one limit
+// of this file's own: n <= 32 (the host work arrays of the precompute).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -159,16 +166,17 @@ int precompute(const mpqp_problem &P, InstDesc &d, double *pool, size_t pool_cap
     return MPQP_OK;
 }
 
+// Every failure path: the error text, and the runtime's last-error state
+// cleared so that it does not surface in a later, valid call.
 int fail(int code, const char *msg)
 {
+    cudaGetLastError();
     set_error_text(msg);
     return code;
 }
 
-}  // namespace
-
-extern "C" int mpqp_region_laws_noalloc(const mpqp_problem *prob, long long n_sets, const uint64_t *masks,
-                                        double *laws, int *sizes, void *stream)
+int noalloc_impl(const mpqp_problem *prob, long long n_sets, const uint64_t *masks, double *laws, int *sizes,
+                 void *stream)
 {
     std::lock_guard<std::mutex> lk(g_mu);
     if (!prob || n_sets < 0 || (n_sets && (!masks || !laws || !sizes)))
@@ -176,8 +184,27 @@ extern "C" int mpqp_region_laws_noalloc(const mpqp_problem *prob, long long n_se
     if (!prob->Q || !prob->c || !prob->H || !prob->A || !prob->b || !prob->F || !prob->At || !prob->bt)
         return fail(MPQP_EINVAL, "mpqp_region_laws_noalloc: null problem array");
     const int n = prob->n, m = prob->m, p = prob->p, ncp = prob->ncp;
-    if (n < 1 || n > 32 || m < 1 || m > kMaxM || p < 1 || p > kMaxP || ncp < 1 || m + ncp > kMaxIds)
+    if (n < 1 || n > 32 || m < 1 || m > kMaxM || p < 1 || p > kMaxP || ncp < 1)
         return fail(MPQP_EINVAL, "mpqp_region_laws_noalloc: sizes out of range (1<=n<=32, 1<=m<=128, 1<=p<=30)");
+    // the allocating entry point's limits (8-bit basis ids)
+    if (m + ncp + n + p > kMaxIds || m + ncp + p + 1 > kMaxIds)
+        return fail(MPQP_EINVAL, "mpqp_region_laws_noalloc: instance too large (m+ncp+n+p must be <= 255)");
+    bool qzero = true;
+    for (int i = 0; i < n * n && qzero; i++) if (prob->Q[i] != 0.0) qzero = false;
+    if (qzero && (p + n + 2) + (m + ncp + 2 * n + 1) > kMaxIds)
+        return fail(MPQP_EINVAL, "mpqp_region_laws_noalloc: mpLP instance too large (m + ncp + 3n + p must be <= 252)");
+    for (int i = 0; i < m; i++)
+        if (!(prob->b[i] >= 0.0)) return fail(MPQP_EORIGIN, "mpqp_region_laws_noalloc: b has a negative entry");
+    for (int i = 0; i < ncp; i++)
+        if (!(prob->bt[i] >= 0.0)) return fail(MPQP_EORIGIN, "mpqp_region_laws_noalloc: CRb has a negative entry");
+    // a call inside a stream capture would record an upload from the host
+    // staging buffer, which later calls rewrite
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing((cudaStream_t)stream, &cap) != cudaSuccess)
+        return fail(MPQP_ECUDA, "mpqp_region_laws_noalloc: cudaStreamIsCapturing failed");
+    if (cap != cudaStreamCaptureStatusNone)
+        return fail(MPQP_EINVAL, "mpqp_region_laws_noalloc: the stream is being captured; calls may not be "
+                                 "captured into a CUDA graph");
     if (n_sets == 0) return MPQP_OK;
     const int kcap = m < n ? m : n;
     for (long long i = 0; i < n_sets; i++) {
@@ -223,12 +250,17 @@ extern "C" int mpqp_region_laws_noalloc(const mpqp_problem *prob, long long n_se
     sd.maxN = d.lp ? n : 0;
     const size_t smem = 4 * laws_smem_per_warp(sd);
     const void *fn = kernel_ptr("laws");
-    int sms = 0, nb = 0;
+    int sms = 0, nb = 0, smem_max = 0;
+    if (cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+        return fail(MPQP_ECUDA, "mpqp_region_laws_noalloc: device attribute query");
+    if (smem > (size_t)smem_max)
+        return fail(MPQP_EINVAL, "mpqp_region_laws_noalloc: kernel does not fit on an SM (shared memory)");
     if (smem > 48 * 1024 && cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return fail(MPQP_ECUDA, "mpqp_region_laws_noalloc: shared-memory attribute");
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, smem) != cudaSuccess || nb < 1)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, smem) != cudaSuccess)
         return fail(MPQP_ECUDA, "mpqp_region_laws_noalloc: occupancy query");
+    if (nb < 1) return fail(MPQP_EINVAL, "mpqp_region_laws_noalloc: kernel does not fit on an SM (shared memory)");
     cudaStream_t s = (cudaStream_t)stream;
     // pageable source: the call returns once the host image has been taken,
     // so the next call may rewrite it
@@ -250,4 +282,21 @@ extern "C" int mpqp_region_laws_noalloc(const mpqp_problem *prob, long long n_se
                            nb * sms, smem, s);
     if (e != cudaSuccess) return fail(MPQP_ECUDA, "mpqp_region_laws_noalloc: kernel launch");
     return MPQP_OK;
+}
+
+}  // namespace
+
+// No C++ exception crosses the C ABI (std::lock_guard can throw).
+extern "C" int mpqp_region_laws_noalloc(const mpqp_problem *prob, long long n_sets, const uint64_t *masks,
+                                        double *laws, int *sizes, void *stream)
+{
+    try {
+        return noalloc_impl(prob, n_sets, masks, laws, sizes, stream);
+    } catch (...) {
+        try {
+            set_error_text("mpqp_region_laws_noalloc: host error");
+        } catch (...) {
+        }
+        return MPQP_ENOMEM;
+    }
 }
