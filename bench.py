@@ -27,6 +27,8 @@ import sys
 import tempfile
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -34,7 +36,15 @@ METRIC = "candidate active sets checked/s at m=62 (mixed FP32/FP64 vs FP64), sam
 UNIT = "candidates/s"
 EXTRA_BUDGET = 1 << 19
 MAIN_KMAX = 6
-CPU_SAMPLE_KMAX = 4
+# CPU sample of the same workload: the main instance's active sets drawn only
+# from its last 40 constraints (a family closed under subsets, so all six
+# levels with the full enumeration's subset tests, warm starts and LPs), plus
+# 3 of the 32 extra instances at their full budget
+CPU_TAIL_FIRST = 22
+CPU_EXTRAS = 3
+# single-core figure: the last 28 constraints only
+CPU_TAIL_FIRST_1CORE = 34
+DETAIL_FILE = "bench_detail.json"
 
 
 def workload():
@@ -120,34 +130,37 @@ def measured_peaks() -> dict:
         return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def lp1_hbm_bytes(probs, kmax, res, elem: int) -> float:
-    """Algorithmic HBM bytes of all LP1 (k_feasibility) launches of one step.
+def lp1_unique_bytes(res) -> float:
+    """Algorithmic bytes of all LP1 (k_feasibility) launches of one step,
+    each item counted once (device counters of the run):
 
-    Per checked candidate (levels >= 1): candidate record 8 B, parent node
-    48 B, parent LP1 tableau (M1+1)*ld1*s and basis ids M1+nv (read).  Per
-    feasible child: node 48 B and hash slot 32 B (write); per child kept as a
-    parent of the next level: its tableau and ids (write).  The model keeps
-    the tableau read for the last-level candidates decided at a certified
-    vertex without one (about 14 % of a last level) and the hash slot of
-    last-level sets (never inserted), so it overstates the bytes by up to
-    about a tenth.
-    """
+    * every distinct parent whose children were checked: its live tableau
+      rows and objective row, basis ids and 48 B node (read once; its other
+      children find it in L2);
+    * per checked candidate (levels >= 1): the 8 B candidate record (read) and
+      its 48 B node slot (written);
+    * per stored child: its live tableau rows, ids (write) and its 32 B hash
+      slot; per certificate-queue entry 32 B, per FP64 re-solve entry 4 B.
+
+    Last-level children decided at a certified vertex do not load their
+    parent, so when all children of a parent are decided that way the model
+    charges a tableau that is not read."""
     total = 0.0
-    for i, pr in enumerate(probs):
-        M1, nv = pr.m + pr.CRA.shape[0], pr.n + pr.p
-        if elem == 4:   # FP32 rows: smallest stride >= nv+1 that is 4 (mod 8)
-            ld1 = (nv + 1 + 3) & ~3
-            ld1 = ld1 if ld1 & 4 else ld1 + 4
-        else:           # FP64 rows: odd stride
-            ld1 = (nv + 1) | 1
-        tab = (((M1 + 1) * ld1 + 3) & ~3) * elem
-        ids = (M1 + nv + 15) & ~15
-        st = res.inst[i]
-        cand = int(st["candidates"]) - 1          # level 0 (empty set) has no parent
-        feas = int(st["feasible"]) - 1
-        stored = int(st["stored"])
-        total += cand * (8 + 48 + tab + ids) + feas * (48 + 32) + stored * (tab + ids)
-    return total
+    for st in res.inst:
+        cand = int(st["candidates"]) - 1          # level 0 (the empty set) is set up by k_level0
+        total += int(st["lp1_parent_bytes"]) + int(st["lp1_store_bytes"]) + cand * (8 + 48)
+        total += int(st["stored"]) * 32 + (int(st["lp1_certified"]) + int(st["lp1_cert_missed"])) * 32
+        total += int(st["fallback_lp1"]) * 4
+    return float(total)
+
+
+def profile_figure(name: str, key: str):
+    """A per-unit figure recorded from an ncu capture under profiles/."""
+    try:
+        with open(os.path.join(ROOT, "profiles", name)) as f:
+            return float(json.load(f)[key])
+    except Exception:
+        return None
 
 
 def opt_algorithmic_bytes(probs, res, elem: int) -> float:
@@ -233,26 +246,45 @@ def whole_job_rate(units_per_rank: float, ms_per_step: float, world: int) -> flo
     return units_per_rank * world / (ms_per_step / 1e3)
 
 
-def cpu_baseline(steps: int = 1, warmup: int = 0) -> dict:
-    """The C oracle (restatement of the reference's algorithm) on the host:
-    the main m=62 instance, all candidates with |S| <= 4, every host thread."""
-    from mpqpcudasolver_gb300 import problems as P
+def _cpu_sample(threads: int, j_first: int, n_extra: int) -> tuple[int, float]:
+    """One pass of the CPU sample: the main instance's sets within constraints
+    [j_first, 62) at every level |S| <= 6, and the first n_extra extra
+    instances to |S| = n under their budget.  Returns (candidates, seconds)."""
     from oracle import oracle as O
-    prob = P.scale_problem(P.random_n12_m62_p6())
+    probs, kmax, budget = workload()
+    t0 = time.perf_counter()
+    n = O.enumerate_tail(probs[0], j_first, k_max=kmax[0], nthreads=threads).n_cand
+    for i in range(1, 1 + n_extra):
+        n += O.enumerate_sets(probs[i], k_max=kmax[i], budget=budget[i], nthreads=threads, keep_records=False).n_cand
+    return n, time.perf_counter() - t0
+
+
+def cpu_baseline(steps: int = 1, warmup: int = 0, single_core: bool = True) -> dict:
+    """The C oracle (restatement of the reference's algorithm) on the host, on
+    a bounded sample with the GPU workload's mix: the m = 62 instance at all
+    six levels (its active sets within the last 40 constraints, a family
+    closed under subsets: every candidate is checked exactly as in the full
+    enumeration) plus 3 of the 32 extra instances at their full budget, every
+    host thread; beside it one host core on a smaller tail (last 28)."""
     threads = os.cpu_count() or 1
     for _ in range(warmup):
-        O.enumerate_sets(prob, k_max=CPU_SAMPLE_KMAX, nthreads=threads, keep_records=False)
-    vals = []
-    n = 0
+        _cpu_sample(threads, CPU_TAIL_FIRST, CPU_EXTRAS)
+    vals, n, secs = [], 0, 0.0
     for _ in range(max(1, steps)):
-        t0 = time.perf_counter()
-        e = O.enumerate_sets(prob, k_max=CPU_SAMPLE_KMAX, nthreads=threads, keep_records=False)
-        dt = time.perf_counter() - t0
-        vals.append(e.n_cand / dt)
-        n = e.n_cand
-    return {"value": statistics.median(vals), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"C oracle, main instance n=12 m=62 p=6, all {n} candidate sets with |S|<={CPU_SAMPLE_KMAX}",
-            "seconds_per_step": n / statistics.median(vals)}
+        n, dt = _cpu_sample(threads, CPU_TAIL_FIRST, CPU_EXTRAS)
+        vals.append(n / dt)
+        secs = dt
+    out = {"value": statistics.median(vals), "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"C oracle: main instance n=12 m=62 p=6, every active set |S|<=6 within constraints "
+                     f"{CPU_TAIL_FIRST}..61, plus extra instances 1..{CPU_EXTRAS} of 32 to |S|=n at budget "
+                     f"{EXTRA_BUDGET} ({n} candidates per step)",
+           "seconds_per_step": secs, "candidates_per_step": n}
+    if single_core:
+        n1, dt1 = _cpu_sample(1, CPU_TAIL_FIRST_1CORE, 0)
+        out["single_core"] = {"value": n1 / dt1, "unit": UNIT, "cores": 1,
+                              "sample": f"main instance, every active set |S|<=6 within constraints "
+                                        f"{CPU_TAIL_FIRST_1CORE}..61 ({n1} candidates)"}
+    return out
 
 
 def mplp_measure(prec, stream, dev, steps: int = 3) -> dict:
@@ -303,12 +335,13 @@ def run_reference(args):
     world, rank, local, dist = dist_setup(args.gpus)
     if rank != 0:
         return 0
-    cb = cpu_baseline(steps=args.steps, warmup=args.warmup)
+    # host work: one untimed pass is warm-up enough (no device, no caches to fill)
+    cb = cpu_baseline(steps=args.steps, warmup=min(args.warmup, 1))
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["seconds_per_step"] * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": config_dict("fp64 (CPU)"),
-            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "single_core")},
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -391,84 +424,99 @@ def run_ours(args):
 
     if rank != 0:
         return 0
-    # rooflines: the dominant (optimality) kernel, and the LP1 kernel beside it
     elem = 4 if prec == solver.MIXED else 8
     tname = "float" if prec == solver.MIXED else "double"
     dominant = max(kt.items(), key=lambda kv: kv[1][0])[0] if kt else None
     peaks = measured_peaks()
     peak_src = peaks["source"] + " (MEASURED_PEAKS.json hbm_gbs)"
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    clocks = clk.summary()
+    mhz = clocks.get("sm_mhz") or 2070.0
 
-    def roofline(kname, step_bytes, units, traffic_file, per_unit_text, timed=None):
-        ms, nl = timed if timed else kt.get(kname, (0.0, 0))
-        nl = max(nl, 1)
-        achieved = step_bytes / (ms / 1e3) / 1e9 if ms > 0 else None
-        return {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
-                "traffic": traffic_per_launch(traffic_file, units / nl),
-                "algorithmic_bytes_per_launch": step_bytes / nl, "units_per_launch": units / nl,
-                "avg_launch_ms": ms / nl, "launches_per_step": nl, "peak_source": peak_src,
-                "per_unit": per_unit_text}
-
-    n_eval = res.total("feasible")
-    # the optimality screen: both stages of the dual route (and the primal
-    # route) as one logical kernel
+    # LP1, the dominant kernel: HBM roofline on the unique bytes it must move,
+    # and the issue roofline beside it (it is issue-bound, not HBM-bound)
+    lp1 = f"k_feasibility<{tname}>"
+    ms_lp1, nl_lp1 = kt.get(lp1, (0.0, 1))
+    nl_lp1 = max(nl_lp1, 1)
+    lp1_cand = res.candidates - len(probs)
+    ubytes = lp1_unique_bytes(res)
+    achieved = ubytes / (ms_lp1 / 1e3) / 1e9 if ms_lp1 > 0 else None
+    tr_pc = profile_figure("lp1_traffic.json", "dram_bytes_per_unit")
+    ipc = profile_figure("lp1_issue.json", "warp_inst_per_unit")
+    issue_ms = ipc * lp1_cand / (sms * 4 * mhz * 1e6) * 1e3 if ipc else None
+    roof = {"bound": "hbm", "kernel": lp1, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
+            "traffic": tr_pc * lp1_cand / nl_lp1 if tr_pc else None,
+            "algorithmic_bytes_per_launch": ubytes / nl_lp1, "units_per_launch": lp1_cand / nl_lp1,
+            "avg_launch_ms": ms_lp1 / nl_lp1, "launches_per_step": nl_lp1, "peak_source": peak_src,
+            "per_unit": "each distinct parent once (live tableau rows + ids + node), 56 B per candidate, each "
+                        "stored child's live rows + ids + 32 B hash slot (device counters of the run)",
+            "issue": {"warp_inst_per_candidate": ipc, "ideal_ms_per_step": issue_ms,
+                      "frac": (issue_ms / ms_lp1) if (issue_ms and ms_lp1 > 0) else None,
+                      "model": "warp instructions per candidate (ncu) x candidates / (SMs x 4 schedulers x "
+                               "median SM clock): the time at one instruction per scheduler per cycle"}}
+    # the optimality screen (second kernel): time and measured DRAM traffic
     screen = [k for k in kt if k.startswith("k_opt_screen")]
-    if screen:
-        opt_name = "+".join(screen)
-        opt_timed = (sum(kt[k][0] for k in screen), max(kt[k][1] for k in screen))
-    else:
-        opt_name, opt_timed = f"k_optimality<{tname}>", None
-    roof = roofline(opt_name, opt_algorithmic_bytes(probs, res, elem), n_eval,
-                    "opt_traffic.json",
-                    "per evaluated (feasible) set: 8*m*(n+p+1) KKT gather + 8*R*(p+2) region tableau + 16 B "
-                    "mask/verdict, plus 2*(R+1)*(p+2)*s per LP2/Chebyshev pivot (s = 4 B FP32)", opt_timed)
+    n_eval = res.total("feasible")
     screen_info = None
     if screen:
-        # The screen is issue-bound and its first stage builds only the
-        # multiplier rows and the box for most sets, so the byte model above
-        # does not describe it: report its time and measured DRAM traffic.
-        ms_s, nl_s = opt_timed
-        tr = traffic_per_launch("opt_traffic.json", n_eval / max(nl_s, 1))
-        screen_info = {"kernel": opt_name, "bound": "issue (not memory)", "ms_per_step": ms_s, "launches_per_step": nl_s,
-                "sets_per_step": n_eval, "dram_traffic_per_launch": tr,
-                "dram_gbs": (tr * nl_s / (ms_s / 1e3) / 1e9) if (tr and ms_s > 0) else None,
-                "dram_frac": (tr * nl_s / (ms_s / 1e3) / 1e9 / peaks["hbm_gbs"]) if (tr and ms_s > 0) else None,
-                "peak": peaks["hbm_gbs"], "unit": "GB/s", "peak_source": peak_src,
-                "note": "first stage one set per 8-thread tile; ncu: 82 % issue active, ~50 B of DRAM per set"}
-    roof_lp1 = roofline(f"k_feasibility<{tname}>", lp1_hbm_bytes(probs, kmax, res, elem),
-                        res.candidates - len(probs), "lp1_traffic.json",
-                        "per candidate (levels >= 1): 8 B record + 48 B parent node + parent LP1 tableau "
-                        "(M1+1)*ld1*s + basis ids; per feasible child 80 B; per stored child its tableau and ids")
+        ms_s = sum(kt[k][0] for k in screen)
+        sp = profile_figure("opt_traffic.json", "dram_bytes_per_unit")
+        si = profile_figure("opt_issue.json", "warp_inst_per_unit")
+        s_issue = si * n_eval / (sms * 4 * mhz * 1e6) * 1e3 if si else None
+        screen_info = {"kernels": "+".join(screen), "ms_per_step": ms_s, "sets_per_step": n_eval,
+                       "dram_gbs": sp * n_eval / (ms_s / 1e3) / 1e9 if sp else None,
+                       "issue_frac": (s_issue / ms_s) if s_issue else None}
+    cert_ms = kt.get("k_lp1_cert", (0.0, 0))[0]
+    opt = res.opt
+    errs = opt["err"][np.isfinite(opt["err"])] if len(opt) else np.zeros(0)
+    reg = opt[opt["region"] == 1] if len(opt) else opt
     cb = cpu_baseline(steps=1)
     mplp = None if args.skip_mplp else mplp_measure(prec, stream, dev)
-    clocks = clk.summary()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64cert" if prec == solver.MIXED else "f64",
         "data": "synthetic (seeded generators)", "config": config_dict(args.precision),
         "candidates_per_step": cand,
-        "pivots_per_s": (res.total("lp1_pivots") + res.total("lp2_pivots") + res.total("cheb_pivots"))
-        * world / (ms_step / 1e3),
-        "regions_per_step": res.total("regions"), "feasible_per_step": res.total("feasible"),
-        "fp64_fallbacks": {"lp1": res.total("fallback_lp1"), "optimality": res.total("fallback_opt")},
-        "fp64_path": fp64,
         "speedup_vs_fp64": (value / world / fp64["value"]) if fp64 else None,
-        # the dominant kernel's roofline; the screen's time and traffic beside it
-        "roofline": roof_lp1 if (dominant or "").startswith("k_feasibility") else roof,
-        "roofline_lp1": roof_lp1,
+        "fp64_path": fp64,
+        "roofline": roof,
+        "lp1_certificate": {"infeasible_certified": res.total("lp1_certified"),
+                            "fp64_resolved": res.total("fallback_lp1"),
+                            "cert_missed": res.total("lp1_cert_missed"), "ms_per_step": cert_ms},
+        "law_error": {"max": float(errs.max()) if errs.size else None,
+                      "max_regions": float(np.nanmax(reg["err"])) if len(reg) else None,
+                      "results": int(len(opt)),
+                      "what": "per optimal set: one FP64 refinement step of its KKT solve, relative to the law"},
         "screen": screen_info,
-        "model_bytes_touched_per_s": model_bytes_touched(probs, res, elem) / (ms_step / 1e3),
-        "kernels_ms_per_step": {k: round(v[0], 3) for k, v in sorted(kt.items(), key=lambda kv: -kv[1][0])},
-        "dominant_kernel": dominant,
-        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
-        "mplp": mplp,
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "single_core")},
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "mpqp_solve_batch (C ABI): host arrays in, plan + upload + run + download + free"},
         "clocks": clocks,
         "gpu_launches": launches * args.steps,
+        "detail": DETAIL_FILE,
     }
-    print(json.dumps(line), flush=True)
+    detail = {
+        "pivots_per_s": (res.total("lp1_pivots") + res.total("lp2_pivots") + res.total("cheb_pivots"))
+        * world / (ms_step / 1e3),
+        "regions_per_step": res.total("regions"), "feasible_per_step": res.total("feasible"),
+        "fp64_fallbacks": {"lp1": res.total("fallback_lp1"), "optimality": res.total("fallback_opt")},
+        "kernels_ms_per_step": {k: round(v[0], 3) for k, v in sorted(kt.items(), key=lambda kv: -kv[1][0])},
+        "kernel_launches_per_step": {k: v[1] for k, v in kt.items()},
+        "dominant_kernel": dominant,
+        "screen_model_bytes_per_s": opt_algorithmic_bytes(probs, res, elem) / (ms_step / 1e3),
+        "model_bytes_touched_per_s": model_bytes_touched(probs, res, elem) / (ms_step / 1e3),
+        "lp1_parents": res.total("lp1_parents"), "lp1_parent_bytes": res.total("lp1_parent_bytes"),
+        "lp1_store_bytes": res.total("lp1_store_bytes"),
+        "mplp": mplp,
+    }
+    try:
+        with open(DETAIL_FILE, "w") as f:
+            json.dump(detail, f, indent=1, default=float)
+    except OSError:
+        pass
+    print(json.dumps(line, default=float), flush=True)
     return 0
 
 

@@ -185,6 +185,11 @@ typedef struct {
      * in FP64; fallback_lp1 counts every re-solve), and of those the ones
      * with a free variable nonbasic in the final basis */
     long long lp1_certified, lp1_cert_missed, lp1_cert_freevar;
+    /* LP1 traffic model (bytes a launch must move, each item once): the
+     * distinct parents whose children were checked (count, and the bytes of
+     * their live tableau rows, basis ids and node records) and the stored
+     * child tableaus with their ids */
+    long long lp1_parents, lp1_parent_bytes, lp1_store_bytes;
 } mpqp_inst_stats;
 
 typedef struct {

@@ -1059,6 +1059,7 @@ static int plan_results_impl(mpqp_plan *P, mpqp_batch_result *&R, bool *complete
         s.lp2_pivots = ic[i].lp2_piv; s.cheb_pivots = ic[i].cheb_piv; s.fallback_lp1 = ic[i].fb_lp1;
         s.fallback_opt = ic[i].fb_opt; s.stored = ic[i].stored;
         s.lp1_certified = ic[i].cert_lp1; s.lp1_cert_missed = ic[i].cert_miss; s.lp1_cert_freevar = ic[i].cert_free;
+        s.lp1_parents = ic[i].parents; s.lp1_parent_bytes = ic[i].par_bytes; s.lp1_store_bytes = ic[i].store_bytes;
         s.feasible_digest = ic[i].feas_digest; s.optimal_digest = ic[i].opt_digest;
         s.region_digest = ic[i].reg_digest;
         s.last_level = ic[i].last_level; s.truncated = ic[i].truncated;

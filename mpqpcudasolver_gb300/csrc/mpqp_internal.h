@@ -138,6 +138,11 @@ struct InstCtl {
     long long cert_miss;        // ... that the certificate could not prove (sent to the FP64 re-solve)
     long long cert_free;        // ... of those, the misses with a free variable nonbasic (no square system)
     long long stored;           // LP1 tableaus written for the next level
+    // LP1 bytes for the roofline: the distinct parents of each checked level
+    // (live tableau rows, basis ids and node, each parent once) and the
+    // stored children (their live rows and ids); lvl_*: the current level,
+    // added when the level is checked (within the budget)
+    long long lvl_parents, parents, lvl_par_bytes, par_bytes, store_bytes;
     // order-independent digests (sum mod 2^64 of a 64-bit hash of each mask)
     unsigned long long feas_digest, opt_digest, reg_digest;
     int stopped;                // budget exhausted or max level reached

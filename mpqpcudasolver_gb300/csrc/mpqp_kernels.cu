@@ -631,7 +631,8 @@ __global__ void k_enumerate(DevBuffers B, int level)
     // inserted, which sets it; the full table otherwise, which is always in bounds)
     const long long hcap = ctl->hcap[pside] >= 16 && ctl->hcap[pside] <= B.hash_cap ? ctl->hcap[pside] : B.hash_cap;
     int cur_inst = -1;
-    long long loc_cand = 0, loc_pruned = 0;
+    long long loc_cand = 0, loc_pruned = 0, loc_par = 0, loc_par_bytes = 0;
+    const int es = B.precision == PREC_MIXED ? 4 : 8;
     for (;;) {
         // parents are claimed 32 at a time (one atomic per chunk: levels
         // past an instance's last level hold many parents that are skipped)
@@ -658,10 +659,13 @@ __global__ void k_enumerate(DevBuffers B, int level)
             if (cur_inst >= 0 && lane == 0) {
                 atomicAdd((unsigned long long *)&B.ictl[cur_inst].lvl_cand, (unsigned long long)loc_cand);
                 atomicAdd((unsigned long long *)&B.ictl[cur_inst].pruned, (unsigned long long)loc_pruned);
+                atomicAdd((unsigned long long *)&B.ictl[cur_inst].lvl_parents, (unsigned long long)loc_par);
+                atomicAdd((unsigned long long *)&B.ictl[cur_inst].lvl_par_bytes, (unsigned long long)loc_par_bytes);
             }
             cur_inst = par.inst;
-            loc_cand = loc_pruned = 0;
+            loc_cand = loc_pruned = loc_par = loc_par_bytes = 0;
         }
+        bool emitted = false;   // this parent has a candidate at this level
         const int jmin = mask_max(par.lo, par.hi) + 1;
         for (int j0 = jmin; j0 < I.m; j0 += 32) {
             const int j = j0 + lane;
@@ -726,6 +730,7 @@ __global__ void k_enumerate(DevBuffers B, int level)
             }
             base = __shfl_sync(FULLMASK, base, 0);
             over = __shfl_sync(FULLMASK, over, 0);
+            emitted |= cnt > 0 && !over;
             if (ok && !over) {
                 const long long idx = base + __popc(okm & ((1u << lane) - 1u));
                 if (idx < B.cand_cap) {
@@ -736,11 +741,20 @@ __global__ void k_enumerate(DevBuffers B, int level)
                 }
             }
         }
+        if (emitted) {
+            // the bytes its children's LP1 stage: live rows + objective row,
+            // basis ids, the node
+            const int rows = es == 4 ? node_rows(par.flags, I.M1) : I.M1;
+            loc_par++;
+            loc_par_bytes += (long long)(rows + 1) * I.ld1 * es + I.ids_bytes + (long long)sizeof(Node);
+        }
     }
     }
     if (cur_inst >= 0 && lane == 0) {
         atomicAdd((unsigned long long *)&B.ictl[cur_inst].lvl_cand, (unsigned long long)loc_cand);
         atomicAdd((unsigned long long *)&B.ictl[cur_inst].pruned, (unsigned long long)loc_pruned);
+        atomicAdd((unsigned long long *)&B.ictl[cur_inst].lvl_parents, (unsigned long long)loc_par);
+        atomicAdd((unsigned long long *)&B.ictl[cur_inst].lvl_par_bytes, (unsigned long long)loc_par_bytes);
     }
 }
 
@@ -819,7 +833,14 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
     ioff = __shfl_sync(FULLMASK, ioff, 0);
     if (idx < 0) return -1;
     if (need_tab) {
-        if (lane == 0) atomicAdd((unsigned long long *)&B.ictl[inst].stored, 1ull);
+        if (lane == 0) {
+            // the bytes the store moves: the live rows and objective row (bulk,
+            // rows_store >= 0) or the whole tableau, and the basis ids
+            const long long tb = rows_store >= 0 ? (long long)(rows_store + 1) * I.ld1 : (long long)I.tab_elems;
+            atomicAdd((unsigned long long *)&B.ictl[inst].stored, 1ull);
+            atomicAdd((unsigned long long *)&B.ictl[inst].store_bytes,
+                      (unsigned long long)(tb * (long long)sizeof(TT) + I.ids_bytes));
+        }
         TT *dst = (TT *)B.tab[side] + toff;
         if (bulk) {
             fence_proxy_async_smem();
@@ -3090,11 +3111,15 @@ __global__ void k_finalize(DevBuffers B, int level)
                 ic->truncated = 1;
             } else {
                 ic->cum_cand += ic->lvl_cand;
+                ic->parents += ic->lvl_parents;
+                ic->par_bytes += ic->lvl_par_bytes;
                 if (ic->lvl_cand > 0) ic->last_level = level;
                 if (level >= I.k_max || ic->lvl_cand == 0) ic->stopped = 1;
             }
         }
         ic->lvl_cand = 0;
+        ic->lvl_parents = 0;
+        ic->lvl_par_bytes = 0;
     }
     __syncthreads();
     if (t == 0) {

@@ -55,7 +55,8 @@ class InstStats(ctypes.Structure):
                                                     "fallback_opt", "stored")] + \
         [(nm, ctypes.c_ulonglong) for nm in ("feasible_digest", "optimal_digest", "region_digest")] + \
         [("last_level", ctypes.c_int), ("truncated", ctypes.c_int)] + \
-        [(nm, ctypes.c_longlong) for nm in ("lp1_certified", "lp1_cert_missed", "lp1_cert_freevar")]
+        [(nm, ctypes.c_longlong) for nm in ("lp1_certified", "lp1_cert_missed", "lp1_cert_freevar", "lp1_parents",
+                                            "lp1_parent_bytes", "lp1_store_bytes")]
 
 
 class BatchResult(ctypes.Structure):
@@ -219,7 +220,8 @@ class Result:
 _INST_DTYPE = np.dtype([(f[0], "<i8") for f in InstStats._fields_[:11]] +
                        [("feasible_digest", "<u8"), ("optimal_digest", "<u8"), ("region_digest", "<u8"),
                         ("last_level", "<i4"), ("truncated", "<i4"), ("lp1_certified", "<i8"),
-                        ("lp1_cert_missed", "<i8"), ("lp1_cert_freevar", "<i8")])
+                        ("lp1_cert_missed", "<i8"), ("lp1_cert_freevar", "<i8"), ("lp1_parents", "<i8"),
+                        ("lp1_parent_bytes", "<i8"), ("lp1_store_bytes", "<i8")])
 _OPT_DTYPE = np.dtype([("mask_lo", "<u8"), ("mask_hi", "<u8"), ("inst", "<i4"), ("level", "<i4"), ("t", "<f8"),
                        ("r", "<f8"), ("region", "<i4"), ("fp64", "<i4"), ("rec", "<i8"), ("err", "<f8")])
 assert _INST_DTYPE.itemsize == ctypes.sizeof(InstStats)

@@ -834,8 +834,10 @@ static int pl_reserve(parent_list *l, int64_t cap, size_t tsz, int M1, int nv)
     return 0;
 }
 
-int orc_enumerate(const orc_problem *pr, const orc_tol *tol, int k_min, int k_max,
-                  int64_t budget, int exhaustive, int nthreads, int keep_records, orc_result *out)
+/* j_first > 0: only the sets whose elements are all >= j_first (a family
+ * closed under subsets, so the subset test is the full enumeration's) */
+static int enumerate_impl(const orc_problem *pr, const orc_tol *tol, int k_min, int k_max, int64_t budget,
+                          int exhaustive, int nthreads, int keep_records, int j_first, orc_result *out)
 {
     memset(out, 0, sizeof(*out));
     orc_data d;
@@ -888,7 +890,7 @@ int orc_enumerate(const orc_problem *pr, const orc_tol *tol, int k_min, int k_ma
         if (!cpar || !cj) { rc = ORC_ENOMEM; goto done; }
         for (int64_t pi = 0; pi < F.n; pi++) {
             const int kp = mask_to_set(F.lo[pi], F.hi[pi], S);
-            const int jmin = kp ? S[kp - 1] + 1 : 0;
+            const int jmin = kp ? S[kp - 1] + 1 : (j_first > 0 ? j_first : 0);
             for (int j = jmin; j < d.m; j++) {
                 int ok = 1;
                 for (int a = 0; a < kp && ok && !exhaustive; a++) {
@@ -999,6 +1001,18 @@ done:
     }
     out->cand = recs;
     return 0;
+}
+
+int orc_enumerate(const orc_problem *pr, const orc_tol *tol, int k_min, int k_max,
+                  int64_t budget, int exhaustive, int nthreads, int keep_records, orc_result *out)
+{
+    return enumerate_impl(pr, tol, k_min, k_max, budget, exhaustive, nthreads, keep_records, 0, out);
+}
+
+int orc_enumerate_tail(const orc_problem *pr, const orc_tol *tol, int k_min, int k_max, int64_t budget,
+                       int nthreads, int j_first, orc_result *out)
+{
+    return enumerate_impl(pr, tol, k_min, k_max, budget, 0, nthreads, 0, j_first, out);
 }
 
 void orc_free_result(orc_result *res)

@@ -104,6 +104,14 @@ int orc_enumerate(const orc_problem *pr, const orc_tol *tol, int k_min, int k_ma
                   int64_t budget, int exhaustive, int nthreads, int keep_records, orc_result *out);
 void orc_free_result(orc_result *res);
 
+/* The same enumeration restricted to the active sets whose elements are all
+ * >= j_first (no records).  Those sets are closed under taking subsets, so
+ * every candidate, its subset test, warm-start chain and LPs are exactly the
+ * full enumeration's: a sample of the full workload with all its levels,
+ * used to time the CPU baseline on a bounded share of a large instance. */
+int orc_enumerate_tail(const orc_problem *pr, const orc_tol *tol, int k_min, int k_max, int64_t budget,
+                       int nthreads, int j_first, orc_result *out);
+
 /* Check one sorted active set S (|S| = k) by replaying the warm-start chain
  * {} -> {s0} -> {s0,s1} -> ... exactly as the enumeration does.  Fills *rec.
  * When laws is non-NULL and S is a region it receives, row-major,

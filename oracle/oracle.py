@@ -87,6 +87,10 @@ def lib():
                                        ctypes.POINTER(OrcResult)]
         _lib.orc_enumerate.restype = ctypes.c_int
         _lib.orc_free_result.argtypes = [ctypes.POINTER(OrcResult)]
+        _lib.orc_enumerate_tail.argtypes = [ctypes.POINTER(OrcProblem), ctypes.POINTER(OrcTol), ctypes.c_int,
+                                            ctypes.c_int, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
+                                            ctypes.POINTER(OrcResult)]
+        _lib.orc_enumerate_tail.restype = ctypes.c_int
         _lib.orc_check_set.argtypes = [ctypes.POINTER(OrcProblem), ctypes.POINTER(OrcTol),
                                        ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.POINTER(OrcCand),
                                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
@@ -159,6 +163,26 @@ def enumerate_sets(prob, k_min: int = 0, k_max: int | None = None, nthreads: int
         cand = np.frombuffer(buf, dtype=CAND_DTYPE).copy()
     out = Enumeration(res.n_cand, res.n_pruned, res.n_feasible, res.n_optimal, res.n_region,
                       res.n_lp1_pivots, res.n_lp2_pivots, res.n_cheb_pivots, res.n_levels, res.truncated, cand)
+    lib().orc_free_result(ctypes.byref(res))
+    return out
+
+
+def enumerate_tail(prob, j_first: int, k_max: int | None = None, nthreads: int = 1, budget: int = 0,
+                   tol: OrcTol | None = None) -> Enumeration:
+    """Counts of the enumeration restricted to the sets whose elements are
+    all >= j_first (closed under subsets: the same candidates, subset tests,
+    warm starts and LPs as the full enumeration, for a bounded sample)."""
+    pp = _Prob(prob)
+    if k_max is None:
+        k_max = prob.n
+    tol = tol or default_tol()
+    res = OrcResult()
+    rc = lib().orc_enumerate_tail(ctypes.byref(pp.s), ctypes.byref(tol), 0, min(k_max, prob.m), int(budget),
+                                  nthreads, int(j_first), ctypes.byref(res))
+    if rc != 0:
+        raise RuntimeError(f"oracle enumeration failed: {rc}")
+    out = Enumeration(res.n_cand, res.n_pruned, res.n_feasible, res.n_optimal, res.n_region,
+                      res.n_lp1_pivots, res.n_lp2_pivots, res.n_cheb_pivots, res.n_levels, res.truncated, None)
     lib().orc_free_result(ctypes.byref(res))
     return out
 
