@@ -331,6 +331,46 @@ def mplp_measure(prec, stream, dev, steps: int = 3) -> dict:
                              "sample": f"C oracle, the first 8 instances to |S| = n ({n_cpu} candidates)"}}
 
 
+DEFAULT_SETTINGS = dict(tile_w=8, feas_warps=4, feas_chunk=32)
+
+
+def settings_compare(stream, dev) -> dict:
+    """The autotuner against the fixed default launch settings (8 threads per
+    screen LP, 4 LP1 warps per block, 32 candidates per claim) on three batch
+    shapes: the bench batch, its main instance alone, and 64 MPC instances
+    (n=12, m=72, p=4) to |S| <= 4.  Device time of one full run (graph), the
+    best of two, each way."""
+    import torch
+    from mpqpcudasolver_gb300 import problems as P
+    from mpqpcudasolver_gb300 import solver
+    probs, kmax, budget = workload()
+    mpc = [P.scale_problem(p) for p in P.mpc_batch(64)]
+    cases = {"bench_batch": (probs, kmax, budget), "main_instance": (probs[:1], kmax[:1], budget[:1]),
+             "mpc64_k4": (mpc, 4, 0)}
+    out = {}
+    for name, (pr, km, bu) in cases.items():
+        row = {}
+        for how, extra in (("default", DEFAULT_SETTINGS), ("tuned", dict(autotune=1))):
+            plan = solver.Plan(pr, precision=solver.MIXED, k_max=km, budget=bu, mem_fraction=0.85, **extra)
+            plan.run(stream.cuda_stream)
+            best = None
+            for _ in range(2):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                plan.run(stream.cuda_stream)
+                e1.record(stream)
+                torch.cuda.synchronize(dev)
+                ms = e0.elapsed_time(e1)
+                best = ms if best is None else min(best, ms)
+            r = plan.results()
+            plan.close()
+            row[how] = {"ms": best, "settings": r.settings, "regions": r.total("regions")}
+        row["speedup"] = row["default"]["ms"] / row["tuned"]["ms"]
+        row["same_regions"] = row["default"]["regions"] == row["tuned"]["regions"]
+        out[name] = row
+    return out
+
+
 def run_reference(args):
     world, rank, local, dist = dist_setup(args.gpus)
     if rank != 0:
@@ -358,7 +398,7 @@ def run_ours(args):
     prec = solver.MIXED if args.precision == "mixed" else solver.FP64
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
-    plan = solver.Plan(probs, precision=prec, k_max=kmax, budget=budget, mem_fraction=0.85)
+    plan = solver.Plan(probs, precision=prec, k_max=kmax, budget=budget, mem_fraction=0.85, autotune=1)
     for _ in range(args.warmup):
         plan.run(stream.cuda_stream)
     res = plan.results()
@@ -385,6 +425,7 @@ def run_ours(args):
     cand = res.candidates
     value = whole_job_rate(cand, ms_step, world)
     launches = plan.launches
+    settings = res.settings
     plan.close()
     del plan
     torch.cuda.synchronize(dev)
@@ -415,7 +456,7 @@ def run_ours(args):
     for _ in range(max(1, args.e2e_steps)):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        r = solver.solve(probs, precision=prec, k_max=kmax, budget=budget, mem_fraction=0.85)
+        r = solver.solve(probs, precision=prec, k_max=kmax, budget=budget, mem_fraction=0.85, autotune=1)
         dt = time.perf_counter() - t0
         e2e_vals.append(r.candidates / dt)
         h2d, d2h = r.h2d_bytes, r.d2h_bytes
@@ -473,6 +514,7 @@ def run_ours(args):
     reg = opt[opt["region"] == 1] if len(opt) else opt
     cb = cpu_baseline(steps=1)
     mplp = None if args.skip_mplp else mplp_measure(prec, stream, dev)
+    tune_cmp = None if (args.skip_tune_compare or prec != solver.MIXED) else settings_compare(stream, dev)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -490,6 +532,11 @@ def run_ours(args):
                       "results": int(len(opt)),
                       "what": "per optimal set: one FP64 refinement step of its KKT solve, relative to the law"},
         "screen": screen_info,
+        "launch_settings": settings,
+        "autotune_vs_default": {k: {"default_ms": v["default"]["ms"], "tuned_ms": v["tuned"]["ms"],
+                                    "tuned": v["tuned"]["settings"], "speedup": v["speedup"],
+                                    "same_regions": v["same_regions"]} for k, v in tune_cmp.items()}
+        if tune_cmp else None,
         "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "single_core")},
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "mpqp_solve_batch (C ABI): host arrays in, plan + upload + run + download + free"},
@@ -530,6 +577,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-mplp", action="store_true", help="leave out the mpLP (Q = 0) measurement")
+    ap.add_argument("--skip-tune-compare", action="store_true",
+                    help="leave out the autotuned-vs-default launch settings comparison")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

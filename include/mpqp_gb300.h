@@ -150,6 +150,19 @@ typedef struct {
                                 bound on instances whose parameter set is a
                                 box (the primal tableau screen elsewhere),
                                 1 the primal tableau screen everywhere      */
+    /* Launch settings (0: the default, or the autotuner's choice):
+     *   tile_w      threads per LP in the first stage of the FP32 screen
+     *               (8, 16 or 32: 4, 2 or 1 LPs per warp)
+     *   feas_warps  warps (one LP each) per LP1 block, 1..4
+     *   feas_chunk  consecutive candidates an LP1 warp claims, 1..32
+     * autotune = 1: settings left at 0 are chosen by timing the candidate
+     * settings on a short slice of the batch (each instance under a small
+     * candidate budget) when the plan is created; the choice is kept per
+     * batch shape (precision, screen mode, rows, free variables, parameters,
+     * instance count) for the rest of the process.  Any setting gives the
+     * same verdicts. */
+    int tile_w, feas_warps, feas_chunk;
+    int autotune;
 } mpqp_options;
 
 /* One optimal active set */
@@ -208,6 +221,8 @@ typedef struct {
     void *rec;                    /* n_rec records (112 bytes each) or NULL */
     long long h2d_bytes;          /* problem data uploaded by the plan      */
     long long d2h_bytes;          /* result bytes copied back               */
+    int tile_w, feas_warps, feas_chunk; /* the launch settings of the run    */
+    int tuned;                    /* 1: chosen by the autotuner             */
 } mpqp_batch_result;
 
 void mpqp_default_options(mpqp_options *opt);

@@ -29,13 +29,13 @@ size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd);
 size_t feas_smem_per_warp(int prec_bytes, const SlotDims &sd);
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd);
 size_t screen_smem_per_warp(const SlotDims &sd, int route);
-size_t screen_tiles_smem(const SlotDims &sd);
+size_t screen_tiles_smem(const SlotDims &sd, int tile_w);
 bool screen_dual_route(int mode, const InstDesc &I, const SlotDims &sd);
 size_t laws_smem_per_warp(const SlotDims &sd);
 const void *kernel_ptr(const char *name);
 cudaError_t launch_enumerate(const DevBuffers &B, int level, int grid, cudaStream_t s);
 cudaError_t launch_feasibility(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int prec,
-                               int grid, size_t smem, cudaStream_t s);
+                               int grid, size_t smem, cudaStream_t s, int warps, int chunk);
 cudaError_t launch_lp1_fp64(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int grid,
                             size_t smem, cudaStream_t s);
 cudaError_t launch_lp1_cert(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int grid,
@@ -44,7 +44,7 @@ size_t cert_smem_per_warp(const SlotDims &sd);
 cudaError_t launch_optimality(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, bool lp,
                               int grid, size_t smem, cudaStream_t s);
 cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode, int route,
-                              int grid, size_t smem, cudaStream_t s);
+                              int grid, size_t smem, cudaStream_t s, int tile_w);
 cudaError_t launch_optimality_fp64(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, bool lp,
                                    int grid, size_t smem, cudaStream_t s);
 cudaError_t launch_level0(const DevBuffers &B, int prec, cudaStream_t s);
@@ -284,8 +284,12 @@ struct mpqp_plan {
     bool pooled = false;        // allocations came from the device pool
     int grid_opt2 = 0;          // grid of the primal route (grid_opt: the dual route)
     int grid_opt3 = 0;          // grid of the dual route's second stage
-    int grid_tiles = 0;         // the dual route's first stage (one set per 8-thread tile)
+    int grid_tiles = 0;         // the dual route's first stage (one set per tile of tile_w threads)
     size_t smem_tiles = 0;
+    // launch settings the autotuner chooses: threads per set in the screen's
+    // first stage, warps per LP1 block, candidates an LP1 warp claims at once
+    int tile_w = 8, feas_warps = 4, feas_chunk = 32;
+    int tuned = 0;              // 1: the settings came from the autotuner (or its cache)
     size_t smem_opt2 = 0;       // shared memory per block of the primal route
     int grid_enum = 0, grid_feas = 0, grid_lp1fb = 0, grid_opt = 0, grid_optfb = 0, grid_cert = 0;
     size_t smem_feas = 0, smem_lp1fb = 0, smem_opt = 0, smem_optfb = 0, smem_cert = 0;
@@ -492,12 +496,14 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
             return MPQP_OK;
         }
         if (P->screen_dual) {
-            L("k_opt_screen<dual>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 0, P->grid_tiles, P->smem_tiles, s));
+            L("k_opt_screen<dual>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 0, P->grid_tiles, P->smem_tiles, s,
+                                                      P->tile_w));
             L("k_opt_screen<dual,rows>",
-              launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 2, P->grid_opt3, P->smem_opt, s));
+              launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 2, P->grid_opt3, P->smem_opt, s, P->tile_w));
         }
         if (P->screen_primal)
-            L("k_opt_screen<primal>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 1, P->grid_opt2, P->smem_opt2, s));
+            L("k_opt_screen<primal>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 1, P->grid_opt2, P->smem_opt2, s,
+                                                        P->tile_w));
         return MPQP_OK;
     };
     // FP64 re-evaluation of the sets the FP32 screen left undecided
@@ -518,7 +524,8 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
     L("k_finalize", launch_finalize(B, 0, s));
     for (int k = 1; k <= P->kmax; k++) {
         L("k_enumerate", launch_enumerate(B, k, P->grid_enum, s));
-        L(feas, launch_feasibility(B, P->tol, P->sd, k, P->prec, P->grid_feas, P->smem_feas, s));
+        L(feas, launch_feasibility(B, P->tol, P->sd, k, P->prec, P->grid_feas, P->smem_feas, s, P->feas_warps,
+                                   P->feas_chunk));
         if (mixed) {
             L("k_lp1_cert", launch_lp1_cert(B, P->tol, P->sd, k, P->grid_cert, P->smem_cert, s));
             L("k_lp1_fp64", launch_lp1_fp64(B, P->tol, P->sd, k, P->grid_lp1fb, P->smem_lp1fb, s));
@@ -540,9 +547,10 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
     return MPQP_OK;
 }
 
-static int mpqp_plan_create_impl(int n_inst, const mpqp_problem *probs, const mpqp_options *opt_in, mpqp_plan **out)
+// The body of mpqp_plan_create (the caller holds g_mu); the launch settings
+// come from the options, 0 selecting the defaults.
+static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_options *opt_in, mpqp_plan **out)
 {
-    std::lock_guard<std::mutex> lk(g_mu);
     *out = nullptr;
     if (n_inst < 1 || !probs) { set_err("no instances"); return MPQP_EINVAL; }
     mpqp_plan *P = new mpqp_plan();
@@ -555,6 +563,15 @@ static int mpqp_plan_create_impl(int n_inst, const mpqp_problem *probs, const mp
         delete P;
         return MPQP_EINVAL;
     }
+    if ((o.tile_w && o.tile_w != 8 && o.tile_w != 16 && o.tile_w != 32) || o.feas_warps < 0 || o.feas_warps > 4 ||
+        o.feas_chunk < 0 || o.feas_chunk > 32) {
+        set_err("launch settings out of range (tile_w 8/16/32, feas_warps 1..4, feas_chunk 1..32)");
+        delete P;
+        return MPQP_EINVAL;
+    }
+    if (o.tile_w) P->tile_w = o.tile_w;
+    if (o.feas_warps) P->feas_warps = o.feas_warps;
+    if (o.feas_chunk) P->feas_chunk = o.feas_chunk;
     P->lp2_screen = o.lp2_screen;
     P->n_inst = n_inst;
     P->probs.assign(probs, probs + n_inst);
@@ -735,13 +752,13 @@ static int mpqp_plan_create_impl(int n_inst, const mpqp_problem *probs, const mp
     CK(cudaMemset(B.hash[1], 0xff, sizeof(HashSlot) * hash_cap));
     CK(cudaMemset(B.ctl, 0, sizeof(Ctl)));
     // kernel geometry
-    P->smem_feas = 4 * feas_smem_per_warp(P->prec == PREC_MIXED ? 4 : 8, sd);
+    P->smem_feas = (size_t)P->feas_warps * feas_smem_per_warp(P->prec == PREC_MIXED ? 4 : 8, sd);
     P->smem_lp1fb = 4 * lp1_smem_per_warp(8, sd);
     P->smem_cert = 4 * cert_smem_per_warp(sd);
     // mixed precision: the grouped FP32 screen, one warp per block
     P->smem_opt = P->prec == PREC_MIXED ? screen_smem_per_warp(sd, 0) : 4 * opt_smem_per_warp(8, sd);
     P->smem_opt2 = screen_smem_per_warp(sd, 1);
-    P->smem_tiles = screen_tiles_smem(sd);
+    P->smem_tiles = screen_tiles_smem(sd, P->tile_w);
     for (const InstDesc &d : P->desc) {
         if (d.lp) P->has_lp = true; else P->has_qp = true;
         if (P->prec != PREC_MIXED) continue;
@@ -750,7 +767,8 @@ static int mpqp_plan_create_impl(int n_inst, const mpqp_problem *probs, const mp
     }
     P->smem_optfb = 4 * opt_smem_per_warp(8, sd);
     if ((rc = grid_for(kernel_ptr("enumerate"), 0, &P->grid_enum)) ||
-        (rc = grid_for(kernel_ptr(P->prec == PREC_MIXED ? "feas32" : "feas64"), P->smem_feas, &P->grid_feas)) ||
+        (rc = grid_for(kernel_ptr(P->prec == PREC_MIXED ? "feas32" : "feas64"), P->smem_feas, &P->grid_feas,
+                       32 * P->feas_warps)) ||
         (rc = grid_for(kernel_ptr("lp1_fp64"), P->smem_lp1fb, &P->grid_lp1fb)) ||
         (rc = grid_for(kernel_ptr("lp1_cert"), P->smem_cert, &P->grid_cert)) ||
         (rc = P->prec == PREC_MIXED
@@ -758,7 +776,10 @@ static int mpqp_plan_create_impl(int n_inst, const mpqp_problem *probs, const mp
                   : grid_for(kernel_ptr("opt64"), P->smem_opt, &P->grid_opt)) ||
         (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_primal"), P->smem_opt2, &P->grid_opt2, 32) : 0) ||
         (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_dual_rows"), P->smem_opt, &P->grid_opt3, 32) : 0) ||
-        (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_dual_tiles"), P->smem_tiles, &P->grid_tiles, 32) : 0) ||
+        (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr(P->tile_w == 8 ? "screen_dual_tiles8"
+                                                          : P->tile_w == 16 ? "screen_dual_tiles16"
+                                                                            : "screen_dual_tiles32"),
+                                               P->smem_tiles, &P->grid_tiles, 32) : 0) ||
         (rc = grid_for(kernel_ptr("opt_fp64"), P->smem_optfb, &P->grid_optfb)) ||
         (rc = P->has_lp && P->prec != PREC_MIXED ? grid_for(kernel_ptr("opt64_lp"), P->smem_opt, &P->grid_opt_lp) : 0) ||
         (rc = P->has_lp ? grid_for(kernel_ptr("opt_fp64_lp"), P->smem_optfb, &P->grid_optfb_lp) : 0)) {
@@ -789,6 +810,137 @@ static int mpqp_plan_create_impl(int n_inst, const mpqp_problem *probs, const mp
     }
     *out = P;
     return MPQP_OK;
+}
+
+// ---------------------------------------------------------------------
+// autotuner
+// ---------------------------------------------------------------------
+// The reference passes its threads per LP (nTPB) and launch shapes from its
+// host code (batched_simplex.cu:1181 and the launches around it).  Here the
+// LPs per block and threads per LP are chosen by measurement: each candidate
+// setting runs a short slice of the batch (every instance under a small
+// candidate budget, the first levels) with an event around every launch,
+// and the setting whose kernels take least is kept.  LP1 (warps per block x
+// candidates per claim) and the screen's first stage (threads per LP) are
+// independent kernels, so they are tuned one after the other.  The choice is
+// cached per batch shape for the process.
+struct TuneKey {
+    int prec, lp2_screen, m1, nv, p1, ninst;
+    bool operator==(const TuneKey &k) const
+    {
+        return prec == k.prec && lp2_screen == k.lp2_screen && m1 == k.m1 && nv == k.nv && p1 == k.p1 &&
+               ninst == k.ninst;
+    }
+};
+struct TuneEntry { TuneKey key; int tile_w, feas_warps, feas_chunk; };
+static int mpqp_plan_run_timed_impl(mpqp_plan *P, void *stream);
+static std::vector<TuneEntry> g_tune_cache;   // guarded by g_mu
+
+static TuneKey tune_key(int n_inst, const mpqp_problem *probs, const mpqp_options &o)
+{
+    TuneKey k{o.precision == MPQP_MIXED ? 1 : 0, o.lp2_screen, 0, 0, 0, 0};
+    for (int i = 0; i < n_inst; i++) {
+        k.m1 = std::max(k.m1, probs[i].m + probs[i].ncp);
+        k.nv = std::max(k.nv, probs[i].n + probs[i].p);
+        k.p1 = std::max(k.p1, probs[i].p + 1);
+    }
+    // shapes within a bucket share the choice: rows by 8, variables by 4,
+    // instance counts by powers of two
+    k.m1 = (k.m1 + 7) / 8;
+    k.nv = (k.nv + 3) / 4;
+    int b = 0;
+    while ((1 << b) < n_inst) b++;
+    k.ninst = b;
+    return k;
+}
+
+// Milliseconds of the kernels whose names start with `prefix` in one timed
+// run of the slice under `o`, the best of two runs; < 0 when the setting
+// cannot run.
+static double tune_trial(int n_inst, const mpqp_problem *slice, const mpqp_options &o, const char *prefix)
+{
+    mpqp_plan *P = nullptr;
+    if (plan_create_locked(n_inst, slice, &o, &P) != MPQP_OK) { cudaGetLastError(); return -1.0; }
+    double best = -1.0;
+    for (int rep = 0; rep < 2; rep++) {
+        if (mpqp_plan_run_timed_impl(P, nullptr) != MPQP_OK) { best = -1.0; break; }
+        if (cudaEventSynchronize(P->ev1) != cudaSuccess) { cudaGetLastError(); best = -1.0; break; }
+        double ms = 0.0;
+        for (size_t i = 0; i < P->kname.size(); i++) {
+            if (strncmp(P->kname[i], prefix, strlen(prefix))) continue;
+            float e = 0;
+            if (cudaEventElapsedTime(&e, P->kev[i], P->kev[i + 1]) == cudaSuccess) ms += e;
+        }
+        if (best < 0 || ms < best) best = ms;
+    }
+    // a run that overflowed its buffers measured nothing comparable
+    Ctl ctl;
+    if (best >= 0 && (cudaMemcpy(&ctl, P->B.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost) != cudaSuccess || ctl.overflow))
+        best = -1.0;
+    cudaGetLastError();
+    mpqp_plan_destroy(P);
+    return best;
+}
+
+static void autotune(int n_inst, const mpqp_problem *probs, mpqp_options &o)
+{
+    const TuneKey key = tune_key(n_inst, probs, o);
+    for (const TuneEntry &e : g_tune_cache)
+        if (e.key == key) {
+            if (!o.tile_w) o.tile_w = e.tile_w;
+            if (!o.feas_warps) o.feas_warps = e.feas_warps;
+            if (!o.feas_chunk) o.feas_chunk = e.feas_chunk;
+            return;
+        }
+    // the slice: every instance under a small budget (its first levels)
+    std::vector<mpqp_problem> slice(probs, probs + n_inst);
+    const long long cap = std::max(1LL << 16, (1LL << 20) / n_inst);
+    for (mpqp_problem &pr : slice) pr.budget = pr.budget > 0 ? std::min(pr.budget, cap) : cap;
+    mpqp_options t = o;
+    t.autotune = 0;
+    t.use_graph = 0;
+    t.record = 0;
+    t.cand_cap = 0; t.node_cap = 0; t.arena_bytes = 0; t.opt_cap = 0;
+    t.mem_fraction = std::min(o.mem_fraction, 0.3);
+    int best_w = o.feas_warps ? o.feas_warps : 4, best_c = o.feas_chunk ? o.feas_chunk : 32;
+    if (!o.feas_warps || !o.feas_chunk) {
+        double best = -1.0;
+        for (int w : {2, 4})
+            for (int c : {8, 16, 32}) {
+                if ((o.feas_warps && w != o.feas_warps) || (o.feas_chunk && c != o.feas_chunk)) continue;
+                t.feas_warps = w; t.feas_chunk = c; t.tile_w = 8;
+                const double ms = tune_trial(n_inst, slice.data(), t, "k_feasibility");
+                if (ms >= 0 && (best < 0 || ms < best)) { best = ms; best_w = w; best_c = c; }
+            }
+    }
+    int best_t = o.tile_w ? o.tile_w : 8;
+    if (!o.tile_w && o.precision == MPQP_MIXED) {
+        double best = -1.0;
+        t.feas_warps = best_w; t.feas_chunk = best_c;
+        for (int tw : {8, 16, 32}) {
+            t.tile_w = tw;
+            const double ms = tune_trial(n_inst, slice.data(), t, "k_opt_screen<dual>");
+            if (ms > 0 && (best < 0 || ms < best)) { best = ms; best_t = tw; }
+        }
+    }
+    if (!o.tile_w) o.tile_w = best_t;
+    if (!o.feas_warps) o.feas_warps = best_w;
+    if (!o.feas_chunk) o.feas_chunk = best_c;
+    g_tune_cache.push_back(TuneEntry{key, o.tile_w, o.feas_warps, o.feas_chunk});
+}
+
+static int mpqp_plan_create_impl(int n_inst, const mpqp_problem *probs, const mpqp_options *opt_in, mpqp_plan **out)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    *out = nullptr;
+    if (n_inst < 1 || !probs) { set_err("no instances"); return MPQP_EINVAL; }
+    mpqp_options o;
+    if (opt_in) o = *opt_in; else mpqp_default_options(&o);
+    const bool tune = o.autotune && (!o.tile_w || !o.feas_warps || !o.feas_chunk);
+    if (tune) autotune(n_inst, probs, o);
+    const int rc = plan_create_locked(n_inst, probs, &o, out);
+    if (rc == MPQP_OK && tune) (*out)->tuned = 1;
+    return rc;
 }
 
 extern "C" int mpqp_plan_create(int n_inst, const mpqp_problem *probs, const mpqp_options *opt_in, mpqp_plan **out)
@@ -1086,6 +1238,7 @@ static int plan_results_impl(mpqp_plan *P, mpqp_batch_result *&R, bool *complete
         o.t = v.t; o.r = v.r; o.region = v.region; o.fp64 = v.fp64; o.rec = v.rec; o.err = v.err;
     }
     R->h2d_bytes = P->h2d_bytes;
+    R->tile_w = P->tile_w; R->feas_warps = P->feas_warps; R->feas_chunk = P->feas_chunk; R->tuned = P->tuned;
     R->d2h_bytes = (long long)(sizeof(Ctl) + sizeof(InstCtl) * P->n_inst + sizeof(OptRec) * nopt);
     if (P->B.rec) {
         long long nrec = std::min(ctl.rec_base, P->B.rec_cap);

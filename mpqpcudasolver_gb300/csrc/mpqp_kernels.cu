@@ -526,11 +526,12 @@ __host__ __device__ inline size_t feas_slot_bytes(int maxM1, int maxLD1, int max
     return lp1_buf_bytes<T>(maxM1, maxLD1, maxNv) + 16;
 }
 
-// candidates a warp claims at a time: consecutive candidates share parents
-// (children of one parent are consecutive in the candidate list), so the
-// first child loads its parent from DRAM and the others find it in L2, and
-// the next candidate's parent is known one candidate ahead (L2 prefetch)
-constexpr int kFeasChunk = 32;
+// candidates a warp claims at a time (a plan setting, at most 32, by default
+// 32): consecutive candidates share parents (children of one parent are
+// consecutive in the candidate list), so the first child loads its parent
+// from DRAM and the others find it in L2, and the next candidate's parent is
+// known one candidate ahead (L2 prefetch)
+constexpr int kFeasChunkMax = 32;
 
 // ---------------------------------------------------------------------
 // bulk (TMA) copies between global and shared memory
@@ -911,7 +912,7 @@ __device__ __noinline__ void queue_undecided_lp1(const DevBuffers &B, int w, con
 //             certified (see below), otherwise the candidate is queued for
 //             the FP64 re-solve.
 template <typename T>
-__global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, SlotDims sd, int level)
+__global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, SlotDims sd, int level, int chunk)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
@@ -937,10 +938,10 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
     lc.reset(-1);
     for (;;) {
         long long w0;
-        if (lane == 0) w0 = (long long)atomicAdd(&ctl->ctr[0], (unsigned long long)kFeasChunk);
+        if (lane == 0) w0 = (long long)atomicAdd(&ctl->ctr[0], (unsigned long long)chunk);
         w0 = __shfl_sync(FULLMASK, w0, 0);
         if (w0 >= wend || abort) break;
-        const int cnt = wend - w0 < kFeasChunk ? (int)(wend - w0) : kFeasChunk;
+        const int cnt = wend - w0 < chunk ? (int)(wend - w0) : chunk;
         const Cand mine = lane < cnt ? B.cand[w0 + lane] : Cand{-1, 0};
         // candidate w's node goes to slot w (also when the FP64 re-solve
         // stores it); a candidate that stores none leaves an invalid record
@@ -2429,21 +2430,23 @@ __host__ __device__ __forceinline__ bool dual_route(int mode, const InstDesc &I,
 }
 
 // ---------------------------------------------------------------------
-// Screen stage 0 on half-warps
+// Screen stage 0 on tiles of a warp
 // ---------------------------------------------------------------------
 // Stage 0 of the dual route works on small LPs -- the k multiplier rows and
 // the 2p box rows (k + 2p <= 44), a basis of p + 1 <= 7 -- so a full warp
-// left half of its lanes idle.  Here each 8-thread tile of a warp screens its
-// own set (four per warp; 16-thread tiles were slower: 124 against 111 ms on
-// the m = 62 batch): the same operations as kkt_factor<float> and
-// lp2_dual_screen, with tile-wide shuffles and reductions.
+// left half of its lanes idle.  Here each W-thread tile of a warp screens its
+// own set (32 / W per warp; W = 8, 16 or 32 is a plan setting the autotuner
+// picks -- on the m = 62 batch 8 was fastest, 111 against 124 ms for 16):
+// the same operations as kkt_factor<float> and lp2_dual_screen, with
+// tile-wide shuffles and reductions.  W >= p + 1 (the basis rows sit in
+// lanes 0..p).
 namespace cgx = cooperative_groups;
-constexpr int kTileShift = 3;
-constexpr int kTileW = 1 << kTileShift;
-constexpr int kTileRows = 48;                  // k + 2p rows, 48 / kTileW slots
-using ScreenTile = cgx::thread_block_tile<kTileW, cgx::thread_block>;
+constexpr int kTileRows = 48;                  // k + 2p rows, ceil(48 / W) slots per lane
+template <int W>
+using ScreenTile = cgx::thread_block_tile<W, cgx::thread_block>;
 
-__device__ __forceinline__ int tile_argmin(const ScreenTile &t, unsigned key, unsigned id, int idx)
+template <int W>
+__device__ __forceinline__ int tile_argmin(const ScreenTile<W> &t, unsigned key, unsigned id, int idx)
 {
     const unsigned kmin = cgx::reduce(t, key, cgx::less<unsigned>());
     if (kmin == 0xffffffffu) return -1;
@@ -2453,17 +2456,19 @@ __device__ __forceinline__ int tile_argmin(const ScreenTile &t, unsigned key, un
     return t.shfl(idx, __ffs(win) - 1);
 }
 
-__device__ __forceinline__ float tile_max(const ScreenTile &t, float v)
+template <int W>
+__device__ __forceinline__ float tile_max(const ScreenTile<W> &t, float v)
 {
 #pragma unroll
-    for (int off = kTileW / 2; off; off >>= 1) v = fmaxf(v, t.shfl_xor(v, off));
+    for (int off = W / 2; off; off >>= 1) v = fmaxf(v, t.shfl_xor(v, off));
     return v;
 }
 
-__device__ __forceinline__ float tile_sum(const ScreenTile &t, float v)
+template <int W>
+__device__ __forceinline__ float tile_sum(const ScreenTile<W> &t, float v)
 {
 #pragma unroll
-    for (int off = kTileW / 2; off; off >>= 1) v += t.shfl_xor(v, off);
+    for (int off = W / 2; off; off >>= 1) v += t.shfl_xor(v, off);
     return v;
 }
 
@@ -2482,7 +2487,8 @@ __host__ __device__ inline size_t tile_slot_bytes(const SlotDims &sd)
 // kkt_factor<float> with the lanes of a tile (the same operations in the same
 // order; R keeps the reciprocal pivot on its diagonal).  Returns 0, or 1 when
 // a pivot ratio fails thr.
-__device__ int kkt_factor_tile(const ScreenTile &t, const KktData<float> &D, const InstDesc &I, uint64_t lo,
+template <int W>
+__device__ int kkt_factor_tile(const ScreenTile<W> &t, const KktData<float> &D, const InstDesc &I, uint64_t lo,
                                uint64_t hi, float thr, float *R, float *Y, float *Lam, int *S, int *k_out,
                                float *rho_out)
 {
@@ -2490,7 +2496,7 @@ __device__ int kkt_factor_tile(const ScreenTile &t, const KktData<float> &D, con
     const int m = I.m, p = I.p, P1 = p + 1;
     const int k = mask_pop(lo, hi);
     *k_out = k;
-    for (int i = tl; i < m; i += kTileW)
+    for (int i = tl; i < m; i += W)
         if (mask_has(lo, hi, i)) S[mask_rank(lo, hi, i)] = i;
     t.sync();
     float rho = 1.0f;
@@ -2510,14 +2516,14 @@ __device__ int kkt_factor_tile(const ScreenTile &t, const KktData<float> &D, con
         fail = t.shfl(fail, 0);
         if (fail) return 1;
         t.sync();
-        for (int b = a + 1 + tl; b < k; b += kTileW) {
+        for (int b = a + 1 + tl; b < k; b += W) {
             float acc = D.Wm[(size_t)S[a] * m + S[b]];
             for (int l = 0; l < a; l++) acc = __fmaf_rn(-R[l * k + a], R[l * k + b], acc);
             R[a * k + b] = acc * R[a * k + a];
         }
         t.sync();
     }
-    for (int cc = tl; cc < P1; cc += kTileW) {
+    for (int cc = tl; cc < P1; cc += W) {
         for (int a = 0; a < k; a++) {
             float acc = (cc < p) ? D.Wh[(size_t)S[a] * p + cc] : D.wc[S[a]];
             for (int l = 0; l < a; l++) acc = __fmaf_rn(-R[l * k + a], Y[l * P1 + cc], acc);
@@ -2534,14 +2540,14 @@ __device__ int kkt_factor_tile(const ScreenTile &t, const KktData<float> &D, con
     return 0;
 }
 
-// lp2_dual_screen with the lanes of a tile: rows r = lane + 16 s (three
-// slots), basis rows in lanes 0..p.  Same pricing, ratio test, pivot and
-// verified bound.
-__device__ int lp2_dual_screen_tile(const ScreenTile &t, const float *T, int m, int R2, int p, const float *blo,
+// lp2_dual_screen with the lanes of a tile: rows r = lane + W s, basis rows
+// in lanes 0..p.  Same pricing, ratio test, pivot and verified bound.
+template <int W>
+__device__ int lp2_dual_screen_tile(const ScreenTile<W> &t, const float *T, int m, int R2, int p, const float *blo,
                                     const float *bhi, float thr, float ethr, float tol_piv, float tol_dj, int max_it,
                                     int degen_switch, int *it_out, float *bound_out)
 {
-    constexpr int NR = kTileRows / kTileW;
+    constexpr int NR = (kTileRows + W - 1) / W;
     constexpr int MP = kDualMaxP;
     constexpr int LD = kDualLd;
     const int lane = t.thread_rank();
@@ -2556,7 +2562,7 @@ __device__ int lp2_dual_screen_tile(const ScreenTile &t, const float *T, int m, 
     for (int c = 0; c < MP; c++) { lo[c] = c < p ? blo[c] : 0.0f; hi[c] = c < p ? bhi[c] : 0.0f; }
     unsigned bkey = 0xffffffffu;
     int bi = -1;
-    for (int r = lane; r < m; r += kTileW) {
+    for (int r = lane; r < m; r += W) {
         float a[8];
         row8(r, a);
         float b = a[7];
@@ -2565,7 +2571,7 @@ __device__ int lp2_dual_screen_tile(const ScreenTile &t, const float *T, int m, 
         const unsigned k = key_signed(b);
         if (bi < 0 || k < bkey) { bkey = k; bi = r; }
     }
-    const int istar = tile_argmin(t, bkey, (unsigned)bi, bi);
+    const int istar = tile_argmin<W>(t, bkey, (unsigned)bi, bi);
     float gi[8];
     row8(istar, gi);
     float binv[MP], pi[MP], binvp = 0.0f, y = 0.0f;
@@ -2589,7 +2595,7 @@ __device__ int lp2_dual_screen_tile(const ScreenTile &t, const float *T, int m, 
     unsigned basic = 0;
 #pragma unroll 1
     for (int s = 0; s < NR; s++) {
-        const int r = lane + kTileW * s;
+        const int r = lane + W * s;
         bool b = r == istar;
         if (r >= m && r < m + p) b = !(T[istar * LD + (r - m)] > 0.0f);
         else if (r >= m + p && r < m + 2 * p) b = T[istar * LD + (r - m - p)] > 0.0f;
@@ -2612,7 +2618,7 @@ __device__ int lp2_dual_screen_tile(const ScreenTile &t, const float *T, int m, 
             }
         }
         const float cy = t.shfl(acc, p);
-        const float num = tile_sum(t, lane < p ? fabsf(acc) * reach : (lane == P1 ? acc : 0.0f));
+        const float num = tile_sum<W>(t, lane < p ? fabsf(acc) * reach : (lane == P1 ? acc : 0.0f));
         thr_row = cy > 0.0f ? fminf(thr, ethr * __fdividef(ey, cy)) : thr;
         return cy > 0.0f ? __fdividef(num, cy) : pos_inf<float>();
     };
@@ -2630,7 +2636,7 @@ __device__ int lp2_dual_screen_tile(const ScreenTile &t, const float *T, int m, 
         float dbest = 0.0f;
 #pragma unroll 1
         for (int s = 0; s < NR; s++) {
-            const int r = lane + kTileW * s;
+            const int r = lane + W * s;
             if (r < R2 && !((basic >> s) & 1u)) {
                 float a[8];
                 row8(r, a);
@@ -2643,13 +2649,13 @@ __device__ int lp2_dual_screen_tile(const ScreenTile &t, const float *T, int m, 
                 }
             }
         }
-        const int q = tile_argmin(t, key, kid, kq);
+        const int q = tile_argmin<W>(t, key, kid, kq);
         if (q < 0) {
             bound = verify();
             proven = bound < -thr_row;
             break;
         }
-        const float dq = t.shfl(dbest, q & (kTileW - 1));
+        const float dq = t.shfl(dbest, q & (W - 1));
         float aq[8];
         row8(q, aq);
         float u = binvp * aq[6];
@@ -2658,7 +2664,7 @@ __device__ int lp2_dual_screen_tile(const ScreenTile &t, const float *T, int m, 
         unsigned rk = 0xffffffffu, rid = 0xffffffffu;
         int rl = -1;
         if (lane < P1 && u > tol_piv) { rk = key_of(__fdividef(fmaxf(y, 0.0f), u)); rid = (unsigned)bidx; rl = lane; }
-        const int l = tile_argmin(t, rk, rid, rl);
+        const int l = tile_argmin<W>(t, rk, rid, rl);
         if (l < 0) break;
         const float ul = t.shfl(u, l);
         const float yl = t.shfl(fmaxf(y, 0.0f), l);
@@ -2680,8 +2686,8 @@ __device__ int lp2_dual_screen_tile(const ScreenTile &t, const float *T, int m, 
         }
         if (own) { y = theta; bidx = q; }
         else if (other) y = __fmaf_rn(-theta, u, y);
-        if (lane == (q & (kTileW - 1))) basic |= 1u << (q >> kTileShift);
-        if (lane == (oldb & (kTileW - 1))) basic &= ~(1u << (oldb >> kTileShift));
+        if (lane == (q & (W - 1))) basic |= 1u << (q / W);
+        if (lane == (oldb & (W - 1))) basic &= ~(1u << (oldb / W));
         it++;
         degen = (theta == 0.0f) ? degen + 1 : 0;
         bland = degen >= degen_switch;
@@ -2691,18 +2697,20 @@ __device__ int lp2_dual_screen_tile(const ScreenTile &t, const float *T, int m, 
     return proven;
 }
 
-// Stage 0 of the dual route, one set per tile (32 / kTileW per warp): KKT factor,
+// Stage 0 of the dual route, one set per tile (32 / W per warp): KKT factor,
 // the multiplier rows and the box, dual bound; the sets it cannot settle go
 // to stage 1 (k_opt_screen<0, 1>), a failed KKT margin to the FP64 queue.
+template <int W>
 __global__ void __launch_bounds__(32, 32) k_opt_screen_tiles(DevBuffers B, Tol tol, SlotDims sd, int level, int mode)
 {
+    static_assert(W >= kDualMaxP + 1 && W <= 32 && (W & (W - 1)) == 0, "tile width");
     extern __shared__ __align__(16) unsigned char smem[];
-    const ScreenTile t = cgx::tiled_partition<kTileW>(cgx::this_thread_block());
+    const ScreenTile<W> t = cgx::tiled_partition<W>(cgx::this_thread_block());
     const int lane = t.thread_rank();
     float *R, *Y, *Lam, *Tb;
     int *S;
     {
-        unsigned char *base = smem + (threadIdx.x / kTileW) * tile_slot_bytes(sd);
+        unsigned char *base = smem + (threadIdx.x / W) * tile_slot_bytes(sd);
         size_t o = 0;
         R = (float *)(base + o); o += align16((size_t)sd.maxK * sd.maxK * 4);
         Y = (float *)(base + o); o += align16((size_t)sd.maxK * sd.maxP1 * 4);
@@ -2736,14 +2744,14 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen_tiles(DevBuffers B, Tol t
         int k = 0, piv = 0;
         float rho = 1.0f, bound = 0.0f;
         bool proven = false, to_rows = false;
-        if (!kkt_factor_tile(t, D, I, nd.lo, nd.hi, tol.margin_licq32, R, Y, Lam, S, &k, &rho)) {
+        if (!kkt_factor_tile<W>(t, D, I, nd.lo, nd.hi, tol.margin_licq32, R, Y, Lam, S, &k, &rho)) {
             to_rows = true;
             if (k > 0 && k + ncp <= tile_rows(sd)) {
                 float bmax = 0.0f;
-                for (int ii = lane; ii < ncp; ii += kTileW) bmax = fmaxf(bmax, fabsf(D.bt[ii]));
-                bmax = tile_max(t, bmax);
+                for (int ii = lane; ii < ncp; ii += W) bmax = fmaxf(bmax, fabsf(D.bt[ii]));
+                bmax = tile_max<W>(t, bmax);
                 float amaxA = 0.0f;
-                for (int a = lane; a < k; a += kTileW) {
+                for (int a = lane; a < k; a += W) {
                     float *tr = Tb + (size_t)a * kDualLd;
                     const float *lam = Lam + a * P1;
                     float rs = 0.0f;
@@ -2755,19 +2763,19 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen_tiles(DevBuffers B, Tol t
                     tr[kRowScaleCol] = rs;
                     amaxA = fmaxf(amaxA, rs);
                 }
-                for (int ii = lane; ii < ncp; ii += kTileW) {
+                for (int ii = lane; ii < ncp; ii += W) {
                     float *tr = Tb + (size_t)(k + ii) * kDualLd;
                     for (int cc = 0; cc < kDualMaxP; cc++) tr[cc] = cc < p ? D.At[ii * p + cc] : 0.0f;
                     tr[6] = 0.0f;
                     tr[7] = D.bt[ii];
                     tr[kRowScaleCol] = 0.0f;
                 }
-                amaxA = tile_max(t, amaxA);
+                amaxA = tile_max<W>(t, amaxA);
                 // error scale per unit of row magnitude: 1 / smallest pivot ratio
                 // times the reach of theta inside the box
                 const float escale = __fdividef(1.0f + (float)p * bmax, rho);
                 t.sync();
-                proven = lp2_dual_screen_tile(t, Tb, k, k + ncp, p, B.fpool + I.f_blo, B.fpool + I.f_bhi,
+                proven = lp2_dual_screen_tile<W>(t, Tb, k, k + ncp, p, B.fpool + I.f_blo, B.fpool + I.f_bhi,
                                               tol.margin_t32 * escale * amaxA, tol.margin_t32 * escale, tol.tol_piv32,
                                               tol.tol_dj32, tol.max_pivots, tol.degen_switch, &piv, &bound);
                 to_rows = !proven;
@@ -3275,7 +3283,7 @@ size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd)
 }
 
 size_t screen_smem_per_warp(const SlotDims &sd, int route) { return screen_warp_bytes(sd, route); }
-size_t screen_tiles_smem(const SlotDims &sd) { return (32 / kTileW) * tile_slot_bytes(sd); }   // a 32-thread block
+size_t screen_tiles_smem(const SlotDims &sd, int tile_w) { return (32 / tile_w) * tile_slot_bytes(sd); }   // a 32-thread block
 bool screen_dual_route(int mode, const InstDesc &I, const SlotDims &sd) { return dual_route(mode, I, sd); }
 
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd)
@@ -3304,7 +3312,9 @@ const void *kernel_ptr(const char *name)
         {"opt_fp64", (const void *)k_optimality_fp64<false>},
         {"opt_fp64_lp", (const void *)k_optimality_fp64<true>},
         {"screen_dual_rows", (const void *)k_opt_screen<0, 1>},
-        {"screen_dual_tiles", (const void *)k_opt_screen_tiles},
+        {"screen_dual_tiles8", (const void *)k_opt_screen_tiles<8>},
+        {"screen_dual_tiles16", (const void *)k_opt_screen_tiles<16>},
+        {"screen_dual_tiles32", (const void *)k_opt_screen_tiles<32>},
         {"screen_primal", (const void *)k_opt_screen<1>},
         {"level0_64", (const void *)k_level0<double>},
         {"level0_32", (const void *)k_level0<float>},
@@ -3326,11 +3336,14 @@ cudaError_t launch_enumerate(const DevBuffers &B, int level, int grid, cudaStrea
     return cudaGetLastError();
 }
 
+// warps: warps per block (1..4, smem = warps x the slot); chunk: candidates
+// a warp claims at a time (1..32)
 cudaError_t launch_feasibility(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int prec,
-                               int grid, size_t smem, cudaStream_t s)
+                               int grid, size_t smem, cudaStream_t s, int warps, int chunk)
 {
-    if (prec == PREC_FP64) k_feasibility<double><<<grid, 128, smem, s>>>(B, tol, sd, level);
-    else k_feasibility<float><<<grid, 128, smem, s>>>(B, tol, sd, level);
+    if (warps < 1 || warps > 4 || chunk < 1 || chunk > kFeasChunkMax) return cudaErrorInvalidValue;
+    if (prec == PREC_FP64) k_feasibility<double><<<grid, 32 * warps, smem, s>>>(B, tol, sd, level, chunk);
+    else k_feasibility<float><<<grid, 32 * warps, smem, s>>>(B, tol, sd, level, chunk);
     return cudaGetLastError();
 }
 
@@ -3358,10 +3371,16 @@ cudaError_t launch_optimality(const DevBuffers &B, const Tol &tol, const SlotDim
 }
 
 cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode, int route,
-                              int grid, size_t smem, cudaStream_t s)
+                              int grid, size_t smem, cudaStream_t s, int tile_w)
 {
-    // route 0: the dual route's first stage, 2: its second stage, 1: the primal route
-    if (route == 0) k_opt_screen_tiles<<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
+    // route 0: the dual route's first stage (tiles of tile_w threads), 2: its
+    // second stage, 1: the primal route
+    if (route == 0) {
+        if (tile_w == 8) k_opt_screen_tiles<8><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
+        else if (tile_w == 16) k_opt_screen_tiles<16><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
+        else if (tile_w == 32) k_opt_screen_tiles<32><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
+        else return cudaErrorInvalidValue;
+    }
     else if (route == 2) k_opt_screen<0, 1><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
     else k_opt_screen<1><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
     return cudaGetLastError();

@@ -40,7 +40,9 @@ class Options(ctypes.Structure):
                 ("max_pivots", ctypes.c_int), ("degen_switch", ctypes.c_int),
                 ("tol_piv32", ctypes.c_double), ("tol_dj32", ctypes.c_double), ("margin_z", ctypes.c_double),
                 ("margin_beta", ctypes.c_double), ("margin_t", ctypes.c_double), ("margin_licq", ctypes.c_double),
-                ("tol_zero_row", ctypes.c_double), ("lp2_screen", ctypes.c_int)]
+                ("tol_zero_row", ctypes.c_double), ("lp2_screen", ctypes.c_int),
+                ("tile_w", ctypes.c_int), ("feas_warps", ctypes.c_int), ("feas_chunk", ctypes.c_int),
+                ("autotune", ctypes.c_int)]
 
 
 class OptSet(ctypes.Structure):
@@ -64,7 +66,8 @@ class BatchResult(ctypes.Structure):
                 ("overflow", ctypes.c_int), ("device_ms", ctypes.c_double),
                 ("inst", ctypes.POINTER(InstStats)), ("n_opt", ctypes.c_longlong), ("opt", ctypes.POINTER(OptSet)),
                 ("n_rec", ctypes.c_longlong), ("rec", ctypes.c_void_p), ("h2d_bytes", ctypes.c_longlong),
-                ("d2h_bytes", ctypes.c_longlong)]
+                ("d2h_bytes", ctypes.c_longlong), ("tile_w", ctypes.c_int), ("feas_warps", ctypes.c_int),
+                ("feas_chunk", ctypes.c_int), ("tuned", ctypes.c_int)]
 
 
 class GPUResults(ctypes.Structure):
@@ -208,6 +211,7 @@ class Result:
     rec: np.ndarray | None    # structured records (record=1)
     h2d_bytes: int = 0
     d2h_bytes: int = 0
+    settings: dict | None = None   # launch settings of the run (tile_w, feas_warps, feas_chunk, tuned)
 
     @property
     def candidates(self) -> int:
@@ -240,7 +244,8 @@ def _convert(rp) -> Result:
         nrec = r.n_rec
         buf = (ctypes.c_char * (nrec * REC_DTYPE.itemsize)).from_address(r.rec)
         rec = np.frombuffer(buf, dtype=REC_DTYPE).copy()
-    return Result(r.status, r.device_ms, r.n_levels, r.overflow, inst, opt, rec, r.h2d_bytes, r.d2h_bytes)
+    settings = dict(tile_w=r.tile_w, feas_warps=r.feas_warps, feas_chunk=r.feas_chunk, tuned=r.tuned)
+    return Result(r.status, r.device_ms, r.n_levels, r.overflow, inst, opt, rec, r.h2d_bytes, r.d2h_bytes, settings)
 
 
 def solve(probs, precision: int = FP64, k_min: int = 0, k_max=None, budget=0, **opts) -> Result:
