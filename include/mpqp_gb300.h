@@ -28,7 +28,12 @@ extern "C" {
  * GPUResults (main.py:12-22); the rest are appended, so a caller that maps
  * only the prefix keeps working.
  *   n_batches        number of enumeration levels that were run
- *   n_splits         number of device launches of the LP kernels
+ *   n_splits         1 + the levels that did not fit device memory whole:
+ *                    the LP1 tableaus of their feasible sets are kept while
+ *                    the arena has room, and the children of the others
+ *                    start LP1 from the root tableau (the reference splits
+ *                    such a level into n_splits chunks, batched_simplex.cu:
+ *                    1141-1158; verdicts are the same either way)
  *   n_feasible_lps   candidate active sets found feasible (LP1)
  *   n_final_lps      candidate active sets found optimal (LP2); their sets
  *                    are in active_sets, row-major n_final_lps x n_x,
@@ -70,8 +75,10 @@ typedef struct GPUResults {
  * A2, xb2  LP2 standard form, M2 x N2 column-major and M2 (main.py:102-118)
  * b2, non_b2  LP2 initial basis / non-basis (main.py:123-128)
  * k_min, k_max  cardinality range of the active sets to report
- * extra_batches, reserved_memory  accepted for compatibility; reserved_memory
- *          (MiB) is left free on the device.
+ * extra_batches  accepted for compatibility (levels split by themselves)
+ * reserved_memory  MiB left free on the device when the call sizes its
+ *          buffers (the environment variable MPQP_ARENA_BYTES caps the LP1
+ *          tableau arena in bytes).
  * The problem data are read back from A1/xb1/A2/xb2; the LP layouts are
  * validated and a malformed input returns a result with status != 0.  Every
  * failure is such a result; NULL only when the host cannot allocate even
@@ -203,6 +210,9 @@ typedef struct {
      * their live tableau rows, basis ids and node records) and the stored
      * child tableaus with their ids */
     long long lp1_parents, lp1_parent_bytes, lp1_store_bytes;
+    /* LP1 solves started from the root tableau because the parent's tableau
+     * did not fit the arena, and the feasible sets kept without a tableau */
+    long long lp1_cold, nodes_without_tableau;
 } mpqp_inst_stats;
 
 typedef struct {
@@ -223,6 +233,9 @@ typedef struct {
     long long d2h_bytes;          /* result bytes copied back               */
     int tile_w, feas_warps, feas_chunk; /* the launch settings of the run    */
     int tuned;                    /* 1: chosen by the autotuner             */
+    int split_levels;             /* levels whose feasible sets did not all
+                                     keep an LP1 tableau (arena full)       */
+    int pad_;
 } mpqp_batch_result;
 
 void mpqp_default_options(mpqp_options *opt);

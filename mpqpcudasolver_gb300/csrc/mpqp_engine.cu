@@ -1212,12 +1212,14 @@ static int plan_results_impl(mpqp_plan *P, mpqp_batch_result *&R, bool *complete
         s.fallback_opt = ic[i].fb_opt; s.stored = ic[i].stored;
         s.lp1_certified = ic[i].cert_lp1; s.lp1_cert_missed = ic[i].cert_miss; s.lp1_cert_freevar = ic[i].cert_free;
         s.lp1_parents = ic[i].parents; s.lp1_parent_bytes = ic[i].par_bytes; s.lp1_store_bytes = ic[i].store_bytes;
+        s.lp1_cold = ic[i].lp1_cold; s.nodes_without_tableau = ic[i].no_tab;
         s.feasible_digest = ic[i].feas_digest; s.optimal_digest = ic[i].opt_digest;
         s.region_digest = ic[i].reg_digest;
         s.last_level = ic[i].last_level; s.truncated = ic[i].truncated;
         nlev = std::max(nlev, ic[i].last_level + 1);
     }
     R->n_levels = nlev;
+    R->split_levels = (int)ctl.split_levels;
     long long nopt = std::min(ctl.n_opt, P->B.opt_cap);
     std::vector<OptRec> ov(nopt);
     if (nopt) CK(cudaMemcpy(ov.data(), P->B.opt, sizeof(OptRec) * nopt, cudaMemcpyDeviceToHost));
@@ -1540,6 +1542,10 @@ static GPUResults *mpqp_impl(const double *AxT, int n_c, int n_x, int n_t, int k
     // one run: launched without a graph, with an event before every launch,
     // so that the device time splits into its LP1 and optimality phases
     o.use_graph = 0;
+    // MPQP_ARENA_BYTES: a cap on the LP1 tableau arena (levels beyond it are
+    // split: see n_splits)
+    const char *ab = getenv("MPQP_ARENA_BYTES");
+    if (ab && atoll(ab) > 0) o.arena_bytes = atoll(ab);
     if (reserved_memory > 0) {
         size_t fb = 0, tb = 0;
         if (cudaMemGetInfo(&fb, &tb) == cudaSuccess) {
@@ -1569,7 +1575,9 @@ static GPUResults *mpqp_impl(const double *AxT, int n_c, int n_x, int n_t, int k
     long long nsel = 0;
     for (long long i = 0; i < nf; i++) if (R->opt[i].level >= kmin) nsel++;
     G->n_batches = R->n_levels;
-    G->n_splits = 1;
+    // 1 + the levels whose feasible sets did not all keep an LP1 tableau in
+    // the arena (their children's LP1 started from the root instead)
+    G->n_splits = 1 + R->split_levels;
     G->n_feasible_lps = (int)R->inst[0].feasible;
     G->n_final_lps = (int)nsel;
     G->time_GPU = R->device_ms * 1e-3;

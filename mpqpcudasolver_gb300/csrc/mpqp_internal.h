@@ -137,6 +137,8 @@ struct InstCtl {
     long long cert_lp1;         // FP32 LP1 optima certified infeasible by the FP64 dual bound
     long long cert_miss;        // ... that the certificate could not prove (sent to the FP64 re-solve)
     long long cert_free;        // ... of those, the misses with a free variable nonbasic (no square system)
+    long long lp1_cold;         // LP1 solves started from the root (the parent kept no tableau)
+    long long no_tab;           // nodes kept without a tableau (the arena was full)
     long long stored;           // LP1 tableaus written for the next level
     // LP1 bytes for the roofline: the distinct parents of each checked level
     // (live tableau rows, basis ids and node, each parent once) and the
@@ -170,6 +172,11 @@ struct Ctl {
     int epoch;                  // run counter; hash tags are (epoch << 8) | level
     int pad;
     long long hcap[2];          // slots of the hash in use per side (a power of 2 <= hash_cap)
+    // 1 once a side's tableau (or ids) arena had no room for a reservation:
+    // later nodes of that level keep no tableau, and their children start
+    // LP1 from the root tableau (the arena's overflow is not an error)
+    int tab_full[2];
+    long long split_levels;     // levels whose parents did not all keep a tableau
 };
 
 // OV_WAIT: a bounded wait for a bulk copy ran out (the launch's results are void)

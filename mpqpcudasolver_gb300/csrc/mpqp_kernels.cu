@@ -812,20 +812,19 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
         // candidate's index)
         idx = pre_idx >= 0 ? pre_idx : (long long)atomicAdd((unsigned long long *)&ctl->n_node[side], 1ull);
         if (idx >= B.node_cap) { atomicOr(&ctl->overflow, OV_NODE); idx = -1; }
-        if (need_tab && idx >= 0) {
+        if (need_tab && idx >= 0 && !*((volatile int *)&ctl->tab_full[side])) {
             const long long told = (long long)atomicAdd((unsigned long long *)&ctl->tab_used[side], (unsigned long long)I.tab_elems);
             const long long iold = (long long)atomicAdd((unsigned long long *)&ctl->ids_used[side], (unsigned long long)I.ids_bytes);
-            toff = side == 0 ? told : B.tab_cap - told - I.tab_elems;
-            ioff = side == 0 ? iold : B.ids_cap - iold - I.ids_bytes;
-            bool bad = false;
-            if (told + I.tab_elems + ctl->tab_used[side ^ 1] > B.tab_cap) { atomicOr(&ctl->overflow, OV_TAB); bad = true; }
-            if (iold + I.ids_bytes + ctl->ids_used[side ^ 1] > B.ids_cap) { atomicOr(&ctl->overflow, OV_IDS); bad = true; }
-            if (bad) {
-                // keep the slot harmless: no tableau, never expanded or evaluated
-                Node nd;
-                nd.lo = lo; nd.hi = hi; nd.inst = inst; nd.flags = 0; nd.tab_off = -1; nd.ids_off = -1; nd.rec = -1;
-                B.node[side][idx] = nd;
-                idx = -1;
+            if (told + I.tab_elems + ctl->tab_used[side ^ 1] > B.tab_cap ||
+                iold + I.ids_bytes + ctl->ids_used[side ^ 1] > B.ids_cap) {
+                // the arena is full: this node and the later ones of the level
+                // keep no tableau (a reservation past the end is abandoned, so
+                // the used counts only overstate); their children start from
+                // the root tableau
+                atomicExch(&ctl->tab_full[side], 1);
+            } else {
+                toff = side == 0 ? told : B.tab_cap - told - I.tab_elems;
+                ioff = side == 0 ? iold : B.ids_cap - iold - I.ids_bytes;
             }
         }
     }
@@ -833,6 +832,22 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
     toff = __shfl_sync(FULLMASK, toff, 0);
     ioff = __shfl_sync(FULLMASK, ioff, 0);
     if (idx < 0) return -1;
+    if (need_tab && toff < 0) {
+        // a node without a tableau (still in the hash: the subset test needs it)
+        if (lane == 0) {
+            atomicAdd((unsigned long long *)&B.ictl[inst].no_tab, 1ull);
+            Node nd;
+            nd.lo = lo; nd.hi = hi; nd.inst = inst;
+            nd.flags = NODE_VALID | (feasible ? NODE_FEASIBLE : 0) | (extra_flags & ~NODE_CERT);
+            nd.tab_off = -1; nd.ids_off = -1; nd.rec = rec;
+            B.node[side][idx] = nd;
+            if (feasible && !B.exhaustive) {
+                if (!hash_insert(B.hash[side], hcap, (ctl->epoch << 8) | level, inst, lo, hi, (int)idx))
+                    atomicOr(&ctl->overflow, OV_HASH);
+            }
+        }
+        return idx;
+    }
     if (need_tab) {
         if (lane == 0) {
             // the bytes the store moves: the live rows and objective row (bulk,
@@ -904,6 +919,45 @@ __device__ __noinline__ void queue_undecided_lp1(const DevBuffers &B, int w, con
     if (qi < B.q_cap) B.q_lp1[qi] = w; else atomicOr(&ctl->overflow, OV_QUEUE);
 }
 
+// LP1 of S' = S u {j} started from the root tableau (all slacks basic) when
+// the parent kept no tableau: the root copied into the warp's slot (after
+// the previous child's bulk store has read it), the root basis ids, and the
+// objective sum_{i in S'} w_i as the sum of those slacks' rows.  Not
+// inlined: the rare path keeps its registers out of the LP1 kernel's loop.
+template <typename T>
+__device__ __forceinline__ void cold_stage_lp1_body(const DevBuffers &B, const InstDesc &I, int inst, T *tab,
+                                                    uint8_t *ids, uint64_t lo, uint64_t hi, int j)
+{
+    const int lane = lane_id();
+    const int M1 = I.M1, nv = I.nv, ld = I.ld1;
+    if (lane == 0) {
+        bulk_wait_read();
+        atomicAdd((unsigned long long *)&B.ictl[inst].lp1_cold, 1ull);
+    }
+    __syncwarp();
+    warp_copy_v<T>(tab, pool_of<T>(B) + root_off<T>(I), I.tab_elems);
+    uint8_t *bid = ids, *nid = ids + M1;
+    for (int i = lane; i < M1; i += 32) bid[i] = (uint8_t)(nv + i);
+    for (int c = lane; c < nv; c += 32) nid[c] = (uint8_t)c;
+    __syncwarp();
+    T *obj = tab + (size_t)M1 * ld;
+    if (j < 64) lo |= 1ull << j; else hi |= 1ull << (j - 64);
+    while (lo | hi) {
+        int i;
+        if (lo) { i = __ffsll((long long)lo) - 1; lo &= lo - 1; }
+        else { i = 64 + __ffsll((long long)hi) - 1; hi &= hi - 1; }
+        const T *row = tab + (size_t)i * ld;
+        for (int cc = lane; cc <= nv; cc += 32) obj[cc] = xadd(obj[cc], row[cc]);
+        __syncwarp();
+    }
+}
+
+__device__ __noinline__ void cold_stage_lp1_f32(const DevBuffers &B, const InstDesc &I, int inst, float *tab,
+                                                uint8_t *ids, uint64_t lo, uint64_t hi, int j)
+{
+    cold_stage_lp1_body<float>(B, I, inst, tab, ids, lo, hi, j);
+}
+
 // ---------------------------------------------------------------------
 // K2: LP1 feasibility, warm-started from the parent
 // ---------------------------------------------------------------------
@@ -969,7 +1023,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
             if (lane < cnt) {
                 const Node &pn = B.node[pside][mine.parent];
                 const InstDesc &Il = B.inst[pn.inst];
-                if ((pn.flags & NODE_CERT) && level == Il.k_max) {
+                if ((pn.flags & NODE_CERT) && pn.ids_off >= 0 && level == Il.k_max) {
                     const uint8_t *pnid = B.ids[pside] + pn.ids_off + Il.M1;
                     const int want = Il.nv + mine.j;
                     for (int cc = 0; cc < Il.nv; cc++) q |= (int)pnid[cc] == want;
@@ -1028,14 +1082,21 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
             continue;
         }
         const int M1 = I.M1, nv = I.nv, ld = I.ld1;
+        // a parent kept without a tableau (the arena was full): the child
+        // starts from the root tableau (all slacks basic) instead
+        const bool cold = par.tab_off < 0;
         // the parent's live rows (FP32 tableaus drop the rows of basic free
         // variables; the objective row follows the live rows)
-        const int prows = node_rows(par.flags, M1);
+        const int prows = cold ? M1 : node_rows(par.flags, M1);
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (cold) {
+            if constexpr (sizeof(T) == 4) cold_stage_lp1_f32(B, I, inst, tab, ids, par.lo, par.hi, c.j);
+            else cold_stage_lp1_body<T>(B, I, inst, tab, ids, par.lo, par.hi, c.j);
+        } else {
         // stage the parent tableau and basis: one bulk copy each, completing
         // on the warp's mbarrier (this warp's earlier accesses to the slot,
         // and the bulk store of the previous child, come first)
-        fence_proxy_async_smem();
-        __syncwarp();
         if (lane == 0) {
             bulk_wait_read();
             const unsigned tb = mixed ? (unsigned)((prows + 1) * ld * sizeof(T)) : (unsigned)(I.tab_elems * sizeof(T));
@@ -1051,18 +1112,21 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
             break;
         }
         parity ^= 1u;
+        }
         uint8_t *bid = ids, *nid = ids + M1;
         T *obj = tab + (size_t)prows * ld;
-        // objective += w_j
-        const int wid = nv + c.j;
-        int rho = -1;
-        for (int i = lane; i < prows; i += 32) if (bid[i] == wid) rho = i;
-        rho = __reduce_max_sync(FULLMASK, rho);
-        if (rho >= 0) {
-            const T *row = tab + (size_t)rho * ld;
-            for (int cc = lane; cc <= nv; cc += 32) obj[cc] = xadd(obj[cc], row[cc]);
-        } else {
-            for (int cc = lane; cc < nv; cc += 32) if (nid[cc] == wid) obj[cc] = obj[cc] - T(1);
+        if (!cold) {
+            // objective += w_j
+            const int wid = nv + c.j;
+            int rho = -1;
+            for (int i = lane; i < prows; i += 32) if (bid[i] == wid) rho = i;
+            rho = __reduce_max_sync(FULLMASK, rho);
+            if (rho >= 0) {
+                const T *row = tab + (size_t)rho * ld;
+                for (int cc = lane; cc <= nv; cc += 32) obj[cc] = xadd(obj[cc], row[cc]);
+            } else {
+                for (int cc = lane; cc < nv; cc += 32) if (nid[cc] == wid) obj[cc] = obj[cc] - T(1);
+            }
         }
         __syncwarp();
         Lp<T> L{tab, ld, prows, nv, nv, bid, nid};
@@ -3135,10 +3199,12 @@ __global__ void k_finalize(DevBuffers B, int level)
         if (B.rec) ctl->rec_base += ctl->n_cand;
         ctl->hcap[level & 1] = hash_cap_for(B, ctl->n_cand);   // what this level's inserts used
         ctl->n_cand = 0;
+        if (ctl->tab_full[level & 1]) ctl->split_levels++;   // this level's children partly without a tableau
         if (level > 0) {
             ctl->n_node[pside] = 0;
             ctl->tab_used[pside] = 0;
             ctl->ids_used[pside] = 0;
+            ctl->tab_full[pside] = 0;
         }
         for (int c = 0; c < kCtlCounters; c++) ctl->ctr[c] = 0;
         ctl->n_q_lp1 = 0;

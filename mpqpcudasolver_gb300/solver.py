@@ -58,7 +58,8 @@ class InstStats(ctypes.Structure):
         [(nm, ctypes.c_ulonglong) for nm in ("feasible_digest", "optimal_digest", "region_digest")] + \
         [("last_level", ctypes.c_int), ("truncated", ctypes.c_int)] + \
         [(nm, ctypes.c_longlong) for nm in ("lp1_certified", "lp1_cert_missed", "lp1_cert_freevar", "lp1_parents",
-                                            "lp1_parent_bytes", "lp1_store_bytes")]
+                                            "lp1_parent_bytes", "lp1_store_bytes", "lp1_cold",
+                                            "nodes_without_tableau")]
 
 
 class BatchResult(ctypes.Structure):
@@ -67,7 +68,8 @@ class BatchResult(ctypes.Structure):
                 ("inst", ctypes.POINTER(InstStats)), ("n_opt", ctypes.c_longlong), ("opt", ctypes.POINTER(OptSet)),
                 ("n_rec", ctypes.c_longlong), ("rec", ctypes.c_void_p), ("h2d_bytes", ctypes.c_longlong),
                 ("d2h_bytes", ctypes.c_longlong), ("tile_w", ctypes.c_int), ("feas_warps", ctypes.c_int),
-                ("feas_chunk", ctypes.c_int), ("tuned", ctypes.c_int)]
+                ("feas_chunk", ctypes.c_int), ("tuned", ctypes.c_int), ("split_levels", ctypes.c_int),
+                ("pad_", ctypes.c_int)]
 
 
 class GPUResults(ctypes.Structure):
@@ -212,6 +214,7 @@ class Result:
     h2d_bytes: int = 0
     d2h_bytes: int = 0
     settings: dict | None = None   # launch settings of the run (tile_w, feas_warps, feas_chunk, tuned)
+    split_levels: int = 0          # levels whose feasible sets did not all keep an LP1 tableau
 
     @property
     def candidates(self) -> int:
@@ -225,7 +228,8 @@ _INST_DTYPE = np.dtype([(f[0], "<i8") for f in InstStats._fields_[:11]] +
                        [("feasible_digest", "<u8"), ("optimal_digest", "<u8"), ("region_digest", "<u8"),
                         ("last_level", "<i4"), ("truncated", "<i4"), ("lp1_certified", "<i8"),
                         ("lp1_cert_missed", "<i8"), ("lp1_cert_freevar", "<i8"), ("lp1_parents", "<i8"),
-                        ("lp1_parent_bytes", "<i8"), ("lp1_store_bytes", "<i8")])
+                        ("lp1_parent_bytes", "<i8"), ("lp1_store_bytes", "<i8"), ("lp1_cold", "<i8"),
+                        ("nodes_without_tableau", "<i8")])
 _OPT_DTYPE = np.dtype([("mask_lo", "<u8"), ("mask_hi", "<u8"), ("inst", "<i4"), ("level", "<i4"), ("t", "<f8"),
                        ("r", "<f8"), ("region", "<i4"), ("fp64", "<i4"), ("rec", "<i8"), ("err", "<f8")])
 assert _INST_DTYPE.itemsize == ctypes.sizeof(InstStats)
@@ -245,7 +249,8 @@ def _convert(rp) -> Result:
         buf = (ctypes.c_char * (nrec * REC_DTYPE.itemsize)).from_address(r.rec)
         rec = np.frombuffer(buf, dtype=REC_DTYPE).copy()
     settings = dict(tile_w=r.tile_w, feas_warps=r.feas_warps, feas_chunk=r.feas_chunk, tuned=r.tuned)
-    return Result(r.status, r.device_ms, r.n_levels, r.overflow, inst, opt, rec, r.h2d_bytes, r.d2h_bytes, settings)
+    return Result(r.status, r.device_ms, r.n_levels, r.overflow, inst, opt, rec, r.h2d_bytes, r.d2h_bytes, settings,
+                  r.split_levels)
 
 
 def solve(probs, precision: int = FP64, k_min: int = 0, k_max=None, budget=0, **opts) -> Result:
