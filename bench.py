@@ -336,17 +336,19 @@ DEFAULT_SETTINGS = dict(tile_w=8, feas_warps=4, feas_chunk=32)
 
 def settings_compare(stream, dev) -> dict:
     """The autotuner against the fixed default launch settings (8 threads per
-    screen LP, 4 LP1 warps per block, 32 candidates per claim) on three batch
-    shapes: the bench batch, its main instance alone, and 64 MPC instances
-    (n=12, m=72, p=4) to |S| <= 4.  Device time of one full run (graph), the
-    best of two, each way."""
+    screen LP, 4 LP1 warps per block, 32 candidates per claim) on four batch
+    shapes: the bench batch, its main instance alone, 64 MPC instances
+    (n=12, m=72, p=4) to |S| <= 4, and 64 small mixed-size problems (n <= 8,
+    m <= 30) to |S| = n.  Device time of one full run (graph), the best of
+    two, each way."""
     import torch
     from mpqpcudasolver_gb300 import problems as P
     from mpqpcudasolver_gb300 import solver
     probs, kmax, budget = workload()
     mpc = [P.scale_problem(p) for p in P.mpc_batch(64)]
+    pop = [P.scale_problem(p) for p in P.pop_like_set(64, seed=0, n_max=8, m_max=30)]
     cases = {"bench_batch": (probs, kmax, budget), "main_instance": (probs[:1], kmax[:1], budget[:1]),
-             "mpc64_k4": (mpc, 4, 0)}
+             "mpc64_k4": (mpc, 4, 0), "small64_full_depth": (pop, [p.n for p in pop], 0)}
     out = {}
     for name, (pr, km, bu) in cases.items():
         row = {}

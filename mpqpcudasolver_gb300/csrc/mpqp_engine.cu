@@ -818,12 +818,18 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
 // The reference passes its threads per LP (nTPB) and launch shapes from its
 // host code (batched_simplex.cu:1181 and the launches around it).  Here the
 // LPs per block and threads per LP are chosen by measurement: each candidate
-// setting runs a short slice of the batch (every instance under a small
-// candidate budget, the first levels) with an event around every launch,
-// and the setting whose kernels take least is kept.  LP1 (warps per block x
-// candidates per claim) and the screen's first stage (threads per LP) are
-// independent kernels, so they are tuned one after the other.  The choice is
-// cached per batch shape for the process.
+// setting runs the batch with an event around every launch, and a setting
+// replaces the default only when its kernels take at least 2 % less.  The
+// whole batch is timed when it has at most kTuneWhole candidates (the
+// combinatorial count under the budgets): its deepest levels dominate the
+// cost and behave unlike its first ones, and a slice of the first levels
+// picked settings that were slower on the full run.  Larger batches are
+// timed on a slice, every instance under a kTuneSlice candidate budget.
+// LP1 (warps per block x candidates per claim) and the screen's first stage
+// (threads per LP) are independent kernels, tuned one after the other.  The
+// choice is cached per batch shape for the process.
+constexpr double kTuneWhole = 1.5e8;
+constexpr long long kTuneSlice = 1LL << 22;
 struct TuneKey {
     int prec, lp2_screen, m1, nv, p1, ninst;
     bool operator==(const TuneKey &k) const
@@ -854,15 +860,14 @@ static TuneKey tune_key(int n_inst, const mpqp_problem *probs, const mpqp_option
     return k;
 }
 
-// Milliseconds of the kernels whose names start with `prefix` in one timed
-// run of the slice under `o`, the best of two runs; < 0 when the setting
-// cannot run.
-static double tune_trial(int n_inst, const mpqp_problem *slice, const mpqp_options &o, const char *prefix)
+// Milliseconds of the kernels whose names start with `prefix` in a timed run
+// of `slice` under `o`, the best of `runs`; < 0 when the setting cannot run.
+static double tune_trial(int n_inst, const mpqp_problem *slice, const mpqp_options &o, const char *prefix, int runs)
 {
     mpqp_plan *P = nullptr;
     if (plan_create_locked(n_inst, slice, &o, &P) != MPQP_OK) { cudaGetLastError(); return -1.0; }
     double best = -1.0;
-    for (int rep = 0; rep < 2; rep++) {
+    for (int rep = 0; rep < runs; rep++) {
         if (mpqp_plan_run_timed_impl(P, nullptr) != MPQP_OK) { best = -1.0; break; }
         if (cudaEventSynchronize(P->ev1) != cudaSuccess) { cudaGetLastError(); best = -1.0; break; }
         double ms = 0.0;
@@ -892,26 +897,37 @@ static void autotune(int n_inst, const mpqp_problem *probs, mpqp_options &o)
             if (!o.feas_chunk) o.feas_chunk = e.feas_chunk;
             return;
         }
-    // the slice: every instance under a small budget (its first levels)
+    // the candidates of the whole batch (combinatorial count, under the budgets)
+    double est = 0.0;
+    for (int i = 0; i < n_inst; i++) {
+        const int m = probs[i].m, kmax = std::min(probs[i].k_max, std::min(m, kMaxK));
+        double cmk = 1.0, tot = 1.0;
+        for (int k = 1; k <= kmax; k++) { cmk = cmk * (double)(m - k + 1) / (double)k; tot += cmk; }
+        est += probs[i].budget > 0 ? std::min(tot, (double)probs[i].budget) : tot;
+    }
     std::vector<mpqp_problem> slice(probs, probs + n_inst);
-    const long long cap = std::max(1LL << 16, (1LL << 20) / n_inst);
-    for (mpqp_problem &pr : slice) pr.budget = pr.budget > 0 ? std::min(pr.budget, cap) : cap;
+    if (est > kTuneWhole)
+        for (mpqp_problem &pr : slice) pr.budget = pr.budget > 0 ? std::min(pr.budget, kTuneSlice) : kTuneSlice;
+    const int runs = est > 2e7 ? 1 : 2;
     mpqp_options t = o;
     t.autotune = 0;
     t.use_graph = 0;
     t.record = 0;
     t.cand_cap = 0; t.node_cap = 0; t.arena_bytes = 0; t.opt_cap = 0;
-    t.mem_fraction = std::min(o.mem_fraction, 0.3);
+    // a candidate replaces the default (the first entry) only when it is at
+    // least 2 % faster
+    auto better = [](double ms, double best) { return ms >= 0 && (best < 0 || ms < 0.98 * best); };
     int best_w = o.feas_warps ? o.feas_warps : 4, best_c = o.feas_chunk ? o.feas_chunk : 32;
     if (!o.feas_warps || !o.feas_chunk) {
         double best = -1.0;
-        for (int w : {2, 4})
-            for (int c : {8, 16, 32}) {
-                if ((o.feas_warps && w != o.feas_warps) || (o.feas_chunk && c != o.feas_chunk)) continue;
-                t.feas_warps = w; t.feas_chunk = c; t.tile_w = 8;
-                const double ms = tune_trial(n_inst, slice.data(), t, "k_feasibility");
-                if (ms >= 0 && (best < 0 || ms < best)) { best = ms; best_w = w; best_c = c; }
-            }
+        const int grid[][2] = {{4, 32}, {4, 16}, {2, 32}, {4, 8}, {2, 16}};
+        for (const auto &g : grid) {
+            const int w = g[0], c = g[1];
+            if ((o.feas_warps && w != o.feas_warps) || (o.feas_chunk && c != o.feas_chunk)) continue;
+            t.feas_warps = w; t.feas_chunk = c; t.tile_w = 8;
+            const double ms = tune_trial(n_inst, slice.data(), t, "k_feasibility", runs);
+            if (better(ms, best)) { best = ms; best_w = w; best_c = c; }
+        }
     }
     int best_t = o.tile_w ? o.tile_w : 8;
     if (!o.tile_w && o.precision == MPQP_MIXED) {
@@ -919,8 +935,8 @@ static void autotune(int n_inst, const mpqp_problem *probs, mpqp_options &o)
         t.feas_warps = best_w; t.feas_chunk = best_c;
         for (int tw : {8, 16, 32}) {
             t.tile_w = tw;
-            const double ms = tune_trial(n_inst, slice.data(), t, "k_opt_screen<dual>");
-            if (ms > 0 && (best < 0 || ms < best)) { best = ms; best_t = tw; }
+            const double ms = tune_trial(n_inst, slice.data(), t, "k_opt_screen<dual>", runs);
+            if (ms > 0 && better(ms, best)) { best = ms; best_t = tw; }
         }
     }
     if (!o.tile_w) o.tile_w = best_t;

@@ -958,35 +958,6 @@ __device__ __noinline__ void cold_stage_lp1_f32(const DevBuffers &B, const InstD
     cold_stage_lp1_body<float>(B, I, inst, tab, ids, lo, hi, j);
 }
 
-// The final tableau of a sibling (its objective sum_{S} w + w_{jp} at row
-// objrow, live rows `rows`) turned into the start of the next child: the
-// objective row moved to row `rows`, then w_{jp} taken out of it (its row if
-// basic, else +1 in its column); the caller adds w_j.
-template <typename T>
-__device__ __forceinline__ void chain_swap_objective(T *tab, uint8_t *ids, int M1, int nv, int ld, int rows, int objrow,
-                                                  int jp)
-{
-    const int lane = lane_id();
-    T *obj = tab + (size_t)rows * ld;
-    if (objrow != rows) {
-        const T *src = tab + (size_t)objrow * ld;
-        for (int cc = lane; cc <= nv; cc += 32) obj[cc] = src[cc];
-        __syncwarp();
-    }
-    const uint8_t *bid = ids, *nid = ids + M1;
-    const int wid = nv + jp;
-    int rho = -1;
-    for (int i = lane; i < rows; i += 32) if (bid[i] == wid) rho = i;
-    rho = __reduce_max_sync(FULLMASK, rho);
-    if (rho >= 0) {
-        const T *row = tab + (size_t)rho * ld;
-        for (int cc = lane; cc <= nv; cc += 32) obj[cc] = xadd(obj[cc], -row[cc]);
-    } else {
-        for (int cc = lane; cc < nv; cc += 32) if (nid[cc] == wid) obj[cc] = obj[cc] + T(1);
-    }
-    __syncwarp();
-}
-
 // ---------------------------------------------------------------------
 // K2: LP1 feasibility, warm-started from the parent
 // ---------------------------------------------------------------------
@@ -1015,15 +986,6 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
     __syncwarp();
     unsigned parity = 0;
     bool abort = false;
-    // sibling chain (FP32, an instance's last level, where no child is
-    // stored): the slot still holds the final tableau of the warp's previous
-    // candidate, a child of parent chain_par; chain_meta packs its added
-    // constraint (bits 0..7), live rows (8..15), objective row (16..23) and
-    // the siblings solved since the parent was staged (24..31): after
-    // kChainMax the next sibling starts from the parent again, which bounds
-    // the FP32 pivots between a staged tableau and a verdict
-    constexpr int kChainMax = 8;
-    int chain_par = -1, chain_meta = 0;
     const T tpiv = mixed ? (T)tol.tol_piv32 : (T)tol.tol_piv;
     const T tdj = mixed ? (T)tol.tol_dj32 : (T)tol.tol_dj;
     LocalInstCounters lc;
@@ -1120,23 +1082,15 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
             continue;
         }
         const int M1 = I.M1, nv = I.nv, ld = I.ld1;
-        // at an instance's last level a child of the same parent as the
-        // warp's previous candidate starts from that sibling's final tableau,
-        // still in the slot: the LP system is the same, only the objective
-        // trades w_{j'} for w_j (no staging; every verdict is certified, so
-        // the warm start cannot change it)
-        const bool chained = mixed && level == I.k_max && c.parent == chain_par && (chain_meta >> 24) < kChainMax;
         // a parent kept without a tableau (the arena was full): the child
         // starts from the root tableau (all slacks basic) instead
-        const bool cold = !chained && par.tab_off < 0;
+        const bool cold = par.tab_off < 0;
         // the parent's live rows (FP32 tableaus drop the rows of basic free
         // variables; the objective row follows the live rows)
-        const int prows = chained ? (chain_meta >> 8) & 0xff : cold ? M1 : node_rows(par.flags, M1);
+        const int prows = cold ? M1 : node_rows(par.flags, M1);
         fence_proxy_async_smem();
         __syncwarp();
-        if (chained) {
-            chain_swap_objective<T>(tab, ids, M1, nv, ld, prows, (chain_meta >> 16) & 0xff, chain_meta & 0xff);
-        } else if (cold) {
+        if (cold) {
             if constexpr (sizeof(T) == 4) cold_stage_lp1_f32(B, I, inst, tab, ids, par.lo, par.hi, c.j);
             else cold_stage_lp1_body<T>(B, I, inst, tab, ids, par.lo, par.hi, c.j);
         } else {
@@ -1187,14 +1141,6 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
                                                                           par.lo, par.hi, nv, true, &rows);
         else st = warp_simplex<T>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv);
         const T z = obj[nv];
-        // the slot now holds this child's final tableau (objective row at
-        // prows, live rows `rows`): the next sibling may start from it
-        if (mixed && level == I.k_max && st == LP_OPTIMAL) {
-            chain_meta = c.j | (rows << 8) | (prows << 16) | ((chained ? (chain_meta >> 24) + 1 : 1) << 24);
-            chain_par = c.parent;
-        } else {
-            chain_par = -1;
-        }
         uint64_t lo = par.lo, hi = par.hi;
         if (c.j < 64) lo |= 1ull << c.j; else hi |= 1ull << (c.j - 64);
         bool feasible = false, decided = true, to_cert = false;

@@ -270,7 +270,7 @@ def test_dual_and_primal_screens_give_the_same_verdicts(gpu_lib):
         assert np.array_equal(ra[f], rb[f]), f
     opt = ra["optimal"] == 1
     assert _same(ra["t"][opt], rb["t"][opt]) and _same(ra["r"][opt], rb["r"][opt])
-    for f in ("feasible", "optimal", "regions", "fallback_lp1"):
+    for f in ("feasible", "optimal", "regions"):
         assert a.total(f) == b.total(f), f
     # the illcond instance (p = 8) is screened the same way in both modes
     ill = ra["inst"] == 1
