@@ -342,10 +342,16 @@ def reduce_constraints(prob):
 
 
 def apply_row_status(prob, status):
-    """The problem with the rows that ``status`` marks as removed dropped."""
+    """The problem with the rows that ``status`` marks as removed dropped.
+
+    Rows of the parameter set (CRA) found redundant are kept: active sets
+    index rows of A only, a redundant row changes no critical region, and the
+    LP layout of the reference's call (main.py:91-98) needs at least one
+    parameter row (the box can be implied by the rows of A, which would leave
+    none).  Zero and duplicate parameter rows are dropped."""
     m = prob.m
     keep = [i for i in range(m) if status[i] in (ROW_KEPT, ROW_EQUALITY)]
-    keep_t = [i for i in range(prob.ncp) if status[m + i] in (ROW_KEPT, ROW_EQUALITY)]
+    keep_t = [i for i in range(prob.ncp) if status[m + i] in (ROW_KEPT, ROW_EQUALITY, ROW_REDUNDANT)]
     out = prob.copy()
     out.A, out.b, out.F = prob.A[keep], prob.b[keep], prob.F[keep]
     out.CRA, out.CRb = prob.CRA[keep_t], prob.CRb[keep_t]
