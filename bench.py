@@ -332,6 +332,49 @@ def mplp_measure(prec, stream, dev, steps: int = 3) -> dict:
 
 
 DEFAULT_SETTINGS = dict(tile_w=8, feas_warps=4, feas_chunk=32)
+CFG2_BUDGET = 1 << 25      # config 2 (n=10, m=43, p=4) to |S| = 10: the levels that fit this many candidates
+CFG5_BUDGET = 1 << 21      # config 5 (64 MPC instances) to |S| = n: per instance
+
+
+def other_configs(stream, dev) -> dict:
+    """The other two GPU configurations of the metric's family, timed in both
+    precisions on device-resident plans (CUDA events, one warm and one timed
+    run each way), with the regions compared:
+    * config 2: the n=10, m=43, p=4 instance, enumerated toward |S| = 10 with
+      superset pruning; the levels that fit 2^25 candidates are checked;
+    * config 5: 64 condensed MPC instances (seeds 0..63, n=12, m=72, p=4),
+      each to |S| = n under a 2^21-candidate budget."""
+    import torch
+    from mpqpcudasolver_gb300 import problems as P
+    from mpqpcudasolver_gb300 import solver
+    cases = {"config2_n10_m43_p4": ([P.scale_problem(P.random_n10_m43_p4())], 10, CFG2_BUDGET),
+             "config5_mpc64": ([P.scale_problem(p) for p in P.mpc_batch(64)], 12, CFG5_BUDGET)}
+    out = {}
+    for name, (probs, kmax, bud) in cases.items():
+        row = {}
+        res = {}
+        for prec, tag in ((solver.MIXED, "mixed"), (solver.FP64, "fp64")):
+            plan = solver.Plan(probs, precision=prec, k_max=kmax, budget=bud, mem_fraction=0.85)
+            plan.run(stream.cuda_stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            plan.run(stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            r = plan.results()
+            plan.close()
+            ms = e0.elapsed_time(e1)
+            res[tag] = r
+            row[tag] = {"ms": ms, "value": r.candidates / (ms / 1e3), "unit": UNIT}
+        a, b = res["mixed"], res["fp64"]
+        row["candidates"] = a.candidates
+        row["deepest_level"] = int(a.inst["last_level"].max())
+        row["truncated_instances"] = int(a.inst["truncated"].sum())
+        row["regions"] = a.total("regions")
+        row["regions_identical"] = same_regions(a, b)
+        row["speedup_mixed_vs_fp64"] = row["mixed"]["value"] / row["fp64"]["value"]
+        out[name] = row
+    return out
 
 
 def settings_compare(stream, dev) -> dict:
@@ -517,6 +560,7 @@ def run_ours(args):
     cb = cpu_baseline(steps=1)
     mplp = None if args.skip_mplp else mplp_measure(prec, stream, dev)
     tune_cmp = None if (args.skip_tune_compare or prec != solver.MIXED) else settings_compare(stream, dev)
+    others = None if args.skip_configs else other_configs(stream, dev)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -535,6 +579,10 @@ def run_ours(args):
                       "what": "per optimal set: one FP64 refinement step of its KKT solve, relative to the law"},
         "screen": screen_info,
         "launch_settings": settings,
+        "other_configs": {k: {"mixed": v["mixed"]["value"], "fp64": v["fp64"]["value"], "unit": UNIT,
+                              "candidates": v["candidates"], "deepest_level": v["deepest_level"],
+                              "regions_identical": v["regions_identical"]} for k, v in others.items()}
+        if others else None,
         "autotune_vs_default": {k: {"default_ms": v["default"]["ms"], "tuned_ms": v["tuned"]["ms"],
                                     "tuned": v["tuned"]["settings"], "speedup": v["speedup"],
                                     "same_regions": v["same_regions"]} for k, v in tune_cmp.items()}
@@ -559,6 +607,8 @@ def run_ours(args):
         "lp1_parents": res.total("lp1_parents"), "lp1_parent_bytes": res.total("lp1_parent_bytes"),
         "lp1_store_bytes": res.total("lp1_store_bytes"),
         "mplp": mplp,
+        "other_configs": others,
+        "autotune_vs_default": tune_cmp,
     }
     try:
         with open(DETAIL_FILE, "w") as f:
@@ -579,6 +629,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-mplp", action="store_true", help="leave out the mpLP (Q = 0) measurement")
+    ap.add_argument("--skip-configs", action="store_true", help="leave out configs 2 and 5")
     ap.add_argument("--skip-tune-compare", action="store_true",
                     help="leave out the autotuned-vs-default launch settings comparison")
     args = ap.parse_args()
