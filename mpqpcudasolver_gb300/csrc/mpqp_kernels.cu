@@ -644,10 +644,27 @@ __global__ void k_enumerate(DevBuffers B, int level)
         const int cnt = npar - p0 < 32 ? (int)(npar - p0) : 32;
         // lane t: whether parent p0 + t is expanded at this level
         bool expand = false;
+        unsigned sbytes = 0;   // the bytes the LP1 kernel stored for this node (tableau rows and ids)
+        int sinst = -1;
         if (lane < cnt) {
             const Node pn = B.node[pside][p0 + lane];
             expand = (pn.flags & NODE_VALID) && (B.exhaustive || (pn.flags & NODE_FEASIBLE)) &&
                      !B.ictl[pn.inst].stopped && level <= B.inst[pn.inst].k_max;
+            if ((pn.flags & NODE_VALID) && pn.tab_off >= 0) {
+                const InstDesc &Ip = B.inst[pn.inst];
+                const int rows = es == 4 ? node_rows(pn.flags, Ip.M1) : Ip.M1;
+                sbytes = (unsigned)((rows + 1) * Ip.ld1 * es + Ip.ids_bytes);
+                sinst = pn.inst;
+            }
+        }
+        {
+            // counted here, once per stored node, rather than by the LP1
+            // kernel's store (an atomic per store there contends): one
+            // atomic per instance present among these 32 nodes
+            const unsigned grp = __match_any_sync(FULLMASK, sinst);
+            const unsigned tot = __reduce_add_sync(grp, sbytes);
+            if (sinst >= 0 && lane == __ffs(grp) - 1)
+                atomicAdd((unsigned long long *)&B.ictl[sinst].store_bytes, (unsigned long long)tot);
         }
         unsigned todo = __ballot_sync(FULLMASK, expand);
     while (todo) {
@@ -849,14 +866,7 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
         return idx;
     }
     if (need_tab) {
-        if (lane == 0) {
-            // the bytes the store moves: the live rows and objective row (bulk,
-            // rows_store >= 0) or the whole tableau, and the basis ids
-            const long long tb = rows_store >= 0 ? (long long)(rows_store + 1) * I.ld1 : (long long)I.tab_elems;
-            atomicAdd((unsigned long long *)&B.ictl[inst].stored, 1ull);
-            atomicAdd((unsigned long long *)&B.ictl[inst].store_bytes,
-                      (unsigned long long)(tb * (long long)sizeof(TT) + I.ids_bytes));
-        }
+        if (lane == 0) atomicAdd((unsigned long long *)&B.ictl[inst].stored, 1ull);
         TT *dst = (TT *)B.tab[side] + toff;
         if (bulk) {
             fence_proxy_async_smem();
