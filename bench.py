@@ -416,6 +416,45 @@ def settings_compare(stream, dev) -> dict:
     return out
 
 
+def basis_sharing_compare(stream, dev) -> dict:
+    """LP2 basis sharing (lp2_warm=1: the first-stage dual LP of each set
+    starts from its parent's final basis) against the default single-row
+    start, on the bench batch: device time of a full run and of the screen's
+    first stage (best of two runs each way), first-stage iterations per LP,
+    the LPs offered a valid parent basis and those that started from it, and
+    the regions compared."""
+    import torch
+    from mpqpcudasolver_gb300 import solver
+    probs, kmax, budget = workload()
+    out = {}
+    regs = {}
+    for how, extra in (("default", {}), ("shared", dict(lp2_warm=1))):
+        plan = solver.Plan(probs, precision=solver.MIXED, k_max=kmax, budget=budget, mem_fraction=0.85,
+                           **DEFAULT_SETTINGS, **extra)
+        plan.run(stream.cuda_stream)
+        best, stage0 = None, None
+        for _ in range(2):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            plan.run(stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            best = e0.elapsed_time(e1) if best is None else min(best, e0.elapsed_time(e1))
+            plan.run_timed()
+            st = plan.kernel_times().get("k_opt_screen<dual>", (0.0, 0))[0]
+            stage0 = st if stage0 is None else min(stage0, st)
+        r = plan.results()
+        plan.close()
+        lps = r.total("lp2_first_stage_lps")
+        out[how] = {"ms": best, "first_stage_ms": stage0, "first_stage_lps": lps,
+                    "iterations_per_lp": r.total("lp2_first_stage_pivots") / max(lps, 1),
+                    "offered": r.total("lp2_warm_offered"), "started": r.total("lp2_warm_started")}
+        regs[how] = r
+    out["regions_identical"] = same_regions(regs["default"], regs["shared"])
+    out["speedup"] = out["default"]["ms"] / out["shared"]["ms"]
+    return out
+
+
 def run_reference(args):
     world, rank, local, dist = dist_setup(args.gpus)
     if rank != 0:
@@ -561,6 +600,7 @@ def run_ours(args):
     mplp = None if args.skip_mplp else mplp_measure(prec, stream, dev)
     tune_cmp = None if (args.skip_tune_compare or prec != solver.MIXED) else settings_compare(stream, dev)
     others = None if args.skip_configs else other_configs(stream, dev)
+    warm_cmp = None if (args.skip_tune_compare or prec != solver.MIXED) else basis_sharing_compare(stream, dev)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -587,6 +627,15 @@ def run_ours(args):
                                     "tuned": v["tuned"]["settings"], "speedup": v["speedup"],
                                     "same_regions": v["same_regions"]} for k, v in tune_cmp.items()}
         if tune_cmp else None,
+        "lp2_basis_sharing": {"default_ms": warm_cmp["default"]["ms"], "shared_ms": warm_cmp["shared"]["ms"],
+                              "first_stage_ms": [warm_cmp["default"]["first_stage_ms"],
+                                                 warm_cmp["shared"]["first_stage_ms"]],
+                              "iterations_per_lp": [warm_cmp["default"]["iterations_per_lp"],
+                                                    warm_cmp["shared"]["iterations_per_lp"]],
+                              "started_share": warm_cmp["shared"]["started"]
+                              / max(warm_cmp["shared"]["first_stage_lps"], 1),
+                              "regions_identical": warm_cmp["regions_identical"]}
+        if warm_cmp else None,
         "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "single_core")},
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "mpqp_solve_batch (C ABI): host arrays in, plan + upload + run + download + free"},
@@ -609,6 +658,7 @@ def run_ours(args):
         "mplp": mplp,
         "other_configs": others,
         "autotune_vs_default": tune_cmp,
+        "lp2_basis_sharing": warm_cmp,
     }
     try:
         with open(DETAIL_FILE, "w") as f:

@@ -170,6 +170,14 @@ typedef struct {
      * same verdicts. */
     int tile_w, feas_warps, feas_chunk;
     int autotune;
+    /* lp2_warm = 1 (MPQP_MIXED): LP2 basis sharing, the reference's
+     * copy_basis_dual_1/2 (batched_simplex.cu:525-590).  The first stage of
+     * the dual screen starts each set's LP from its parent set's final basis
+     * (S minus its largest element), inverted on the device; a singular or
+     * infeasible basis falls back to the usual single-row start.  Off by
+     * default: slower on the measured workloads (the verdicts are the same
+     * either way). */
+    int lp2_warm;
 } mpqp_options;
 
 /* One optimal active set */
@@ -213,6 +221,10 @@ typedef struct {
     /* LP1 solves started from the root tableau because the parent's tableau
      * did not fit the arena, and the feasible sets kept without a tableau */
     long long lp1_cold, nodes_without_tableau;
+    /* the first stage of the dual screen (mixed precision): LPs run and
+     * their iterations; with lp2_warm, the LPs offered a valid parent basis
+     * and those that started from it */
+    long long lp2_first_stage_lps, lp2_first_stage_pivots, lp2_warm_offered, lp2_warm_started;
 } mpqp_inst_stats;
 
 typedef struct {

@@ -569,6 +569,11 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
         delete P;
         return MPQP_EINVAL;
     }
+    if (o.lp2_warm != 0 && o.lp2_warm != 1) {
+        set_err("lp2_warm must be 0 or 1");
+        delete P;
+        return MPQP_EINVAL;
+    }
     if (o.tile_w) P->tile_w = o.tile_w;
     if (o.feas_warps) P->feas_warps = o.feas_warps;
     if (o.feas_chunk) P->feas_chunk = o.feas_chunk;
@@ -684,7 +689,8 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
     if (arena_bytes <= 0) {
         const double used = (double)cand_cap * 12 + (double)node_cap * (2 * sizeof(Node) + 4) +
                             (double)hash_cap * 2 * sizeof(HashSlot) +
-                            (P->prec == PREC_MIXED ? (double)cand_cap / 8 * 48 : 0.0);   // certificate queue
+                            (P->prec == PREC_MIXED ? (double)cand_cap / 8 * 48 : 0.0) +  // certificate queue
+                            (o.lp2_warm && P->prec == PREC_MIXED ? 16.0 * (double)node_cap : 0.0);   // LP2 bases
         arena_bytes = (long long)std::max(usable - used, (double)(64 << 20));
         if (all_budget) {
             // parents of the deepest checked level hold at most the budget
@@ -740,6 +746,10 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
     AL(B.cert_q, (size_t)B.cert_stride * B.cert_cap);
     AL(B.opt, sizeof(OptRec) * opt_cap);
     if (rec_cap) AL(B.rec, sizeof(CandRec) * rec_cap);
+    if (o.lp2_warm && P->prec == PREC_MIXED) {
+        AL(B.lp2b[0], sizeof(unsigned long long) * node_cap);
+        AL(B.lp2b[1], sizeof(unsigned long long) * node_cap);
+    }
     AL(B.ictl, sizeof(InstCtl) * n_inst);
     AL(B.ctl, sizeof(Ctl));
 #undef AL
@@ -751,6 +761,10 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
     CK(cudaMemset(B.hash[0], 0xff, sizeof(HashSlot) * hash_cap));
     CK(cudaMemset(B.hash[1], 0xff, sizeof(HashSlot) * hash_cap));
     CK(cudaMemset(B.ctl, 0, sizeof(Ctl)));
+    if (B.lp2b[0]) {
+        CK(cudaMemset(B.lp2b[0], 0xff, sizeof(unsigned long long) * node_cap));
+        CK(cudaMemset(B.lp2b[1], 0xff, sizeof(unsigned long long) * node_cap));
+    }
     // kernel geometry
     P->smem_feas = (size_t)P->feas_warps * feas_smem_per_warp(P->prec == PREC_MIXED ? 4 : 8, sd);
     P->smem_lp1fb = 4 * lp1_smem_per_warp(8, sd);
@@ -776,10 +790,15 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
                   : grid_for(kernel_ptr("opt64"), P->smem_opt, &P->grid_opt)) ||
         (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_primal"), P->smem_opt2, &P->grid_opt2, 32) : 0) ||
         (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_dual_rows"), P->smem_opt, &P->grid_opt3, 32) : 0) ||
-        (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr(P->tile_w == 8 ? "screen_dual_tiles8"
-                                                          : P->tile_w == 16 ? "screen_dual_tiles16"
-                                                                            : "screen_dual_tiles32"),
-                                               P->smem_tiles, &P->grid_tiles, 32) : 0) ||
+        (rc = P->prec == PREC_MIXED
+                  ? grid_for(kernel_ptr(P->B.lp2b[0] ? (P->tile_w == 8 ? "screen_dual_tiles8w"
+                                                       : P->tile_w == 16 ? "screen_dual_tiles16w"
+                                                                         : "screen_dual_tiles32w")
+                                                    : (P->tile_w == 8 ? "screen_dual_tiles8"
+                                                       : P->tile_w == 16 ? "screen_dual_tiles16"
+                                                                         : "screen_dual_tiles32")),
+                             P->smem_tiles, &P->grid_tiles, 32)
+                  : 0) ||
         (rc = grid_for(kernel_ptr("opt_fp64"), P->smem_optfb, &P->grid_optfb)) ||
         (rc = P->has_lp && P->prec != PREC_MIXED ? grid_for(kernel_ptr("opt64_lp"), P->smem_opt, &P->grid_opt_lp) : 0) ||
         (rc = P->has_lp ? grid_for(kernel_ptr("opt_fp64_lp"), P->smem_optfb, &P->grid_optfb_lp) : 0)) {
@@ -1229,6 +1248,8 @@ static int plan_results_impl(mpqp_plan *P, mpqp_batch_result *&R, bool *complete
         s.lp1_certified = ic[i].cert_lp1; s.lp1_cert_missed = ic[i].cert_miss; s.lp1_cert_freevar = ic[i].cert_free;
         s.lp1_parents = ic[i].parents; s.lp1_parent_bytes = ic[i].par_bytes; s.lp1_store_bytes = ic[i].store_bytes;
         s.lp1_cold = ic[i].lp1_cold; s.nodes_without_tableau = ic[i].no_tab;
+        s.lp2_first_stage_lps = ic[i].s0_lps; s.lp2_first_stage_pivots = ic[i].s0_piv;
+        s.lp2_warm_offered = ic[i].warm_try; s.lp2_warm_started = ic[i].warm_used;
         s.feasible_digest = ic[i].feas_digest; s.optimal_digest = ic[i].opt_digest;
         s.region_digest = ic[i].reg_digest;
         s.last_level = ic[i].last_level; s.truncated = ic[i].truncated;

@@ -145,6 +145,10 @@ struct InstCtl {
     // stored children (their live rows and ids); lvl_*: the current level,
     // added when the level is checked (within the budget)
     long long lvl_parents, parents, lvl_par_bytes, par_bytes, store_bytes;
+    // first stage of the dual screen: LPs run and their iterations; with
+    // LP2 basis sharing, the LPs offered the parent's final basis and those
+    // that started from it
+    long long s0_lps, s0_piv, warm_try, warm_used;
     // order-independent digests (sum mod 2^64 of a 64-bit hash of each mask)
     unsigned long long feas_digest, opt_digest, reg_digest;
     int stopped;                // budget exhausted or max level reached
@@ -218,6 +222,8 @@ struct DevBuffers {
     long long opt_cap;
     CandRec *rec;               // may be null
     long long rec_cap;
+    unsigned long long *lp2b[2]; // LP2 basis sharing (may be null): per node, the final basis of its
+                                 // first-stage dual LP (p + 1 row numbers, 0xff past them or none)
     InstCtl *ictl;
     Ctl *ctl;
     int exhaustive;             // 1: every combination is a candidate (no pruning)

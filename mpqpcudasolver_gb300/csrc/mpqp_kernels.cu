@@ -2616,10 +2616,23 @@ __device__ int kkt_factor_tile(const ScreenTile<W> &t, const KktData<float> &D, 
 
 // lp2_dual_screen with the lanes of a tile: rows r = lane + W s, basis rows
 // in lanes 0..p.  Same pricing, ratio test, pivot and verified bound.
-template <int W>
+// WARM: the LP may start from the final basis of the parent set's LP
+// (`warm`, p + 1 row numbers of the parent's layout, 0xff = none), the
+// reference's basis sharing between sets at Hamming distance one
+// (batched_simplex.cu:525-590).  The set S u {j} has j above every element
+// of S, so the parent's multiplier rows keep their numbers and its box rows
+// move down one.  The basis matrix is inverted in the tile (Gauss-Jordan with
+// partial pivoting); a singular or primal-infeasible basis falls back to the
+// single-row start, as the reference resets to its initial basis.  *warm_out:
+// 0 no basis offered, 1 offered and rejected, 2 started from it; *basis_out:
+// this LP's final basis (8 bytes, 0xff past p + 1).
+constexpr float kWarmPivMin = 1e-7f;
+
+template <int W, bool WARM = false>
 __device__ int lp2_dual_screen_tile(const ScreenTile<W> &t, const float *T, int m, int R2, int p, const float *blo,
                                     const float *bhi, float thr, float ethr, float tol_piv, float tol_dj, int max_it,
-                                    int degen_switch, int *it_out, float *bound_out)
+                                    int degen_switch, int *it_out, float *bound_out, const uint8_t *warm = nullptr,
+                                    unsigned long long *basis_out = nullptr, int *warm_out = nullptr)
 {
     constexpr int NR = (kTileRows + W - 1) / W;
     constexpr int MP = kDualMaxP;
@@ -2634,6 +2647,87 @@ __device__ int lp2_dual_screen_tile(const ScreenTile<W> &t, const float *T, int 
     float lo[MP], hi[MP];
 #pragma unroll
     for (int c = 0; c < MP; c++) { lo[c] = c < p ? blo[c] : 0.0f; hi[c] = c < p ? bhi[c] : 0.0f; }
+    float binv[MP], pi[MP], binvp = 0.0f, y = 0.0f, pip = 0.0f;
+    int bidx = -1;
+    unsigned basic = 0;
+    bool warm_ok = false;
+    if constexpr (WARM) {
+        int wb = -1;
+        if (warm && lane < P1) {
+            const int r = warm[lane];
+            wb = r == 0xff ? -1 : (r < m - 1 ? r : r + 1);
+        }
+        bool ok = t.all(lane >= P1 || (wb >= 0 && wb < R2));
+        if (warm_out) *warm_out = warm ? (ok ? 1 : 0) : 0;
+        if (warm && ok) {
+            // lane e < P1: equation e of [B | I] (e < p: the g column e of the
+            // basic rows, e = p: their c column)
+            const int col = lane < p ? lane : 6;
+            float Bv[MP + 1], Iv[MP + 1];
+#pragma unroll
+            for (int i = 0; i <= MP; i++) {
+                const int bi = t.shfl(wb, i < P1 ? i : 0);
+                Bv[i] = (i < P1 && lane < P1) ? T[bi * LD + col] : 0.0f;
+                Iv[i] = i == lane ? 1.0f : 0.0f;
+            }
+            bool used = lane >= P1;
+            int src = 0;
+#pragma unroll
+            for (int i = 0; i <= MP; i++) {
+                if (i < P1 && ok) {
+                    const unsigned key = used ? 0xffffffffu : ~__float_as_uint(fabsf(Bv[i]));
+                    const int pl = tile_argmin<W>(t, key, (unsigned)lane, lane);   // -1: column i all zero
+                    const float pv = t.shfl(Bv[i], pl < 0 ? 0 : pl);
+                    if (pl < 0 || !(fabsf(pv) > kWarmPivMin)) ok = false;
+                    else {
+                        const float inv = __fdividef(1.0f, pv);
+                        const float f = lane == pl ? 0.0f : Bv[i] * inv;
+#pragma unroll
+                        for (int c = 0; c <= MP; c++) {
+                            const float rb = t.shfl(Bv[c], pl), ri = t.shfl(Iv[c], pl);
+                            Bv[c] = lane == pl ? rb * inv : __fmaf_rn(-f, rb, Bv[c]);
+                            Iv[c] = lane == pl ? ri * inv : __fmaf_rn(-f, ri, Iv[c]);
+                        }
+                        if (lane == pl) used = true;
+                        if (lane == i) src = pl;
+                    }
+                }
+            }
+            if (ok) {
+                // lane i: row i of B^-1 (the row of the lane that pivoted column i)
+#pragma unroll
+                for (int c = 0; c < MP; c++) {
+                    const float v = t.shfl(Iv[c], src);
+                    binv[c] = (lane < P1 && c < p) ? v : 0.0f;
+                }
+                float vp = 0.0f;
+#pragma unroll
+                for (int c = 0; c <= MP; c++) { const float v = t.shfl(Iv[c], src); if (c == p) vp = v; }
+                binvp = lane < P1 ? vp : 0.0f;
+                y = binvp;
+                ok = t.all(lane >= P1 || y >= 0.0f);
+            }
+            if (ok) {
+                bidx = lane < P1 ? wb : -1;
+                const float hb = lane < P1 ? T[wb * LD + 7] : 0.0f;
+#pragma unroll
+                for (int c = 0; c < MP; c++) pi[c] = tile_sum<W>(t, hb * binv[c]);
+                pip = tile_sum<W>(t, hb * binvp);
+#pragma unroll
+                for (int i = 0; i <= MP; i++) {
+                    const int bi = t.shfl(wb, i < P1 ? i : 0);
+                    if (i < P1 && lane == (bi & (W - 1))) basic |= 1u << (bi / W);
+                }
+                warm_ok = true;
+                if (warm_out) *warm_out = 2;
+            } else {
+                binvp = 0.0f; y = 0.0f;
+#pragma unroll
+                for (int c = 0; c < MP; c++) binv[c] = 0.0f;
+            }
+        }
+    }
+    if (!warm_ok) {
     unsigned bkey = 0xffffffffu;
     int bi = -1;
     for (int r = lane; r < m; r += W) {
@@ -2648,9 +2742,7 @@ __device__ int lp2_dual_screen_tile(const ScreenTile<W> &t, const float *T, int 
     const int istar = tile_argmin<W>(t, bkey, (unsigned)bi, bi);
     float gi[8];
     row8(istar, gi);
-    float binv[MP], pi[MP], binvp = 0.0f, y = 0.0f;
-    float pip = gi[7];
-    int bidx = -1;
+    pip = gi[7];
 #pragma unroll
     for (int c = 0; c < MP; c++) {
         binv[c] = 0.0f;
@@ -2666,7 +2758,6 @@ __device__ int lp2_dual_screen_tile(const ScreenTile<W> &t, const float *T, int 
         }
     }
     if (lane == 0) { bidx = istar; y = 1.0f; binvp = 1.0f; }
-    unsigned basic = 0;
 #pragma unroll 1
     for (int s = 0; s < NR; s++) {
         const int r = lane + W * s;
@@ -2674,6 +2765,7 @@ __device__ int lp2_dual_screen_tile(const ScreenTile<W> &t, const float *T, int 
         if (r >= m && r < m + p) b = !(T[istar * LD + (r - m)] > 0.0f);
         else if (r >= m + p && r < m + 2 * p) b = T[istar * LD + (r - m - p)] > 0.0f;
         if (b) basic |= 1u << s;
+    }
     }
     float reach = 0.0f;
 #pragma unroll
@@ -2768,14 +2860,25 @@ __device__ int lp2_dual_screen_tile(const ScreenTile<W> &t, const float *T, int 
     }
     *it_out = it;
     *bound_out = bound;
+    if constexpr (WARM) {
+        unsigned long long word = ~0ull;
+#pragma unroll
+        for (int i = 0; i <= MP; i++) {
+            const int b = t.shfl(bidx, i);
+            if (i < P1) word = (word & ~(0xffull << (8 * i))) | ((unsigned long long)(b & 0xff) << (8 * i));
+        }
+        if (basis_out) *basis_out = word;
+    }
     return proven;
 }
 
 // Stage 0 of the dual route, one set per tile (32 / W per warp): KKT factor,
 // the multiplier rows and the box, dual bound; the sets it cannot settle go
 // to stage 1 (k_opt_screen<0, 1>), a failed KKT margin to the FP64 queue.
-template <int W>
-__global__ void __launch_bounds__(32, 32) k_opt_screen_tiles(DevBuffers B, Tol tol, SlotDims sd, int level, int mode)
+// WARM: the dual LP starts from the parent set's final basis when that basis
+// is valid for this set (B.lp2b; the parent of node x is candidate x's).
+template <int W, bool WARM = false>
+__global__ void __launch_bounds__(32, WARM ? 24 : 32) k_opt_screen_tiles(DevBuffers B, Tol tol, SlotDims sd, int level, int mode)
 {
     static_assert(W >= kDualMaxP + 1 && W <= 32 && (W & (W - 1)) == 0, "tile width");
     extern __shared__ __align__(16) unsigned char smem[];
@@ -2800,6 +2903,12 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen_tiles(DevBuffers B, Tol t
     auto flush = [&]() {
         if (lc.inst >= 0 && lane == 0) {
             atomicAdd((unsigned long long *)&B.ictl[lc.inst].lp2_piv, (unsigned long long)lc.c);
+            atomicAdd((unsigned long long *)&B.ictl[lc.inst].s0_lps, (unsigned long long)lc.d);
+            atomicAdd((unsigned long long *)&B.ictl[lc.inst].s0_piv, (unsigned long long)lc.c);
+            if (WARM) {
+                atomicAdd((unsigned long long *)&B.ictl[lc.inst].warm_try, (unsigned long long)lc.f);
+                atomicAdd((unsigned long long *)&B.ictl[lc.inst].warm_used, (unsigned long long)lc.g);
+            }
         }
     };
     for (;;) {
@@ -2807,6 +2916,7 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen_tiles(DevBuffers B, Tol t
         if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[3], 1ull);
         x = t.shfl(x, 0);
         if (x >= nn) break;
+        if (WARM && lane == 0) B.lp2b[side][x] = ~0ull;   // no basis unless this set's LP runs
         const Node nd = B.node[side][x];
         if ((nd.flags & (NODE_VALID | NODE_FEASIBLE)) != (NODE_VALID | NODE_FEASIBLE)) continue;
         const InstDesc &I = B.inst[nd.inst];
@@ -2849,10 +2959,24 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen_tiles(DevBuffers B, Tol t
                 // times the reach of theta inside the box
                 const float escale = __fdividef(1.0f + (float)p * bmax, rho);
                 t.sync();
-                proven = lp2_dual_screen_tile<W>(t, Tb, k, k + ncp, p, B.fpool + I.f_blo, B.fpool + I.f_bhi,
-                                              tol.margin_t32 * escale * amaxA, tol.margin_t32 * escale, tol.tol_piv32,
-                                              tol.tol_dj32, tol.max_pivots, tol.degen_switch, &piv, &bound);
+                const uint8_t *warm = nullptr;
+                if (WARM && level >= 1) {
+                    const int par = B.cand[x].parent;
+                    if (par >= 0) warm = reinterpret_cast<const uint8_t *>(B.lp2b[side ^ 1] + par);
+                }
+                unsigned long long bword = ~0ull;
+                int wst = 0;
+                proven = lp2_dual_screen_tile<W, WARM>(t, Tb, k, k + ncp, p, B.fpool + I.f_blo, B.fpool + I.f_bhi,
+                                                    tol.margin_t32 * escale * amaxA, tol.margin_t32 * escale,
+                                                    tol.tol_piv32, tol.tol_dj32, tol.max_pivots, tol.degen_switch,
+                                                    &piv, &bound, warm, &bword, &wst);
                 to_rows = !proven;
+                lc.d++;
+                if (WARM) {
+                    if (lane == 0) B.lp2b[side][x] = bword;
+                    lc.f += wst >= 1;
+                    lc.g += wst == 2;
+                }
                 t.sync();
             }
         }
@@ -3391,6 +3515,9 @@ const void *kernel_ptr(const char *name)
         {"screen_dual_tiles8", (const void *)k_opt_screen_tiles<8>},
         {"screen_dual_tiles16", (const void *)k_opt_screen_tiles<16>},
         {"screen_dual_tiles32", (const void *)k_opt_screen_tiles<32>},
+        {"screen_dual_tiles8w", (const void *)k_opt_screen_tiles<8, true>},
+        {"screen_dual_tiles16w", (const void *)k_opt_screen_tiles<16, true>},
+        {"screen_dual_tiles32w", (const void *)k_opt_screen_tiles<32, true>},
         {"screen_primal", (const void *)k_opt_screen<1>},
         {"level0_64", (const void *)k_level0<double>},
         {"level0_32", (const void *)k_level0<float>},
@@ -3451,7 +3578,12 @@ cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDim
 {
     // route 0: the dual route's first stage (tiles of tile_w threads), 2: its
     // second stage, 1: the primal route
-    if (route == 0) {
+    if (route == 0 && B.lp2b[0]) {
+        if (tile_w == 8) k_opt_screen_tiles<8, true><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
+        else if (tile_w == 16) k_opt_screen_tiles<16, true><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
+        else if (tile_w == 32) k_opt_screen_tiles<32, true><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
+        else return cudaErrorInvalidValue;
+    } else if (route == 0) {
         if (tile_w == 8) k_opt_screen_tiles<8><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
         else if (tile_w == 16) k_opt_screen_tiles<16><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
         else if (tile_w == 32) k_opt_screen_tiles<32><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);

@@ -42,7 +42,7 @@ class Options(ctypes.Structure):
                 ("margin_beta", ctypes.c_double), ("margin_t", ctypes.c_double), ("margin_licq", ctypes.c_double),
                 ("tol_zero_row", ctypes.c_double), ("lp2_screen", ctypes.c_int),
                 ("tile_w", ctypes.c_int), ("feas_warps", ctypes.c_int), ("feas_chunk", ctypes.c_int),
-                ("autotune", ctypes.c_int)]
+                ("autotune", ctypes.c_int), ("lp2_warm", ctypes.c_int)]
 
 
 class OptSet(ctypes.Structure):
@@ -59,7 +59,8 @@ class InstStats(ctypes.Structure):
         [("last_level", ctypes.c_int), ("truncated", ctypes.c_int)] + \
         [(nm, ctypes.c_longlong) for nm in ("lp1_certified", "lp1_cert_missed", "lp1_cert_freevar", "lp1_parents",
                                             "lp1_parent_bytes", "lp1_store_bytes", "lp1_cold",
-                                            "nodes_without_tableau")]
+                                            "nodes_without_tableau", "lp2_first_stage_lps",
+                                            "lp2_first_stage_pivots", "lp2_warm_offered", "lp2_warm_started")]
 
 
 class BatchResult(ctypes.Structure):
@@ -229,7 +230,9 @@ _INST_DTYPE = np.dtype([(f[0], "<i8") for f in InstStats._fields_[:11]] +
                         ("last_level", "<i4"), ("truncated", "<i4"), ("lp1_certified", "<i8"),
                         ("lp1_cert_missed", "<i8"), ("lp1_cert_freevar", "<i8"), ("lp1_parents", "<i8"),
                         ("lp1_parent_bytes", "<i8"), ("lp1_store_bytes", "<i8"), ("lp1_cold", "<i8"),
-                        ("nodes_without_tableau", "<i8")])
+                        ("nodes_without_tableau", "<i8"), ("lp2_first_stage_lps", "<i8"),
+                        ("lp2_first_stage_pivots", "<i8"), ("lp2_warm_offered", "<i8"),
+                        ("lp2_warm_started", "<i8")])
 _OPT_DTYPE = np.dtype([("mask_lo", "<u8"), ("mask_hi", "<u8"), ("inst", "<i4"), ("level", "<i4"), ("t", "<f8"),
                        ("r", "<f8"), ("region", "<i4"), ("fp64", "<i4"), ("rec", "<i8"), ("err", "<f8")])
 assert _INST_DTYPE.itemsize == ctypes.sizeof(InstStats)

@@ -119,6 +119,10 @@ def test_entry_points_reject_bad_arguments_before_any_device_work(lib):
     opts.lp2_screen = 7
     assert lib.mpqp_plan_create(1, ps.arr, ctypes.byref(opts), ctypes.byref(h)) == solver.EINVAL and not h.value
     assert "lp2_screen" in solver.last_error()
+    opts.lp2_screen = 0
+    opts.lp2_warm = 3
+    assert lib.mpqp_plan_create(1, ps.arr, ctypes.byref(opts), ctypes.byref(h)) == solver.EINVAL and not h.value
+    assert "lp2_warm" in solver.last_error()
     assert lib.mpqp_region_laws(None, 1, None, None, None) == solver.EINVAL
     assert lib.mpqp_region_laws(ps.arr, -1, None, None, None) == solver.EINVAL
     assert lib.mpqp_region_laws(ps.arr, 0, None, None, None) == solver.OK      # nothing to do
