@@ -96,6 +96,73 @@ static inline int odd_up(int x) { return (x & 1) ? x : x + 1; }
 // conflict-free for 128-bit shared-memory accesses
 static inline int four_mod8_up(int x) { int y = (x + 3) & ~3; return (y & 4) ? y : y + 4; }
 
+// The FP32 LP1 root.  From the origin (every slack basic, b >= 0), each
+// free variable (x, theta) is pivoted into the basis by a ratio test in the
+// direction whose blocking row has the larger pivot, so the basic solution
+// stays feasible; a free variable unbounded both ways stays nonbasic.  The
+// rows of basic free variables are dropped (they never leave the basis and
+// no later decision reads them) and the objective row follows the live rows.
+// Every FP32 LP1 solve descends from this root, so none carries rows of free
+// variables or prices a free column with a zero reduced cost.  root_f gets
+// the tableau (stride ld1, tab_elems) followed by the basis ids as numbers
+// (bid over M1, 255 past the live rows, then nid over nv); d.root_rows the
+// live rows.  Pivots in FP64: T_r /= T_rq (T_rq -> 1 / T_rq), then
+// T_i -= T_iq T_r (T_iq -> -T_iq / T_rq), the Tucker pivot of the kernels.
+static void prepivot_root_f(InstDesc &d, std::vector<double> &root_f)
+{
+    const int ld = d.ld1, nv = d.nv, M1 = d.M1;
+    std::vector<double> T(root_f.begin(), root_f.begin() + (size_t)(M1 + 1) * ld);
+    std::vector<int> bid(M1), nid(nv);
+    for (int i = 0; i < M1; i++) bid[i] = nv + i;
+    for (int j = 0; j < nv; j++) nid[j] = j;
+    for (int q = 0; q < nv; q++) {
+        double cmax = 0.0;
+        for (int i = 0; i < M1; i++) if (bid[i] >= nv) cmax = std::max(cmax, std::fabs(T[(size_t)i * ld + q]));
+        if (!(cmax > 0.0)) continue;
+        int r = -1;
+        double ra = 0.0;
+        for (int dir = 1; dir >= -1; dir -= 2) {
+            int rd = -1;
+            double rr = 0.0, rad = 0.0;
+            for (int i = 0; i < M1; i++) {
+                if (bid[i] < nv) continue;
+                const double a = dir * T[(size_t)i * ld + q];
+                if (!(a > 1e-9 * cmax)) continue;
+                const double ratio = std::max(T[(size_t)i * ld + nv], 0.0) / a;
+                if (rd < 0 || ratio < rr || (ratio == rr && a > rad)) { rd = i; rr = ratio; rad = a; }
+            }
+            if (rd >= 0 && rad > ra) { r = rd; ra = rad; }
+        }
+        if (r < 0) continue;
+        double *R = T.data() + (size_t)r * ld;
+        const double inv = 1.0 / R[q];
+        for (int j = 0; j <= nv; j++) if (j != q) R[j] *= inv;
+        R[q] = inv;
+        for (int i = 0; i <= M1; i++) {
+            if (i == r) continue;
+            double *Ti = T.data() + (size_t)i * ld;
+            const double f = Ti[q];
+            if (f == 0.0) continue;
+            for (int j = 0; j <= nv; j++) if (j != q) Ti[j] -= f * R[j];
+            Ti[q] = -f * inv;
+        }
+        std::swap(bid[r], nid[q]);
+    }
+    std::vector<double> out((size_t)d.tab_elems + M1 + nv, 0.0);
+    int rows = 0;
+    for (int i = 0; i < M1; i++) {
+        if (bid[i] < nv) continue;
+        for (int j = 0; j <= nv; j++) out[(size_t)rows * ld + j] = T[(size_t)i * ld + j];
+        out[(size_t)d.tab_elems + rows] = bid[i];
+        rows++;
+    }
+    for (int j = 0; j <= nv; j++) out[(size_t)rows * ld + j] = T[(size_t)M1 * ld + j];
+    for (int i = rows; i < M1; i++) out[(size_t)d.tab_elems + i] = 255;
+    for (int j = 0; j < nv; j++) out[(size_t)d.tab_elems + M1 + j] = nid[j];
+    root_f.swap(out);
+    d.root_rows = rows;
+}
+
 static void fwd_sub(const double *L, int n, const double *rhs, int rs, double *y, int ys)
 {
     for (int i = 0; i < n; i++) {
@@ -245,6 +312,7 @@ static int prepare_instance(const mpqp_problem &P, Prepared &out, int prec)
     };
     fill_root(out.root, d.ld1d);
     fill_root(out.root_f, d.ld1);
+    prepivot_root_f(d, out.root_f);
     // parameter box: row c reads s theta_c <= bt_c (s > 0), row p + c reads
     // s' theta_c <= bt_{p+c} (s' < 0), nothing else nonzero
     d.box = ncp == 2 * p;

@@ -76,7 +76,8 @@ struct InstDesc {
     int box;                    // 1: At = [diag(+); diag(-)] (rows c, then p + c), a box
     int lp;                     // 1: Q = 0 (mpLP)
     int ld2lp;                  // mpLP, |S| < n: FP64 LP2 row stride (>= p + n + 3, odd)
-    int pad_lp;
+    int root_rows;              // live rows of the FP32 LP1 root (its basis ids follow it in the
+                                // FP32 pool at f_root + tab_elems: bid over M1, then nid over nv)
 };
 
 struct Node {                   // a feasible (or, when exhaustive, any) active set

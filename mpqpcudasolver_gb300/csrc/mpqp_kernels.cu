@@ -947,17 +947,33 @@ __device__ __forceinline__ void cold_stage_lp1_body(const DevBuffers &B, const I
     __syncwarp();
     warp_copy_v<T>(tab, pool_of<T>(B) + root_off<T>(I), I.tab_elems);
     uint8_t *bid = ids, *nid = ids + M1;
-    for (int i = lane; i < M1; i += 32) bid[i] = (uint8_t)(nv + i);
-    for (int c = lane; c < nv; c += 32) nid[c] = (uint8_t)c;
+    int rows = M1;
+    if constexpr (sizeof(T) == 4) {
+        // the FP32 root (free variables basic, their rows dropped) and its ids
+        const float *rid = B.fpool + I.f_root + I.tab_elems;
+        for (int i = lane; i < M1 + nv; i += 32) ids[i] = (uint8_t)(int)rid[i];
+        rows = I.root_rows;
+    } else {
+        for (int i = lane; i < M1; i += 32) bid[i] = (uint8_t)(nv + i);
+        for (int c = lane; c < nv; c += 32) nid[c] = (uint8_t)c;
+    }
     __syncwarp();
-    T *obj = tab + (size_t)M1 * ld;
+    T *obj = tab + (size_t)rows * ld;
     if (j < 64) lo |= 1ull << j; else hi |= 1ull << (j - 64);
     while (lo | hi) {
         int i;
         if (lo) { i = __ffsll((long long)lo) - 1; lo &= lo - 1; }
         else { i = 64 + __ffsll((long long)hi) - 1; hi &= hi - 1; }
-        const T *row = tab + (size_t)i * ld;
-        for (int cc = lane; cc <= nv; cc += 32) obj[cc] = xadd(obj[cc], row[cc]);
+        // w_i basic: its row joins the objective; nonbasic: -1 in its column
+        int rho = -1;
+        for (int r = lane; r < rows; r += 32) if (bid[r] == nv + i) rho = r;
+        rho = __reduce_max_sync(FULLMASK, rho);
+        if (rho >= 0) {
+            const T *row = tab + (size_t)rho * ld;
+            for (int cc = lane; cc <= nv; cc += 32) obj[cc] = xadd(obj[cc], row[cc]);
+        } else {
+            for (int cc = lane; cc < nv; cc += 32) if (nid[cc] == nv + i) obj[cc] = obj[cc] - T(1);
+        }
         __syncwarp();
     }
 }
@@ -1097,7 +1113,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         const bool cold = par.tab_off < 0;
         // the parent's live rows (FP32 tableaus drop the rows of basic free
         // variables; the objective row follows the live rows)
-        const int prows = cold ? M1 : node_rows(par.flags, M1);
+        const int prows = cold ? (mixed ? I.root_rows : M1) : node_rows(par.flags, M1);
         fence_proxy_async_smem();
         __syncwarp();
         if (cold) {
@@ -1406,11 +1422,13 @@ __global__ void __launch_bounds__(128) k_lp1_cert(DevBuffers B, Tol tol, SlotDim
         const Node par = B.node[pside][c.parent];
         const int inst = par.inst;
         const InstDesc &I = B.inst[inst];
-        const int nv = I.nv, ld = I.ld1d, ldf = I.ld1;
+        const int nv = I.nv, ld = I.ld1d;
         uint64_t lo = par.lo, hi = par.hi;
         if (c.j < 64) lo |= 1ull << c.j; else hi |= 1ull << (c.j - 64);
+        // the constraint rows: the FP64 root tableau (its FP32 copy, rounded
+        // here, feeds the LU; the FP32 LP1 root is pre-pivoted and does not
+        // hold them)
         const double *G = B.dpool + I.o_root;
-        const float *Gf = B.fpool + I.f_root;
         // lane cc < nv: the slack nonbasic in column cc (negative: a free variable)
         const int nb = lane < nv ? (int)e[4 + lane] - nv : 0;
         const bool all_slack = __all_sync(FULLMASK, nb >= 0) && nv <= nvm;
@@ -1421,7 +1439,7 @@ __global__ void __launch_bounds__(128) k_lp1_cert(DevBuffers B, Tol tol, SlotDim
             // the basic slacks i of S' of G[i][v]; by = their beta_i (y_i = 1)
             for (int cc = 0; cc < nv; cc++) {
                 const int i = __shfl_sync(FULLMASK, nb, cc);
-                if (lane < nv) { Mdr[cc] = G[(size_t)i * ld + lane]; Mfr[cc] = Gf[(size_t)i * ldf + lane]; }
+                if (lane < nv) { Mdr[cc] = G[(size_t)i * ld + lane]; Mfr[cc] = (float)Mdr[cc]; }
             }
             double rhs = 0.0, by = 0.0;
             uint64_t rl = lo, rh = hi;
@@ -3252,11 +3270,19 @@ __global__ void k_level0(DevBuffers B)
     const T *src = pool_of<T>(B) + root_off<T>(I);
     warp_copy_v<T>(dst, src, I.tab_elems);
     uint8_t *ids = B.ids[0] + ioff;
-    for (int i = lane; i < I.M1; i += 32) ids[i] = (uint8_t)(I.nv + i);
-    for (int j = lane; j < I.nv; j += 32) ids[I.M1 + j] = (uint8_t)j;
+    if constexpr (sizeof(T) == 4) {
+        // the FP32 root has its free variables basic (their rows dropped);
+        // its basis ids follow the tableau in the pool
+        const float *rid = B.fpool + I.f_root + I.tab_elems;
+        for (int i = lane; i < I.M1 + I.nv; i += 32) ids[i] = (uint8_t)(int)rid[i];
+    } else {
+        for (int i = lane; i < I.M1; i += 32) ids[i] = (uint8_t)(I.nv + i);
+        for (int j = lane; j < I.nv; j += 32) ids[I.M1 + j] = (uint8_t)j;
+    }
     if (lane == 0) {
         Node nd;
-        nd.lo = 0; nd.hi = 0; nd.inst = inst; nd.flags = NODE_VALID | NODE_FEASIBLE; nd.tab_off = toff; nd.ids_off = ioff;
+        nd.lo = 0; nd.hi = 0; nd.inst = inst; nd.tab_off = toff; nd.ids_off = ioff;
+        nd.flags = NODE_VALID | NODE_FEASIBLE | (sizeof(T) == 4 ? (I.root_rows + 1) << kNodeRowsShift : 0);
         nd.rec = (B.rec && inst < B.rec_cap) ? inst : -1;
         B.node[0][inst] = nd;
         if (!B.exhaustive) {
