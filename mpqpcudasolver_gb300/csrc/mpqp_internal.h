@@ -97,6 +97,10 @@ enum NodeFlags : int { NODE_FEASIBLE = 1, NODE_VALID = 2, NODE_CERT = 8 };
 // (rows of basic free variables dropped, the objective row right after them);
 // 0: all M1 rows
 constexpr int kNodeRowsShift = 8;
+// bits 17..24: 1 + the live columns of the stored FP32 LP1 tableau (the
+// columns of the set's own nonbasic slacks, fixed at zero for every
+// descendant, moved past the right-hand side); 0: all nv columns
+constexpr int kNodeColsShift = 17;
 
 struct Cand { int parent; int j; };
 

@@ -62,6 +62,12 @@ __device__ __forceinline__ int node_rows(int flags, int M1)
     return r > 0 ? r - 1 : M1;
 }
 
+__device__ __forceinline__ int node_cols(int flags, int nv)
+{
+    const int c = (flags >> kNodeColsShift) & 0xff;
+    return c > 0 ? c - 1 : nv;
+}
+
 // number of mask bits below position i
 __device__ __forceinline__ int mask_rank(uint64_t lo, uint64_t hi, int i)
 {
@@ -300,7 +306,9 @@ __device__ int warp_simplex(const Lp<T> &L, T tol_piv, T tol_dj, int max_piv, in
 // hold the objective row (lane j: column j; lane ncols: right-hand side) and
 // lanes 0..ncols-1 the nonbasic ids.  The constraint rows stay in shared
 // memory; the objective row and the ids are written back on return.  Ids
-// below ncols are free variables (nfree = ncols in both LPs).
+// below nfree are free variables (nfree >= ncols: an LP1 tableau whose fixed
+// slack columns were moved past the right-hand side has fewer columns than
+// free variables).
 constexpr int kFastRows = 96;
 constexpr int kFastChunks = 6;
 
@@ -312,13 +320,12 @@ constexpr int kFastChunks = 6;
 // row is dropped -- the last row moves into its place and nrows shrinks;
 // *nrows_out receives the final count (the objective row stays where it was).
 template <int NCH, int NRS>
-__device__ int simplex_fast32(float *tab, int ld, int nrows, int ncols, uint8_t *bid, uint8_t *nid, float tol_piv,
-                              float tol_dj, int max_piv, int degen_switch, int *piv_out, uint64_t fix_lo,
-                              uint64_t fix_hi, int fix_base, bool compact, int *nrows_out)
+__device__ int simplex_fast32(float *tab, int ld, int nrows, int ncols, int nfree, uint8_t *bid, uint8_t *nid,
+                              float tol_piv, float tol_dj, int max_piv, int degen_switch, int *piv_out,
+                              uint64_t fix_lo, uint64_t fix_hi, int fix_base, bool compact, int *nrows_out)
 {
     constexpr int NR = NRS;
     const int lane = lane_id();
-    const int nfree = ncols;
     int rowoff[NR], bidr[NR];
     bool valid[NR];
 #pragma unroll
@@ -461,12 +468,12 @@ __device__ __forceinline__ int simplex_fast32_rows(const Lp<float> &L, float tol
                                                    int fix_base, bool compact, int *nrows_out)
 {
     if (L.nrows <= 32)
-        return simplex_fast32<NCH, 1>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv,
+        return simplex_fast32<NCH, 1>(L.tab, L.ld, L.nrows, L.ncols, L.nfree, L.bid, L.nid, tol_piv, tol_dj, max_piv,
                                       degen_switch, piv_out, fix_lo, fix_hi, fix_base, compact, nrows_out);
     if (L.nrows <= 64)
-        return simplex_fast32<NCH, 2>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv,
+        return simplex_fast32<NCH, 2>(L.tab, L.ld, L.nrows, L.ncols, L.nfree, L.bid, L.nid, tol_piv, tol_dj, max_piv,
                                       degen_switch, piv_out, fix_lo, fix_hi, fix_base, compact, nrows_out);
-    return simplex_fast32<NCH, 3>(L.tab, L.ld, L.nrows, L.ncols, L.bid, L.nid, tol_piv, tol_dj, max_piv,
+    return simplex_fast32<NCH, 3>(L.tab, L.ld, L.nrows, L.ncols, L.nfree, L.bid, L.nid, tol_piv, tol_dj, max_piv,
                                   degen_switch, piv_out, fix_lo, fix_hi, fix_base, compact, nrows_out);
 }
 
@@ -480,7 +487,7 @@ __device__ __forceinline__ int warp_simplex_f32(const Lp<float> &L, float tol_pi
 {
     static_assert(MAXCH >= 1 && MAXCH <= kFastChunks, "chunk count");
     const int nch = (L.ncols + 4) >> 2;
-    if (L.nrows <= kFastRows && L.nfree == L.ncols && (L.ld & 3) == 0 && nch <= MAXCH) {
+    if (L.nrows <= kFastRows && (L.ld & 3) == 0 && nch <= MAXCH) {
         switch (nch) {
         case 1: return simplex_fast32_rows<1>(L, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base, compact, nrows_out);
         case 2: return simplex_fast32_rows<2>(L, tol_piv, tol_dj, max_piv, degen_switch, piv_out, fix_lo, fix_hi, fix_base, compact, nrows_out);
@@ -816,7 +823,7 @@ template <typename TT, typename TS>
 __device__ long long store_node(const DevBuffers &B, int side, int level, const InstDesc &I, int inst,
                                 uint64_t lo, uint64_t hi, bool feasible, const TS *tab, const uint8_t *ids,
                                 long long rec, long long hcap, int extra_flags, int src_ld = 0, bool bulk = false,
-                                long long pre_idx = -1, int rows_store = -1)
+                                long long pre_idx = -1, int rows_store = -1, int cols_store = -1)
 {
     const int lane = lane_id();
     Ctl *ctl = B.ctl;
@@ -897,7 +904,8 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
         Node nd;
         nd.lo = lo; nd.hi = hi; nd.inst = inst;
         nd.flags = NODE_VALID | (feasible ? NODE_FEASIBLE : 0) | extra_flags |
-                   (rows_store >= 0 ? (rows_store + 1) << kNodeRowsShift : 0);
+                   (rows_store >= 0 ? (rows_store + 1) << kNodeRowsShift : 0) |
+                   (cols_store >= 0 ? (cols_store + 1) << kNodeColsShift : 0);
         nd.tab_off = toff; nd.ids_off = ioff; nd.rec = rec;
         B.node[side][idx] = nd;
         // the hash serves the subset test of the next level only
@@ -907,6 +915,46 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
         }
     }
     return idx;
+}
+
+// Before an FP32 LP1 tableau is stored for the next level: each live column
+// whose nonbasic variable is a slack of the set (lo, hi) -- fixed at zero in
+// every descendant's LP, so never priced or updated usefully again -- moves
+// past the right-hand side.  Per such column c: the last live column takes
+// its place, the right-hand side moves one left, and c goes where the
+// right-hand side was (rows 0..nrows, the objective row included); its id
+// moves past the live ids.  Returns the live columns left.  The children's
+// row updates then cover ncols + 1 <= 4 NCH values with fewer chunks.
+__device__ __noinline__ int retire_fixed_columns(float *tab, int ld, int nrows, int ncols, uint8_t *nid, int nv,
+                                                 uint64_t lo, uint64_t hi)
+{
+    const int lane = lane_id();
+    for (;;) {
+        bool f = false;
+        if (lane < ncols) {
+            const int id = (int)nid[lane] - nv;
+            f = id >= 0 && id < 128 && mask_has(lo, hi, id);
+        }
+        const unsigned fm = __ballot_sync(FULLMASK, f) & (ncols >= 32 ? FULLMASK : ((1u << ncols) - 1u));
+        if (!fm || ncols > 32) break;
+        const int c = 31 - __clz(fm);   // the highest such column first
+        const int last = ncols - 1;
+        for (int r = lane; r <= nrows; r += 32) {
+            float *row = tab + (size_t)r * ld;
+            const float vc = row[c], vl = row[last], vb = row[ncols];
+            row[c] = vl;
+            row[last] = vb;
+            row[ncols] = vc;
+        }
+        if (lane == 0) {
+            const uint8_t t = nid[c];
+            nid[c] = nid[last];
+            nid[last] = t;
+        }
+        __syncwarp();
+        ncols = last;
+    }
+    return ncols;
 }
 
 // An FP32 LP1 candidate without a final verdict, by one lane: with nid (the
@@ -1114,6 +1162,9 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         // the parent's live rows (FP32 tableaus drop the rows of basic free
         // variables; the objective row follows the live rows)
         const int prows = cold ? (mixed ? I.root_rows : M1) : node_rows(par.flags, M1);
+        // the parent's live columns (FP32: the parent's own fixed slack
+        // columns sit past the right-hand side, which is column pcols)
+        const int pcols = (mixed && !cold) ? node_cols(par.flags, nv) : nv;
         fence_proxy_async_smem();
         __syncwarp();
         if (cold) {
@@ -1149,13 +1200,13 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
             rho = __reduce_max_sync(FULLMASK, rho);
             if (rho >= 0) {
                 const T *row = tab + (size_t)rho * ld;
-                for (int cc = lane; cc <= nv; cc += 32) obj[cc] = xadd(obj[cc], row[cc]);
+                for (int cc = lane; cc <= pcols; cc += 32) obj[cc] = xadd(obj[cc], row[cc]);
             } else {
-                for (int cc = lane; cc < nv; cc += 32) if (nid[cc] == wid) obj[cc] = obj[cc] - T(1);
+                for (int cc = lane; cc < pcols; cc += 32) if (nid[cc] == wid) obj[cc] = obj[cc] - T(1);
             }
         }
         __syncwarp();
-        Lp<T> L{tab, ld, prows, nv, nv, bid, nid};
+        Lp<T> L{tab, ld, prows, pcols, nv, bid, nid};
         int piv = 0;
         int st;
         int rows = prows;   // live rows after the simplex
@@ -1166,7 +1217,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         if constexpr (sizeof(T) == 4) st = warp_simplex_f32<kFastChunks>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv,
                                                                           par.lo, par.hi, nv, true, &rows);
         else st = warp_simplex<T>(L, tpiv, tdj, tol.max_pivots, tol.degen_switch, &piv);
-        const T z = obj[nv];
+        const T z = obj[pcols];
         uint64_t lo = par.lo, hi = par.hi;
         if (c.j < 64) lo |= 1ull << c.j; else hi |= 1ull << (c.j - 64);
         bool feasible = false, decided = true, to_cert = false;
@@ -1186,17 +1237,17 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
                     int j = 0;
                     if constexpr (sizeof(T) == 4) {
                         // FP32 rows are 16-byte aligned: four entries per access
-                        for (; j + 4 <= nv; j += 4) {
+                        for (; j + 4 <= pcols; j += 4) {
                             const float4 v = reinterpret_cast<const float4 *>(Ti)[j >> 2];
                             gmax = fmaxf(gmax, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
                         }
                     }
-                    for (; j < nv; j++) { const T a = xabs(Ti[j]); if (a > gmax) gmax = a; }
+                    for (; j < pcols; j++) { const T a = xabs(Ti[j]); if (a > gmax) gmax = a; }
                     const int id = bid[i];
                     if (id < nv) continue;
                     const int ci = id - nv;
                     if (ci < I.m && mask_has(lo, hi, ci)) s_basic = true;
-                    const T bb = Ti[nv];
+                    const T bb = Ti[pcols];
                     if (bb < minb) minb = bb;
                 }
                 s_basic = __any_sync(FULLMASK, s_basic);
@@ -1237,13 +1288,22 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         }
         if (feasible) { lc.a++; lc.c += (long long)mask_digest(lo, hi); }
         if (feasible || B.exhaustive) {
-            if (mixed && rows != prows && level < I.k_max) {
-                // the objective row follows the live rows in the stored tableau
-                for (int cc = lane; cc < ld; cc += 32) tab[(size_t)rows * ld + cc] = obj[cc];
-                __syncwarp();
+            int cols = -1;
+            if (mixed && level < I.k_max) {
+                if (rows != prows) {
+                    // the objective row follows the live rows in the stored tableau
+                    for (int cc = lane; cc < ld; cc += 32) tab[(size_t)rows * ld + cc] = obj[cc];
+                    __syncwarp();
+                }
+                // certified: every slack of S' is nonbasic, and fixed in every
+                // descendant -- its column moves past the right-hand side
+                if constexpr (sizeof(T) == 4)
+                    cols = feasible && !B.exhaustive
+                               ? retire_fixed_columns(tab, ld, rows, pcols, nid, nv, lo, hi) : pcols;
             }
             store_node<T, T>(B, side, level, I, inst, lo, hi, feasible, tab, ids, rec, hcap,
-                             mixed && feasible ? NODE_CERT : 0, 0, true, nbase + t, mixed ? rows : -1);
+                             mixed && feasible ? NODE_CERT : 0, 0, true, nbase + t, mixed ? rows : -1,
+                             mixed ? cols : -1);
         }
         if (at_vertex && feasible && level == I.k_max) {
             // later siblings whose new slack is nonbasic at this vertex
