@@ -441,7 +441,8 @@ def basis_sharing_compare(stream, dev) -> dict:
             torch.cuda.synchronize(dev)
             best = e0.elapsed_time(e1) if best is None else min(best, e0.elapsed_time(e1))
             plan.run_timed()
-            st = plan.kernel_times().get("k_opt_screen<dual>", (0.0, 0))[0]
+            st = sum(v[0] for kname, v in plan.kernel_times().items()
+                     if kname in ("k_opt_screen<dual>", "k_opt_screen<dual,lanes>"))
             stage0 = st if stage0 is None else min(stage0, st)
         r = plan.results()
         plan.close()

@@ -30,6 +30,9 @@ size_t feas_smem_per_warp(int prec_bytes, const SlotDims &sd);
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd);
 size_t screen_smem_per_warp(const SlotDims &sd, int route);
 size_t screen_tiles_smem(const SlotDims &sd, int tile_w);
+size_t screen_lanes_smem();
+cudaError_t launch_opt_screen_lanes(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode,
+                                    int grid, size_t smem, cudaStream_t s);
 bool screen_dual_route(int mode, const InstDesc &I, const SlotDims &sd);
 size_t laws_smem_per_warp(const SlotDims &sd);
 const void *kernel_ptr(const char *name);
@@ -354,6 +357,8 @@ struct mpqp_plan {
     int grid_opt3 = 0;          // grid of the dual route's second stage
     int grid_tiles = 0;         // the dual route's first stage (one set per tile of tile_w threads)
     size_t smem_tiles = 0;
+    int grid_lanes = 0;         // ... at levels |S| <= kLaneMaxK: one set per thread
+    size_t smem_lanes = 0;
     // launch settings the autotuner chooses: threads per set in the screen's
     // first stage, warps per LP1 block, candidates an LP1 warp claims at once
     int tile_w = 8, feas_warps = 4, feas_chunk = 32;
@@ -564,8 +569,12 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
             return MPQP_OK;
         }
         if (P->screen_dual) {
-            L("k_opt_screen<dual>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 0, P->grid_tiles, P->smem_tiles, s,
-                                                      P->tile_w));
+            if (level <= kLaneMaxK && !B.lp2b[0])
+                L("k_opt_screen<dual,lanes>", launch_opt_screen_lanes(B, P->tol, P->sd, level, P->lp2_screen,
+                                                                      P->grid_lanes, P->smem_lanes, s));
+            else
+                L("k_opt_screen<dual>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 0, P->grid_tiles,
+                                                          P->smem_tiles, s, P->tile_w));
             L("k_opt_screen<dual,rows>",
               launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 2, P->grid_opt3, P->smem_opt, s, P->tile_w));
         }
@@ -841,6 +850,7 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
     P->smem_opt = P->prec == PREC_MIXED ? screen_smem_per_warp(sd, 0) : 4 * opt_smem_per_warp(8, sd);
     P->smem_opt2 = screen_smem_per_warp(sd, 1);
     P->smem_tiles = screen_tiles_smem(sd, P->tile_w);
+    P->smem_lanes = screen_lanes_smem();
     for (const InstDesc &d : P->desc) {
         if (d.lp) P->has_lp = true; else P->has_qp = true;
         if (P->prec != PREC_MIXED) continue;
@@ -867,6 +877,8 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
                                                                          : "screen_dual_tiles32")),
                              P->smem_tiles, &P->grid_tiles, 32)
                   : 0) ||
+        (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_dual_lanes"), P->smem_lanes, &P->grid_lanes, 32)
+                                    : 0) ||
         (rc = grid_for(kernel_ptr("opt_fp64"), P->smem_optfb, &P->grid_optfb)) ||
         (rc = P->has_lp && P->prec != PREC_MIXED ? grid_for(kernel_ptr("opt64_lp"), P->smem_opt, &P->grid_opt_lp) : 0) ||
         (rc = P->has_lp ? grid_for(kernel_ptr("opt_fp64_lp"), P->smem_optfb, &P->grid_optfb_lp) : 0)) {

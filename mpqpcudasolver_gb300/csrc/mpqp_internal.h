@@ -164,6 +164,10 @@ struct InstCtl {
 
 constexpr int kCtlCounters = 12;
 
+// levels whose sets have at most this many elements run the first stage of
+// the FP32 dual screen with one set per thread (k_opt_screen_lanes)
+constexpr int kLaneMaxK = 6;
+
 struct Ctl {
     long long n_cand;           // candidates at the current level
     long long n_node[2];        // nodes per ping-pong side

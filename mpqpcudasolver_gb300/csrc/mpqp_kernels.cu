@@ -3087,6 +3087,344 @@ __global__ void __launch_bounds__(32, WARM ? 24 : 32) k_opt_screen_tiles(DevBuff
     flush();
 }
 
+// Stage 0 of the dual route with one set per thread, for the levels with
+// |S| <= kLaneMaxK: the operations of k_opt_screen_tiles -- the KKT factor
+// with its LICQ margin, the multiplier rows and the box, lp2_dual_screen from
+// the best single-row start, the bound verified from max(y, 0) -- run
+// serially by one thread per set, 32 consecutive sets per warp.  A tile of 8
+// lanes spends most of its instructions on shuffles, syncs and lanes left
+// idle by k, p + 1 <= 7; here every lane works on its own set.  Each thread
+// keeps its arrays in its own column of the warp's shared memory (element e
+// at e * 32 + lane: no bank conflicts, whatever the threads' positions).
+// The only differences from the tile: the R stride (kLaneMaxK) and the order
+// of one sum in the verified bound (a few ulps, inside its error margin).
+constexpr int kLaneP1 = kDualMaxP + 1;
+// words per thread: R, Y/Lambda (in place), B^-1 rows (p columns and the c
+// column), y, the multiplier rows' error scales, S, the basic rows
+constexpr int kLaneWords = kLaneMaxK * kLaneMaxK + kLaneMaxK * kLaneP1 + kLaneP1 * kDualMaxP + 3 * kLaneP1 +
+                           2 * kLaneMaxK;
+
+__global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, SlotDims sd, int level, int mode)
+{
+    extern __shared__ __align__(16) float lsm[];
+    constexpr int KM = kLaneMaxK, P7 = kLaneP1, MP = kDualMaxP;
+    const int lane = lane_id();
+    float *R = lsm + lane;                 // R[a][b] at (a KM + b) 32
+    float *Lm = R + KM * KM * 32;          // Y, then Lambda: [a][cc] at (a P7 + cc) 32
+    float *Bi = Lm + KM * P7 * 32;         // B^-1 row i, column c < p: (i MP + c) 32
+    float *Bp = Bi + P7 * MP * 32;         // B^-1 row i, the c column
+    float *Yv = Bp + P7 * 32;              // y_i
+    float *Sc = Yv + P7 * 32;              // error scale of multiplier row a
+    int *Sx = (int *)(Sc + KM * 32);       // S[a]
+    int *Bx = Sx + KM * 32;                // basic row of basic variable i
+    const int side = level & 1;
+    Ctl *ctl = B.ctl;
+    const long long nn = ctl->n_node[side] < B.node_cap ? ctl->n_node[side] : B.node_cap;
+    LocalInstCounters lc;
+    lc.reset(-1);
+    auto flush = [&]() {
+        if (lc.inst >= 0) {
+            atomicAdd((unsigned long long *)&B.ictl[lc.inst].lp2_piv, (unsigned long long)lc.c);
+            atomicAdd((unsigned long long *)&B.ictl[lc.inst].s0_lps, (unsigned long long)lc.d);
+            atomicAdd((unsigned long long *)&B.ictl[lc.inst].s0_piv, (unsigned long long)lc.c);
+        }
+    };
+    for (;;) {
+        long long x0;
+        if (lane == 0) x0 = (long long)atomicAdd(&ctl->ctr[3], 32ull);
+        x0 = __shfl_sync(FULLMASK, x0, 0);
+        if (x0 >= nn) break;
+        const long long x = x0 + lane;
+        if (x >= nn) continue;
+        const Node nd = B.node[side][x];
+        if ((nd.flags & (NODE_VALID | NODE_FEASIBLE)) != (NODE_VALID | NODE_FEASIBLE)) continue;
+        const InstDesc &I = B.inst[nd.inst];
+        if (level < I.k_min) continue;
+        if (!dual_route(mode, I, sd)) continue;
+        if (nd.inst != lc.inst) { flush(); lc.reset(nd.inst); }
+        const KktData<float> D = kkt_data<float>(B, I);
+        const int m = I.m, p = I.p, ncp = I.ncp, P1 = p + 1;
+        int k = 0;
+        {
+            uint64_t lo = nd.lo, hi = nd.hi;
+            while ((lo | hi) && k < KM) {
+                int i;
+                if (lo) { i = __ffsll((long long)lo) - 1; lo &= lo - 1; }
+                else { i = 64 + __ffsll((long long)hi) - 1; hi &= hi - 1; }
+                Sx[k * 32] = i;
+                k++;
+            }
+            if (lo | hi) k = KM + 1;   // larger than this kernel takes: FP64 decides
+        }
+        // KKT factor (kkt_factor's operations, R keeps the reciprocal pivots)
+        float rho = 1.0f;
+        bool fail = k > KM;
+        const float thr = tol.margin_licq32;
+        for (int a = 0; a < k && !fail; a++) {
+            const int sa = Sx[a * 32];
+            const float d0 = D.Wm[(size_t)sa * m + sa];
+            float acc = d0;
+            for (int l = 0; l < a; l++) acc = __fmaf_rn(-R[(l * KM + a) * 32], R[(l * KM + a) * 32], acc);
+            if (!(acc > thr * d0)) { fail = true; break; }
+            const float ra = __frcp_rn(__fsqrt_rn(acc));
+            R[(a * KM + a) * 32] = ra;
+            const float rr = __fdividef(acc, d0);
+            if (rr < rho) rho = rr;
+            for (int b = a + 1; b < k; b++) {
+                float acc2 = D.Wm[(size_t)sa * m + Sx[b * 32]];
+                for (int l = 0; l < a; l++) acc2 = __fmaf_rn(-R[(l * KM + a) * 32], R[(l * KM + b) * 32], acc2);
+                R[(a * KM + b) * 32] = acc2 * ra;
+            }
+        }
+        int piv = 0;
+        bool proven = false, to_rows = !fail;
+        if (!fail && k > 0) {
+            for (int cc = 0; cc < P1; cc++) {
+                for (int a = 0; a < k; a++) {
+                    const int sa = Sx[a * 32];
+                    float acc = (cc < p) ? D.Wh[(size_t)sa * p + cc] : D.wc[sa];
+                    for (int l = 0; l < a; l++) acc = __fmaf_rn(-R[(l * KM + a) * 32], Lm[(l * P7 + cc) * 32], acc);
+                    Lm[(a * P7 + cc) * 32] = acc * R[(a * KM + a) * 32];
+                }
+                for (int a = k - 1; a >= 0; a--) {
+                    float acc = Lm[(a * P7 + cc) * 32];
+                    for (int l = a + 1; l < k; l++) acc = __fmaf_rn(-R[(a * KM + l) * 32], Lm[(l * P7 + cc) * 32], acc);
+                    Lm[(a * P7 + cc) * 32] = acc * R[(a * KM + a) * 32];
+                }
+            }
+            // the multiplier rows' error scales, the box's reach
+            float amaxA = 0.0f, bmax = 0.0f;
+            for (int a = 0; a < k; a++) {
+                float rs = 0.0f;
+                for (int cc = 0; cc < p; cc++) rs += fabsf(Lm[(a * P7 + cc) * 32]);
+                rs += fabsf(Lm[(a * P7 + p) * 32]);
+                Sc[a * 32] = rs;
+                amaxA = fmaxf(amaxA, rs);
+            }
+            for (int ii = 0; ii < ncp; ii++) bmax = fmaxf(bmax, fabsf(D.bt[ii]));
+            const float escale = __fdividef(1.0f + (float)p * bmax, rho);
+            const float thr_lp = tol.margin_t32 * escale * amaxA, ethr = tol.margin_t32 * escale;
+            const float *blo = B.fpool + I.f_blo, *bhi = B.fpool + I.f_bhi;
+            const int R2 = k + ncp;
+            // row r of the dual layout: g (p columns), c, h
+            auto row8 = [&](int r, float *a8) {
+                if (r < k) {
+#pragma unroll
+                    for (int c = 0; c < MP; c++) a8[c] = c < p ? Lm[(r * P7 + c) * 32] : 0.0f;
+                    a8[6] = 1.0f;
+                    a8[7] = -Lm[(r * P7 + p) * 32];
+                } else {
+                    const int ii = r - k;
+#pragma unroll
+                    for (int c = 0; c < MP; c++) a8[c] = c < p ? D.At[ii * p + c] : 0.0f;
+                    a8[6] = 0.0f;
+                    a8[7] = D.bt[ii];
+                }
+            };
+            // best single-row bound over the multiplier rows
+            int istar = -1;
+            unsigned bkey = 0xffffffffu;
+            for (int r = 0; r < k; r++) {
+                float a8[8];
+                row8(r, a8);
+                float b = a8[7];
+#pragma unroll
+                for (int c = 0; c < MP; c++) {
+                    const float lc_ = c < p ? blo[c] : 0.0f, hc_ = c < p ? bhi[c] : 0.0f;
+                    b -= a8[c] > 0.0f ? a8[c] * lc_ : a8[c] * hc_;
+                }
+                const unsigned kk = key_signed(b);
+                if (istar < 0 || kk < bkey) { bkey = kk; istar = r; }
+            }
+            float gi[8];
+            row8(istar, gi);
+            float pi[MP];
+            float pip = gi[7];
+            unsigned basic = 1u << istar;
+            for (int i = 0; i < P1; i++) {
+                for (int c = 0; c < MP; c++) Bi[(i * MP + c) * 32] = 0.0f;
+                Bp[i * 32] = 0.0f;
+                Yv[i * 32] = 0.0f;
+            }
+#pragma unroll
+            for (int c = 0; c < MP; c++) {
+                pi[c] = 0.0f;
+                if (c < p) {
+                    const bool upper = !(gi[c] > 0.0f);
+                    const int row = k + (upper ? c : p + c);
+                    const float sc = D.At[(row - k) * p + c];
+                    pi[c] = upper ? bhi[c] : blo[c];
+                    const float yc = __fdividef(-gi[c], sc);
+                    pip = __fmaf_rn(yc, D.bt[row - k], pip);
+                    Bx[(1 + c) * 32] = row;
+                    Yv[(1 + c) * 32] = yc;
+                    Bi[((1 + c) * MP + c) * 32] = __fdividef(1.0f, sc);
+                    Bp[(1 + c) * 32] = yc;
+                    basic |= 1u << row;
+                }
+            }
+            Bx[0] = istar;
+            Yv[0] = 1.0f;
+            Bp[0] = 1.0f;
+            float thr_row = thr_lp;
+            auto verify = [&]() -> float {
+                float acc[MP + 2], ey = 0.0f;
+#pragma unroll
+                for (int v = 0; v < MP + 2; v++) acc[v] = 0.0f;
+                for (int i = 0; i < P1; i++) {
+                    const float yi = fmaxf(Yv[i * 32], 0.0f);
+                    const int ri = Bx[i * 32];
+                    float a8[8];
+                    row8(ri, a8);
+#pragma unroll
+                    for (int v = 0; v < MP + 2; v++) {
+                        // v < p: column v; v == p: c (6); v == p + 1: h (7)
+                        if (v <= P1) acc[v] = __fmaf_rn(yi, v < p ? a8[v] : (v == p ? a8[6] : a8[7]), acc[v]);
+                    }
+                    ey = __fmaf_rn(yi, ri < k ? Sc[ri * 32] : 0.0f, ey);
+                }
+                float cy = 0.0f, num = 0.0f;
+#pragma unroll
+                for (int v = 0; v < MP + 2; v++) {
+                    if (v < p) num += fabsf(acc[v]) * fmaxf(fabsf(blo[v]), fabsf(bhi[v]));
+                    else if (v == p) cy = acc[v];
+                    else if (v == P1) num += acc[v];
+                }
+                thr_row = cy > 0.0f ? fminf(thr_lp, ethr * __fdividef(ey, cy)) : thr_lp;
+                return cy > 0.0f ? __fdividef(num, cy) : pos_inf<float>();
+            };
+            int it = 0, degen = 0;
+            bool bland = false;
+            float bound = pos_inf<float>();
+            for (;;) {
+                if (pip < -thr_lp) {
+                    bound = verify();
+                    if (bound < -thr_row) { proven = true; break; }
+                }
+                if (it >= tol.max_pivots) break;
+                // pricing: the most negative reduced cost, smallest row on ties
+                int q = -1;
+                unsigned key = 0xffffffffu;
+                float dq = 0.0f;
+                for (int r = 0; r < R2; r++) {
+                    if ((basic >> r) & 1u) continue;
+                    float a8[8];
+                    row8(r, a8);
+                    float d = __fmaf_rn(-pip, a8[6], a8[7]);
+#pragma unroll
+                    for (int c = 0; c < MP; c++) d = __fmaf_rn(-pi[c], a8[c], d);
+                    if (d < -tol.tol_dj32) {
+                        const unsigned kk = bland ? 0u : ~key_of(-d);
+                        if (q < 0 || kk < key) { key = kk; q = r; dq = d; }
+                    }
+                }
+                if (q < 0) {
+                    bound = verify();
+                    proven = bound < -thr_row;
+                    break;
+                }
+                float aq[8];
+                row8(q, aq);
+                // ratio test over the basic variables: smallest max(y, 0) / u, smallest row on ties
+                float u[P7];
+                int l = -1, lrow = 0x7fffffff;
+                unsigned rk = 0xffffffffu;
+#pragma unroll
+                for (int i = 0; i < P7; i++) {
+                    u[i] = 0.0f;
+                    if (i < P1) {
+                        float ui = Bp[i * 32] * aq[6];
+#pragma unroll
+                        for (int c = 0; c < MP; c++) ui = __fmaf_rn(Bi[(i * MP + c) * 32], aq[c], ui);
+                        u[i] = ui;
+                        if (ui > tol.tol_piv32) {
+                            const unsigned kk = key_of(__fdividef(fmaxf(Yv[i * 32], 0.0f), ui));
+                            const int bi = Bx[i * 32];
+                            if (l < 0 || kk < rk || (kk == rk && bi < lrow)) { rk = kk; l = i; lrow = bi; }
+                        }
+                    }
+                }
+                if (l < 0) break;
+                float ul = 0.0f;
+#pragma unroll
+                for (int i = 0; i < P7; i++) if (i == l) ul = u[i];
+                const float yl = fmaxf(Yv[l * 32], 0.0f);
+                const int oldb = Bx[l * 32];
+                const float inv = __fdividef(1.0f, ul);
+                const float theta = yl * inv;
+                const float fp = dq * inv;
+#pragma unroll
+                for (int c = 0; c < MP; c++) {
+                    const float rj = Bi[(l * MP + c) * 32];
+#pragma unroll
+                    for (int i = 0; i < P7; i++) {
+                        if (i < P1) {
+                            float &bic = Bi[(i * MP + c) * 32];
+                            bic = i == l ? rj * inv : __fmaf_rn(-(u[i] * inv), rj, bic);
+                        }
+                    }
+                    pi[c] = __fmaf_rn(fp, rj, pi[c]);
+                }
+                {
+                    const float rj = Bp[l * 32];
+#pragma unroll
+                    for (int i = 0; i < P7; i++) {
+                        if (i < P1) {
+                            float &bp = Bp[i * 32];
+                            bp = i == l ? rj * inv : __fmaf_rn(-(u[i] * inv), rj, bp);
+                        }
+                    }
+                    pip = __fmaf_rn(fp, rj, pip);
+                }
+#pragma unroll
+                for (int i = 0; i < P7; i++) {
+                    if (i < P1) {
+                        if (i == l) { Yv[i * 32] = theta; Bx[i * 32] = q; }
+                        else Yv[i * 32] = __fmaf_rn(-theta, u[i], Yv[i * 32]);
+                    }
+                }
+                basic |= 1u << q;
+                basic &= ~(1u << oldb);
+                it++;
+                degen = (theta == 0.0f) ? degen + 1 : 0;
+                bland = degen >= tol.degen_switch;
+            }
+            piv = it;
+            to_rows = !proven;
+            lc.d++;
+            if (proven && nd.rec >= 0 && B.rec) {
+                OptResult res;
+                res.licq = 1; res.lp2_status = LP_BOUND; res.lp2_piv = piv;
+                res.cheb_status = LP_SKIPPED; res.cheb_piv = 0; res.optimal = 0; res.region = 0;
+                res.t = (double)bound; res.r = __longlong_as_double(0x7ff8000000000000LL);
+                res.decided = true;
+                write_opt(B, nd, level, res, false);
+            }
+        }
+        lc.c += piv;
+        if (!proven) {
+            // stage 1 takes the sets with a KKT factor; a failed KKT margin goes to FP64
+            if (to_rows) {
+                const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_scr, 1ull);
+                if (qi < B.q_cap) B.q_lp1[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
+            } else {
+                const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_opt, 1ull);
+                if (qi < B.q_cap) B.q_opt[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
+            }
+        }
+    }
+    flush();
+}
+
+size_t screen_lanes_smem() { return (size_t)kLaneWords * 32 * sizeof(float); }
+
+cudaError_t launch_opt_screen_lanes(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode,
+                                    int grid, size_t smem, cudaStream_t s)
+{
+    k_opt_screen_lanes<<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
+    return cudaGetLastError();
+}
+
 // ROUTE 1: the primal route, every set of the level.  ROUTE 0 with STAGE 1:
 // the dual route's second stage -- the sets its first stage
 // (k_opt_screen_tiles) could not settle from the multiplier rows and the
@@ -3601,6 +3939,7 @@ const void *kernel_ptr(const char *name)
         {"screen_dual_tiles8", (const void *)k_opt_screen_tiles<8>},
         {"screen_dual_tiles16", (const void *)k_opt_screen_tiles<16>},
         {"screen_dual_tiles32", (const void *)k_opt_screen_tiles<32>},
+        {"screen_dual_lanes", (const void *)k_opt_screen_lanes},
         {"screen_dual_tiles8w", (const void *)k_opt_screen_tiles<8, true>},
         {"screen_dual_tiles16w", (const void *)k_opt_screen_tiles<16, true>},
         {"screen_dual_tiles32w", (const void *)k_opt_screen_tiles<32, true>},
