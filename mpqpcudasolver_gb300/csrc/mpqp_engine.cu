@@ -32,7 +32,7 @@ size_t screen_smem_per_warp(const SlotDims &sd, int route);
 size_t screen_tiles_smem(const SlotDims &sd, int tile_w);
 size_t screen_lanes_smem();
 cudaError_t launch_opt_screen_lanes(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode,
-                                    int grid, size_t smem, cudaStream_t s);
+                                    int grid, size_t smem, cudaStream_t s, int cap);
 bool screen_dual_route(int mode, const InstDesc &I, const SlotDims &sd);
 size_t laws_smem_per_warp(const SlotDims &sd);
 const void *kernel_ptr(const char *name);
@@ -359,6 +359,7 @@ struct mpqp_plan {
     size_t smem_tiles = 0;
     int grid_lanes = 0;         // ... at levels |S| <= kLaneMaxK: one set per thread
     size_t smem_lanes = 0;
+    int lane_cap = 4;           // pivots of its first pass (MPQP_SCREEN_CAP), the rest rerun uncapped
     // launch settings the autotuner chooses: threads per set in the screen's
     // first stage, warps per LP1 block, candidates an LP1 warp claims at once
     int tile_w = 8, feas_warps = 4, feas_chunk = 32;
@@ -569,10 +570,13 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
             return MPQP_OK;
         }
         if (P->screen_dual) {
-            if (level <= kLaneMaxK && !B.lp2b[0])
+            if (level <= kLaneMaxK && !B.lp2b[0]) {
                 L("k_opt_screen<dual,lanes>", launch_opt_screen_lanes(B, P->tol, P->sd, level, P->lp2_screen,
-                                                                      P->grid_lanes, P->smem_lanes, s));
-            else
+                                                                      P->grid_lanes, P->smem_lanes, s,
+                                                                      P->lane_cap));
+                L("k_opt_screen<dual,lanes,rerun>", launch_opt_screen_lanes(B, P->tol, P->sd, level, P->lp2_screen,
+                                                                            P->grid_lanes, P->smem_lanes, s, 0));
+            } else
                 L("k_opt_screen<dual>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 0, P->grid_tiles,
                                                           P->smem_tiles, s, P->tile_w));
             L("k_opt_screen<dual,rows>",
@@ -766,7 +770,7 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
     if (arena_bytes <= 0) {
         const double used = (double)cand_cap * 12 + (double)node_cap * (2 * sizeof(Node) + 4) +
                             (double)hash_cap * 2 * sizeof(HashSlot) +
-                            (P->prec == PREC_MIXED ? (double)cand_cap / 8 * 48 : 0.0) +  // certificate queue
+                            (P->prec == PREC_MIXED ? (double)cand_cap / 8 * 48 + (double)cand_cap : 0.0) +  // certificate and rerun queues
                             (o.lp2_warm && P->prec == PREC_MIXED ? 16.0 * (double)node_cap : 0.0);   // LP2 bases
         arena_bytes = (long long)std::max(usable - used, (double)(64 << 20));
         if (all_budget) {
@@ -820,6 +824,8 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
     AL(B.cand, sizeof(Cand) * cand_cap);
     AL(B.q_lp1, sizeof(int) * cand_cap);
     AL(B.q_opt, sizeof(int) * cand_cap);
+    B.q_s0_cap = P->prec == PREC_MIXED ? std::max(cand_cap / 4, (long long)4096) : 0;
+    if (B.q_s0_cap) AL(B.q_s0, sizeof(int) * B.q_s0_cap);
     AL(B.cert_q, (size_t)B.cert_stride * B.cert_cap);
     AL(B.opt, sizeof(OptRec) * opt_cap);
     if (rec_cap) AL(B.rec, sizeof(CandRec) * rec_cap);
@@ -851,6 +857,7 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
     P->smem_opt2 = screen_smem_per_warp(sd, 1);
     P->smem_tiles = screen_tiles_smem(sd, P->tile_w);
     P->smem_lanes = screen_lanes_smem();
+    if (const char *e = getenv("MPQP_SCREEN_CAP")) P->lane_cap = std::max(1, atoi(e));
     for (const InstDesc &d : P->desc) {
         if (d.lp) P->has_lp = true; else P->has_qp = true;
         if (P->prec != PREC_MIXED) continue;

@@ -179,6 +179,7 @@ struct Ctl {
     long long n_q_lp1, n_q_opt; // FP64 fallback queue lengths
     long long n_q_scr;          // sets the first stage of the dual screen left to its second
     long long n_q_cert;         // FP32 LP1 optima waiting for the FP64 dual certificate
+    long long n_q_s0;           // first-stage dual LPs cut off at the iteration cap, run again uncapped
     unsigned long long ctr[kCtlCounters];  // work counters (reset every level)
     int overflow;               // bit mask of overflowed buffers
     int level;
@@ -222,6 +223,8 @@ struct DevBuffers {
     long long cand_cap;
     int *q_lp1;                 // candidate indices for the FP64 LP1 re-solve
     int *q_opt;                 // node indices for the FP64 optimality re-solve
+    int *q_s0;                  // node indices for the uncapped rerun of the first-stage dual LP
+    long long q_s0_cap;         // (a full queue sends a set to the second stage instead)
     long long q_cap;
     uint8_t *cert_q;            // certificate queue: entries of cert_stride bytes, an int candidate
                                 // index then the nv nonbasic ids of its final FP32 basis

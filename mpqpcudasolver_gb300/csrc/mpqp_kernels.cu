@@ -3104,7 +3104,14 @@ constexpr int kLaneP1 = kDualMaxP + 1;
 constexpr int kLaneWords = kLaneMaxK * kLaneMaxK + kLaneMaxK * kLaneP1 + kLaneP1 * kDualMaxP + 3 * kLaneP1 +
                            2 * kLaneMaxK;
 
-__global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, SlotDims sd, int level, int mode)
+// cap > 0 (the first pass over the level's nodes): an LP still running after
+// cap pivots stops, and its set goes to B.q_s0; cap = 0: the second pass,
+// over B.q_s0, runs them to the end (the same LP from the same start, so the
+// same result as one uncapped pass).  The 32 sets of a warp then mostly share
+// a pivot count in the first pass, instead of all waiting for the slowest
+// (a few percent of the sets need 5 to 25 pivots).
+__global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, SlotDims sd, int level, int mode,
+                                                         int cap)
 {
     extern __shared__ __align__(16) float lsm[];
     constexpr int KM = kLaneMaxK, P7 = kLaneP1, MP = kDualMaxP;
@@ -3119,7 +3126,8 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
     int *Bx = Sx + KM * 32;                // basic row of basic variable i
     const int side = level & 1;
     Ctl *ctl = B.ctl;
-    const long long nn = ctl->n_node[side] < B.node_cap ? ctl->n_node[side] : B.node_cap;
+    const long long nn = cap > 0 ? (ctl->n_node[side] < B.node_cap ? ctl->n_node[side] : B.node_cap)
+                                 : (ctl->n_q_s0 < B.q_s0_cap ? ctl->n_q_s0 : B.q_s0_cap);
     LocalInstCounters lc;
     lc.reset(-1);
     auto flush = [&]() {
@@ -3129,13 +3137,14 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
             atomicAdd((unsigned long long *)&B.ictl[lc.inst].s0_piv, (unsigned long long)lc.c);
         }
     };
+    const int max_it = cap > 0 ? cap : tol.max_pivots;
     for (;;) {
         long long x0;
-        if (lane == 0) x0 = (long long)atomicAdd(&ctl->ctr[3], 32ull);
+        if (lane == 0) x0 = (long long)atomicAdd(&ctl->ctr[cap > 0 ? 3 : 9], 32ull);
         x0 = __shfl_sync(FULLMASK, x0, 0);
         if (x0 >= nn) break;
-        const long long x = x0 + lane;
-        if (x >= nn) continue;
+        if (x0 + lane >= nn) continue;
+        const long long x = cap > 0 ? x0 + lane : (long long)B.q_s0[x0 + lane];
         const Node nd = B.node[side][x];
         if ((nd.flags & (NODE_VALID | NODE_FEASIBLE)) != (NODE_VALID | NODE_FEASIBLE)) continue;
         const InstDesc &I = B.inst[nd.inst];
@@ -3294,14 +3303,14 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
                 return cy > 0.0f ? __fdividef(num, cy) : pos_inf<float>();
             };
             int it = 0, degen = 0;
-            bool bland = false;
+            bool bland = false, capped = false;
             float bound = pos_inf<float>();
             for (;;) {
                 if (pip < -thr_lp) {
                     bound = verify();
                     if (bound < -thr_row) { proven = true; break; }
                 }
-                if (it >= tol.max_pivots) break;
+                if (it >= max_it) { capped = cap > 0; break; }
                 // pricing: the most negative reduced cost, smallest row on ties
                 int q = -1;
                 unsigned key = 0xffffffffu;
@@ -3389,6 +3398,11 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
                 degen = (theta == 0.0f) ? degen + 1 : 0;
                 bland = degen >= tol.degen_switch;
             }
+            if (capped) {
+                // the uncapped pass runs this set again from the start
+                const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_s0, 1ull);
+                if (qi < B.q_s0_cap) { B.q_s0[qi] = (int)x; continue; }
+            }
             piv = it;
             to_rows = !proven;
             lc.d++;
@@ -3419,9 +3433,9 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
 size_t screen_lanes_smem() { return (size_t)kLaneWords * 32 * sizeof(float); }
 
 cudaError_t launch_opt_screen_lanes(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode,
-                                    int grid, size_t smem, cudaStream_t s)
+                                    int grid, size_t smem, cudaStream_t s, int cap)
 {
-    k_opt_screen_lanes<<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
+    k_opt_screen_lanes<<<grid, 32, smem, s>>>(B, tol, sd, level, mode, cap);
     return cudaGetLastError();
 }
 
@@ -3769,6 +3783,7 @@ __global__ void k_finalize(DevBuffers B, int level)
         ctl->n_q_cert = 0;
         ctl->n_q_opt = 0;
         ctl->n_q_scr = 0;
+        ctl->n_q_s0 = 0;
         ctl->level = level;
     }
 }
