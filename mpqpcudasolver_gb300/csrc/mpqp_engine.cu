@@ -359,7 +359,7 @@ struct mpqp_plan {
     size_t smem_tiles = 0;
     int grid_lanes = 0;         // ... at levels |S| <= kLaneMaxK: one set per thread
     size_t smem_lanes = 0;
-    int lane_cap = 4;           // pivots of its first pass (MPQP_SCREEN_CAP), the rest rerun uncapped
+    int lane_cap = 3;           // pivots of its first pass (MPQP_SCREEN_CAP), the rest rerun uncapped
     // launch settings the autotuner chooses: threads per set in the screen's
     // first stage, warps per LP1 block, candidates an LP1 warp claims at once
     int tile_w = 8, feas_warps = 4, feas_chunk = 32;

@@ -3099,25 +3099,23 @@ __global__ void __launch_bounds__(32, WARM ? 24 : 32) k_opt_screen_tiles(DevBuff
 // The only differences from the tile: the R stride (kLaneMaxK) and the order
 // of one sum in the verified bound (a few ulps, inside its error margin).
 constexpr int kLaneP1 = kDualMaxP + 1;
-// words per thread: R, Y/Lambda (in place), B^-1 rows (p columns and the c
-// column), y, the multiplier rows' error scales, S, the basic rows
-constexpr int kLaneWords = kLaneMaxK * kLaneMaxK + kLaneMaxK * kLaneP1 + kLaneP1 * kDualMaxP + 3 * kLaneP1 +
-                           2 * kLaneMaxK;
+// words per thread: Lambda, B^-1 rows (p columns and the c column), y, the
+// multiplier rows' error scales, S, the basic rows (R and Y live in registers)
+constexpr int kLaneWords = kLaneMaxK * kLaneP1 + kLaneP1 * kDualMaxP + 3 * kLaneP1 + 2 * kLaneMaxK;
 
 // cap > 0 (the first pass over the level's nodes): an LP still running after
 // cap pivots stops, and its set goes to B.q_s0; cap = 0: the second pass,
 // over B.q_s0, runs them to the end (the same LP from the same start, so the
 // same result as one uncapped pass).  The 32 sets of a warp then mostly share
 // a pivot count in the first pass, instead of all waiting for the slowest
-// (a few percent of the sets need 5 to 25 pivots).
+// (a fifth of the sets need 4 to 25 pivots).
 __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, SlotDims sd, int level, int mode,
                                                          int cap)
 {
     extern __shared__ __align__(16) float lsm[];
     constexpr int KM = kLaneMaxK, P7 = kLaneP1, MP = kDualMaxP;
     const int lane = lane_id();
-    float *R = lsm + lane;                 // R[a][b] at (a KM + b) 32
-    float *Lm = R + KM * KM * 32;          // Y, then Lambda: [a][cc] at (a P7 + cc) 32
+    float *Lm = lsm + lane;                // Lambda: [a][cc] at (a P7 + cc) 32
     float *Bi = Lm + KM * P7 * 32;         // B^-1 row i, column c < p: (i MP + c) 32
     float *Bp = Bi + P7 * MP * 32;         // B^-1 row i, the c column
     float *Yv = Bp + P7 * 32;              // y_i
@@ -3165,50 +3163,92 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
             }
             if (lo | hi) k = KM + 1;   // larger than this kernel takes: FP64 decides
         }
-        // KKT factor (kkt_factor's operations, R keeps the reciprocal pivots)
+        // KKT factor (kkt_factor's operations in the same order, R keeping the
+        // reciprocal pivots), unrolled over k <= KM so that R, Y and Lambda
+        // stay in registers; Lambda then goes to shared memory for the LP,
+        // which reads its rows by index
         float rho = 1.0f;
         bool fail = k > KM;
         const float thr = tol.margin_licq32;
-        for (int a = 0; a < k && !fail; a++) {
-            const int sa = Sx[a * 32];
-            const float d0 = D.Wm[(size_t)sa * m + sa];
-            float acc = d0;
-            for (int l = 0; l < a; l++) acc = __fmaf_rn(-R[(l * KM + a) * 32], R[(l * KM + a) * 32], acc);
-            if (!(acc > thr * d0)) { fail = true; break; }
-            const float ra = __frcp_rn(__fsqrt_rn(acc));
-            R[(a * KM + a) * 32] = ra;
-            const float rr = __fdividef(acc, d0);
-            if (rr < rho) rho = rr;
-            for (int b = a + 1; b < k; b++) {
-                float acc2 = D.Wm[(size_t)sa * m + Sx[b * 32]];
-                for (int l = 0; l < a; l++) acc2 = __fmaf_rn(-R[(l * KM + a) * 32], R[(l * KM + b) * 32], acc2);
-                R[(a * KM + b) * 32] = acc2 * ra;
+        int Sr[KM];
+        float Rr[KM][KM];
+#pragma unroll
+        for (int a = 0; a < KM; a++) {
+            Sr[a] = a < k ? Sx[a * 32] : 0;
+#pragma unroll
+            for (int b = 0; b < KM; b++) Rr[a][b] = 0.0f;
+        }
+#pragma unroll
+        for (int a = 0; a < KM; a++) {
+            if (a < k && !fail) {
+                const float d0 = D.Wm[(size_t)Sr[a] * m + Sr[a]];
+                float acc = d0;
+#pragma unroll
+                for (int l = 0; l < a; l++) acc = __fmaf_rn(-Rr[l][a], Rr[l][a], acc);
+                if (!(acc > thr * d0)) fail = true;
+                else {
+                    const float ra = __frcp_rn(__fsqrt_rn(acc));
+                    Rr[a][a] = ra;
+                    const float rr = __fdividef(acc, d0);
+                    if (rr < rho) rho = rr;
+#pragma unroll
+                    for (int b = a + 1; b < KM; b++) {
+                        if (b < k) {
+                            float acc2 = D.Wm[(size_t)Sr[a] * m + Sr[b]];
+#pragma unroll
+                            for (int l = 0; l < a; l++) acc2 = __fmaf_rn(-Rr[l][a], Rr[l][b], acc2);
+                            Rr[a][b] = acc2 * ra;
+                        }
+                    }
+                }
             }
         }
         int piv = 0;
         bool proven = false, to_rows = !fail;
         if (!fail && k > 0) {
-            for (int cc = 0; cc < P1; cc++) {
-                for (int a = 0; a < k; a++) {
-                    const int sa = Sx[a * 32];
-                    float acc = (cc < p) ? D.Wh[(size_t)sa * p + cc] : D.wc[sa];
-                    for (int l = 0; l < a; l++) acc = __fmaf_rn(-R[(l * KM + a) * 32], Lm[(l * P7 + cc) * 32], acc);
-                    Lm[(a * P7 + cc) * 32] = acc * R[(a * KM + a) * 32];
-                }
-                for (int a = k - 1; a >= 0; a--) {
-                    float acc = Lm[(a * P7 + cc) * 32];
-                    for (int l = a + 1; l < k; l++) acc = __fmaf_rn(-R[(a * KM + l) * 32], Lm[(l * P7 + cc) * 32], acc);
-                    Lm[(a * P7 + cc) * 32] = acc * R[(a * KM + a) * 32];
+            float Lr[KM][P7];
+#pragma unroll
+            for (int cc = 0; cc < P7; cc++) {
+#pragma unroll
+                for (int a = 0; a < KM; a++) Lr[a][cc] = 0.0f;
+                if (cc < P1) {
+#pragma unroll
+                    for (int a = 0; a < KM; a++) {
+                        if (a < k) {
+                            float acc = (cc < p) ? D.Wh[(size_t)Sr[a] * p + cc] : D.wc[Sr[a]];
+#pragma unroll
+                            for (int l = 0; l < a; l++) acc = __fmaf_rn(-Rr[l][a], Lr[l][cc], acc);
+                            Lr[a][cc] = acc * Rr[a][a];
+                        }
+                    }
+#pragma unroll
+                    for (int a = KM - 1; a >= 0; a--) {
+                        if (a < k) {
+                            float acc = Lr[a][cc];
+#pragma unroll
+                            for (int l = a + 1; l < KM; l++)
+                                if (l < k) acc = __fmaf_rn(-Rr[a][l], Lr[l][cc], acc);
+                            Lr[a][cc] = acc * Rr[a][a];
+                        }
+                    }
                 }
             }
-            // the multiplier rows' error scales, the box's reach
+            // Lambda to shared memory; the multiplier rows' error scales, the box's reach
             float amaxA = 0.0f, bmax = 0.0f;
-            for (int a = 0; a < k; a++) {
-                float rs = 0.0f;
-                for (int cc = 0; cc < p; cc++) rs += fabsf(Lm[(a * P7 + cc) * 32]);
-                rs += fabsf(Lm[(a * P7 + p) * 32]);
-                Sc[a * 32] = rs;
-                amaxA = fmaxf(amaxA, rs);
+#pragma unroll
+            for (int a = 0; a < KM; a++) {
+                if (a < k) {
+                    float rs = 0.0f, rl = 0.0f;
+#pragma unroll
+                    for (int cc = 0; cc < P7; cc++) {
+                        if (cc < P1) Lm[(a * P7 + cc) * 32] = Lr[a][cc];
+                        if (cc < p) rs += fabsf(Lr[a][cc]);
+                        if (cc == p) rl = Lr[a][cc];
+                    }
+                    rs += fabsf(rl);
+                    Sc[a * 32] = rs;
+                    amaxA = fmaxf(amaxA, rs);
+                }
             }
             for (int ii = 0; ii < ncp; ii++) bmax = fmaxf(bmax, fabsf(D.bt[ii]));
             const float escale = __fdividef(1.0f + (float)p * bmax, rho);
