@@ -442,7 +442,7 @@ def basis_sharing_compare(stream, dev) -> dict:
             best = e0.elapsed_time(e1) if best is None else min(best, e0.elapsed_time(e1))
             plan.run_timed()
             st = sum(v[0] for kname, v in plan.kernel_times().items()
-                     if kname in ("k_opt_screen<dual>", "k_opt_screen<dual,lanes>"))
+                     if kname.startswith("k_opt_screen<dual") and kname != "k_opt_screen<dual,rows>")
             stage0 = st if stage0 is None else min(stage0, st)
         r = plan.results()
         plan.close()
