@@ -628,9 +628,16 @@ struct LocalInstCounters {
     __device__ void reset(int i) { inst = i; a = b = c = d = e = f = g = 0; }
 };
 
+// Children of 32 parents at a time, flattened: lane l takes the l-th child of
+// the chunk in (parent, j) order -- its parent found by a binary search over
+// the parents' child offsets -- so the warp's 32 subset tests are 32 children
+// whatever each parent's count (at the deepest levels a parent has about six).
+// Candidates keep the (parent, j) order within a group of 32; the counters
+// and the budget are kept per instance among the lanes of a group.
 __global__ void k_enumerate(DevBuffers B, int level)
 {
     const int lane = lane_id();
+    const unsigned below = (1u << lane) - 1u;
     const int pside = (level - 1) & 1;
     Ctl *ctl = B.ctl;
     const long long npar = ctl->n_node[pside] < B.node_cap ? ctl->n_node[pside] : B.node_cap;
@@ -638,9 +645,8 @@ __global__ void k_enumerate(DevBuffers B, int level)
     // slots the previous level's inserts used (every expandable parent was
     // inserted, which sets it; the full table otherwise, which is always in bounds)
     const long long hcap = ctl->hcap[pside] >= 16 && ctl->hcap[pside] <= B.hash_cap ? ctl->hcap[pside] : B.hash_cap;
-    int cur_inst = -1;
-    long long loc_cand = 0, loc_pruned = 0, loc_par = 0, loc_par_bytes = 0;
     const int es = B.precision == PREC_MIXED ? 4 : 8;
+    const HashSlot *tab = B.hash[pside];
     for (;;) {
         // parents are claimed 32 at a time (one atomic per chunk: levels
         // past an instance's last level hold many parents that are skipped)
@@ -649,19 +655,27 @@ __global__ void k_enumerate(DevBuffers B, int level)
         p0 = __shfl_sync(FULLMASK, p0, 0);
         if (p0 >= npar) break;
         const int cnt = npar - p0 < 32 ? (int)(npar - p0) : 32;
-        // lane t: whether parent p0 + t is expanded at this level
+        // lane t: parent p0 + t, whether it is expanded, its first child
+        // element and child count
         bool expand = false;
         unsigned sbytes = 0;   // the bytes the LP1 kernel stored for this node (tableau rows and ids)
-        int sinst = -1;
+        int sinst = -1, pinst = -1, jmin = 0, nch = 0;
+        uint64_t plo = 0, phi = 0;
+        int prows = 0;
         if (lane < cnt) {
             const Node pn = B.node[pside][p0 + lane];
             expand = (pn.flags & NODE_VALID) && (B.exhaustive || (pn.flags & NODE_FEASIBLE)) &&
                      !B.ictl[pn.inst].stopped && level <= B.inst[pn.inst].k_max;
+            const InstDesc &Ip = B.inst[pn.inst];
+            prows = es == 4 ? node_rows(pn.flags, Ip.M1) : Ip.M1;
             if ((pn.flags & NODE_VALID) && pn.tab_off >= 0) {
-                const InstDesc &Ip = B.inst[pn.inst];
-                const int rows = es == 4 ? node_rows(pn.flags, Ip.M1) : Ip.M1;
-                sbytes = (unsigned)((rows + 1) * Ip.ld1 * es + Ip.ids_bytes);
+                sbytes = (unsigned)((prows + 1) * Ip.ld1 * es + Ip.ids_bytes);
                 sinst = pn.inst;
+            }
+            if (expand) {
+                plo = pn.lo; phi = pn.hi; pinst = pn.inst;
+                jmin = mask_max(pn.lo, pn.hi) + 1;
+                nch = Ip.m > jmin ? Ip.m - jmin : 0;
             }
         }
         {
@@ -673,37 +687,38 @@ __global__ void k_enumerate(DevBuffers B, int level)
             if (sinst >= 0 && lane == __ffs(grp) - 1)
                 atomicAdd((unsigned long long *)&B.ictl[sinst].store_bytes, (unsigned long long)tot);
         }
-        unsigned todo = __ballot_sync(FULLMASK, expand);
-    while (todo) {
-        const int t = __ffs(todo) - 1;
-        todo &= todo - 1;
-        const long long pi = p0 + t;
-        const Node par = B.node[pside][pi];
-        const InstDesc &I = B.inst[par.inst];
-        if (par.inst != cur_inst) {
-            if (cur_inst >= 0 && lane == 0) {
-                atomicAdd((unsigned long long *)&B.ictl[cur_inst].lvl_cand, (unsigned long long)loc_cand);
-                atomicAdd((unsigned long long *)&B.ictl[cur_inst].pruned, (unsigned long long)loc_pruned);
-                atomicAdd((unsigned long long *)&B.ictl[cur_inst].lvl_parents, (unsigned long long)loc_par);
-                atomicAdd((unsigned long long *)&B.ictl[cur_inst].lvl_par_bytes, (unsigned long long)loc_par_bytes);
-            }
-            cur_inst = par.inst;
-            loc_cand = loc_pruned = loc_par = loc_par_bytes = 0;
+        // exclusive offsets of the parents' children
+        int incl = nch;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int v = __shfl_up_sync(FULLMASK, incl, off);
+            if (lane >= off) incl += v;
         }
-        bool emitted = false;   // this parent has a candidate at this level
-        const int jmin = mask_max(par.lo, par.hi) + 1;
-        for (int j0 = jmin; j0 < I.m; j0 += 32) {
-            const int j = j0 + lane;
-            const bool valid = j < I.m;
+        const int total = __shfl_sync(FULLMASK, incl, 31);
+        const int excl = incl - nch;
+        unsigned emitted = 0;   // bit t: parent t has a candidate at this level
+        for (int g0 = 0; g0 < total; g0 += 32) {
+            const int idx = g0 + lane;
+            const bool valid = idx < total;
+            // the parent of child idx: the last lane whose offset is <= idx
+            // (it has children: the next offset is larger)
+            int t = 0;
+#pragma unroll
+            for (int step = 16; step; step >>= 1) {
+                const int e = __shfl_sync(FULLMASK, excl, t + step);
+                if (e <= idx) t += step;
+            }
+            const uint64_t clo0 = __shfl_sync(FULLMASK, plo, t), chi0 = __shfl_sync(FULLMASK, phi, t);
+            const int cinst = __shfl_sync(FULLMASK, pinst, t);
+            const int j = __shfl_sync(FULLMASK, jmin, t) + (idx - __shfl_sync(FULLMASK, excl, t));
             bool ok = valid;
             if (ok && !B.exhaustive) {
-                uint64_t lo = par.lo, hi = par.hi;
+                uint64_t lo = clo0, hi = chi0;
                 if (j < 64) lo |= 1ull << j; else hi |= 1ull << (j - 64);
                 // the subsets child minus a, a in the parent, four at a time: the
                 // home slots of all four are read before any is checked, so the
                 // random accesses overlap; a collision probes on from there
-                uint64_t rlo = par.lo, rhi = par.hi;
-                const HashSlot *tab = B.hash[pside];
+                uint64_t rlo = clo0, rhi = chi0;
                 while (ok && (rlo | rhi)) {
                     constexpr int G = 4;
                     uint64_t slo[G], shi[G], sidx[G];
@@ -717,7 +732,7 @@ __global__ void k_enumerate(DevBuffers B, int level)
                             else { a = 64 + __ffsll((long long)rhi) - 1; rhi &= rhi - 1; }
                             slo[g] = lo; shi[g] = hi;
                             if (a < 64) slo[g] &= ~(1ull << a); else shi[g] &= ~(1ull << (a - 64));
-                            sidx[g] = hash_key(par.inst, slo[g], shi[g]) & (uint64_t)(hcap - 1);
+                            sidx[g] = hash_key(cinst, slo[g], shi[g]) & (uint64_t)(hcap - 1);
                             n = g + 1;
                         }
                     }
@@ -728,58 +743,65 @@ __global__ void k_enumerate(DevBuffers B, int level)
                     for (int g = 0; g < G; g++) {
                         if (g < n && ok) {
                             if (hs[g].tag != tag_prev) ok = false;
-                            else if (!(hs[g].lo == slo[g] && hs[g].hi == shi[g] && hs[g].inst == par.inst))
-                                ok = hash_find_from(tab, hcap, tag_prev, par.inst, slo[g], shi[g],
+                            else if (!(hs[g].lo == slo[g] && hs[g].hi == shi[g] && hs[g].inst == cinst))
+                                ok = hash_find_from(tab, hcap, tag_prev, cinst, slo[g], shi[g],
                                                     (sidx[g] + 1) & (uint64_t)(hcap - 1)) >= 0;
                         }
                     }
                 }
             }
-            const unsigned okm = __ballot_sync(FULLMASK, ok);
-            const unsigned vm = __ballot_sync(FULLMASK, valid);
-            const int cnt = __popc(okm);
-            loc_pruned += __popc(vm & ~okm);
+            // per instance among the group's lanes: pruned count, the budget,
+            // and one range of candidate slots
+            const unsigned grp = __match_any_sync(FULLMASK, valid ? cinst : -1);
+            const unsigned okm = __ballot_sync(FULLMASK, ok) & grp;
+            const int leader = __ffs(grp) - 1;
             long long base = 0;
             int over = 0;
-            if (lane == 0 && cnt) {
-                if (I.budget > 0) {
-                    // the level is checked only if the whole level fits the
-                    // budget; past that point nothing needs to be written
-                    const long long old = (long long)atomicAdd((unsigned long long *)&B.ictl[par.inst].lvl_cand,
-                                                               (unsigned long long)cnt);
-                    over = B.ictl[par.inst].cum_cand + old + cnt > I.budget;
-                } else {
-                    loc_cand += cnt;
+            if (valid && lane == leader) {
+                const int cntg = __popc(okm), pr = __popc(grp) - cntg;
+                if (pr) atomicAdd((unsigned long long *)&B.ictl[cinst].pruned, (unsigned long long)pr);
+                if (cntg) {
+                    const InstDesc &I = B.inst[cinst];
+                    const long long old = (long long)atomicAdd((unsigned long long *)&B.ictl[cinst].lvl_cand,
+                                                               (unsigned long long)cntg);
+                    // with a budget, the level is checked only if the whole
+                    // level fits it; past that point nothing needs to be written
+                    over = I.budget > 0 && B.ictl[cinst].cum_cand + old + cntg > I.budget;
+                    if (!over) base = (long long)atomicAdd((unsigned long long *)&ctl->n_cand, (unsigned long long)cntg);
                 }
-                if (!over) base = (long long)atomicAdd((unsigned long long *)&ctl->n_cand, (unsigned long long)cnt);
             }
-            base = __shfl_sync(FULLMASK, base, 0);
-            over = __shfl_sync(FULLMASK, over, 0);
-            emitted |= cnt > 0 && !over;
-            if (ok && !over) {
-                const long long idx = base + __popc(okm & ((1u << lane) - 1u));
-                if (idx < B.cand_cap) {
-                    B.cand[idx].parent = (int)pi;
-                    B.cand[idx].j = j;
+            base = __shfl_sync(FULLMASK, base, leader);
+            over = __shfl_sync(FULLMASK, over, leader);
+            const bool put = ok && !over;
+            if (put) {
+                const long long ci = base + __popc(okm & below);
+                if (ci < B.cand_cap) {
+                    B.cand[ci].parent = (int)(p0 + t);
+                    B.cand[ci].j = j;
                 } else {
                     atomicOr(&ctl->overflow, OV_CAND);
                 }
             }
+            emitted |= __reduce_or_sync(FULLMASK, put ? 1u << t : 0u);
         }
-        if (emitted) {
-            // the bytes its children's LP1 stage: live rows + objective row,
-            // basis ids, the node
-            const int rows = es == 4 ? node_rows(par.flags, I.M1) : I.M1;
-            loc_par++;
-            loc_par_bytes += (long long)(rows + 1) * I.ld1 * es + I.ids_bytes + (long long)sizeof(Node);
+        {
+            // the bytes the children's LP1 stages of each parent with a
+            // candidate: live rows + objective row, basis ids, the node
+            const bool em = (emitted >> lane) & 1u;
+            const int ei = em ? pinst : -1;
+            const unsigned grp = __match_any_sync(FULLMASK, ei);
+            const unsigned n_em = __popc(grp);
+            unsigned bytes = 0;   // a few KB each: 32 of them fit 32 bits
+            if (em) {
+                const InstDesc &Ip = B.inst[pinst];
+                bytes = (unsigned)((prows + 1) * Ip.ld1 * es + Ip.ids_bytes + (int)sizeof(Node));
+            }
+            const unsigned tot = __reduce_add_sync(grp, bytes);
+            if (em && lane == __ffs(grp) - 1) {
+                atomicAdd((unsigned long long *)&B.ictl[pinst].lvl_parents, (unsigned long long)n_em);
+                atomicAdd((unsigned long long *)&B.ictl[pinst].lvl_par_bytes, (unsigned long long)tot);
+            }
         }
-    }
-    }
-    if (cur_inst >= 0 && lane == 0) {
-        atomicAdd((unsigned long long *)&B.ictl[cur_inst].lvl_cand, (unsigned long long)loc_cand);
-        atomicAdd((unsigned long long *)&B.ictl[cur_inst].pruned, (unsigned long long)loc_pruned);
-        atomicAdd((unsigned long long *)&B.ictl[cur_inst].lvl_parents, (unsigned long long)loc_par);
-        atomicAdd((unsigned long long *)&B.ictl[cur_inst].lvl_par_bytes, (unsigned long long)loc_par_bytes);
     }
 }
 
