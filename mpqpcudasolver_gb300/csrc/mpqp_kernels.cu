@@ -3377,13 +3377,29 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
                 int q = -1;
                 unsigned key = 0xffffffffu;
                 float dq = 0.0f;
-                for (int r = 0; r < R2; r++) {
+                for (int r = 0; r < k; r++) {
                     if ((basic >> r) & 1u) continue;
                     float a8[8];
                     row8(r, a8);
                     float d = __fmaf_rn(-pip, a8[6], a8[7]);
 #pragma unroll
                     for (int c = 0; c < MP; c++) d = __fmaf_rn(-pi[c], a8[c], d);
+                    if (d < -tol.tol_dj32) {
+                        const unsigned kk = bland ? 0u : ~key_of(-d);
+                        if (q < 0 || kk < key) { key = kk; q = r; dq = d; }
+                    }
+                }
+                // a box row has one nonzero g (column c) and c = 0: its reduced
+                // cost h - pi_c g_c is the general sum's value (the other terms
+                // add exact zeros)
+                for (int ii = 0; ii < ncp; ii++) {
+                    const int r = k + ii;
+                    if ((basic >> r) & 1u) continue;
+                    const int cb = ii < p ? ii : ii - p;
+                    float pc = 0.0f;
+#pragma unroll
+                    for (int c = 0; c < MP; c++) if (c == cb) pc = pi[c];
+                    const float d = __fmaf_rn(-pc, D.At[ii * p + cb], D.bt[ii]);
                     if (d < -tol.tol_dj32) {
                         const unsigned kk = bland ? 0u : ~key_of(-d);
                         if (q < 0 || kk < key) { key = kk; q = r; dq = d; }
