@@ -168,6 +168,12 @@ struct Lp {
 __device__ __forceinline__ unsigned key_of(float v) { return __float_as_uint(v); }
 __device__ __forceinline__ unsigned long long key_of(double v) { return (unsigned long long)__double_as_longlong(v); }
 __device__ __forceinline__ unsigned key_none(float) { return 0xffffffffu; }
+// Order-preserving unsigned image of any non-NaN float (negative included).
+__device__ __forceinline__ unsigned key_signed(float v)
+{
+    const unsigned u = __float_as_uint(v);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
 __device__ __forceinline__ unsigned long long key_none(double) { return ~0ull; }
 
 // Warp-wide smallest (key, id); returns the winning lane's idx, or -1.  Ids
@@ -1254,29 +1260,49 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
                 // (~ |B^-1 N|), by which the FP32 errors of the basic values grow
                 bool s_basic = false;
                 T minb = pos_inf<T>(), gmax = T(1);
-                for (int i = lane; i < rows; i += 32) {
-                    const T *Ti = tab + (size_t)i * ld;
-                    int j = 0;
-                    if constexpr (sizeof(T) == 4) {
-                        // FP32 rows are 16-byte aligned: four entries per access
-                        for (; j + 4 <= pcols; j += 4) {
-                            const float4 v = reinterpret_cast<const float4 *>(Ti)[j >> 2];
+                if constexpr (sizeof(T) == 4) {
+                    // FP32 rows are 16-byte aligned: four entries per access;
+                    // the chunk holding the right-hand side (column pcols)
+                    // gives that row's beta and its last live columns
+                    const int cend = pcols >> 2, rem = pcols & 3;
+                    for (int i = lane; i < rows; i += 32) {
+                        const float *Ti = tab + (size_t)i * ld;
+                        for (int c4 = 0; c4 < cend; c4++) {
+                            const float4 v = reinterpret_cast<const float4 *>(Ti)[c4];
                             gmax = fmaxf(gmax, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
                         }
+                        const float4 v = reinterpret_cast<const float4 *>(Ti)[cend];
+                        gmax = fmaxf(gmax, fmaxf(fmaxf(rem > 0 ? fabsf(v.x) : 0.0f, rem > 1 ? fabsf(v.y) : 0.0f),
+                                                 rem > 2 ? fabsf(v.z) : 0.0f));
+                        const int id = bid[i];
+                        if (id < nv) continue;
+                        const int ci = id - nv;
+                        if (ci < I.m && mask_has(lo, hi, ci)) s_basic = true;
+                        const float bb = rem == 0 ? v.x : rem == 1 ? v.y : rem == 2 ? v.z : v.w;
+                        if (bb < minb) minb = bb;
                     }
-                    for (; j < pcols; j++) { const T a = xabs(Ti[j]); if (a > gmax) gmax = a; }
-                    const int id = bid[i];
-                    if (id < nv) continue;
-                    const int ci = id - nv;
-                    if (ci < I.m && mask_has(lo, hi, ci)) s_basic = true;
-                    const T bb = Ti[pcols];
-                    if (bb < minb) minb = bb;
-                }
-                s_basic = __any_sync(FULLMASK, s_basic);
+                    s_basic = __any_sync(FULLMASK, s_basic);
+                    // the warp's max and min by integer reductions on order-preserving images
+                    gmax = __uint_as_float(__reduce_max_sync(FULLMASK, __float_as_uint(gmax)));   // gmax >= 1
+                    const unsigned km = __reduce_min_sync(FULLMASK, key_signed(minb));
+                    minb = __uint_as_float((km & 0x80000000u) ? (km & 0x7fffffffu) : ~km);
+                } else {
+                    for (int i = lane; i < rows; i += 32) {
+                        const T *Ti = tab + (size_t)i * ld;
+                        for (int j = 0; j < pcols; j++) { const T a = xabs(Ti[j]); if (a > gmax) gmax = a; }
+                        const int id = bid[i];
+                        if (id < nv) continue;
+                        const int ci = id - nv;
+                        if (ci < I.m && mask_has(lo, hi, ci)) s_basic = true;
+                        const T bb = Ti[pcols];
+                        if (bb < minb) minb = bb;
+                    }
+                    s_basic = __any_sync(FULLMASK, s_basic);
 #pragma unroll
-                for (int off = 16; off; off >>= 1) {
-                    const T o = __shfl_xor_sync(FULLMASK, minb, off); if (o < minb) minb = o;
-                    const T g = __shfl_xor_sync(FULLMASK, gmax, off); if (g > gmax) gmax = g;
+                    for (int off = 16; off; off >>= 1) {
+                        const T o = __shfl_xor_sync(FULLMASK, minb, off); if (o < minb) minb = o;
+                        const T g = __shfl_xor_sync(FULLMASK, gmax, off); if (g > gmax) gmax = g;
+                    }
                 }
                 lp1_growth = (float)gmax;
                 lp1_minbeta = (float)minb;
@@ -2367,12 +2393,6 @@ __global__ void __launch_bounds__(128) k_optimality_fp64(DevBuffers B, Tol tol, 
 // ---------------------------------------------------------------------
 // FP32 LP2 screen of the mixed path
 // ---------------------------------------------------------------------
-// Order-preserving unsigned image of any non-NaN float (negative included).
-__device__ __forceinline__ unsigned key_signed(float v)
-{
-    const unsigned u = __float_as_uint(v);
-    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
 
 __device__ __forceinline__ float warp_max(float v)
 {
