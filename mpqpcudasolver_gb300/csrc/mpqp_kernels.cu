@@ -2635,6 +2635,17 @@ __host__ __device__ __forceinline__ bool dual_route(int mode, const InstDesc &I,
 // tile-wide shuffles and reductions.  W >= p + 1 (the basis rows sit in
 // lanes 0..p).
 namespace cgx = cooperative_groups;
+
+// A slot of a device queue for each thread that calls this together with
+// others: one atomic per group of threads that arrive converged.
+__device__ __forceinline__ long long queue_slot(long long *counter)
+{
+    const cgx::coalesced_group g = cgx::coalesced_threads();
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd((unsigned long long *)counter, (unsigned long long)g.size());
+    base = g.shfl(base, 0);
+    return (long long)base + g.thread_rank();
+}
 constexpr int kTileRows = 48;                  // k + 2p rows, ceil(48 / W) slots per lane
 template <int W>
 using ScreenTile = cgx::thread_block_tile<W, cgx::thread_block>;
@@ -3498,7 +3509,7 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
             }
             if (capped) {
                 // the uncapped pass runs this set again from the start
-                const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_s0, 1ull);
+                const long long qi = queue_slot(&ctl->n_q_s0);
                 if (qi < B.q_s0_cap) { B.q_s0[qi] = (int)x; continue; }
             }
             piv = it;
@@ -3517,10 +3528,10 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
         if (!proven) {
             // stage 1 takes the sets with a KKT factor; a failed KKT margin goes to FP64
             if (to_rows) {
-                const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_scr, 1ull);
+                const long long qi = queue_slot(&ctl->n_q_scr);
                 if (qi < B.q_cap) B.q_lp1[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
             } else {
-                const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_opt, 1ull);
+                const long long qi = queue_slot(&ctl->n_q_opt);
                 if (qi < B.q_cap) B.q_opt[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
             }
         }
