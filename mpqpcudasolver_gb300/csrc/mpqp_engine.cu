@@ -34,6 +34,7 @@ size_t screen_lanes_smem();
 cudaError_t launch_opt_screen_lanes(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode,
                                     int grid, size_t smem, cudaStream_t s, int cap);
 bool screen_dual_route(int mode, const InstDesc &I, const SlotDims &sd);
+bool screen_lanes_route(int mode, const InstDesc &I, const SlotDims &sd);
 size_t laws_smem_per_warp(const SlotDims &sd);
 const void *kernel_ptr(const char *name);
 cudaError_t launch_enumerate(const DevBuffers &B, int level, int grid, cudaStream_t s);
@@ -350,6 +351,7 @@ struct mpqp_plan {
     int prec = PREC_FP64;
     int lp2_screen = 0;         // mixed precision: 0 dual bound on box instances, 1 primal tableau screen
     bool screen_dual = false, screen_primal = false;   // which FP32 screen routes the instances need
+    bool lanes_lp = false;      // mpLP instances the one-set-per-thread first stage takes
     bool has_qp = false, has_lp = false;   // mpQP / mpLP (Q = 0) instances in the batch
     int grid_opt_lp = 0, grid_optfb_lp = 0;   // FP64 optimality kernels of the mpLP instances
     bool pooled = false;        // allocations came from the device pool
@@ -569,14 +571,15 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
                   launch_optimality(B, P->tol, P->sd, level, true, P->grid_opt_lp, P->smem_opt, s));
             return MPQP_OK;
         }
+        const bool lanes = level <= kLaneMaxK && !B.lp2b[0] && (P->screen_dual || P->lanes_lp);
+        if (lanes) {
+            L("k_opt_screen<dual,lanes>", launch_opt_screen_lanes(B, P->tol, P->sd, level, P->lp2_screen,
+                                                                  P->grid_lanes, P->smem_lanes, s, P->lane_cap));
+            L("k_opt_screen<dual,lanes,rerun>", launch_opt_screen_lanes(B, P->tol, P->sd, level, P->lp2_screen,
+                                                                        P->grid_lanes, P->smem_lanes, s, 0));
+        }
         if (P->screen_dual) {
-            if (level <= kLaneMaxK && !B.lp2b[0]) {
-                L("k_opt_screen<dual,lanes>", launch_opt_screen_lanes(B, P->tol, P->sd, level, P->lp2_screen,
-                                                                      P->grid_lanes, P->smem_lanes, s,
-                                                                      P->lane_cap));
-                L("k_opt_screen<dual,lanes,rerun>", launch_opt_screen_lanes(B, P->tol, P->sd, level, P->lp2_screen,
-                                                                            P->grid_lanes, P->smem_lanes, s, 0));
-            } else
+            if (!lanes)
                 L("k_opt_screen<dual>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 0, P->grid_tiles,
                                                           P->smem_tiles, s, P->tile_w));
             L("k_opt_screen<dual,rows>",
@@ -699,6 +702,9 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
         d.f_Wm = put(fp, pr.Wm); d.f_Wh = put(fp, pr.Wh); d.f_wc = put(fp, pr.wc);
         d.f_At = put(fp, pr.At); d.f_bt = put(fp, pr.bt); d.f_root = put(fp, pr.root_f);
         d.f_blo = put(fp, pr.blo); d.f_bhi = put(fp, pr.bhi);
+        // mpLP: FP32 copies of A H and A c right after the box (at f_bhi +
+        // align4(p) and after them: the multiplier law of the FP32 screen)
+        if (d.lp) { put(fp, pr.WhL); put(fp, pr.wcL); }
         P->desc.push_back(d);
         P->kmax = std::max(P->kmax, d.k_max);
         sd.maxM1 = std::max(sd.maxM1, d.M1);
@@ -863,6 +869,7 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
         if (P->prec != PREC_MIXED) continue;
         if (screen_dual_route(P->lp2_screen, d, sd)) P->screen_dual = true;
         else P->screen_primal = true;
+        if (d.lp && screen_lanes_route(P->lp2_screen, d, sd)) P->lanes_lp = true;
     }
     P->smem_optfb = 4 * opt_smem_per_warp(8, sd);
     if ((rc = grid_for(kernel_ptr("enumerate"), 0, &P->grid_enum)) ||
@@ -1264,9 +1271,8 @@ static void run_parallel(unsigned T, F f)
 }
 
 // indices of the optimal-set records in (inst, level, set) order
-static std::vector<uint32_t> sorted_opt_order(const std::vector<OptRec> &ov)
+static std::vector<uint32_t> sorted_opt_order(const OptRec *ov, size_t n)
 {
-    const size_t n = ov.size();
     OptKeys K;
     K.hi.resize(n); K.lo.resize(n); K.grp.resize(n);
     for (size_t i = 0; i < n; i++) {
@@ -1353,7 +1359,7 @@ static int plan_results_impl(mpqp_plan *P, mpqp_batch_result *&R, bool *complete
     // those integer keys (high mask word, low mask word, then instance and
     // level) moves indices, not records, and skips every digit that all sets
     // share.
-    std::vector<uint32_t> order = sorted_opt_order(ov);
+    std::vector<uint32_t> order = sorted_opt_order(ov.data(), ov.size());
     R->n_opt = nopt;
     R->opt = (mpqp_opt_set *)calloc(nopt ? nopt : 1, sizeof(mpqp_opt_set));
     if (!R->opt) throw std::bad_alloc();

@@ -2623,6 +2623,15 @@ __host__ __device__ __forceinline__ bool dual_route(int mode, const InstDesc &I,
     return mode == 0 && I.box && !I.lp && I.p <= kDualMaxP && I.m + I.ncp <= kDualMaxRows && sd.maxLD2 >= kDualLd;
 }
 
+// The instances whose sets the one-set-per-thread first stage takes at the
+// levels |S| <= kLaneMaxK: the dual route's, and the mpLP instances whose
+// parameter set is a box (their multiplier law is -Psi(theta); the sets it
+// leaves go to FP64, which also decides the mpLP's stationarity rows)
+__host__ __device__ __forceinline__ bool lanes_route(int mode, const InstDesc &I, const SlotDims &sd)
+{
+    return I.lp ? (mode == 0 && I.box && I.p <= kDualMaxP) : dual_route(mode, I, sd);
+}
+
 // ---------------------------------------------------------------------
 // Screen stage 0 on tiles of a warp
 // ---------------------------------------------------------------------
@@ -3200,10 +3209,14 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
         if ((nd.flags & (NODE_VALID | NODE_FEASIBLE)) != (NODE_VALID | NODE_FEASIBLE)) continue;
         const InstDesc &I = B.inst[nd.inst];
         if (level < I.k_min) continue;
-        if (!dual_route(mode, I, sd)) continue;
+        if (!lanes_route(mode, I, sd)) continue;
         if (nd.inst != lc.inst) { flush(); lc.reset(nd.inst); }
         const KktData<float> D = kkt_data<float>(B, I);
         const int m = I.m, p = I.p, ncp = I.ncp, P1 = p + 1;
+        // the right-hand sides of the multiplier law: [Wh | wc] (mpQP:
+        // Lambda), or for an mpLP [A H | A c] (Psi; its multipliers are -Psi)
+        const float *WhX = I.lp ? B.fpool + I.f_bhi + ((p + 3) & ~3) : D.Wh;
+        const float *wcX = I.lp ? WhX + (((size_t)m * p + 3) & ~(size_t)3) : D.wc;
         int k = 0;
         {
             uint64_t lo = nd.lo, hi = nd.hi;
@@ -3268,7 +3281,7 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
 #pragma unroll
                     for (int a = 0; a < KM; a++) {
                         if (a < k) {
-                            float acc = (cc < p) ? D.Wh[(size_t)Sr[a] * p + cc] : D.wc[Sr[a]];
+                            float acc = (cc < p) ? WhX[(size_t)Sr[a] * p + cc] : wcX[Sr[a]];
 #pragma unroll
                             for (int l = 0; l < a; l++) acc = __fmaf_rn(-Rr[l][a], Lr[l][cc], acc);
                             Lr[a][cc] = acc * Rr[a][a];
@@ -3526,8 +3539,9 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
         }
         lc.c += piv;
         if (!proven) {
-            // stage 1 takes the sets with a KKT factor; a failed KKT margin goes to FP64
-            if (to_rows) {
+            // stage 1 takes the sets with a KKT factor; a failed KKT margin, and
+            // every mpLP set, goes to FP64
+            if (to_rows && !I.lp) {
                 const long long qi = queue_slot(&ctl->n_q_scr);
                 if (qi < B.q_cap) B.q_lp1[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
             } else {
@@ -3593,6 +3607,9 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
         const InstDesc &I = B.inst[nd.inst];
         if (level < I.k_min) continue;
         if (dual_route(mode, I, sd) != (ROUTE == 0)) continue;
+        // mpLP sets of levels the one-set-per-thread stage takes (launched
+        // whenever basis sharing is off)
+        if (ROUTE == 1 && I.lp && level <= kLaneMaxK && !B.lp2b[0] && lanes_route(mode, I, sd)) continue;
         if (nd.inst != lc.inst) {
             if (lc.inst >= 0 && lane == 0) {
                 atomicAdd((unsigned long long *)&B.ictl[lc.inst].optimal, (unsigned long long)lc.a);
@@ -4033,6 +4050,7 @@ size_t lp1_smem_per_warp(int prec_bytes, const SlotDims &sd)
 size_t screen_smem_per_warp(const SlotDims &sd, int route) { return screen_warp_bytes(sd, route); }
 size_t screen_tiles_smem(const SlotDims &sd, int tile_w) { return (32 / tile_w) * tile_slot_bytes(sd); }   // a 32-thread block
 bool screen_dual_route(int mode, const InstDesc &I, const SlotDims &sd) { return dual_route(mode, I, sd); }
+bool screen_lanes_route(int mode, const InstDesc &I, const SlotDims &sd) { return lanes_route(mode, I, sd); }
 
 size_t opt_smem_per_warp(int prec_bytes, const SlotDims &sd)
 {
