@@ -351,7 +351,7 @@ struct mpqp_plan {
     int prec = PREC_FP64;
     int lp2_screen = 0;         // mixed precision: 0 dual bound on box instances, 1 primal tableau screen
     bool screen_dual = false, screen_primal = false;   // which FP32 screen routes the instances need
-    bool lanes_lp = false;      // mpLP instances the one-set-per-thread first stage takes
+    bool lanes_lp = false;      // mpLP instances the first stage of the dual screen takes
     bool has_qp = false, has_lp = false;   // mpQP / mpLP (Q = 0) instances in the batch
     int grid_opt_lp = 0, grid_optfb_lp = 0;   // FP64 optimality kernels of the mpLP instances
     bool pooled = false;        // allocations came from the device pool
@@ -577,11 +577,14 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
                                                                   P->grid_lanes, P->smem_lanes, s, P->lane_cap));
             L("k_opt_screen<dual,lanes,rerun>", launch_opt_screen_lanes(B, P->tol, P->sd, level, P->lp2_screen,
                                                                         P->grid_lanes, P->smem_lanes, s, 0));
+            if (P->lanes_lp)
+                L("k_opt_screen<dual,stationarity>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 3,
+                                                                       P->grid_tiles, P->smem_tiles, s, P->tile_w));
         }
+        if (!lanes && (P->screen_dual || P->lanes_lp))
+            L("k_opt_screen<dual>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 0, P->grid_tiles,
+                                                      P->smem_tiles, s, P->tile_w));
         if (P->screen_dual) {
-            if (!lanes)
-                L("k_opt_screen<dual>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 0, P->grid_tiles,
-                                                          P->smem_tiles, s, P->tile_w));
             L("k_opt_screen<dual,rows>",
               launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 2, P->grid_opt3, P->smem_opt, s, P->tile_w));
         }
@@ -702,9 +705,13 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
         d.f_Wm = put(fp, pr.Wm); d.f_Wh = put(fp, pr.Wh); d.f_wc = put(fp, pr.wc);
         d.f_At = put(fp, pr.At); d.f_bt = put(fp, pr.bt); d.f_root = put(fp, pr.root_f);
         d.f_blo = put(fp, pr.blo); d.f_bhi = put(fp, pr.bhi);
-        // mpLP: FP32 copies of A H and A c right after the box (at f_bhi +
-        // align4(p) and after them: the multiplier law of the FP32 screen)
-        if (d.lp) { put(fp, pr.WhL); put(fp, pr.wcL); }
+        // mpLP: FP32 copies of the multiplier law's right-hand sides and of
+        // the stationarity residual's data for the FP32 screen
+        d.f_WhL = d.f_wcL = d.f_AT = d.f_Hm = d.f_cv = -1;
+        if (d.lp) {
+            d.f_WhL = put(fp, pr.WhL); d.f_wcL = put(fp, pr.wcL);
+            d.f_AT = put(fp, pr.QiAT); d.f_Hm = put(fp, pr.Hm); d.f_cv = put(fp, pr.cv);
+        }
         P->desc.push_back(d);
         P->kmax = std::max(P->kmax, d.k_max);
         sd.maxM1 = std::max(sd.maxM1, d.M1);
@@ -868,8 +875,8 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
         if (d.lp) P->has_lp = true; else P->has_qp = true;
         if (P->prec != PREC_MIXED) continue;
         if (screen_dual_route(P->lp2_screen, d, sd)) P->screen_dual = true;
+        else if (d.lp && screen_lanes_route(P->lp2_screen, d, sd)) P->lanes_lp = true;
         else P->screen_primal = true;
-        if (d.lp && screen_lanes_route(P->lp2_screen, d, sd)) P->lanes_lp = true;
     }
     P->smem_optfb = 4 * opt_smem_per_warp(8, sd);
     if ((rc = grid_for(kernel_ptr("enumerate"), 0, &P->grid_enum)) ||

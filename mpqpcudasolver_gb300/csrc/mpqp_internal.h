@@ -72,8 +72,10 @@ struct InstDesc {
     long long o_WhL, o_wcL, o_Hm, o_cv;
     // offsets (elements) into the FP32 pool
     long long f_Wm, f_Wh, f_wc, f_At, f_bt, f_root;
-    long long f_blo, f_bhi;     // parameter box lo <= theta <= hi (FP32), valid when box; an mpLP's
-                                // A H (m x p) and A c (m) follow at f_bhi + align4(p), align4(m p) apart
+    long long f_blo, f_bhi;     // parameter box lo <= theta <= hi (FP32), valid when box
+    // mpLP only (else -1): FP32 copies of A H, A c (the multiplier law) and of
+    // A^T (n x m), H, c (the stationarity residual)
+    long long f_WhL, f_wcL, f_AT, f_Hm, f_cv;
     int box;                    // 1: At = [diag(+); diag(-)] (rows c, then p + c), a box
     int lp;                     // 1: Q = 0 (mpLP)
     int ld2lp;                  // mpLP, |S| < n: FP64 LP2 row stride (>= p + n + 3, odd)

@@ -2623,13 +2623,24 @@ __host__ __device__ __forceinline__ bool dual_route(int mode, const InstDesc &I,
     return mode == 0 && I.box && !I.lp && I.p <= kDualMaxP && I.m + I.ncp <= kDualMaxRows && sd.maxLD2 >= kDualLd;
 }
 
-// The instances whose sets the one-set-per-thread first stage takes at the
-// levels |S| <= kLaneMaxK: the dual route's, and the mpLP instances whose
-// parameter set is a box (their multiplier law is -Psi(theta); the sets it
-// leaves go to FP64, which also decides the mpLP's stationarity rows)
+// The instances whose sets the first stage of the dual screen takes (one set
+// per thread at the levels |S| <= kLaneMaxK, one per tile above them): the
+// dual route's, and the mpLP instances whose parameter set is a box (their
+// multiplier law is -Psi(theta); the sets it leaves go to FP64, which also
+// decides the mpLP's stationarity rows)
 __host__ __device__ __forceinline__ bool lanes_route(int mode, const InstDesc &I, const SlotDims &sd)
 {
     return I.lp ? (mode == 0 && I.box && I.p <= kDualMaxP) : dual_route(mode, I, sd);
+}
+
+// The FP32 data of the multiplier law: Wm and the right-hand sides [Wh | wc]
+// (mpQP: Lambda), or for an mpLP [A H | A c] (Psi = (A_S A_S^T)^-1 [A_S H |
+// A_S c], its multipliers -Psi)
+__device__ __forceinline__ KktData<float> multiplier_data(const DevBuffers &B, const InstDesc &I)
+{
+    KktData<float> D = kkt_data<float>(B, I);
+    if (I.lp) { D.Wh = B.fpool + I.f_WhL; D.wc = B.fpool + I.f_wcL; }
+    return D;
 }
 
 // ---------------------------------------------------------------------
@@ -2687,10 +2698,12 @@ __device__ __forceinline__ float tile_sum(const ScreenTile<W> &t, float v)
 }
 
 // Stage-0 slot of one tile: R (maxK^2), Y and Lambda (maxK x P1), S, the
-// dual-layout rows (k + 2p <= maxK + 2 kDualMaxP rows of kDualLd floats)
+// dual-layout rows (k + 2p, and 2n more for an mpLP, of kDualLd floats)
 __host__ __device__ inline int tile_rows(const SlotDims &sd)
 {
-    return sd.maxK + 2 * kDualMaxP < kTileRows ? sd.maxK + 2 * kDualMaxP : kTileRows;
+    // an mpLP set with |S| < n adds 2n stationarity residual rows
+    const int r = sd.maxK + 2 * kDualMaxP + 2 * sd.maxN;
+    return r < kTileRows ? r : kTileRows;
 }
 __host__ __device__ inline size_t tile_slot_bytes(const SlotDims &sd)
 {
@@ -3012,13 +3025,67 @@ __device__ int lp2_dual_screen_tile(const ScreenTile<W> &t, const float *T, int 
     return proven;
 }
 
+// The stationarity residual rows of an mpLP set with |S| = k < n, in the dual
+// layout at T: the residual of x's stationarity (c + H theta) - A_S^T
+// Psi(theta) = r0 + E theta must stay within tol_feas in every component
+// (the reference's LP2 equalities, main.py:107-108), so the rows
+//   (r0 + E theta)_i + t <= tol_feas,   -(r0 + E theta)_i + t <= tol_feas
+// (2n rows, a t coefficient of 1) hold at t = 0 wherever the set can be
+// optimal, and a verified bound below zero over them, the multiplier rows
+// and the box proves "not optimal".  E_i = H_i - sum_l A_{S_l,i} Psi_l and
+// r0_i = c_i - sum_l A_{S_l,i} Psi_l,p from the FP32 Psi in Lam; each row's
+// error scale is sum_l |A_{S_l,i}| (the l-th multiplier row's magnitude) plus
+// |H_i| + |c_i|.  Returns this lane's largest error scale.
+template <int W>
+__device__ float mplp_residual_rows(const ScreenTile<W> &t, const DevBuffers &B, const InstDesc &I, const int *S,
+                                    const float *Lam, int k, float tol_feas, float *T)
+{
+    const int n = I.n, m = I.m, p = I.p, P1 = p + 1;
+    const float *AT = B.fpool + I.f_AT, *Hm = B.fpool + I.f_Hm, *cv = B.fpool + I.f_cv;
+    float amax = 0.0f;
+    for (int i = t.thread_rank(); i < n; i += W) {
+        float e[kDualMaxP];
+        float r0 = cv[i], rs = fabsf(cv[i]);
+#pragma unroll
+        for (int c = 0; c < kDualMaxP; c++) {
+            e[c] = c < p ? Hm[i * p + c] : 0.0f;
+            rs += fabsf(e[c]);
+        }
+        for (int l = 0; l < k; l++) {
+            const float a = AT[(size_t)i * m + S[l]];
+            const float *lam = Lam + l * P1;
+            float ls = fabsf(lam[p]);
+#pragma unroll
+            for (int c = 0; c < kDualMaxP; c++)
+                if (c < p) { e[c] = __fmaf_rn(-a, lam[c], e[c]); ls += fabsf(lam[c]); }
+            r0 = __fmaf_rn(-a, lam[p], r0);
+            rs = __fmaf_rn(fabsf(a), ls, rs);
+        }
+        float *tp = T + (size_t)(2 * i) * kDualLd, *tn = tp + kDualLd;
+#pragma unroll
+        for (int c = 0; c < kDualMaxP; c++) { tp[c] = e[c]; tn[c] = -e[c]; }
+        tp[6] = 1.0f; tn[6] = 1.0f;
+        tp[7] = tol_feas - r0; tn[7] = tol_feas + r0;
+        tp[kRowScaleCol] = rs; tn[kRowScaleCol] = rs;
+        amax = fmaxf(amax, rs);
+    }
+    return amax;
+}
+
 // Stage 0 of the dual route, one set per tile (32 / W per warp): KKT factor,
 // the multiplier rows and the box, dual bound; the sets it cannot settle go
 // to stage 1 (k_opt_screen<0, 1>), a failed KKT margin to the FP64 queue.
+// An mpLP set with |S| < n also takes its stationarity residual rows into
+// the LP (mplp_residual_rows), so that a set whose residual cannot vanish
+// inside the box is settled here.
 // WARM: the dual LP starts from the parent set's final basis when that basis
 // is valid for this set (B.lp2b; the parent of node x is candidate x's).
+// src 0: every node of the level; src 1: the mpLP sets with |S| < n that the
+// one-set-per-thread stage left (its queue in q_lp1, shared with stage 1,
+// which takes only the mpQP sets), their LPs counted as pivots only.
 template <int W, bool WARM = false>
-__global__ void __launch_bounds__(32, WARM ? 24 : 32) k_opt_screen_tiles(DevBuffers B, Tol tol, SlotDims sd, int level, int mode)
+__global__ void __launch_bounds__(32, 24) k_opt_screen_tiles(DevBuffers B, Tol tol, SlotDims sd, int level, int mode,
+                                                                         int src)
 {
     static_assert(W >= kDualMaxP + 1 && W <= 32 && (W & (W - 1)) == 0, "tile width");
     extern __shared__ __align__(16) unsigned char smem[];
@@ -3037,14 +3104,17 @@ __global__ void __launch_bounds__(32, WARM ? 24 : 32) k_opt_screen_tiles(DevBuff
     }
     const int side = level & 1;
     Ctl *ctl = B.ctl;
-    const long long nn = ctl->n_node[side] < B.node_cap ? ctl->n_node[side] : B.node_cap;
+    const long long nn = src == 0 ? (ctl->n_node[side] < B.node_cap ? ctl->n_node[side] : B.node_cap)
+                                  : (ctl->n_q_scr < B.q_cap ? ctl->n_q_scr : B.q_cap);
     LocalInstCounters lc;
     lc.reset(-1);
     auto flush = [&]() {
         if (lc.inst >= 0 && lane == 0) {
             atomicAdd((unsigned long long *)&B.ictl[lc.inst].lp2_piv, (unsigned long long)lc.c);
-            atomicAdd((unsigned long long *)&B.ictl[lc.inst].s0_lps, (unsigned long long)lc.d);
-            atomicAdd((unsigned long long *)&B.ictl[lc.inst].s0_piv, (unsigned long long)lc.c);
+            if (src == 0) {
+                atomicAdd((unsigned long long *)&B.ictl[lc.inst].s0_lps, (unsigned long long)lc.d);
+                atomicAdd((unsigned long long *)&B.ictl[lc.inst].s0_piv, (unsigned long long)lc.c);
+            }
             if (WARM) {
                 atomicAdd((unsigned long long *)&B.ictl[lc.inst].warm_try, (unsigned long long)lc.f);
                 atomicAdd((unsigned long long *)&B.ictl[lc.inst].warm_used, (unsigned long long)lc.g);
@@ -3053,19 +3123,20 @@ __global__ void __launch_bounds__(32, WARM ? 24 : 32) k_opt_screen_tiles(DevBuff
     };
     for (;;) {
         long long x;
-        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[3], 1ull);
+        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[src == 0 ? 3 : 10], 1ull);
         x = t.shfl(x, 0);
         if (x >= nn) break;
-        if (WARM && lane == 0) B.lp2b[side][x] = ~0ull;   // no basis unless this set's LP runs
+        if (src != 0) x = B.q_lp1[x];
+        if (WARM && src == 0 && lane == 0) B.lp2b[side][x] = ~0ull;   // no basis unless this set's LP runs
         const Node nd = B.node[side][x];
         if ((nd.flags & (NODE_VALID | NODE_FEASIBLE)) != (NODE_VALID | NODE_FEASIBLE)) continue;
         const InstDesc &I = B.inst[nd.inst];
         if (level < I.k_min) continue;
-        if (!dual_route(mode, I, sd)) continue;
+        if (!lanes_route(mode, I, sd) || (src != 0 && !I.lp)) continue;
         if (nd.inst != lc.inst) { flush(); lc.reset(nd.inst); }
-        const KktData<float> D = kkt_data<float>(B, I);
+        const KktData<float> D = multiplier_data(B, I);
         const int p = I.p, ncp = I.ncp, P1 = p + 1;
-        int k = 0, piv = 0;
+        int k = 0, piv = 0, nres = 0;
         float rho = 1.0f, bound = 0.0f;
         bool proven = false, to_rows = false;
         if (!kkt_factor_tile<W>(t, D, I, nd.lo, nd.hi, tol.margin_licq32, R, Y, Lam, S, &k, &rho)) {
@@ -3094,25 +3165,31 @@ __global__ void __launch_bounds__(32, WARM ? 24 : 32) k_opt_screen_tiles(DevBuff
                     tr[7] = D.bt[ii];
                     tr[kRowScaleCol] = 0.0f;
                 }
+                if (I.lp && k < I.n && k + ncp + 2 * I.n <= tile_rows(sd)) {
+                    amaxA = fmaxf(amaxA, mplp_residual_rows<W>(t, B, I, S, Lam, k, (float)tol.tol_feas,
+                                                               Tb + (size_t)(k + ncp) * kDualLd));
+                    nres = 2 * I.n;
+                }
                 amaxA = tile_max<W>(t, amaxA);
                 // error scale per unit of row magnitude: 1 / smallest pivot ratio
                 // times the reach of theta inside the box
                 const float escale = __fdividef(1.0f + (float)p * bmax, rho);
                 t.sync();
                 const uint8_t *warm = nullptr;
-                if (WARM && level >= 1) {
+                if (WARM && src == 0 && level >= 1) {
                     const int par = B.cand[x].parent;
                     if (par >= 0) warm = reinterpret_cast<const uint8_t *>(B.lp2b[side ^ 1] + par);
                 }
                 unsigned long long bword = ~0ull;
                 int wst = 0;
-                proven = lp2_dual_screen_tile<W, WARM>(t, Tb, k, k + ncp, p, B.fpool + I.f_blo, B.fpool + I.f_bhi,
-                                                    tol.margin_t32 * escale * amaxA, tol.margin_t32 * escale,
-                                                    tol.tol_piv32, tol.tol_dj32, tol.max_pivots, tol.degen_switch,
-                                                    &piv, &bound, warm, &bword, &wst);
+                proven = lp2_dual_screen_tile<W, WARM>(t, Tb, k, k + ncp + nres, p, B.fpool + I.f_blo,
+                                                    B.fpool + I.f_bhi, tol.margin_t32 * escale * amaxA,
+                                                    tol.margin_t32 * escale, tol.tol_piv32, tol.tol_dj32,
+                                                    tol.max_pivots, tol.degen_switch, &piv, &bound, warm, &bword,
+                                                    &wst);
                 to_rows = !proven;
                 lc.d++;
-                if (WARM) {
+                if (WARM && src == 0) {
                     if (lane == 0) B.lp2b[side][x] = bword;
                     lc.f += wst >= 1;
                     lc.g += wst == 2;
@@ -3122,9 +3199,10 @@ __global__ void __launch_bounds__(32, WARM ? 24 : 32) k_opt_screen_tiles(DevBuff
         }
         lc.c += piv;
         if (!proven) {
-            // stage 1 takes the sets with a KKT factor; a failed KKT margin goes to FP64
+            // stage 1 takes the sets with a KKT factor; a failed KKT margin, and
+            // every mpLP set, goes to FP64
             if (lane == 0) {
-                if (to_rows) {
+                if (to_rows && !I.lp) {
                     const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_scr, 1ull);
                     if (qi < B.q_cap) B.q_lp1[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
                 } else {
@@ -3211,12 +3289,9 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
         if (level < I.k_min) continue;
         if (!lanes_route(mode, I, sd)) continue;
         if (nd.inst != lc.inst) { flush(); lc.reset(nd.inst); }
-        const KktData<float> D = kkt_data<float>(B, I);
+        const KktData<float> D = multiplier_data(B, I);
         const int m = I.m, p = I.p, ncp = I.ncp, P1 = p + 1;
-        // the right-hand sides of the multiplier law: [Wh | wc] (mpQP:
-        // Lambda), or for an mpLP [A H | A c] (Psi; its multipliers are -Psi)
-        const float *WhX = I.lp ? B.fpool + I.f_bhi + ((p + 3) & ~3) : D.Wh;
-        const float *wcX = I.lp ? WhX + (((size_t)m * p + 3) & ~(size_t)3) : D.wc;
+        const float *WhX = D.Wh, *wcX = D.wc;
         int k = 0;
         {
             uint64_t lo = nd.lo, hi = nd.hi;
@@ -3539,9 +3614,10 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
         }
         lc.c += piv;
         if (!proven) {
-            // stage 1 takes the sets with a KKT factor; a failed KKT margin, and
-            // every mpLP set, goes to FP64
-            if (to_rows && !I.lp) {
+            // stage 1 takes the mpQP sets with a KKT factor, the tile stage with
+            // the stationarity rows the mpLP sets with |S| < n; a failed KKT
+            // margin, and every other mpLP set, goes to FP64
+            if (to_rows && (!I.lp || (k < I.n && k + ncp + 2 * I.n <= tile_rows(sd)))) {
                 const long long qi = queue_slot(&ctl->n_q_scr);
                 if (qi < B.q_cap) B.q_lp1[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
             } else {
@@ -3607,9 +3683,9 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
         const InstDesc &I = B.inst[nd.inst];
         if (level < I.k_min) continue;
         if (dual_route(mode, I, sd) != (ROUTE == 0)) continue;
-        // mpLP sets of levels the one-set-per-thread stage takes (launched
-        // whenever basis sharing is off)
-        if (ROUTE == 1 && I.lp && level <= kLaneMaxK && !B.lp2b[0] && lanes_route(mode, I, sd)) continue;
+        // mpLP sets the first stage of the dual screen takes (one set per
+        // thread at |S| <= kLaneMaxK, tiles above or with basis sharing)
+        if (ROUTE == 1 && I.lp && lanes_route(mode, I, sd)) continue;
         if (nd.inst != lc.inst) {
             if (lc.inst >= 0 && lane == 0) {
                 atomicAdd((unsigned long long *)&B.ictl[lc.inst].optimal, (unsigned long long)lc.a);
@@ -4144,16 +4220,18 @@ cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDim
                               int grid, size_t smem, cudaStream_t s, int tile_w)
 {
     // route 0: the dual route's first stage (tiles of tile_w threads), 2: its
-    // second stage, 1: the primal route
+    // second stage, 1: the primal route, 3: the tile stage over the mpLP sets
+    // the one-set-per-thread stage queued (their stationarity rows)
+    const int src = route == 3 ? 1 : 0;
     if (route == 0 && B.lp2b[0]) {
-        if (tile_w == 8) k_opt_screen_tiles<8, true><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
-        else if (tile_w == 16) k_opt_screen_tiles<16, true><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
-        else if (tile_w == 32) k_opt_screen_tiles<32, true><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
+        if (tile_w == 8) k_opt_screen_tiles<8, true><<<grid, 32, smem, s>>>(B, tol, sd, level, mode, 0);
+        else if (tile_w == 16) k_opt_screen_tiles<16, true><<<grid, 32, smem, s>>>(B, tol, sd, level, mode, 0);
+        else if (tile_w == 32) k_opt_screen_tiles<32, true><<<grid, 32, smem, s>>>(B, tol, sd, level, mode, 0);
         else return cudaErrorInvalidValue;
-    } else if (route == 0) {
-        if (tile_w == 8) k_opt_screen_tiles<8><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
-        else if (tile_w == 16) k_opt_screen_tiles<16><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
-        else if (tile_w == 32) k_opt_screen_tiles<32><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
+    } else if (route == 0 || route == 3) {
+        if (tile_w == 8) k_opt_screen_tiles<8><<<grid, 32, smem, s>>>(B, tol, sd, level, mode, src);
+        else if (tile_w == 16) k_opt_screen_tiles<16><<<grid, 32, smem, s>>>(B, tol, sd, level, mode, src);
+        else if (tile_w == 32) k_opt_screen_tiles<32><<<grid, 32, smem, s>>>(B, tol, sd, level, mode, src);
         else return cudaErrorInvalidValue;
     }
     else if (route == 2) k_opt_screen<0, 1><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);

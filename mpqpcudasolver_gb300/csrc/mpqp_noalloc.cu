@@ -49,7 +49,7 @@ using namespace mq;
 namespace {
 
 constexpr size_t kScratchBytes = (size_t)MPQP_NOALLOC_SCRATCH_BYTES;
-constexpr size_t kDescBytes = 256;           // InstDesc slot at the start
+constexpr size_t kDescBytes = 512;           // InstDesc slot at the start
 static_assert(sizeof(InstDesc) <= kDescBytes, "InstDesc outgrew its scratch slot");
 constexpr int kMaxDevices = 64;
 

@@ -81,6 +81,23 @@ def test_mplp_mixed_same_sets_as_fp64(gpu_lib, case):
     assert b.inst[0]["lp2_first_stage_lps"] > 0
 
 
+@pytest.mark.parametrize("tile_w", [8, 16, 32])
+def test_mplp_first_stage_above_six(gpu_lib, tile_w):
+    """The sets with |S| > 6 of an mpLP over a box take the first stage one
+    set per tile (k_opt_screen_tiles, the multiplier rows -Psi and the box):
+    with the checks confined to |S| = 7, 8 it runs LPs, settles some sets,
+    and the verdicts stay those of the FP64 path."""
+    prob = P.scale_problem(P.random_mplp(8, 24, 3, seed=6))
+    a = solver.solve([prob], precision=solver.FP64, k_min=7, k_max=8)
+    b = solver.solve([prob], precision=solver.MIXED, k_min=7, k_max=8, tile_w=tile_w)
+    assert a.status == b.status == 0
+    for f in ("feasible_digest", "optimal_digest", "region_digest", "feasible", "optimal", "regions", "candidates"):
+        assert a.inst[0][f] == b.inst[0][f], f
+    lps, fb = b.inst[0]["lp2_first_stage_lps"], b.inst[0]["fallback_opt"]
+    assert lps > 0 and fb < lps, (lps, fb)
+    print("tile", tile_w, "first-stage LPs", lps, "FP64 fallbacks", fb, "optimal", b.inst[0]["optimal"])
+
+
 @pytest.mark.parametrize("precision", [solver.FP64, solver.MIXED])
 def test_batch_of_mpqp_and_mplp_instances(gpu_lib, precision):
     probs = [P.scale_problem(p) for p in (P.random_n4_m10_p2(), P.random_mplp(6, 24, 3, seed=2),
