@@ -225,6 +225,9 @@ typedef struct {
      * their iterations; with lp2_warm, the LPs offered a valid parent basis
      * and those that started from it */
     long long lp2_first_stage_lps, lp2_first_stage_pivots, lp2_warm_offered, lp2_warm_started;
+    /* mixed precision: sets found not optimal in FP64 from the final basis
+     * of the FP32 dual screen, without the FP64 LP2 (counted in fallback_opt) */
+    long long lp2_certified;
 } mpqp_inst_stats;
 
 typedef struct {

@@ -839,6 +839,13 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
     AL(B.q_opt, sizeof(int) * cand_cap);
     B.q_s0_cap = P->prec == PREC_MIXED ? std::max(cand_cap / 4, (long long)4096) : 0;
     if (B.q_s0_cap) AL(B.q_s0, sizeof(int) * B.q_s0_cap);
+    // sets the FP32 dual screen found not optimal below its margin's reach: a
+    // sixteenth of the candidates (a full queue sends the rest to q_opt)
+    B.q_c2_cap = P->prec == PREC_MIXED ? std::max(cand_cap / 16, (long long)4096) : 0;
+    if (B.q_c2_cap) {
+        AL(B.q_c2, sizeof(int) * B.q_c2_cap);
+        AL(B.q_c2b, sizeof(unsigned long long) * B.q_c2_cap);
+    }
     AL(B.cert_q, (size_t)B.cert_stride * B.cert_cap);
     AL(B.opt, sizeof(OptRec) * opt_cap);
     if (rec_cap) AL(B.rec, sizeof(CandRec) * rec_cap);
@@ -1350,6 +1357,7 @@ static int plan_results_impl(mpqp_plan *P, mpqp_batch_result *&R, bool *complete
         s.lp1_cold = ic[i].lp1_cold; s.nodes_without_tableau = ic[i].no_tab;
         s.lp2_first_stage_lps = ic[i].s0_lps; s.lp2_first_stage_pivots = ic[i].s0_piv;
         s.lp2_warm_offered = ic[i].warm_try; s.lp2_warm_started = ic[i].warm_used;
+        s.lp2_certified = ic[i].cert_lp2;
         s.feasible_digest = ic[i].feas_digest; s.optimal_digest = ic[i].opt_digest;
         s.region_digest = ic[i].reg_digest;
         s.last_level = ic[i].last_level; s.truncated = ic[i].truncated;

@@ -126,7 +126,8 @@ struct CandRec {                // identical field layout to the oracle's record
     int32_t lp2_status, lp2_pivots, cheb_status, cheb_pivots;
     double t, r;
     int32_t inst, fp64;         // instance; bit0 LP1 / bit1 LP2 decided in FP64, bit2 LP1
-                                // infeasible by the FP64 dual certificate of the final FP32 basis
+                                // infeasible by the FP64 dual certificate of the final FP32 basis,
+                                // bit3 LP2 not optimal by the FP64 check of the FP32 dual basis
     float lp1_growth;           // FP32 LP1: max |T_ij| of the final tableau (mixed precision)
     float lp1_minbeta;          // FP32 LP1: smallest basic slack value
     double lp1_bound;           // FP64 dual certificate: the lower bound on z* it proved (NaN: none)
@@ -145,6 +146,7 @@ struct InstCtl {
     long long cert_lp1;         // FP32 LP1 optima certified infeasible by the FP64 dual bound
     long long cert_miss;        // ... that the certificate could not prove (sent to the FP64 re-solve)
     long long cert_free;        // ... of those, the misses with a free variable nonbasic (no square system)
+    long long cert_lp2;         // sets found not optimal by the FP64 check of their FP32 dual basis
     long long lp1_cold;         // LP1 solves started from the root (the parent kept no tableau)
     long long no_tab;           // nodes kept without a tableau (the arena was full)
     long long stored;           // LP1 tableaus written for the next level
@@ -183,6 +185,7 @@ struct Ctl {
     long long n_q_scr;          // sets the first stage of the dual screen left to its second
     long long n_q_cert;         // FP32 LP1 optima waiting for the FP64 dual certificate
     long long n_q_s0;           // first-stage dual LPs cut off at the iteration cap, run again uncapped
+    long long n_q_c2;           // sets for the FP64 kernel with an FP32 dual basis to check first
     unsigned long long ctr[kCtlCounters];  // work counters (reset every level)
     int overflow;               // bit mask of overflowed buffers
     int level;
@@ -228,6 +231,9 @@ struct DevBuffers {
     int *q_opt;                 // node indices for the FP64 optimality re-solve
     int *q_s0;                  // node indices for the uncapped rerun of the first-stage dual LP
     long long q_s0_cap;         // (a full queue sends a set to the second stage instead)
+    int *q_c2;                  // node indices for the FP64 kernel whose FP32 dual bound was negative
+    unsigned long long *q_c2b;  // ... and their final FP32 dual bases (p + 1 row numbers, a byte each)
+    long long q_c2_cap;         // (a full queue sends a set to q_opt without its basis)
     long long q_cap;
     uint8_t *cert_q;            // certificate queue: entries of cert_stride bytes, an int candidate
                                 // index then the nv nonbasic ids of its final FP32 basis

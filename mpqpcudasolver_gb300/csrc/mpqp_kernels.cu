@@ -1685,8 +1685,14 @@ __device__ __forceinline__ bool nonzero_row(const T *g, int p, double tz)
     return gmax > (T)tz * (ah > T(1) ? ah : T(1));
 }
 
+constexpr int kDualMaxP = 6;      // p <= 6
+constexpr int kDualMaxRows = 96;
+constexpr int kDualLd = 12;       // row stride of the dual layout (conflict-free 128-bit loads)
+enum : int { LP_BOUND = 6 };      // record status: "not optimal" proven by a dual bound (t = the bound)
+
 struct OptResult {
     int licq, lp2_status, lp2_piv, cheb_status, cheb_piv, optimal, region;
+    int cert = 0;       // 1: "not optimal" by the FP64 check of the FP32 dual basis (lp2_cert64)
     double t, r;
     double err;         // estimated relative error of the law (law_error), NaN when not computed
     bool decided;
@@ -2199,11 +2205,141 @@ __device__ void chebyshev_ball(const Tol &tol, const InstDesc &I, OptWs<T> &ws, 
     }
 }
 
+// FP64 check of a "not optimal" that the FP32 dual screen found but could not
+// accept under its error margin (ill-conditioned KKT factors), run by the FP64
+// kernel right after its KKT factor.  `basis` holds the p + 1 rows (numbered
+// as region_rows orders them, one byte each) of the screen's final dual basis.
+// Only those rows are formed in FP64 (region_rows' operations in its order,
+// into Gb, (p + 1) x (p + 1) doubles); y solves [g_B | c_B]^T y = e_t in FP32
+// (Gauss-Jordan with partial pivoting, equation e in lane e: any y serves),
+// and for y+ = max(y, 0) and every feasible (theta, t) of LP2 with theta in
+// the box
+//     t <= (h_B.y+ + sum_c |(g_B^T y+)_c| reach_c) / (c_B.y+),
+// evaluated in FP64 (the weak duality of lp2_dual_screen).  A bound below
+// min(0, tol_opt) by more than 1e-7 of the magnitude of its terms leaves the
+// FP64 LP2 optimum of the same rows below tol_opt, so the set is not optimal
+// without the LP.  Returns 1 when proven; *bound_out the bound (NaN: none).
+__device__ __noinline__ int lp2_cert64(const KktData<double> &D, const InstDesc &I, const int *S, const double *Lam,
+                                       int k, unsigned long long basis, double tol_opt, double *Gb,
+                                       double *bound_out)
+{
+    constexpr int MP = kDualMaxP;
+    const int lane = lane_id();
+    const int m = I.m, p = I.p, P1 = p + 1;
+    *bound_out = __longlong_as_double(0x7ff8000000000000LL);
+    int b = -1;
+    if (lane < P1) {
+        const unsigned v = (unsigned)(basis >> (8 * lane)) & 0xffu;
+        b = v == 0xffu ? -1 : (int)v;
+    }
+    if (!__all_sync(FULLMASK, lane >= P1 || (b >= 0 && b < m + I.ncp))) return 0;
+    // the basic rows [g | h]: entry (i, c) in lane i * P1 + c (two rounds)
+    for (int e = lane; e < P1 * P1; e += 32) {
+        const int i = e / P1, c = e - i * P1;
+        const int r = (int)((basis >> (8 * i)) & 0xffu);
+        double v;
+        if (r < k) {
+            v = c < p ? Lam[r * P1 + c] : -Lam[r * P1 + p];
+        } else if (r < m) {
+            int ci = r - k;                                  // the (r - k)-th constraint outside S
+            for (int l = 0; l < k; l++) if (S[l] <= ci) ci++;
+            const double *wmi = D.Wm + (size_t)ci * m;
+            double acc = c < p ? -D.Wh[(size_t)ci * p + c] : D.wc[ci];
+            for (int l = 0; l < k; l++) {
+                const double w = wmi[S[l]];
+                acc = c < p ? xfma(w, Lam[l * P1 + c], acc) : xfma(-w, Lam[l * P1 + p], acc);
+            }
+            v = acc;
+        } else {
+            v = c < p ? D.At[(size_t)(r - m) * p + c] : D.bt[r - m];
+        }
+        Gb[e] = v;
+    }
+    __syncwarp();
+    // y in FP32: lane e < P1 holds equation e over the unknowns y_0..y_p
+    float a[MP + 2];
+#pragma unroll
+    for (int i = 0; i <= MP; i++) {
+        const int bi = __shfl_sync(FULLMASK, b, i < P1 ? i : 0);
+        a[i] = (i < P1 && lane < P1) ? (lane < p ? (float)Gb[i * P1 + lane] : (bi < m ? 1.0f : 0.0f)) : 0.0f;
+    }
+    a[MP + 1] = lane == p ? 1.0f : 0.0f;
+    bool used = lane >= P1;
+    int src = 0;
+#pragma unroll
+    for (int i = 0; i <= MP; i++) {
+        if (i < P1) {
+            float best = used ? -1.0f : fabsf(a[i]);
+            int bl = lane;
+#pragma unroll
+            for (int off = 16; off; off >>= 1) {
+                const float ob = __shfl_xor_sync(FULLMASK, best, off);
+                const int ol = __shfl_xor_sync(FULLMASK, bl, off);
+                if (ob > best || (ob == best && ol < bl)) { best = ob; bl = ol; }
+            }
+            if (!(best > 0.0f)) return 0;                   // singular basis
+            const float inv = 1.0f / __shfl_sync(FULLMASK, a[i], bl);
+            const float f = lane == bl ? 0.0f : a[i] * inv;
+#pragma unroll
+            for (int c = 0; c <= MP + 1; c++) {
+                const float rb = __shfl_sync(FULLMASK, a[c], bl);
+                a[c] = lane == bl ? rb * inv : __fmaf_rn(-f, rb, a[c]);
+            }
+            if (lane == bl) used = true;
+            if (lane == i) src = bl;
+        }
+    }
+    const float yv = __shfl_sync(FULLMASK, a[MP + 1], src);
+    const double yp = lane < P1 ? (double)fmaxf(yv, 0.0f) : 0.0;   // fmaxf maps NaN to 0: still y >= 0
+    // FP64: lane c < p (g_B^T y+)_c and sum y+ |g|; lane p c_B.y+; lane p + 1 h_B.y+ and sum y+ |h|
+    double acc = 0.0, aab = 0.0;
+#pragma unroll
+    for (int i = 0; i <= MP; i++) {
+        if (i < P1) {
+            const double yi = __shfl_sync(FULLMASK, yp, i);
+            const int bi = __shfl_sync(FULLMASK, b, i);
+            if (lane < p) {
+                const double g = Gb[i * P1 + lane];
+                acc = fma(yi, g, acc);
+                aab = fma(yi, fabs(g), aab);
+            } else if (lane == p) {
+                if (bi < m) acc += yi;
+            } else if (lane == P1) {
+                const double h = Gb[i * P1 + p];
+                acc = fma(yi, h, acc);
+                aab = fma(yi, fabs(h), aab);
+            }
+        }
+    }
+    // |theta_c| <= reach_c inside the box (rows c: s theta_c <= bt_c, p + c: -s' theta_c <= bt_{p+c}),
+    // widened by 1e-12 for the rounding of the two quotients
+    double reach = 0.0;
+    if (lane < p) {
+        const double hi = D.bt[lane] / D.At[(size_t)lane * p + lane];
+        const double lo = D.bt[p + lane] / D.At[(size_t)(p + lane) * p + lane];
+        reach = fmax(fabs(lo), fabs(hi)) * (1.0 + 1e-12);
+    }
+    const double cy = __shfl_sync(FULLMASK, acc, p);
+    double num = lane < p ? fabs(acc) * reach : (lane == P1 ? acc : 0.0);
+    double mag = lane < p ? aab * reach : (lane == P1 ? aab : 0.0);
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+        num += __shfl_xor_sync(FULLMASK, num, off);
+        mag += __shfl_xor_sync(FULLMASK, mag, off);
+    }
+    if (!(cy > 0.0)) return 0;
+    const double bound = num / cy;
+    *bound_out = bound;
+    return bound < fmin(0.0, tol_opt) - 1e-7 * (mag / cy) ? 1 : 0;
+}
+
 // Optimality and region verdict of one feasible set (the FP64 path; the FP32
 // screen of the mixed path is k_opt_screen).  LP: the instance is an mpLP.
+// basis (mixed precision, mpQP over a box): the FP32 dual screen's final
+// basis, checked by lp2_cert64 before the LP2 (~0: none).
 template <typename T, bool LP = false>
 __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const InstDesc &I, uint64_t lo, uint64_t hi,
-                                     OptWs<T> &ws)
+                                     OptWs<T> &ws, unsigned long long basis = ~0ull)
 {
     const int lane = lane_id();
     const int m = I.m, p = I.p, ncp = I.ncp, P1 = p + 1, R2 = m + ncp;
@@ -2211,7 +2347,7 @@ __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const 
     const KktData<T> D = kkt_data<T>(B, I);
     OptResult res;
     res.licq = 1; res.lp2_status = LP_SKIPPED; res.lp2_piv = 0; res.cheb_status = LP_SKIPPED; res.cheb_piv = 0;
-    res.optimal = 0; res.region = 0;
+    res.optimal = 0; res.region = 0; res.cert = 0;
     res.t = __longlong_as_double(0x7ff8000000000000LL); res.r = res.t; res.err = res.t;
     res.decided = true;
     const T tpiv = (T)tol.tol_piv;
@@ -2224,6 +2360,18 @@ __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const 
     if constexpr (LP) {
         static_assert(sizeof(T) == 8, "mpLP instances are evaluated in FP64");
         mplp_multipliers(B, I, k, ws);
+    }
+    if constexpr (sizeof(T) == 8 && !LP) {
+        if (basis != ~0ull) {
+            double bound;
+            if (lp2_cert64(D, I, ws.S, ws.Lam, k, basis, tol.tol_opt, ws.Tb, &bound)) {
+                res.lp2_status = LP_BOUND;
+                res.t = bound;
+                res.cert = 1;
+                return res;
+            }
+            __syncwarp();
+        }
     }
     region_rows<T, false, LP>(D, I, lo, hi, k, ws);
     if constexpr (LP) {
@@ -2300,6 +2448,7 @@ __device__ void write_opt(const DevBuffers &B, const Node &nd, int level, const 
         R.cheb_status = res.cheb_status; R.cheb_pivots = res.cheb_piv;
         R.t = res.t; R.r = res.r;
         if (fp64) R.fp64 |= 2;
+        if (res.cert) R.fp64 |= 8;
     }
 }
 
@@ -2363,19 +2512,26 @@ __global__ void __launch_bounds__(128) k_optimality_fp64(DevBuffers B, Tol tol, 
     OptWs<double> ws(smem + wib * slot, sd);
     const int side = level & 1;
     Ctl *ctl = B.ctl;
+    // the FP64 queue, then (mpQP) the sets queued with an FP32 dual basis to check first
     const long long nq = ctl->n_q_opt < B.q_cap ? ctl->n_q_opt : B.q_cap;
+    const long long nc = LP ? 0 : (ctl->n_q_c2 < B.q_c2_cap ? ctl->n_q_c2 : B.q_c2_cap);
     for (;;) {
         long long x;
         if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[LP ? 7 : 4], 1ull);
         x = __shfl_sync(FULLMASK, x, 0);
-        if (x >= nq) break;
-        const Node nd = B.node[side][B.q_opt[x]];
+        if (x >= nq + nc) break;
+        unsigned long long basis = ~0ull;
+        int xn;
+        if (x < nq) xn = B.q_opt[x];
+        else { xn = B.q_c2[x - nq]; basis = B.q_c2b[x - nq]; }
+        const Node nd = B.node[side][xn];
         const InstDesc &I = B.inst[nd.inst];
         if ((I.lp != 0) != LP) continue;
-        const OptResult res = eval_optimality<double, LP>(B, tol, I, nd.lo, nd.hi, ws);
+        const OptResult res = eval_optimality<double, LP>(B, tol, I, nd.lo, nd.hi, ws, basis);
         if (lane == 0) {
             InstCtl *ic = &B.ictl[nd.inst];
             atomicAdd((unsigned long long *)&ic->fb_opt, 1ull);
+            if (res.cert) atomicAdd((unsigned long long *)&ic->cert_lp2, 1ull);
             atomicAdd((unsigned long long *)&ic->lp2_piv, (unsigned long long)res.lp2_piv);
             atomicAdd((unsigned long long *)&ic->cheb_piv, (unsigned long long)res.cheb_piv);
             if (res.optimal) atomicAdd((unsigned long long *)&ic->optimal, 1ull);
@@ -2408,10 +2564,6 @@ __device__ __forceinline__ float warp_sum(float v)
     return v;
 }
 
-constexpr int kDualMaxP = 6;      // p <= 6
-constexpr int kDualMaxRows = 96;
-constexpr int kDualLd = 12;       // row stride of the dual layout (conflict-free 128-bit loads)
-enum : int { LP_BOUND = 6 };      // record status: "not optimal" proven by a dual bound (t = the bound)
 
 // Dual bound of LP2 for an instance whose parameter set is a box
 // lo <= theta <= hi (constraint rows m..m+2p-1: theta_c <= hi_c scaled, then
@@ -2438,7 +2590,7 @@ enum : int { LP_BOUND = 6 };      // record status: "not optimal" proven by a du
 // (column kRowScaleCol), which is at most thr
 __device__ int lp2_dual_screen(const float *T, int m, int R2, int p, const float *blo, const float *bhi, float thr,
                                float ethr, float tol_piv, float tol_dj, int max_it, int degen_switch, int *it_out,
-                               float *bound_out)
+                               float *bound_out, unsigned long long *basis_out = nullptr)
 {
     constexpr int NR = kDualMaxRows / 32;
     constexpr int MP = kDualMaxP;
@@ -2598,6 +2750,16 @@ __device__ int lp2_dual_screen(const float *T, int m, int R2, int p, const float
     }
     *it_out = it;
     *bound_out = bound;
+    if (basis_out) {
+        // the final basis, row numbers of lanes 0..p (0xff past p)
+        unsigned long long word = ~0ull;
+#pragma unroll
+        for (int i = 0; i <= MP; i++) {
+            const int bi = __shfl_sync(FULLMASK, bidx, i);
+            if (i < P1) word = (word & ~(0xffull << (8 * i))) | ((unsigned long long)(bi & 0xff) << (8 * i));
+        }
+        *basis_out = word;
+    }
     return proven;
 }
 
@@ -3702,6 +3864,7 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
         bool decided = false;
         int status = LP_SKIPPED, piv = 0;
         float t = 0.0f;
+        unsigned long long dbasis = ~0ull;
         // mpLP instances (Q = 0) take the primal route and are not screened:
         // every set goes to FP64 (dual_route excludes them)
         if (!(ROUTE == 1 && I.lp) && !kkt_factor<float>(D, I, nd.lo, nd.hi, tol.margin_licq32, ws, &k, &rho)) {
@@ -3735,7 +3898,7 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
                 int pivB = 0;
                 decided = lp2_dual_screen(Tb, m, R2, p, B.fpool + I.f_blo, B.fpool + I.f_bhi, tol.margin_t32 * scale,
                                           tol.margin_t32 * __fdividef(1.0f + (float)p * bmax, rho), tol.tol_piv32,
-                                          tol.tol_dj32, tol.max_pivots, tol.degen_switch, &pivB, &bound);
+                                          tol.tol_dj32, tol.max_pivots, tol.degen_switch, &pivB, &bound, &dbasis);
                 piv += pivB;
                 status = LP_BOUND;
                 t = bound;
@@ -3802,8 +3965,17 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
         lc.c += piv;
         if (!decided) {
             if (lane == 0) {
-                const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_opt, 1ull);
-                if (qi < B.q_cap) B.q_opt[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
+                // a negative FP32 dual bound that the margin did not accept: the
+                // FP64 kernel checks its basis first (lp2_cert64)
+                bool queued = false;
+                if (ROUTE == 0 && status == LP_BOUND && t < 0.0f && dbasis != ~0ull) {
+                    const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_c2, 1ull);
+                    if (qi < B.q_c2_cap) { B.q_c2[qi] = (int)x; B.q_c2b[qi] = dbasis; queued = true; }
+                }
+                if (!queued) {
+                    const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_opt, 1ull);
+                    if (qi < B.q_cap) B.q_opt[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
+                }
             }
             __syncwarp();
             continue;
@@ -3986,6 +4158,7 @@ __global__ void k_finalize(DevBuffers B, int level)
         ctl->n_q_opt = 0;
         ctl->n_q_scr = 0;
         ctl->n_q_s0 = 0;
+        ctl->n_q_c2 = 0;
         ctl->level = level;
     }
 }
