@@ -133,7 +133,10 @@ struct CandRec {                // identical field layout to the oracle's record
     double lp1_bound;           // FP64 dual certificate: the lower bound on z* it proved (NaN: none)
 };
 
-struct HashSlot { uint64_t lo, hi; int inst; int tag; int val; int pad; };
+// key = (plan id << 32) | tag, tag = (epoch << 8) | level: an entry matches
+// only the plan, run and level that wrote it, so a plan's hash memory (from
+// the pool, possibly an earlier plan's) needs no clearing
+struct HashSlot { uint64_t lo, hi; unsigned long long key; int inst; int val; };
 
 // Per-instance level bookkeeping
 struct InstCtl {
@@ -224,6 +227,7 @@ struct DevBuffers {
     uint8_t *ids[2];
     long long ids_cap;
     HashSlot *hash[2];
+    unsigned plan_id;           // unique per plan within the process (the upper half of hash keys)
     long long hash_cap;         // power of two
     Cand *cand;
     long long cand_cap;

@@ -111,41 +111,35 @@ __device__ __forceinline__ long long hash_cap_for(const DevBuffers &B, long long
 }
 
 // probing from slot s (the key's home slot, or later after a collision)
-__device__ int hash_find_from(const HashSlot *tab, long long cap, int tag, int inst, uint64_t lo, uint64_t hi,
-                              uint64_t s)
+__device__ __forceinline__ unsigned long long hash_slot_key(unsigned plan, int tag)
+{
+    return ((unsigned long long)plan << 32) | (unsigned)tag;
+}
+
+__device__ int hash_find_from(const HashSlot *tab, long long cap, unsigned long long key, int inst, uint64_t lo,
+                              uint64_t hi, uint64_t s)
 {
     for (long long probe = 0; probe < cap; probe++) {
         const HashSlot *h = tab + s;
-        if (h->tag != tag) return -1;
+        if (h->key != key) return -1;
         if (h->lo == lo && h->hi == hi && h->inst == inst) return h->val;
         s = (s + 1) & (uint64_t)(cap - 1);
     }
     return -1;
 }
 
-__device__ int hash_find(const HashSlot *tab, long long cap, int tag, int inst, uint64_t lo, uint64_t hi)
-{
-    uint64_t s = hash_key(inst, lo, hi) & (uint64_t)(cap - 1);
-    for (long long probe = 0; probe < cap; probe++) {
-        const HashSlot *h = tab + s;
-        if (h->tag != tag) return -1;
-        if (h->lo == lo && h->hi == hi && h->inst == inst) return h->val;
-        s = (s + 1) & (uint64_t)(cap - 1);
-    }
-    return -1;
-}
-
-__device__ bool hash_insert(HashSlot *tab, long long cap, int tag, int inst, uint64_t lo, uint64_t hi, int val)
+__device__ bool hash_insert(HashSlot *tab, long long cap, unsigned long long key, int inst, uint64_t lo, uint64_t hi,
+                            int val)
 {
     uint64_t s = hash_key(inst, lo, hi) & (uint64_t)(cap - 1);
     for (long long probe = 0; probe < cap; probe++) {
         HashSlot *h = tab + s;
-        const int t = *((volatile int *)&h->tag);
-        if (t != tag && atomicCAS(&h->tag, t, tag) == t) {
+        const unsigned long long t = *((volatile unsigned long long *)&h->key);
+        if (t != key && atomicCAS(&h->key, t, key) == t) {
             h->lo = lo; h->hi = hi; h->inst = inst; h->val = val;
             return true;
         }
-        if (t == tag) s = (s + 1) & (uint64_t)(cap - 1);
+        if (t == key) s = (s + 1) & (uint64_t)(cap - 1);
     }
     return false;
 }
@@ -647,7 +641,8 @@ __global__ void k_enumerate(DevBuffers B, int level)
     const int pside = (level - 1) & 1;
     Ctl *ctl = B.ctl;
     const long long npar = ctl->n_node[pside] < B.node_cap ? ctl->n_node[pside] : B.node_cap;
-    const int tag_prev = (ctl->epoch << 8) | (level - 1);  // tag of the previous level's hash entries
+    // key of the previous level's hash entries
+    const unsigned long long tag_prev = hash_slot_key(B.plan_id, (ctl->epoch << 8) | (level - 1));
     // slots the previous level's inserts used (every expandable parent was
     // inserted, which sets it; the full table otherwise, which is always in bounds)
     const long long hcap = ctl->hcap[pside] >= 16 && ctl->hcap[pside] <= B.hash_cap ? ctl->hcap[pside] : B.hash_cap;
@@ -748,7 +743,7 @@ __global__ void k_enumerate(DevBuffers B, int level)
 #pragma unroll
                     for (int g = 0; g < G; g++) {
                         if (g < n && ok) {
-                            if (hs[g].tag != tag_prev) ok = false;
+                            if (hs[g].key != tag_prev) ok = false;
                             else if (!(hs[g].lo == slo[g] && hs[g].hi == shi[g] && hs[g].inst == cinst))
                                 ok = hash_find_from(tab, hcap, tag_prev, cinst, slo[g], shi[g],
                                                     (sidx[g] + 1) & (uint64_t)(hcap - 1)) >= 0;
@@ -894,7 +889,8 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
             nd.tab_off = -1; nd.ids_off = -1; nd.rec = rec;
             B.node[side][idx] = nd;
             if (feasible && !B.exhaustive) {
-                if (!hash_insert(B.hash[side], hcap, (ctl->epoch << 8) | level, inst, lo, hi, (int)idx))
+                if (!hash_insert(B.hash[side], hcap, hash_slot_key(B.plan_id, (ctl->epoch << 8) | level), inst, lo, hi,
+                                 (int)idx))
                     atomicOr(&ctl->overflow, OV_HASH);
             }
         }
@@ -938,7 +934,8 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
         B.node[side][idx] = nd;
         // the hash serves the subset test of the next level only
         if (feasible && !B.exhaustive && need_tab) {
-            if (!hash_insert(B.hash[side], hcap, (ctl->epoch << 8) | level, inst, lo, hi, (int)idx))
+            if (!hash_insert(B.hash[side], hcap, hash_slot_key(B.plan_id, (ctl->epoch << 8) | level), inst, lo, hi,
+                                 (int)idx))
                 atomicOr(&ctl->overflow, OV_HASH);
         }
     }
@@ -4072,7 +4069,8 @@ __global__ void k_level0(DevBuffers B)
         nd.rec = (B.rec && inst < B.rec_cap) ? inst : -1;
         B.node[0][inst] = nd;
         if (!B.exhaustive) {
-            hash_insert(B.hash[0], hash_cap_for(B, B.n_inst), ctl->epoch << 8, inst, 0, 0, inst);
+            hash_insert(B.hash[0], hash_cap_for(B, B.n_inst), hash_slot_key(B.plan_id, ctl->epoch << 8), inst, 0, 0,
+                        inst);
         }
         if (nd.rec >= 0) {
             CandRec &R = B.rec[nd.rec];
