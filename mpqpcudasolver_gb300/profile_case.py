@@ -66,7 +66,8 @@ def main(argv=None):
                       "device_ms": r.device_ms, "timed_ms": r2.device_ms,
                       "cand_per_s": r.candidates / (r.device_ms / 1e3),
                       "kernels": {k: [round(v[0], 3), v[1]] for k, v in kt.items()},
-                      "fallbacks": [r.total("fallback_lp1"), r.total("fallback_opt")]}))
+                      "fallbacks": [r.total("fallback_lp1"), r.total("fallback_opt")],
+                      "lp2_certified": r.total("lp2_certified")}))
     plan.close()
     if r.status != 0 or r2.status != 0:
         print(f"status {r.status} / {r2.status}: {solver.last_error()}", file=sys.stderr)
