@@ -135,8 +135,12 @@ struct CandRec {                // identical field layout to the oracle's record
 
 // key = (plan id << 32) | tag, tag = (epoch << 8) | level: an entry matches
 // only the plan, run and level that wrote it, so a plan's hash memory (from
-// the pool, possibly an earlier plan's) needs no clearing
-struct HashSlot { uint64_t lo, hi; unsigned long long key; int inst; int val; };
+// the pool, possibly an earlier plan's) needs no clearing.  fp: the set's
+// 64-bit hash (instance and mask; its low bits are the home slot).  Two sets
+// share an fp with probability 2^-64; a set then found in place of an absent
+// subset is only left unpruned, and its LP1 (a superset of an infeasible set)
+// is infeasible, so no verdict depends on it.
+struct HashSlot { unsigned long long key; uint64_t fp; };
 
 // Per-instance level bookkeeping
 struct InstCtl {

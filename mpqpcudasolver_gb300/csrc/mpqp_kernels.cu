@@ -116,27 +116,26 @@ __device__ __forceinline__ unsigned long long hash_slot_key(unsigned plan, int t
     return ((unsigned long long)plan << 32) | (unsigned)tag;
 }
 
-__device__ int hash_find_from(const HashSlot *tab, long long cap, unsigned long long key, int inst, uint64_t lo,
-                              uint64_t hi, uint64_t s)
+__device__ int hash_find_from(const HashSlot *tab, long long cap, unsigned long long key, uint64_t fp, uint64_t s)
 {
     for (long long probe = 0; probe < cap; probe++) {
         const HashSlot *h = tab + s;
         if (h->key != key) return -1;
-        if (h->lo == lo && h->hi == hi && h->inst == inst) return h->val;
+        if (h->fp == fp) return 1;
         s = (s + 1) & (uint64_t)(cap - 1);
     }
     return -1;
 }
 
-__device__ bool hash_insert(HashSlot *tab, long long cap, unsigned long long key, int inst, uint64_t lo, uint64_t hi,
-                            int val)
+__device__ bool hash_insert(HashSlot *tab, long long cap, unsigned long long key, int inst, uint64_t lo, uint64_t hi)
 {
-    uint64_t s = hash_key(inst, lo, hi) & (uint64_t)(cap - 1);
+    const uint64_t fp = hash_key(inst, lo, hi);
+    uint64_t s = fp & (uint64_t)(cap - 1);
     for (long long probe = 0; probe < cap; probe++) {
         HashSlot *h = tab + s;
         const unsigned long long t = *((volatile unsigned long long *)&h->key);
         if (t != key && atomicCAS(&h->key, t, key) == t) {
-            h->lo = lo; h->hi = hi; h->inst = inst; h->val = val;
+            h->fp = fp;
             return true;
         }
         if (t == key) s = (s + 1) & (uint64_t)(cap - 1);
@@ -722,18 +721,19 @@ __global__ void k_enumerate(DevBuffers B, int level)
                 uint64_t rlo = clo0, rhi = chi0;
                 while (ok && (rlo | rhi)) {
                     constexpr int G = 4;
-                    uint64_t slo[G], shi[G], sidx[G];
+                    uint64_t sfp[G], sidx[G];
                     int n = 0;
 #pragma unroll
                     for (int g = 0; g < G; g++) {
-                        slo[g] = 0; shi[g] = 0; sidx[g] = 0;
+                        sfp[g] = 0; sidx[g] = 0;
                         if (rlo | rhi) {
                             int a;
                             if (rlo) { a = __ffsll((long long)rlo) - 1; rlo &= rlo - 1; }
                             else { a = 64 + __ffsll((long long)rhi) - 1; rhi &= rhi - 1; }
-                            slo[g] = lo; shi[g] = hi;
-                            if (a < 64) slo[g] &= ~(1ull << a); else shi[g] &= ~(1ull << (a - 64));
-                            sidx[g] = hash_key(cinst, slo[g], shi[g]) & (uint64_t)(hcap - 1);
+                            uint64_t slo = lo, shi = hi;
+                            if (a < 64) slo &= ~(1ull << a); else shi &= ~(1ull << (a - 64));
+                            sfp[g] = hash_key(cinst, slo, shi);
+                            sidx[g] = sfp[g] & (uint64_t)(hcap - 1);
                             n = g + 1;
                         }
                     }
@@ -744,8 +744,8 @@ __global__ void k_enumerate(DevBuffers B, int level)
                     for (int g = 0; g < G; g++) {
                         if (g < n && ok) {
                             if (hs[g].key != tag_prev) ok = false;
-                            else if (!(hs[g].lo == slo[g] && hs[g].hi == shi[g] && hs[g].inst == cinst))
-                                ok = hash_find_from(tab, hcap, tag_prev, cinst, slo[g], shi[g],
+                            else if (hs[g].fp != sfp[g])
+                                ok = hash_find_from(tab, hcap, tag_prev, sfp[g],
                                                     (sidx[g] + 1) & (uint64_t)(hcap - 1)) >= 0;
                         }
                     }
@@ -889,8 +889,7 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
             nd.tab_off = -1; nd.ids_off = -1; nd.rec = rec;
             B.node[side][idx] = nd;
             if (feasible && !B.exhaustive) {
-                if (!hash_insert(B.hash[side], hcap, hash_slot_key(B.plan_id, (ctl->epoch << 8) | level), inst, lo, hi,
-                                 (int)idx))
+                if (!hash_insert(B.hash[side], hcap, hash_slot_key(B.plan_id, (ctl->epoch << 8) | level), inst, lo, hi))
                     atomicOr(&ctl->overflow, OV_HASH);
             }
         }
@@ -934,8 +933,7 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
         B.node[side][idx] = nd;
         // the hash serves the subset test of the next level only
         if (feasible && !B.exhaustive && need_tab) {
-            if (!hash_insert(B.hash[side], hcap, hash_slot_key(B.plan_id, (ctl->epoch << 8) | level), inst, lo, hi,
-                                 (int)idx))
+            if (!hash_insert(B.hash[side], hcap, hash_slot_key(B.plan_id, (ctl->epoch << 8) | level), inst, lo, hi))
                 atomicOr(&ctl->overflow, OV_HASH);
         }
     }
@@ -4069,8 +4067,7 @@ __global__ void k_level0(DevBuffers B)
         nd.rec = (B.rec && inst < B.rec_cap) ? inst : -1;
         B.node[0][inst] = nd;
         if (!B.exhaustive) {
-            hash_insert(B.hash[0], hash_cap_for(B, B.n_inst), hash_slot_key(B.plan_id, ctl->epoch << 8), inst, 0, 0,
-                        inst);
+            hash_insert(B.hash[0], hash_cap_for(B, B.n_inst), hash_slot_key(B.plan_id, ctl->epoch << 8), inst, 0, 0);
         }
         if (nd.rec >= 0) {
             CandRec &R = B.rec[nd.rec];
