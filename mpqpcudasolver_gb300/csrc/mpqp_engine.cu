@@ -33,7 +33,7 @@ size_t screen_smem_per_warp(const SlotDims &sd, int route);
 size_t screen_tiles_smem(const SlotDims &sd, int tile_w);
 size_t screen_lanes_smem();
 cudaError_t launch_opt_screen_lanes(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode,
-                                    int grid, size_t smem, cudaStream_t s, int cap);
+                                    int grid, size_t smem, cudaStream_t s, int pass, int cap);
 bool screen_dual_route(int mode, const InstDesc &I, const SlotDims &sd);
 bool screen_lanes_route(int mode, const InstDesc &I, const SlotDims &sd);
 size_t laws_smem_per_warp(const SlotDims &sd);
@@ -363,7 +363,8 @@ struct mpqp_plan {
     size_t smem_tiles = 0;
     int grid_lanes = 0;         // ... at levels |S| <= kLaneMaxK: one set per thread
     size_t smem_lanes = 0;
-    int lane_cap = 3;           // pivots of its first pass (MPQP_SCREEN_CAP), the rest rerun uncapped
+    int lane_cap = 3;           // pivots of its first pass (MPQP_SCREEN_CAP)
+    int lane_cap2 = 6;          // ... of its second (MPQP_SCREEN_CAP2; 0: uncapped, no third pass)
     // launch settings the autotuner chooses: threads per set in the screen's
     // first stage, warps per LP1 block, candidates an LP1 warp claims at once
     int tile_w = 8, feas_warps = 4, feas_chunk = 32;
@@ -576,9 +577,13 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
         const bool lanes = level <= kLaneMaxK && !B.lp2b[0] && (P->screen_dual || P->lanes_lp);
         if (lanes) {
             L("k_opt_screen<dual,lanes>", launch_opt_screen_lanes(B, P->tol, P->sd, level, P->lp2_screen,
-                                                                  P->grid_lanes, P->smem_lanes, s, P->lane_cap));
+                                                                  P->grid_lanes, P->smem_lanes, s, 0, P->lane_cap));
             L("k_opt_screen<dual,lanes,rerun>", launch_opt_screen_lanes(B, P->tol, P->sd, level, P->lp2_screen,
-                                                                        P->grid_lanes, P->smem_lanes, s, 0));
+                                                                        P->grid_lanes, P->smem_lanes, s, 1,
+                                                                        P->lane_cap2));
+            if (P->lane_cap2 > 0)
+                L("k_opt_screen<dual,lanes,rerun2>", launch_opt_screen_lanes(B, P->tol, P->sd, level, P->lp2_screen,
+                                                                             P->grid_lanes, P->smem_lanes, s, 2, 0));
             if (P->lanes_lp)
                 L("k_opt_screen<dual,stationarity>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 3,
                                                                        P->grid_tiles, P->smem_tiles, s, P->tile_w));
@@ -841,6 +846,8 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
     AL(B.q_opt, sizeof(int) * cand_cap);
     B.q_s0_cap = P->prec == PREC_MIXED ? std::max(cand_cap / 4, (long long)4096) : 0;
     if (B.q_s0_cap) AL(B.q_s0, sizeof(int) * B.q_s0_cap);
+    B.q_s1_cap = P->prec == PREC_MIXED ? std::max(cand_cap / 16, (long long)4096) : 0;
+    if (B.q_s1_cap) AL(B.q_s1, sizeof(int) * B.q_s1_cap);
     // sets the FP32 dual screen found not optimal below its margin's reach: a
     // sixteenth of the candidates (a full queue sends the rest to q_opt)
     B.q_c2_cap = P->prec == PREC_MIXED ? std::max(cand_cap / 16, (long long)4096) : 0;
@@ -883,6 +890,8 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
     P->smem_tiles = screen_tiles_smem(sd, P->tile_w);
     P->smem_lanes = screen_lanes_smem();
     if (const char *e = getenv("MPQP_SCREEN_CAP")) P->lane_cap = std::max(1, atoi(e));
+    if (const char *e = getenv("MPQP_SCREEN_CAP2")) P->lane_cap2 = std::max(0, atoi(e));
+    if (P->lane_cap2 > 0 && P->lane_cap2 <= P->lane_cap) P->lane_cap2 = 0;
     for (const InstDesc &d : P->desc) {
         if (d.lp) P->has_lp = true; else P->has_qp = true;
         if (P->prec != PREC_MIXED) continue;

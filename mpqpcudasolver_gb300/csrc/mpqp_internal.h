@@ -191,7 +191,8 @@ struct Ctl {
     long long n_q_lp1, n_q_opt; // FP64 fallback queue lengths
     long long n_q_scr;          // sets the first stage of the dual screen left to its second
     long long n_q_cert;         // FP32 LP1 optima waiting for the FP64 dual certificate
-    long long n_q_s0;           // first-stage dual LPs cut off at the iteration cap, run again uncapped
+    long long n_q_s0;           // first-stage dual LPs cut off at the first pass's cap, run again
+    long long n_q_s1;           // ... and those cut off again at the second pass's cap
     long long n_q_c2;           // sets for the FP64 kernel with an FP32 dual basis to check first
     unsigned long long ctr[kCtlCounters];  // work counters (reset every level)
     int overflow;               // bit mask of overflowed buffers
@@ -237,8 +238,10 @@ struct DevBuffers {
     long long cand_cap;
     int *q_lp1;                 // candidate indices for the FP64 LP1 re-solve
     int *q_opt;                 // node indices for the FP64 optimality re-solve
-    int *q_s0;                  // node indices for the uncapped rerun of the first-stage dual LP
+    int *q_s0;                  // node indices for the second pass of the first-stage dual LP
     long long q_s0_cap;         // (a full queue sends a set to the second stage instead)
+    int *q_s1;                  // node indices for its third pass (uncapped)
+    long long q_s1_cap;
     int *q_c2;                  // node indices for the FP64 kernel whose FP32 dual bound was negative
     unsigned long long *q_c2b;  // ... and their final FP32 dual bases (p + 1 row numbers, a byte each)
     long long q_c2_cap;         // (a full queue sends a set to q_opt without its basis)

@@ -3400,14 +3400,15 @@ constexpr int kLaneP1 = kDualMaxP + 1;
 // multiplier rows' error scales, S, the basic rows (R and Y live in registers)
 constexpr int kLaneWords = kLaneMaxK * kLaneP1 + kLaneP1 * kDualMaxP + 3 * kLaneP1 + 2 * kLaneMaxK;
 
-// cap > 0 (the first pass over the level's nodes): an LP still running after
-// cap pivots stops, and its set goes to B.q_s0; cap = 0: the second pass,
-// over B.q_s0, runs them to the end (the same LP from the same start, so the
-// same result as one uncapped pass).  The 32 sets of a warp then mostly share
-// a pivot count in the first pass, instead of all waiting for the slowest
-// (a fifth of the sets need 4 to 25 pivots).
+// pass 0 runs over the level's nodes, pass 1 over B.q_s0, pass 2 over B.q_s1.
+// cap > 0: an LP still running after cap pivots stops, and its set goes to the
+// next pass's queue (q_s0 after pass 0, q_s1 after pass 1); cap = 0: the LP
+// runs to the end.  Each pass runs an LP again from the same start, so the
+// result is that of one uncapped pass.  The 32 sets of a warp then mostly
+// share a pivot count, instead of all waiting for the slowest (a fifth of the
+// sets need 4 to 25 pivots).
 __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, SlotDims sd, int level, int mode,
-                                                         int cap)
+                                                         int pass, int cap)
 {
     extern __shared__ __align__(16) float lsm[];
     constexpr int KM = kLaneMaxK, P7 = kLaneP1, MP = kDualMaxP;
@@ -3421,8 +3422,9 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
     int *Bx = Sx + KM * 32;                // basic row of basic variable i
     const int side = level & 1;
     Ctl *ctl = B.ctl;
-    const long long nn = cap > 0 ? (ctl->n_node[side] < B.node_cap ? ctl->n_node[side] : B.node_cap)
-                                 : (ctl->n_q_s0 < B.q_s0_cap ? ctl->n_q_s0 : B.q_s0_cap);
+    const long long nn = pass == 0 ? (ctl->n_node[side] < B.node_cap ? ctl->n_node[side] : B.node_cap)
+                       : pass == 1 ? (ctl->n_q_s0 < B.q_s0_cap ? ctl->n_q_s0 : B.q_s0_cap)
+                                   : (ctl->n_q_s1 < B.q_s1_cap ? ctl->n_q_s1 : B.q_s1_cap);
     LocalInstCounters lc;
     lc.reset(-1);
     auto flush = [&]() {
@@ -3435,11 +3437,11 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
     const int max_it = cap > 0 ? cap : tol.max_pivots;
     for (;;) {
         long long x0;
-        if (lane == 0) x0 = (long long)atomicAdd(&ctl->ctr[cap > 0 ? 3 : 9], 32ull);
+        if (lane == 0) x0 = (long long)atomicAdd(&ctl->ctr[pass == 0 ? 3 : (pass == 1 ? 9 : 11)], 32ull);
         x0 = __shfl_sync(FULLMASK, x0, 0);
         if (x0 >= nn) break;
         if (x0 + lane >= nn) continue;
-        const long long x = cap > 0 ? x0 + lane : (long long)B.q_s0[x0 + lane];
+        const long long x = pass == 0 ? x0 + lane : (long long)(pass == 1 ? B.q_s0 : B.q_s1)[x0 + lane];
         const Node nd = B.node[side][x];
         if ((nd.flags & (NODE_VALID | NODE_FEASIBLE)) != (NODE_VALID | NODE_FEASIBLE)) continue;
         const InstDesc &I = B.inst[nd.inst];
@@ -3753,9 +3755,15 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
                 bland = degen >= tol.degen_switch;
             }
             if (capped) {
-                // the uncapped pass runs this set again from the start
-                const long long qi = queue_slot(&ctl->n_q_s0);
-                if (qi < B.q_s0_cap) { B.q_s0[qi] = (int)x; continue; }
+                // the next pass runs this set again from the start (a full
+                // queue sends it to the second stage)
+                if (pass == 0) {
+                    const long long qi = queue_slot(&ctl->n_q_s0);
+                    if (qi < B.q_s0_cap) { B.q_s0[qi] = (int)x; continue; }
+                } else {
+                    const long long qi = queue_slot(&ctl->n_q_s1);
+                    if (qi < B.q_s1_cap) { B.q_s1[qi] = (int)x; continue; }
+                }
             }
             piv = it;
             to_rows = !proven;
@@ -3789,9 +3797,9 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
 size_t screen_lanes_smem() { return (size_t)kLaneWords * 32 * sizeof(float); }
 
 cudaError_t launch_opt_screen_lanes(const DevBuffers &B, const Tol &tol, const SlotDims &sd, int level, int mode,
-                                    int grid, size_t smem, cudaStream_t s, int cap)
+                                    int grid, size_t smem, cudaStream_t s, int pass, int cap)
 {
-    k_opt_screen_lanes<<<grid, 32, smem, s>>>(B, tol, sd, level, mode, cap);
+    k_opt_screen_lanes<<<grid, 32, smem, s>>>(B, tol, sd, level, mode, pass, cap);
     return cudaGetLastError();
 }
 
@@ -4153,6 +4161,7 @@ __global__ void k_finalize(DevBuffers B, int level)
         ctl->n_q_opt = 0;
         ctl->n_q_scr = 0;
         ctl->n_q_s0 = 0;
+        ctl->n_q_s1 = 0;
         ctl->n_q_c2 = 0;
         ctl->level = level;
     }

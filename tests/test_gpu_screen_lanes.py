@@ -3,13 +3,14 @@
 At levels with |S| <= 6 the first stage runs one set per thread
 (k_opt_screen_lanes): a first pass stops each dual LP after a few pivots
 (MPQP_SCREEN_CAP, default 3) and queues the set; a second pass reruns the
-queued sets uncapped from the same start; a set that does not fit the rerun
-queue goes to the second stage (all region rows) instead.  None of this may
-change a verdict: every "not optimal" is re-verified from max(y, 0), and
-every other set is decided by a later stage or in FP64.  So the feasible,
-optimal and region sets, and the FP64 t* and r*, must not depend on the cap
--- at cap 1 most sets are rerun and the rerun queue overflows, at 1000 none
-is -- and must equal the oracle's.
+queued sets from the same start, stopping again after MPQP_SCREEN_CAP2
+pivots (default 6; 0: uncapped), and a third pass runs those to the end; a
+set that does not fit a rerun queue goes to the second stage (all region
+rows) instead.  None of this may change a verdict: every "not optimal" is
+re-verified from max(y, 0), and every other set is decided by a later stage
+or in FP64.  So the feasible, optimal and region sets, and the FP64 t* and
+r*, must not depend on the caps -- at caps 1 and 2 most sets are rerun twice
+and the rerun queues overflow, at 1000 none is -- and must equal the oracle's.
 """
 import numpy as np
 import pytest
@@ -35,12 +36,14 @@ def test_pivot_cap_and_rerun_keep_every_verdict(gpu_lib, case, monkeypatch):
     probs = [P.scale_problem(p) for p in make()]
     kw = dict(k_max=kmax, cand_cap=1 << 22, arena_bytes=1 << 30)
     runs = {}
-    for cap in ("3", "1", "1000"):
-        monkeypatch.setenv("MPQP_SCREEN_CAP", cap)
+    for cap in ("3", "1", "1000", "3/0"):
+        c1, _, c2 = cap.partition("/")
+        monkeypatch.setenv("MPQP_SCREEN_CAP", c1)
+        monkeypatch.setenv("MPQP_SCREEN_CAP2", c2 or ("2" if c1 == "1" else "6"))
         runs[cap] = solver.solve(probs, precision=solver.MIXED, **kw)
         assert runs[cap].status == 0
     base = runs["3"]
-    for cap in ("1", "1000"):
+    for cap in ("1", "1000", "3/0"):
         for f in FIELDS:
             assert np.array_equal(base.inst[f], runs[cap].inst[f]), (cap, f)
         a, b = base.opt, runs[cap].opt
