@@ -359,6 +359,7 @@ struct mpqp_plan {
     bool pooled = false;        // allocations came from the device pool
     int grid_opt2 = 0;          // grid of the primal route (grid_opt: the dual route)
     int grid_opt3 = 0;          // grid of the dual route's second stage
+    int grid_opt_lprows = 0;    // the dual route's second stage for mpLP sets with |S| = n
     int grid_tiles = 0;         // the dual route's first stage (one set per tile of tile_w threads)
     size_t smem_tiles = 0;
     int grid_lanes = 0;         // ... at levels |S| <= kLaneMaxK: one set per thread
@@ -591,6 +592,10 @@ static int enqueue(mpqp_plan *P, cudaStream_t s, bool timed)
         if (!lanes && (P->screen_dual || P->lanes_lp))
             L("k_opt_screen<dual>", launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 0, P->grid_tiles,
                                                       P->smem_tiles, s, P->tile_w));
+        if (P->lanes_lp)
+            L("k_opt_screen<dual,rows,mplp>",
+              launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 6, P->grid_opt_lprows, P->smem_opt, s,
+                                P->tile_w));
         if (P->screen_dual) {
             L("k_opt_screen<dual,rows>",
               launch_opt_screen(B, P->tol, P->sd, level, P->lp2_screen, 2, P->grid_opt3, P->smem_opt, s, P->tile_w));
@@ -910,6 +915,9 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
                   : grid_for(kernel_ptr("opt64"), P->smem_opt, &P->grid_opt)) ||
         (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_primal"), P->smem_opt2, &P->grid_opt2, 32) : 0) ||
         (rc = P->prec == PREC_MIXED ? grid_for(kernel_ptr("screen_dual_rows"), P->smem_opt, &P->grid_opt3, 32) : 0) ||
+        (rc = P->prec == PREC_MIXED && P->lanes_lp ? grid_for(kernel_ptr("screen_dual_rows_lp"), P->smem_opt,
+                                                              &P->grid_opt_lprows, 32)
+                                                   : 0) ||
         (rc = P->prec == PREC_MIXED
                   ? grid_for(kernel_ptr(P->B.lp2b[0] ? (P->tile_w == 8 ? "screen_dual_tiles8w"
                                                        : P->tile_w == 16 ? "screen_dual_tiles16w"

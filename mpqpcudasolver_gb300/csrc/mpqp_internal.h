@@ -174,7 +174,7 @@ struct InstCtl {
     int pad;
 };
 
-constexpr int kCtlCounters = 12;
+constexpr int kCtlCounters = 13;
 
 // levels whose sets have at most this many elements run the first stage of
 // the FP32 dual screen with one set per thread (k_opt_screen_lanes)

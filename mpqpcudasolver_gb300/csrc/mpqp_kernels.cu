@@ -1871,16 +1871,17 @@ __device__ int kkt_factor(const KktData<T> &D, const InstDesc &I, uint64_t lo, u
 // max(1, max |g|) over all rows, the start value and growth reference of LP2.
 template <typename T, bool track = false, bool LP = false>
 __device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, uint64_t hi, int k, OptWs<T> &ws,
-                         T *out = nullptr, int ldo = 0, int hcol = 0, T *t0_out = nullptr, T *g0_out = nullptr)
+                         T *out = nullptr, int ldo = 0, int hcol = 0, T *t0_out = nullptr, T *g0_out = nullptr,
+                         bool lpm = LP)
 {
     const int lane = lane_id();
     const int m = I.m, p = I.p, ncp = I.ncp, P1 = p + 1;
     const int *S = ws.S;
     const T *Lam = ws.Lam;
-    // lambda rows: Lambda (mpQP) or Psi (LP: an mpLP instance; never with
-    // track, which the FP32 screen uses and which sums |Lambda| of these rows)
-    static_assert(!(LP && track), "the FP32 screen does not take mpLP instances");
-    const T *LamL = LP ? ws.Psi : Lam;
+    // lambda rows: Lambda (mpQP) or Psi (lpm: an mpLP instance, whose
+    // inactive rows come from Gamma in Lam; the error scales of those rows
+    // then sum |Gamma_l|, not the multiplier rows' |Psi_l|)
+    const T *LamL = lpm ? ws.Psi : Lam;
     T *G = out ? out : ws.G;
     const int ldg = out ? ldo : P1, hc = out ? hcol : p;
     T amax = T(0);
@@ -1899,7 +1900,14 @@ __device__ T region_rows(const KktData<T> &D, const InstDesc &I, uint64_t lo, ui
         G[a * ldg + hc] = h;
         if (want_t0 && h < tmin) tmin = h;
         if (track) {
-            rs += xabs(LamL[a * P1 + p]); labs[a] = rs; if (rs > amax) amax = rs;
+            rs += xabs(LamL[a * P1 + p]); if (rs > amax) amax = rs;
+            if (lpm) {
+                T gs = T(0);
+                for (int cc = 0; cc <= p; cc++) gs += xabs(Lam[a * P1 + cc]);
+                labs[a] = gs;
+            } else {
+                labs[a] = rs;
+            }
             if (out) G[a * ldg + kRowScaleCol] = rs;
         }
     }
@@ -2214,9 +2222,9 @@ __device__ void chebyshev_ball(const Tol &tol, const InstDesc &I, OptWs<T> &ws, 
 // min(0, tol_opt) by more than 1e-7 of the magnitude of its terms leaves the
 // FP64 LP2 optimum of the same rows below tol_opt, so the set is not optimal
 // without the LP.  Returns 1 when proven; *bound_out the bound (NaN: none).
-__device__ __noinline__ int lp2_cert64(const KktData<double> &D, const InstDesc &I, const int *S, const double *Lam,
-                                       int k, unsigned long long basis, double tol_opt, double *Gb,
-                                       double *bound_out)
+__device__ __noinline__ int lp2_cert64(const KktData<double> &D, const InstDesc &I, const int *S, const double *LamM,
+                                       const double *Lam, int k, unsigned long long basis, double tol_opt,
+                                       double *Gb, double *bound_out)
 {
     constexpr int MP = kDualMaxP;
     const int lane = lane_id();
@@ -2234,7 +2242,7 @@ __device__ __noinline__ int lp2_cert64(const KktData<double> &D, const InstDesc 
         const int r = (int)((basis >> (8 * i)) & 0xffu);
         double v;
         if (r < k) {
-            v = c < p ? Lam[r * P1 + c] : -Lam[r * P1 + p];
+            v = c < p ? LamM[r * P1 + c] : -LamM[r * P1 + p];
         } else if (r < m) {
             int ci = r - k;                                  // the (r - k)-th constraint outside S
             for (int l = 0; l < k; l++) if (S[l] <= ci) ci++;
@@ -2356,10 +2364,11 @@ __device__ OptResult eval_optimality(const DevBuffers &B, const Tol &tol, const 
         static_assert(sizeof(T) == 8, "mpLP instances are evaluated in FP64");
         mplp_multipliers(B, I, k, ws);
     }
-    if constexpr (sizeof(T) == 8 && !LP) {
-        if (basis != ~0ull) {
+    // mpQP, and mpLP with |S| = n (the same LP2 rows, multipliers -Psi)
+    if constexpr (sizeof(T) == 8) {
+        if (basis != ~0ull && (!LP || k == I.n)) {
             double bound;
-            if (lp2_cert64(D, I, ws.S, ws.Lam, k, basis, tol.tol_opt, ws.Tb, &bound)) {
+            if (lp2_cert64(D, I, ws.S, LP ? ws.Psi : ws.Lam, ws.Lam, k, basis, tol.tol_opt, ws.Tb, &bound)) {
                 res.lp2_status = LP_BOUND;
                 res.t = bound;
                 res.cert = 1;
@@ -2507,9 +2516,9 @@ __global__ void __launch_bounds__(128) k_optimality_fp64(DevBuffers B, Tol tol, 
     OptWs<double> ws(smem + wib * slot, sd);
     const int side = level & 1;
     Ctl *ctl = B.ctl;
-    // the FP64 queue, then (mpQP) the sets queued with an FP32 dual basis to check first
+    // the FP64 queue, then the sets queued with an FP32 dual basis to check first
     const long long nq = ctl->n_q_opt < B.q_cap ? ctl->n_q_opt : B.q_cap;
-    const long long nc = LP ? 0 : (ctl->n_q_c2 < B.q_c2_cap ? ctl->n_q_c2 : B.q_c2_cap);
+    const long long nc = ctl->n_q_c2 < B.q_c2_cap ? ctl->n_q_c2 : B.q_c2_cap;
     for (;;) {
         long long x;
         if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[LP ? 7 : 4], 1ull);
@@ -2765,7 +2774,8 @@ __host__ __device__ inline size_t screen_warp_bytes(const SlotDims &sd, int rout
 {
     return align16((size_t)sd.maxK * sd.maxK * 4) + 2 * align16((size_t)sd.maxK * sd.maxP1 * 4) +
            align16((size_t)sd.maxK * sizeof(int)) + align16((size_t)(sd.maxR2 + 1) * sd.maxLD2 * 4) +
-           align16((size_t)sd.maxR2 + sd.maxP1) + (route == 1 ? align16((size_t)sd.maxR2 * sd.maxP1 * 4) : 0);
+           align16((size_t)sd.maxR2 + sd.maxP1) + (route == 1 ? align16((size_t)sd.maxR2 * sd.maxP1 * 4) : 0) +
+           (route != 1 && sd.maxN ? align16((size_t)sd.maxK * sd.maxP1 * 4) : 0);
 }
 
 // The FP32 screen of every feasible set of a level, one warp per set.  Only a
@@ -2788,6 +2798,38 @@ __host__ __device__ __forceinline__ bool dual_route(int mode, const InstDesc &I,
 __host__ __device__ __forceinline__ bool lanes_route(int mode, const InstDesc &I, const SlotDims &sd)
 {
     return I.lp ? (mode == 0 && I.box && I.p <= kDualMaxP) : dual_route(mode, I, sd);
+}
+
+// mpLP in the FP32 screen: Lam holds Gamma = (A_S A_S^T)^-1 [F_S | b_S] after
+// kkt_factor<float>; the multiplier law Psi = (A_S A_S^T)^-1 [A_S H | A_S c]
+// (FP32 copies of A H, A c) from the same factor, reciprocal pivots on R's
+// diagonal, in place per column (lane per column).  Out of line, so that the
+// mpQP sets' path keeps its registers.
+__device__ __noinline__ void mplp_multipliers_f(const float *WhL, const float *wcL, int p, int k, OptWs<float> &ws)
+{
+    const int P1 = p + 1;
+    for (int cc = lane_id(); cc < P1; cc += 32) {
+        for (int a = 0; a < k; a++) {
+            float acc = cc < p ? WhL[(size_t)ws.S[a] * p + cc] : wcL[ws.S[a]];
+            for (int l = 0; l < a; l++) acc = __fmaf_rn(-ws.R[l * k + a], ws.Psi[l * P1 + cc], acc);
+            ws.Psi[a * P1 + cc] = acc * ws.R[a * k + a];
+        }
+        for (int a = k - 1; a >= 0; a--) {
+            float acc = ws.Psi[a * P1 + cc];
+            for (int l = a + 1; l < k; l++) acc = __fmaf_rn(-ws.R[a * k + l], ws.Psi[l * P1 + cc], acc);
+            ws.Psi[a * P1 + cc] = acc * ws.R[a * k + a];
+        }
+    }
+    __syncwarp();
+}
+
+// mpLP sets with |S| = n over a box also take the dual route's second stage:
+// their LP2 rows are the mpQP ones with Gamma for Lambda in the inactive rows
+// and multiplier rows from Psi
+__host__ __device__ __forceinline__ bool rows_route_lp(int mode, const InstDesc &I, const SlotDims &sd, int k)
+{
+    return I.lp && k == I.n && mode == 0 && I.box && I.p <= kDualMaxP && I.m + I.ncp <= kDualMaxRows &&
+           sd.maxLD2 >= kDualLd;
 }
 
 // The FP32 data of the multiplier law: Wm and the right-hand sides [Wh | wc]
@@ -3289,7 +3331,7 @@ __global__ void __launch_bounds__(32, 24) k_opt_screen_tiles(DevBuffers B, Tol t
         if ((nd.flags & (NODE_VALID | NODE_FEASIBLE)) != (NODE_VALID | NODE_FEASIBLE)) continue;
         const InstDesc &I = B.inst[nd.inst];
         if (level < I.k_min) continue;
-        if (!lanes_route(mode, I, sd) || (src != 0 && !I.lp)) continue;
+        if (!lanes_route(mode, I, sd) || (src != 0 && (!I.lp || level >= I.n))) continue;
         if (nd.inst != lc.inst) { flush(); lc.reset(nd.inst); }
         const KktData<float> D = multiplier_data(B, I);
         const int p = I.p, ncp = I.ncp, P1 = p + 1;
@@ -3356,10 +3398,10 @@ __global__ void __launch_bounds__(32, 24) k_opt_screen_tiles(DevBuffers B, Tol t
         }
         lc.c += piv;
         if (!proven) {
-            // stage 1 takes the sets with a KKT factor; a failed KKT margin, and
-            // every mpLP set, goes to FP64
+            // stage 1 takes the sets with a KKT factor (of an mpLP only those with
+            // |S| = n); a failed KKT margin, and every other mpLP set, goes to FP64
             if (lane == 0) {
-                if (to_rows && !I.lp) {
+                if (to_rows && (!I.lp || (src == 0 && rows_route_lp(mode, I, sd, k)))) {
                     const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_scr, 1ull);
                     if (qi < B.q_cap) B.q_lp1[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
                 } else {
@@ -3779,10 +3821,10 @@ __global__ void __launch_bounds__(32) k_opt_screen_lanes(DevBuffers B, Tol tol, 
         }
         lc.c += piv;
         if (!proven) {
-            // stage 1 takes the mpQP sets with a KKT factor, the tile stage with
-            // the stationarity rows the mpLP sets with |S| < n; a failed KKT
-            // margin, and every other mpLP set, goes to FP64
-            if (to_rows && (!I.lp || (k < I.n && k + ncp + 2 * I.n <= tile_rows(sd)))) {
+            // stage 1 takes the sets with a KKT factor (of an mpLP those with |S|
+            // = n), the tile stage with the stationarity rows the mpLP sets with
+            // |S| < n; a failed KKT margin, and every other mpLP set, goes to FP64
+            if (to_rows && (!I.lp || (k < I.n && k + ncp + 2 * I.n <= tile_rows(sd)) || rows_route_lp(mode, I, sd, k))) {
                 const long long qi = queue_slot(&ctl->n_q_scr);
                 if (qi < B.q_cap) B.q_lp1[qi] = (int)x; else atomicOr(&ctl->overflow, OV_QUEUE);
             } else {
@@ -3811,7 +3853,10 @@ cudaError_t launch_opt_screen_lanes(const DevBuffers &B, const Tol &tol, const S
 template <int ROUTE, int STAGE = 0>
 __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, SlotDims sd, int level, int mode)
 {
-    static_assert((ROUTE == 0) == (STAGE == 1), "the dual route's first stage is k_opt_screen_tiles");
+    static_assert((ROUTE == 0) == (STAGE >= 1), "the dual route's first stage is k_opt_screen_tiles");
+    // STAGE 2: the second stage for the mpLP sets with |S| = n (multiplier
+    // rows from Psi), its own instance so that the mpQP one keeps its registers
+    constexpr bool LPR = STAGE == 2;
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = lane_id();
     OptWs<float> ws;
@@ -3828,6 +3873,7 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
         ws.G = ROUTE == 1 ? (float *)(smem + o) : nullptr;
         ws.Tb = nullptr; ws.ids = nullptr;
         ws.Psi = ws.Phi = nullptr;
+        if (ROUTE == 0 && sd.maxN) ws.Psi = (float *)(smem + o);   // mpLP multiplier law (second stage)
     }
     const int side = level & 1;
     Ctl *ctl = B.ctl;
@@ -3837,17 +3883,18 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
     lc.reset(-1);
     for (;;) {
         long long x;
-        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[STAGE == 1 ? 6 : (ROUTE == 0 ? 3 : 5)], 1ull);
+        if (lane == 0) x = (long long)atomicAdd(&ctl->ctr[STAGE == 2 ? 12 : (STAGE == 1 ? 6 : (ROUTE == 0 ? 3 : 5))], 1ull);
         x = __shfl_sync(FULLMASK, x, 0);
         if (x >= nn) break;
         // stage 1 reads the queue of stage 0 (kept in q_lp1: the LP1 queue is
         // consumed before the screen runs)
-        if (STAGE == 1) x = B.q_lp1[x];
+        if (STAGE >= 1) x = B.q_lp1[x];
         const Node nd = B.node[side][x];
         if ((nd.flags & (NODE_VALID | NODE_FEASIBLE)) != (NODE_VALID | NODE_FEASIBLE)) continue;
         const InstDesc &I = B.inst[nd.inst];
         if (level < I.k_min) continue;
-        if (dual_route(mode, I, sd) != (ROUTE == 0)) continue;
+        if (LPR ? !rows_route_lp(mode, I, sd, level) : dual_route(mode, I, sd) != (ROUTE == 0)) continue;
+        constexpr bool lp_rows = LPR;
         // mpLP sets the first stage of the dual screen takes (one set per
         // thread at |S| <= kLaneMaxK, tiles above or with basis sharing)
         if (ROUTE == 1 && I.lp && lanes_route(mode, I, sd)) continue;
@@ -3880,9 +3927,10 @@ __global__ void __launch_bounds__(32, 32) k_opt_screen(DevBuffers B, Tol tol, Sl
             bmax = warp_max(bmax);
             {
             float t0, g0;
+            if constexpr (lp_rows) mplp_multipliers_f(B.fpool + I.f_WhL, B.fpool + I.f_wcL, p, k, ws);
             // dual: rows straight into the dual layout; primal: rows into G,
             // kept unpivoted for the bound that verifies the verdict
-            const float amax = dual ? region_rows<float, true>(D, I, nd.lo, nd.hi, k, ws, Tb, kDualLd, 7, &t0, &g0)
+            const float amax = dual ? region_rows<float, true, LPR>(D, I, nd.lo, nd.hi, k, ws, Tb, kDualLd, 7, &t0, &g0)
                                     : region_rows<float, true>(D, I, nd.lo, nd.hi, k, ws, nullptr, 0, 0, &t0, &g0);
             // error scale of the FP32 rows: row magnitude / smallest Cholesky
             // pivot ratio, times the reach of theta inside the box (rho >
@@ -4331,6 +4379,7 @@ const void *kernel_ptr(const char *name)
         {"opt_fp64", (const void *)k_optimality_fp64<false>},
         {"opt_fp64_lp", (const void *)k_optimality_fp64<true>},
         {"screen_dual_rows", (const void *)k_opt_screen<0, 1>},
+        {"screen_dual_rows_lp", (const void *)k_opt_screen<0, 2>},
         {"screen_dual_tiles8", (const void *)k_opt_screen_tiles<8>},
         {"screen_dual_tiles16", (const void *)k_opt_screen_tiles<16>},
         {"screen_dual_tiles32", (const void *)k_opt_screen_tiles<32>},
@@ -4412,6 +4461,7 @@ cudaError_t launch_opt_screen(const DevBuffers &B, const Tol &tol, const SlotDim
         else return cudaErrorInvalidValue;
     }
     else if (route == 2) k_opt_screen<0, 1><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
+    else if (route == 6) k_opt_screen<0, 2><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
     else k_opt_screen<1><<<grid, 32, smem, s>>>(B, tol, sd, level, mode);
     return cudaGetLastError();
 }

@@ -98,6 +98,26 @@ def test_mplp_first_stage_above_six(gpu_lib, tile_w):
     print("tile", tile_w, "first-stage LPs", lps, "FP64 fallbacks", fb, "optimal", b.inst[0]["optimal"])
 
 
+def test_mplp_second_stage_and_basis_check(gpu_lib):
+    """mpLP sets with |S| = n that the first stage leaves take the dual
+    route's second stage (multiplier rows from Psi, region rows from Gamma),
+    and those whose FP32 bound is negative but inside its margin the FP64
+    check of their dual basis: on eight instances of the mpLP batch the
+    verdicts equal the FP64 path's and the check settles sets."""
+    probs = [P.scale_problem(p) for p in P.mplp_batch()[:8]]
+    a = solver.solve(probs, precision=solver.FP64)
+    b = solver.solve(probs, precision=solver.MIXED)
+    assert a.status == b.status == 0
+    for f in ("feasible_digest", "optimal_digest", "region_digest", "feasible", "optimal", "regions", "candidates"):
+        assert np.array_equal(a.inst[f], b.inst[f]), f
+    ka = np.lexsort([a.opt["mask_lo"], a.opt["mask_hi"], a.opt["inst"]])
+    kb = np.lexsort([b.opt["mask_lo"], b.opt["mask_hi"], b.opt["inst"]])
+    assert _same(a.opt["t"][ka], b.opt["t"][kb]) and _same(a.opt["r"][ka], b.opt["r"][kb])
+    assert b.total("lp2_certified") > 0
+    print("mpLP batch (8): FP64 optimality evaluations", b.total("fallback_opt"), "settled by the basis check",
+          b.total("lp2_certified"), "of", b.total("feasible"), "feasible sets")
+
+
 @pytest.mark.parametrize("precision", [solver.FP64, solver.MIXED])
 def test_batch_of_mpqp_and_mplp_instances(gpu_lib, precision):
     probs = [P.scale_problem(p) for p in (P.random_n4_m10_p2(), P.random_mplp(6, 24, 3, seed=2),
