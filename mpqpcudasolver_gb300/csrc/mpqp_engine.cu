@@ -16,7 +16,6 @@
 #include <cstring>
 #include <exception>
 #include <new>
-#include <atomic>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -67,7 +66,6 @@ using namespace mq;
 
 // the last error text of each calling thread (mpqp_last_error)
 static thread_local std::string g_err;
-static std::atomic<unsigned> g_next_plan_id{1u};   // hash keys: unique per plan in the process
 static std::mutex g_mu;
 
 static void set_err(const std::string &s) { g_err = s; }
@@ -875,11 +873,10 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
     CK(cudaMemcpy((void *)B.dpool, dp.data(), sizeof(double) * dp.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy((void *)B.fpool, fp.data(), sizeof(float) * fp.size(), cudaMemcpyHostToDevice));
     P->h2d_bytes = (long long)(sizeof(InstDesc) * n_inst + sizeof(double) * dp.size() + sizeof(float) * fp.size());
-    // the hash is not cleared: a slot counts only when its 64-bit key (this
-    // plan's id, the run's epoch, the level) and its mask equal a query's, so
-    // an earlier plan's entries in pooled memory (another plan id) and any
+    // the hash is not cleared: a slot counts only when its tag (the run's
+    // epoch from the device's counter, and the level) and its fingerprint
+    // equal a query's, so an earlier plan's entries in pooled memory and any
     // other leftover bytes read as empty slots
-    B.plan_id = g_next_plan_id.fetch_add(1u);
     CK(cudaMemset(B.ctl, 0, sizeof(Ctl)));
     if (B.lp2b[0]) {
         CK(cudaMemset(B.lp2b[0], 0xff, sizeof(unsigned long long) * node_cap));

@@ -133,14 +133,11 @@ struct CandRec {                // identical field layout to the oracle's record
     double lp1_bound;           // FP64 dual certificate: the lower bound on z* it proved (NaN: none)
 };
 
-// key = (plan id << 32) | tag, tag = (epoch << 8) | level: an entry matches
-// only the plan, run and level that wrote it, so a plan's hash memory (from
-// the pool, possibly an earlier plan's) needs no clearing.  fp: the set's
-// 64-bit hash (instance and mask; its low bits are the home slot).  Two sets
-// share an fp with probability 2^-64; a set then found in place of an absent
-// subset is only left unpruned, and its LP1 (a superset of an infeasible set)
-// is infeasible, so no verdict depends on it.
-struct HashSlot { unsigned long long key; uint64_t fp; };
+// w = (tag << 40) | bits 24..63 of the set's 64-bit hash; tag = a function
+// of the run's epoch (drawn from one counter per device) and the level, never
+// 0.  An entry matches only the run and level that wrote it, so a plan's hash
+// memory (from the pool, possibly an earlier plan's) needs no clearing.
+struct HashSlot { unsigned long long w; };
 
 // Per-instance level bookkeeping
 struct InstCtl {
@@ -197,7 +194,7 @@ struct Ctl {
     unsigned long long ctr[kCtlCounters];  // work counters (reset every level)
     int overflow;               // bit mask of overflowed buffers
     int level;
-    int epoch;                  // run counter; hash tags are (epoch << 8) | level
+    int epoch;                  // this run's number from the device's counter (hash tags)
     int pad;
     long long hcap[2];          // slots of the hash in use per side (a power of 2 <= hash_cap)
     // 1 once a side's tableau (or ids) arena had no room for a reservation:
@@ -232,7 +229,6 @@ struct DevBuffers {
     uint8_t *ids[2];
     long long ids_cap;
     HashSlot *hash[2];
-    unsigned plan_id;           // unique per plan within the process (the upper half of hash keys)
     long long hash_cap;         // power of two
     Cand *cand;
     long long cand_cap;

@@ -110,35 +110,49 @@ __device__ __forceinline__ long long hash_cap_for(const DevBuffers &B, long long
     return c < B.hash_cap ? c : B.hash_cap;
 }
 
-// probing from slot s (the key's home slot, or later after a collision)
-__device__ __forceinline__ unsigned long long hash_slot_key(unsigned plan, int tag)
+// Hash slots are 8 bytes: a 24-bit tag (the run and the level) above 40 bits
+// of the set's 64-bit hash (its bits 24..63; the low bits pick the home
+// slot).  Runs draw their epochs from one counter per device (g_hash_epoch),
+// so the entries of another level, run or plan -- and any other leftover
+// bytes, or the zeros of fresh memory (tag 0 is never used) -- read as empty
+// slots, except a stale entry whose tag matches by wrap-around (one level of a
+// run 2^18 runs earlier): it only lengthens the probe.  Two sets share a
+// fingerprint with probability 2^-40 per probe of the same home slot; a set
+// then found in place of an absent subset is only left unpruned, and its LP1
+// (a superset of an infeasible set) is infeasible, so no verdict depends on it.
+__device__ unsigned g_hash_epoch;
+constexpr unsigned long long kFpMask = (1ull << 40) - 1;
+
+__device__ __forceinline__ unsigned long long hash_tag(int epoch, int level)
 {
-    return ((unsigned long long)plan << 32) | (unsigned)tag;
+    return (unsigned long long)(((unsigned)epoch * 64u + (unsigned)level) % 0xffffffu + 1u);
 }
 
-__device__ int hash_find_from(const HashSlot *tab, long long cap, unsigned long long key, uint64_t fp, uint64_t s)
+__device__ int hash_find_from(const HashSlot *tab, long long cap, unsigned long long tag, uint64_t fp, uint64_t s)
 {
+    const unsigned long long f40 = fp >> 24;
     for (long long probe = 0; probe < cap; probe++) {
-        const HashSlot *h = tab + s;
-        if (h->key != key) return -1;
-        if (h->fp == fp) return 1;
+        const unsigned long long w = tab[s].w;
+        if ((w >> 40) != tag) return -1;
+        if ((w & kFpMask) == f40) return 1;
         s = (s + 1) & (uint64_t)(cap - 1);
     }
     return -1;
 }
 
-__device__ bool hash_insert(HashSlot *tab, long long cap, unsigned long long key, int inst, uint64_t lo, uint64_t hi)
+__device__ bool hash_insert(HashSlot *tab, long long cap, unsigned long long tag, int inst, uint64_t lo, uint64_t hi)
 {
     const uint64_t fp = hash_key(inst, lo, hi);
+    const unsigned long long w = (tag << 40) | (fp >> 24);
     uint64_t s = fp & (uint64_t)(cap - 1);
     for (long long probe = 0; probe < cap; probe++) {
-        HashSlot *h = tab + s;
-        const unsigned long long t = *((volatile unsigned long long *)&h->key);
-        if (t != key && atomicCAS(&h->key, t, key) == t) {
-            h->fp = fp;
-            return true;
+        unsigned long long *h = &tab[s].w;
+        const unsigned long long t = *((volatile unsigned long long *)h);
+        if ((t >> 40) != tag) {
+            if (atomicCAS(h, t, w) == t) return true;
+            continue;   // lost the slot to another insert: read it again
         }
-        if (t == key) s = (s + 1) & (uint64_t)(cap - 1);
+        s = (s + 1) & (uint64_t)(cap - 1);
     }
     return false;
 }
@@ -641,7 +655,7 @@ __global__ void k_enumerate(DevBuffers B, int level)
     Ctl *ctl = B.ctl;
     const long long npar = ctl->n_node[pside] < B.node_cap ? ctl->n_node[pside] : B.node_cap;
     // key of the previous level's hash entries
-    const unsigned long long tag_prev = hash_slot_key(B.plan_id, (ctl->epoch << 8) | (level - 1));
+    const unsigned long long tag_prev = hash_tag(ctl->epoch, level - 1);
     // slots the previous level's inserts used (every expandable parent was
     // inserted, which sets it; the full table otherwise, which is always in bounds)
     const long long hcap = ctl->hcap[pside] >= 16 && ctl->hcap[pside] <= B.hash_cap ? ctl->hcap[pside] : B.hash_cap;
@@ -743,8 +757,8 @@ __global__ void k_enumerate(DevBuffers B, int level)
 #pragma unroll
                     for (int g = 0; g < G; g++) {
                         if (g < n && ok) {
-                            if (hs[g].key != tag_prev) ok = false;
-                            else if (hs[g].fp != sfp[g])
+                            if ((hs[g].w >> 40) != tag_prev) ok = false;
+                            else if ((hs[g].w & kFpMask) != (sfp[g] >> 24))
                                 ok = hash_find_from(tab, hcap, tag_prev, sfp[g],
                                                     (sidx[g] + 1) & (uint64_t)(hcap - 1)) >= 0;
                         }
@@ -889,7 +903,7 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
             nd.tab_off = -1; nd.ids_off = -1; nd.rec = rec;
             B.node[side][idx] = nd;
             if (feasible && !B.exhaustive) {
-                if (!hash_insert(B.hash[side], hcap, hash_slot_key(B.plan_id, (ctl->epoch << 8) | level), inst, lo, hi))
+                if (!hash_insert(B.hash[side], hcap, hash_tag(ctl->epoch, level), inst, lo, hi))
                     atomicOr(&ctl->overflow, OV_HASH);
             }
         }
@@ -933,7 +947,7 @@ __device__ long long store_node(const DevBuffers &B, int side, int level, const 
         B.node[side][idx] = nd;
         // the hash serves the subset test of the next level only
         if (feasible && !B.exhaustive && need_tab) {
-            if (!hash_insert(B.hash[side], hcap, hash_slot_key(B.plan_id, (ctl->epoch << 8) | level), inst, lo, hi))
+            if (!hash_insert(B.hash[side], hcap, hash_tag(ctl->epoch, level), inst, lo, hi))
                 atomicOr(&ctl->overflow, OV_HASH);
         }
     }
@@ -4123,7 +4137,7 @@ __global__ void k_level0(DevBuffers B)
         nd.rec = (B.rec && inst < B.rec_cap) ? inst : -1;
         B.node[0][inst] = nd;
         if (!B.exhaustive) {
-            hash_insert(B.hash[0], hash_cap_for(B, B.n_inst), hash_slot_key(B.plan_id, ctl->epoch << 8), inst, 0, 0);
+            hash_insert(B.hash[0], hash_cap_for(B, B.n_inst), hash_tag(ctl->epoch, 0), inst, 0, 0);
         }
         if (nd.rec >= 0) {
             CandRec &R = B.rec[nd.rec];
@@ -4159,10 +4173,9 @@ __global__ void k_reset(DevBuffers B)
         B.ictl[i] = z;
     }
     if (t == 0) {
-        const int e = B.ctl->epoch;
         Ctl z = {};
         *B.ctl = z;
-        B.ctl->epoch = e + 1;
+        B.ctl->epoch = (int)(atomicAdd(&g_hash_epoch, 1u) & 0x7fffffffu);
     }
 }
 
