@@ -1,9 +1,10 @@
 """Plans on pooled device memory: no hash clearing between plans.
 
 A plan takes its buffers from a per-device pool that keeps freed memory, and
-its subset-test hash is never cleared: each slot's key carries the plan's
-id, the run's epoch and the level, so another plan's entries (or any other
-leftover bytes) read as empty slots.  Here plans of different problems run
+its subset-test hash is never cleared: each slot's tag comes from the run's
+epoch (one counter per device, so no two runs of any plans share one) and
+the level, so another plan's entries (or any other leftover bytes) read as
+empty slots.  Here plans of different problems run
 back to back on the same pooled memory, and a repeated problem must give the
 same candidates, pruned and feasible counts and the same feasible, optimal and
 region sets as its first run; after the pool is released the same holds.
