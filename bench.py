@@ -139,7 +139,7 @@ def lp1_unique_bytes(res) -> float:
       children find it in L2);
     * per checked candidate (levels >= 1): the 8 B candidate record (read) and
       its 48 B node slot (written);
-    * per stored child: its live tableau rows, ids (write) and its 32 B hash
+    * per stored child: its live tableau rows, ids (write) and its 8 B hash
       slot; per certificate-queue entry 32 B, per FP64 re-solve entry 4 B.
 
     Last-level children decided at a certified vertex do not load their
@@ -149,7 +149,7 @@ def lp1_unique_bytes(res) -> float:
     for st in res.inst:
         cand = int(st["candidates"]) - 1          # level 0 (the empty set) is set up by k_level0
         total += int(st["lp1_parent_bytes"]) + int(st["lp1_store_bytes"]) + cand * (8 + 48)
-        total += int(st["stored"]) * 32 + (int(st["lp1_certified"]) + int(st["lp1_cert_missed"])) * 32
+        total += int(st["stored"]) * 8 + (int(st["lp1_certified"]) + int(st["lp1_cert_missed"])) * 32
         total += int(st["fallback_lp1"]) * 4
     return float(total)
 
@@ -576,7 +576,7 @@ def run_ours(args):
             "algorithmic_bytes_per_launch": ubytes / nl_lp1, "units_per_launch": lp1_cand / nl_lp1,
             "avg_launch_ms": ms_lp1 / nl_lp1, "launches_per_step": nl_lp1, "peak_source": peak_src,
             "per_unit": "each distinct parent once (live tableau rows + ids + node), 56 B per candidate, each "
-                        "stored child's live rows + ids + 32 B hash slot (device counters of the run)",
+                        "stored child's live rows + ids + 8 B hash slot (device counters of the run)",
             "issue": {"warp_inst_per_candidate": ipc, "ideal_ms_per_step": issue_ms,
                       "frac": (issue_ms / ms_lp1) if (issue_ms and ms_lp1 > 0) else None,
                       "model": "warp instructions per candidate (ncu) x candidates / (SMs x 4 schedulers x "
