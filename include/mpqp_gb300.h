@@ -228,6 +228,10 @@ typedef struct {
     /* mixed precision: sets found not optimal in FP64 from the final basis
      * of the FP32 dual screen, without the FP64 LP2 (counted in fallback_opt) */
     long long lp2_certified;
+    /* mixed precision: last-level FP32 LP1 optima whose smallest basic slack
+     * lay inside the FP32 margin, found feasible by the FP64 vertex check of
+     * their final basis (no FP64 re-solve) */
+    long long lp1_vertex_checked;
 } mpqp_inst_stats;
 
 typedef struct {

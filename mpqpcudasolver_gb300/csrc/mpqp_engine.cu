@@ -824,7 +824,8 @@ static int plan_create_locked(int n_inst, const mpqp_problem *probs, const mpqp_
     B.q_cap = cand_cap;
     // certificate queue (mixed precision): FP32 LP1 optima that are not
     // certified feasible; beyond its capacity they go to the FP64 re-solve
-    B.cert_stride = (int)((4 + std::min(sd.maxNv, 32) + 15) & ~15);
+    // an int (the candidate), the nonbasic ids, a float (the tableau's growth)
+    B.cert_stride = (int)((8 + std::min(sd.maxNv, 32) + 15) & ~15);
     B.cert_cap = P->prec == PREC_MIXED ? std::max(cand_cap / 8, (long long)4096) : 0;
     B.opt_cap = opt_cap;
     B.rec_cap = rec_cap;
@@ -1377,6 +1378,7 @@ static int plan_results_impl(mpqp_plan *P, mpqp_batch_result *&R, bool *complete
         s.lp2_first_stage_lps = ic[i].s0_lps; s.lp2_first_stage_pivots = ic[i].s0_piv;
         s.lp2_warm_offered = ic[i].warm_try; s.lp2_warm_started = ic[i].warm_used;
         s.lp2_certified = ic[i].cert_lp2;
+        s.lp1_vertex_checked = ic[i].vtx_lp1;
         s.feasible_digest = ic[i].feas_digest; s.optimal_digest = ic[i].opt_digest;
         s.region_digest = ic[i].reg_digest;
         s.last_level = ic[i].last_level; s.truncated = ic[i].truncated;

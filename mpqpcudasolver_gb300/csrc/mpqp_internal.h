@@ -127,7 +127,8 @@ struct CandRec {                // identical field layout to the oracle's record
     double t, r;
     int32_t inst, fp64;         // instance; bit0 LP1 / bit1 LP2 decided in FP64, bit2 LP1
                                 // infeasible by the FP64 dual certificate of the final FP32 basis,
-                                // bit3 LP2 not optimal by the FP64 check of the FP32 dual basis
+                                // bit3 LP2 not optimal by the FP64 check of the FP32 dual basis,
+                                // bit4 LP1 feasible by the FP64 vertex check of the final FP32 basis
     float lp1_growth;           // FP32 LP1: max |T_ij| of the final tableau (mixed precision)
     float lp1_minbeta;          // FP32 LP1: smallest basic slack value
     double lp1_bound;           // FP64 dual certificate: the lower bound on z* it proved (NaN: none)
@@ -151,6 +152,7 @@ struct InstCtl {
     long long cert_miss;        // ... that the certificate could not prove (sent to the FP64 re-solve)
     long long cert_free;        // ... of those, the misses with a free variable nonbasic (no square system)
     long long cert_lp2;         // sets found not optimal by the FP64 check of their FP32 dual basis
+    long long vtx_lp1;          // last-level LP1 optima found feasible by the FP64 vertex check
     long long lp1_cold;         // LP1 solves started from the root (the parent kept no tableau)
     long long no_tab;           // nodes kept without a tableau (the arena was full)
     long long stored;           // LP1 tableaus written for the next level

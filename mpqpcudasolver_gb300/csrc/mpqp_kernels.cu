@@ -998,15 +998,21 @@ __device__ __noinline__ int retire_fixed_columns(float *tab, int ld, int nrows, 
 // nonbasic ids of its final basis) to the FP64 dual certificate's queue, else
 // -- or when that queue is full -- to the FP64 re-solve.  Not inlined: the
 // LP1 kernel's registers stay with its simplex.
-__device__ __noinline__ void queue_undecided_lp1(const DevBuffers &B, int w, const uint8_t *nid, int nv)
+// Entries of the certificate queue: the candidate (its complement when the
+// entry asks for the FP64 vertex check instead of the dual certificate), the
+// nonbasic ids of its final FP32 basis, and the final tableau's growth (in
+// the entry's last 4 bytes).
+__device__ __noinline__ void queue_undecided_lp1(const DevBuffers &B, int w, const uint8_t *nid, int nv,
+                                                 bool vertex = false, float growth = 0.0f)
 {
     Ctl *ctl = B.ctl;
     if (nid) {
         const long long ci = (long long)atomicAdd((unsigned long long *)&ctl->n_q_cert, 1ull);
         if (ci < B.cert_cap) {
             uint8_t *e = B.cert_q + ci * B.cert_stride;
-            *reinterpret_cast<int *>(e) = w;
+            *reinterpret_cast<int *>(e) = vertex ? ~w : w;
             for (int c = 0; c < nv; c++) e[4 + c] = nid[c];
+            *reinterpret_cast<float *>(e + B.cert_stride - 4) = growth;
             return;
         }
     }
@@ -1257,7 +1263,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
         const T z = obj[pcols];
         uint64_t lo = par.lo, hi = par.hi;
         if (c.j < 64) lo |= 1ull << c.j; else hi |= 1ull << (c.j - 64);
-        bool feasible = false, decided = true, to_cert = false;
+        bool feasible = false, decided = true, to_cert = false, to_vtx = false;
         float lp1_growth = 0.0f, lp1_minbeta = 0.0f;
         if (!mixed) {
             feasible = (st == LP_OPTIMAL) && ((double)z <= tol.tol_feas);
@@ -1323,6 +1329,11 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
                 else {
                     decided = false;
                     to_cert = z > (T)tol.margin_z32 && nv <= 32 && !B.exhaustive;
+                    // every slack of S' nonbasic and the smallest basic slack
+                    // positive but inside the FP32 margin: at the instance's last
+                    // level (no tableau to store) the FP64 vertex check decides
+                    to_vtx = !to_cert && !s_basic && minb > (T)0 && level == I.k_max && nv <= 32 &&
+                             !B.exhaustive;
                 }
             }
         }
@@ -1339,7 +1350,7 @@ __global__ void __launch_bounds__(128) k_feasibility(DevBuffers B, Tol tol, Slot
             R.lp1_bound = __longlong_as_double(0x7ff8000000000000LL);
         }
         if (!decided) {
-            if (lane == 0) queue_undecided_lp1(B, (int)w, to_cert ? nid : nullptr, nv);
+            if (lane == 0) queue_undecided_lp1(B, (int)w, (to_cert || to_vtx) ? nid : nullptr, nv, to_vtx, lp1_growth);
             __syncwarp();
             continue;
         }
@@ -1484,6 +1495,9 @@ __global__ void __launch_bounds__(128) k_lp1_fp64(DevBuffers B, Tol tol, SlotDim
 // stride odd); instances with nv > 32 never reach this kernel.
 constexpr int kCertSolves = 3;
 constexpr double kCertResid = 1e-13;
+// the FP64 vertex check's margin on the basic slacks, per unit of the final
+// FP32 tableau's growth (the FP32 test uses margin_beta = 3e-5)
+constexpr double kVertexMargin = 1e-10;
 
 __host__ __device__ inline size_t cert_slot_bytes(int maxNv)
 {
@@ -1534,7 +1548,11 @@ __global__ void __launch_bounds__(128) k_lp1_cert(DevBuffers B, Tol tol, SlotDim
         x = __shfl_sync(FULLMASK, x, 0);
         if (x >= nq) break;
         const uint8_t *e = B.cert_q + x * B.cert_stride;
-        const int w = *reinterpret_cast<const int *>(e);
+        const int w0 = *reinterpret_cast<const int *>(e);
+        // w0 < 0: the FP64 vertex check of a last-level candidate (below)
+        const bool vtx = w0 < 0;
+        const int w = vtx ? ~w0 : w0;
+        const float growth = *reinterpret_cast<const float *>(e + B.cert_stride - 4);
         const Cand c = B.cand[w];
         const Node par = B.node[pside][c.parent];
         const int inst = par.inst;
@@ -1552,13 +1570,21 @@ __global__ void __launch_bounds__(128) k_lp1_cert(DevBuffers B, Tol tol, SlotDim
         bool ok = all_slack;
         double bound = 0.0;
         if (ok) {
+            double rhs = 0.0, by = 0.0;
+            if (vtx) {
+                // the vertex: lane c row c of P (P[c][v] = G[nb_c][v]), rhs_c =
+                // beta of row nb_c -- the nonbasic slacks at zero
+                if (lane < nv) {
+                    for (int v = 0; v < nv; v++) { Mdr[v] = G[(size_t)nb * ld + v]; Mfr[v] = (float)Mdr[v]; }
+                    rhs = G[(size_t)nb * ld + nv];
+                }
+            } else {
             // lane v: row v of M (M[v][cc] = G[nb_cc][v]) and rhs_v = -sum over
             // the basic slacks i of S' of G[i][v]; by = their beta_i (y_i = 1)
             for (int cc = 0; cc < nv; cc++) {
                 const int i = __shfl_sync(FULLMASK, nb, cc);
                 if (lane < nv) { Mdr[cc] = G[(size_t)i * ld + lane]; Mfr[cc] = (float)Mdr[cc]; }
             }
-            double rhs = 0.0, by = 0.0;
             uint64_t rl = lo, rh = hi;
             while (rl | rh) {
                 int i;
@@ -1567,6 +1593,7 @@ __global__ void __launch_bounds__(128) k_lp1_cert(DevBuffers B, Tol tol, SlotDim
                 if (__any_sync(FULLMASK, lane < nv && nb == i)) continue;   // nonbasic: its y is unknown
                 if (lane < nv) rhs = __dsub_rn(rhs, G[(size_t)i * ld + lane]);
                 by = __dadd_rn(by, G[(size_t)i * ld + nv]);
+            }
             }
             __syncwarp();
             // FP32 LU with partial pivoting: the pivot of column col is the
@@ -1630,6 +1657,33 @@ __global__ void __launch_bounds__(128) k_lp1_cert(DevBuffers B, Tol tol, SlotDim
                 const float ymax = warp_max_f(lane < nv ? fabsf((float)y) : 0.0f);
                 const float rres = warp_max_f(lane < nv ? fabsf((float)rr) : 0.0f);
                 ok = rres <= (float)kCertResid * (amax * ymax + rhsmax) && ymax == ymax && ymax <= 1e30f;
+                if (vtx) {
+                    // every basic slack of the vertex (u = y, lane v) clearly
+                    // positive in FP64: s_i = beta_i - G_i u > kVertexMargin *
+                    // max(1, growth of the final FP32 tableau); the slacks of S'
+                    // are nonbasic, so the vertex is feasible and z* = 0
+                    if (lane < nv) yv[lane] = y;
+                    __syncwarp();
+                    const double thr = kVertexMargin * fmax(1.0, (double)growth);
+                    bool bad = !ok;
+                    double smin = pos_inf<double>();
+                    for (int b0 = 0; b0 < I.M1; b0 += 32) {
+                        const int i = b0 + lane;
+                        bool nonbasic = false;
+                        for (int cc = 0; cc < nv; cc++) nonbasic |= __shfl_sync(FULLMASK, nb, cc) == i;
+                        if (i < I.M1 && !nonbasic) {
+                            double si = G[(size_t)i * ld + nv];
+                            for (int v = 0; v < nv; v++) si = fma(-G[(size_t)i * ld + v], yv[v], si);
+                            if (!(si > thr)) bad = true;
+                            smin = fmin(smin, si);
+                        }
+                    }
+                    ok = !__any_sync(FULLMASK, bad);
+#pragma unroll
+                    for (int off = 16; off; off >>= 1) smin = fmin(smin, __shfl_xor_sync(FULLMASK, smin, off));
+                    bound = smin;
+                    __syncwarp();
+                } else {
                 // dual feasibility after scaling, and beta.y / s
                 double smax = 1.0, byn = 0.0;
                 bool bad = false;
@@ -1644,7 +1698,29 @@ __global__ void __launch_bounds__(128) k_lp1_cert(DevBuffers B, Tol tol, SlotDim
                 byn = warp_sum_d(byn);
                 bound = __dadd_rn(by, byn) / smax;
                 ok = ok && !bad && bound > tol.tol_feas;
+                }
             }
+        }
+        if (vtx) {
+            // the vertex check: a feasible node of the instance's last level
+            // (no tableau), else the FP64 re-solve
+            const long long rec = (B.rec && ctl->rec_base + w < B.rec_cap) ? ctl->rec_base + w : -1;
+            if (ok) {
+                if (lane == 0) {
+                    InstCtl *ic = &B.ictl[inst];
+                    atomicAdd((unsigned long long *)&ic->vtx_lp1, 1ull);
+                    atomicAdd((unsigned long long *)&ic->feasible, 1ull);
+                    atomicAdd(&ic->feas_digest, mask_digest(lo, hi));
+                    if (rec >= 0) { B.rec[rec].feasible = 1; B.rec[rec].fp64 |= 16; B.rec[rec].lp1_bound = bound; }
+                }
+                store_node<float, double>(B, level & 1, level, I, inst, lo, hi, true, nullptr, nullptr, rec, 0, 0, 0,
+                                          false, w);
+            } else if (lane == 0) {
+                const long long qi = (long long)atomicAdd((unsigned long long *)&ctl->n_q_lp1, 1ull);
+                if (qi < B.q_cap) B.q_lp1[qi] = w; else atomicOr(&ctl->overflow, OV_QUEUE);
+            }
+            __syncwarp();
+            continue;
         }
         if (lane == 0) {
             InstCtl *ic = &B.ictl[inst];

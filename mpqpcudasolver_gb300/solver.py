@@ -61,7 +61,7 @@ class InstStats(ctypes.Structure):
                                             "lp1_parent_bytes", "lp1_store_bytes", "lp1_cold",
                                             "nodes_without_tableau", "lp2_first_stage_lps",
                                             "lp2_first_stage_pivots", "lp2_warm_offered", "lp2_warm_started",
-                                            "lp2_certified")]
+                                            "lp2_certified", "lp1_vertex_checked")]
 
 
 class BatchResult(ctypes.Structure):
@@ -233,7 +233,7 @@ _INST_DTYPE = np.dtype([(f[0], "<i8") for f in InstStats._fields_[:11]] +
                         ("lp1_parent_bytes", "<i8"), ("lp1_store_bytes", "<i8"), ("lp1_cold", "<i8"),
                         ("nodes_without_tableau", "<i8"), ("lp2_first_stage_lps", "<i8"),
                         ("lp2_first_stage_pivots", "<i8"), ("lp2_warm_offered", "<i8"),
-                        ("lp2_warm_started", "<i8"), ("lp2_certified", "<i8")])
+                        ("lp2_warm_started", "<i8"), ("lp2_certified", "<i8"), ("lp1_vertex_checked", "<i8")])
 _OPT_DTYPE = np.dtype([("mask_lo", "<u8"), ("mask_hi", "<u8"), ("inst", "<i4"), ("level", "<i4"), ("t", "<f8"),
                        ("r", "<f8"), ("region", "<i4"), ("fp64", "<i4"), ("rec", "<i8"), ("err", "<f8")])
 assert _INST_DTYPE.itemsize == ctypes.sizeof(InstStats)
