@@ -648,7 +648,8 @@ def run_ours(args):
         "pivots_per_s": (res.total("lp1_pivots") + res.total("lp2_pivots") + res.total("cheb_pivots"))
         * world / (ms_step / 1e3),
         "regions_per_step": res.total("regions"), "feasible_per_step": res.total("feasible"),
-        "fp64_fallbacks": {"lp1": res.total("fallback_lp1"), "optimality": res.total("fallback_opt"),
+        "fp64_fallbacks": {"lp1": res.total("fallback_lp1"), "lp1_by_vertex_check": res.total("lp1_vertex_checked"),
+                           "optimality": res.total("fallback_opt"),
                            "optimality_by_basis_check": res.total("lp2_certified")},
         "kernels_ms_per_step": {k: round(v[0], 3) for k, v in sorted(kt.items(), key=lambda kv: -kv[1][0])},
         "kernel_launches_per_step": {k: v[1] for k, v in kt.items()},

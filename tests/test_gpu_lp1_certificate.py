@@ -81,3 +81,32 @@ def test_fp32_infeasible_verdicts_are_certified_or_resolved(gpu_lib, case):
     print(case, "infeasible", int(infeasible.sum()), "certified", int(cert.sum()), "re-solved",
           int(resolved.sum()), "cert missed", res.total("lp1_cert_missed"), "free-variable misses",
           res.total("lp1_cert_freevar"))
+
+
+VERTEX = 16
+
+
+@pytest.mark.parametrize("case", ["m62-k4", "n10m43p4-k4"])
+def test_fp64_vertex_check_of_last_level_optima(gpu_lib, case):
+    """At an instance's last level, an FP32 LP1 optimum with every slack of S'
+    nonbasic and a smallest basic slack inside the FP32 margin is decided by
+    the FP64 vertex check of its final basis instead of an FP64 re-solve:
+    every set it accepts is feasible for the oracle, lies at the last level,
+    and carries a positive smallest slack; the counter equals the records."""
+    make = {"m62-k4": P.random_n12_m62_p6, "n10m43p4-k4": P.random_n10_m43_p4}[case]
+    kmax = 4
+    prob = P.scale_problem(make())
+    ref = O.enumerate_sets(prob, k_max=kmax, nthreads=8)
+    res = solver.solve([prob], precision=solver.MIXED, k_max=kmax, record=1, rec_cap=ref.n_cand + 16,
+                       cand_cap=ref.n_cand + 1024, arena_bytes=1 << 29)
+    assert res.status == 0 and res.overflow == 0
+    g, o = _sorted(res.rec), _sorted(ref.cand)
+    assert np.array_equal(g["mask_lo"], o["mask_lo"]) and np.array_equal(g["mask_hi"], o["mask_hi"])
+    assert np.array_equal(g["feasible"], o["feasible"])
+    vtx = (g["fp64"] & VERTEX) != 0
+    assert np.all(o["feasible"][vtx] == 1)
+    assert np.all(g["level"][vtx] == kmax)
+    assert np.all(g["lp1_bound"][vtx] > 0.0)
+    assert not np.any(vtx & ((g["fp64"] & (CERT | RESOLVED)) != 0))
+    assert res.total("lp1_vertex_checked") == int(vtx.sum()) > 0
+    print(case, "vertex checks", int(vtx.sum()), "FP64 re-solves", res.total("fallback_lp1"))
